@@ -1,0 +1,315 @@
+"""Benchmark: histories/s of the 8-group two-zone k-eigenvalue problem.
+
+Workload (the GPU-scale plain-method configuration): 8 groups, a 30 cm fuel
+cube inside a 60 cm reflector cube, vacuum outside, seeded cross sections,
+1e6 histories per cycle, FP64 tracking.  A step is one active k-eigenvalue
+cycle: transport of 1e6 source particles, fission-bank compaction and
+resampling of the next source.  ``value`` times the steps with CUDA events
+on the engine's stream, with the bank resident in HBM; ``e2e`` times the
+same workload through the C ABI's host-buffer call (mc_transport_bank), with
+the source copied in from pinned host memory and the fission bank copied
+back every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the reference path on the host cores: the CPU
+oracle (a restatement of the reference's transport loop, all host threads)
+on the same problem.  N>1 (torchrun) runs independent replicas, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "histories/s on 1 GB300, plain vs surrogate-TSL at matched k_eff sigma/spectrum chi2"
+UNIT = "histories/s"
+WORKLOAD = "8-group two-zone k-eigenvalue (fuel cube 30 cm in reflector cube 60 cm), 1e6 histories/cycle"
+BYTES_PER_EVENT = 128  # minimal SoA particle state read + write per event
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed
+    region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+
+        def read():
+            for line in self.proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+
+        self.thread = threading.Thread(target=read, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm = [float(s[0]) for s in self.samples if len(s) >= 8 and s[0].replace(".", "").isdigit()]
+        smax = [float(s[1]) for s in self.samples if len(s) >= 8 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 8 for i in range(4)
+                          if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def problem(histories: int):
+    from minimc_gb300 import synth
+
+    return synth.two_zone_cubes(histories=histories, inactive=20, active=50)
+
+
+def cpu_baseline(xml: str, histories: int, threads: int, cycles: int) -> dict:
+    """Times the CPU oracle (reference algorithm, minstd streams) on the host
+    cores: `cycles` cycles of `histories` histories from the initial source."""
+    from oracle.build import Oracle
+
+    o = Oracle(xml)
+    r = o.run_keigenvalue(histories, 1, 1, cycles - 1, threads=threads)
+    hps = histories * cycles / r["seconds"]
+    return {"value": hps, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{cycles} cycles x {histories} histories of the same problem (CPU oracle, "
+                      f"{threads} threads), {r['seconds']:.1f} s"}
+
+
+def run_reference(args) -> None:
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    hist = args.histories
+    xml = problem(hist).xml()
+    threads = os.cpu_count() or 1
+    # warm-up: one short cycle
+    from oracle.build import Oracle
+
+    Oracle(xml).run_keigenvalue(min(hist, 100_000), 1, 1, 0, threads=threads)
+    times = []
+    o = Oracle(xml)
+    # each step: one cycle of the workload on all host threads (the first
+    # cycle starts from the point source; the bank converges in a few cycles)
+    r = o.run_keigenvalue(hist, 1, args.warmup, args.steps, threads=threads)
+    secs = r["seconds"]
+    cycles = args.warmup + args.steps
+    value = hist * cycles / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / cycles,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "histories_per_cycle": hist, "rng": "minstd (reference streams)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{cycles} cycles x {hist} histories (CPU oracle restating the reference path)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from minimc_gb300 import RNG_PHILOX, SITE_DTYPE, Context
+
+    hist = args.histories
+    prob = problem(hist)
+    prob.seed = 1 + rank
+    xml = prob.xml()
+    ctx = Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_xml(xml)
+    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident cycles
+    ctx.keig_begin(**opts)
+    for _ in range(args.warmup):
+        ctx.keig_cycle(False)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
+    st0 = ctx.keig_status()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    t_wall = time.perf_counter()
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        ctx.keig_cycle(True)
+        ev[i][1].record(stream)
+        flush.zero_()  # L2 flush between timed steps (outside the event pair)
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    st1 = ctx.keig_status()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    k_out = ctx.keig_end()
+    events = st1.events - st0.events
+    transport_ms = st1.transport_ms - st0.transport_ms
+    launches = st1.launches - st0.launches
+    # max over ranks
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = hist * args.steps * ws / (total_ms / 1e3)
+    e_h = events / (hist * args.steps)
+    peak, peak_kind = peaks()
+    alg_bytes = e_h * BYTES_PER_EVENT * hist  # per transport launch (one per step)
+    launch_ms = transport_ms / args.steps
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("k_history_mg_per_launch_bytes")
+
+    # ---- end to end through the host-buffer ABI call
+    n_sites = hist
+    host_src = torch.empty(n_sites * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    src = host_src.numpy().view(SITE_DTYPE)
+    cap = n_sites * max(1, ctx.info.max_yield)
+    host_bank = torch.empty(cap * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    bank = host_bank.numpy().view(SITE_DTYPE)
+    rng = np.random.default_rng(1234 + rank)
+    # converged starting source: the last device bank is not exposed, so start
+    # from isotropic sites at the origin and let the warm-up steps spread them
+    src["x"] = src["y"] = src["z"] = 0.0
+    mu = rng.uniform(-1, 1, n_sites)
+    ph = rng.uniform(0, 2 * np.pi, n_sites)
+    st = np.sqrt(1 - mu * mu)
+    src["u"], src["v"], src["w"] = mu, st * np.cos(ph), st * np.sin(ph)
+    src["energy"] = 1.0
+    src["key"] = np.arange(n_sites, dtype=np.uint64)
+    e2e_times = []
+    h2d = n_sites * SITE_DTYPE.itemsize
+    d2h_total = 0
+    for i in range(args.warmup + args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        m = ctx.transport_bank_into(src, bank)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append(t1 - t0)
+            d2h_total += m * SITE_DTYPE.itemsize
+        # caller-side resampling of the next source (outside the timed call)
+        idx = rng.integers(0, m, n_sites)
+        nxt = bank[idx]
+        src[:] = nxt
+        src["key"] = np.arange(n_sites, dtype=np.uint64) + (i + 1) * n_sites
+    e2e_s = sum(e2e_times)
+    e2e_value = hist * args.steps * ws / e2e_s
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(xml, args.cpu_histories, os.cpu_count() or 1, args.cpu_cycles)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories_per_cycle": hist, "groups": 8, "rng": "philox",
+                       "fast_math": bool(args.fast), "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas{ws}" if ws > 1 else "single GPU",
+                       "schedule": "history (fused)", "block": args.block},
+            "k_eff_last": float(k_out.k_mean) if k_out.k_mean else None,
+            "events_per_history": e_h,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_history_mg", "algorithmic_bytes_per_launch": alg_bytes,
+                         "launch_ms": launch_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": int(d2h_total / max(1, args.steps)),
+                    "call": "mc_transport_bank (pinned host banks)"},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--histories", type=int, default=1_000_000)
+    ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--fast", type=int, default=0)
+    ap.add_argument("--cpu-histories", type=int, default=1_000_000)
+    ap.add_argument("--cpu-cycles", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,257 @@
+/*
+ * minimc_gb300 — C ABI of the GB300 particle-history engine.
+ *
+ * The reference (minimc v0.5.1) has no FFI layer.  Its extension points are
+ * C++ abstract classes, and the per-particle transport call
+ *
+ *     Bank TransportMethod::Transport(Particle&, EstimatorSetProxy&,
+ *                                     const World&) const noexcept
+ *     (src/TransportMethod.hpp:42-43)
+ *
+ * cannot be batched, so this library drops in one level up, where
+ * Driver::Solve() (src/Driver.hpp:30) runs every history.  Each entry point
+ * below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns MC_OK (0) or a negative MC_ERR_* code; no C++
+ *     exception crosses this boundary.  mc_last_error() returns the message,
+ *     which uses the reference's exception text where the reference has one.
+ *   - One mc_ctx per host thread.  A context owns all device memory it uses;
+ *     calls are ordered on the context's stream and synchronous on return
+ *     unless stated otherwise.
+ *   - Host pointers are plain arrays; nothing here takes or returns a torch
+ *     type.  Lengths are element counts.
+ *   - Groups are numbered 1..G with 1 the fastest group, as in the reference
+ *     (src/BasicTypes.hpp:17-21).  Energies are in MeV.
+ */
+#ifndef MINIMC_GB300_H
+#define MINIMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MC_OK 0
+#define MC_ERR_INPUT (-1)      /* bad problem input or argument           */
+#define MC_ERR_OOM (-2)        /* device allocation failed                */
+#define MC_ERR_DEVICE (-3)     /* CUDA runtime error                      */
+#define MC_ERR_TIMEOUT (-4)    /* a bounded device wait ran out           */
+#define MC_ERR_LOST (-5)       /* a particle left every cell              */
+#define MC_ERR_RESAMPLE (-6)   /* thermal-scattering resample limit hit   */
+#define MC_ERR_STATE (-7)      /* call out of order (e.g. no problem)     */
+#define MC_ERR_OVERFLOW (-8)   /* bank, stack or per-history tally full   */
+#define MC_ERR_EVENT_CAP (-9)  /* a particle reached the event cap        */
+
+/* ---- options ------------------------------------------------------------ */
+/* Random-number streams.
+ * MC_RNG_PHILOX: counter-based Philox4x32-10 stream per history (default).
+ * MC_RNG_MINSTD: the reference's own streams: std::minstd_rand per particle,
+ *   seeded exactly as src/Source.cpp:143-154 and src/Particle.cpp:96-100 do,
+ *   consumed through the C++ standard's generate_canonical, so a history
+ *   follows the same random walk as the reference's. */
+#define MC_RNG_PHILOX 0
+#define MC_RNG_MINSTD 1
+
+/* How the event loop is scheduled on the device. */
+#define MC_SCHEDULE_AUTO 0     /* autotuner's choice                      */
+#define MC_SCHEDULE_HISTORY 1  /* fused kernel, one history per thread,
+                                  dead lanes refilled from the queue      */
+#define MC_SCHEDULE_EVENT 2    /* event kernels over compacted queues     */
+
+typedef struct mc_ctx mc_ctx;
+
+typedef struct {
+  uint64_t histories;   /* 0: the problem's <histories>                  */
+  uint64_t seed;        /* 0: the problem's <seed> (default 1)           */
+  uint32_t inactive;    /* k-eigenvalue: 0 and active==0 -> from problem */
+  uint32_t active;
+  int32_t rng;          /* MC_RNG_*                                      */
+  int32_t schedule;     /* MC_SCHEDULE_*                                 */
+  uint32_t max_events;  /* per-particle event cap; 0 -> 1000000          */
+  int32_t block_size;   /* 0 -> autotuned                                */
+  int32_t fast_math;    /* 1: FP32 sampling arithmetic (Philox only);
+                           geometry and positions stay FP64            */
+  int32_t reserved[7];
+} mc_run_opts;
+
+/* A particle in a bank: the state that Bank/Particle carry between
+ * Transport calls (src/Particle.hpp:104-131).  64 bytes. */
+typedef struct {
+  double x, y, z;   /* position, cm                                      */
+  double u, v, w;   /* direction cosines                                 */
+  double energy;    /* MeV, or the group number for multigroup problems  */
+  uint64_t key;     /* RNG seed (minstd) or stream key (Philox)          */
+} mc_site;
+
+typedef struct {
+  int32_t problem;      /* 0 fixed source, 1 k-eigenvalue                */
+  int32_t energy_mode;  /* 0 multigroup, 1 continuous energy             */
+  int32_t tracking;     /* 0 surface, 1 cell delta                       */
+  int32_t n_cells, n_surfaces, n_materials, n_nuclides;
+  int32_t groups;
+  int32_t n_estimators;
+  int32_t n_tsl;
+  uint64_t histories, seed;
+  uint32_t inactive, active;
+  uint64_t total_bins;  /* sum of estimator bin counts                  */
+  uint32_t max_yield;   /* upper bound on secondaries per fission       */
+  int32_t reserved[7];
+} mc_problem_info;
+
+typedef struct {
+  char name[64];
+  int32_t kind;         /* 0 current, 1 track length                    */
+  int32_t target;       /* surface (current) or cell (track length)     */
+  uint64_t offset;      /* first bin in the flattened tally arrays      */
+  uint64_t n_bins;
+  uint64_t cosine_bins, energy_bins;
+} mc_estimator_info;
+
+/* Per-run results.  sum/sum_sq are caller-owned host arrays of
+ * mc_problem_info.total_bins doubles (may be NULL).  They receive, per bin,
+ * the sum over histories of each history's score and of its square, which is
+ * what Scorable keeps (src/Scorable.cpp:101-106). */
+typedef struct {
+  double* sum;
+  double* sum_sq;
+  uint32_t* history_events;  /* optional [histories]: events per history   */
+  int8_t* history_fate;      /* optional [histories]: last event of the
+                                source particle (Particle::Event order)   */
+  uint64_t histories;
+  uint64_t events;           /* collisions + crossings (+ virtual)         */
+  uint64_t secondaries;      /* particles banked                           */
+  uint64_t lost, capped, overflow, resample_failures;
+  double transport_ms;       /* device time of the transport kernels       */
+  uint64_t launches;         /* kernels launched                           */
+  double reserved[4];
+} mc_tally_out;
+
+/* k-eigenvalue results.  k_cycle: caller-owned [inactive+active]; tallies
+ * are accumulated over active cycles, one history per source particle. */
+typedef struct {
+  double* k_cycle;
+  uint64_t* bank_size;       /* optional [inactive+active]                  */
+  double* sum;
+  double* sum_sq;
+  double k_mean, k_std;      /* over active cycles                          */
+  double k_tracklength_mean; /* track-length estimate over active cycles    */
+  uint64_t events, lost, capped, overflow;
+  double transport_ms;
+  uint64_t launches;
+  double reserved[4];
+} mc_keig_out;
+
+/* ---- context ------------------------------------------------------------ */
+int mc_create(mc_ctx** out, int device);
+void mc_destroy(mc_ctx* ctx);
+/* Copies the last error message (NUL-terminated, truncated to n). */
+int mc_last_error(const mc_ctx* ctx, char* buf, size_t n);
+/* Runs subsequent work on a caller stream (cudaStream_t as void*). */
+int mc_set_stream(mc_ctx* ctx, void* cuda_stream);
+int mc_version(void);
+
+/* ---- problem ------------------------------------------------------------ */
+/* Driver::Create(path) (src/Driver.cpp:18-35) + World(root)
+ * (src/World.cpp:20-24): parses the XML text, builds the world, nuclear
+ * data, source and estimators, and uploads them.  Relative data-file paths
+ * resolve against base_dir (NULL or "" = current directory). */
+int mc_load_xml(mc_ctx* ctx, const char* xml_text, const char* base_dir);
+int mc_problem_info_get(mc_ctx* ctx, mc_problem_info* out);
+
+/* Geometry semantics (applies to later runs and probes of this context).
+ * MC_GEOMETRY_ROBUST (default): after a surface crossing the crossed
+ *   surface's side follows the direction of travel and that surface is
+ *   ignored until the next collision, so a grazing particle cannot stay on a
+ *   surface and leave the geometry; CylinderX::Contains compares rho^2 with
+ *   r^2.
+ * MC_GEOMETRY_REFERENCE: the reference's exact semantics -- relocation by a
+ *   point test after a 10*DBL_EPSILON nudge (src/TransportMethod.cpp:68-72)
+ *   and CylinderX::Contains comparing sqrt(rho^2) with r^2
+ *   (src/CSGSurface.cpp:173). */
+#define MC_GEOMETRY_ROBUST 0
+#define MC_GEOMETRY_REFERENCE 1
+int mc_set_geometry_mode(mc_ctx* ctx, int32_t mode);
+int mc_estimator_info_get(mc_ctx* ctx, int32_t index, mc_estimator_info* out);
+/* Name of cell/surface/material/nuclide by index (kind 0/1/2/3). */
+int mc_object_name(mc_ctx* ctx, int32_t kind, int32_t index, char* buf, size_t n);
+
+/* ---- solvers ------------------------------------------------------------ */
+/* FixedSource::Solve (src/FixedSource.cpp:22-77): histories i = 0..n-1 start
+ * from Source::Sample(seed + i); secondaries are transported within their
+ * history; tallies are committed per history. */
+int mc_run_fixed_source(mc_ctx* ctx, const mc_run_opts* opts, mc_tally_out* out);
+
+/* KEigenvalue::Solve (src/KEigenvalue.cpp:36-84; a stub in the reference,
+ * completed here): cycle 0 starts from Source::Sample(1..N); each cycle
+ * transports N particles, banks fission sites (Multigroup::Fission /
+ * ContinuousFission::Interact), sets k_cycle = sites/N and draws the next N
+ * sources uniformly from the bank. */
+int mc_run_keigenvalue(mc_ctx* ctx, const mc_run_opts* opts, mc_keig_out* out);
+
+/* Cycle-by-cycle form of mc_run_keigenvalue, for callers that drive the
+ * cycle loop.  begin samples the initial source; cycle transports the
+ * current source and prepares the next one (k of the cycle in *k); end
+ * fills out. */
+int mc_keig_begin(mc_ctx* ctx, const mc_run_opts* opts);
+int mc_keig_cycle(mc_ctx* ctx, int32_t active, double* k);
+int mc_keig_end(mc_ctx* ctx, mc_keig_out* out);
+/* Running totals of the cycles run so far (events, transport_ms, launches,
+ * counters); k_cycle/bank_size/sum/sum_sq are filled when non-NULL. */
+int mc_keig_status(mc_ctx* ctx, mc_keig_out* out);
+
+/* Batched Particle::Transport (src/Particle.cpp:42-44) over a host bank:
+ * copies n sites in, transports each until it dies, and copies the fission
+ * sites they banked (Particle::MoveSecondariesTo, src/Particle.cpp:102-104)
+ * back, ordered by source index.  *n_out receives the number of sites;
+ * MC_ERR_OVERFLOW if it exceeds cap (the first cap sites are returned).
+ * keys of the input sites seed each particle's stream.  Tallies are
+ * accumulated into the context's estimators (see mc_tallies_get). */
+int mc_transport_bank(mc_ctx* ctx, const mc_site* sites, uint64_t n, int32_t rng,
+                      mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
+int mc_tallies_reset(mc_ctx* ctx);
+int mc_tallies_get(mc_ctx* ctx, double* sum, double* sum_sq);
+
+/* ---- deterministic kernels, for parity checks --------------------------- */
+/* World::FindCellContaining (src/World.cpp:26-37): first cell in XML order
+ * containing each point; -1 where the reference throws. xyz: [n][3]. */
+int mc_find_cell(mc_ctx* ctx, const double* xyz, uint64_t n, int32_t* cell);
+/* Cell::NearestSurface (src/Cell.cpp:37-51). */
+int mc_nearest_surface(mc_ctx* ctx, const int32_t* cell, const double* xyz, const double* uvw,
+                       uint64_t n, int32_t* surface, double* distance);
+/* CSGSurface::Distance / Contains (src/CSGSurface.cpp:71-174). */
+int mc_surface_distance(mc_ctx* ctx, int32_t surface, const double* xyz, const double* uvw,
+                        uint64_t n, double* distance);
+int mc_surface_contains(mc_ctx* ctx, int32_t surface, const double* xyz, uint64_t n,
+                        int8_t* contains);
+/* Material::GetMicroscopicTotal / GetMicroscopicMajorant (src/Material.cpp:41-61)
+ * for a neutron in `cell` at xyz with the given energy (MeV or group). */
+int mc_material_xs(mc_ctx* ctx, int32_t cell, const double* xyz, const double* energy,
+                   uint64_t n, double* total, double* majorant);
+/* ContinuousMap::at bracket (src/ContinuousMap.hpp:21-56) on the energy grid
+ * of a nuclide's total cross section: the std::map::upper_bound position,
+ * found through the unionized grid. */
+int mc_energy_index(mc_ctx* ctx, int32_t nuclide, const double* energy, uint64_t n,
+                    int64_t* upper_index);
+
+/* ---- thermal scattering (ThermalScattering.cpp) --------------------------- */
+#define MC_TSL_POD 0   /* POD reconstruction, SampleBeta/SampleAlpha        */
+#define MC_TSL_MLP 1   /* MLP surrogate (POD outside the trained box)       */
+/* ThermalScattering::Scatter (src/ThermalScattering.cpp:159-171) at the
+ * sampler level: for each (E,T) draws beta then alpha.  Failures (resample
+ * limit) leave NaN and are counted in *failures. */
+int mc_sample_tsl(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
+                  uint64_t n, uint64_t seed, int32_t method, double* beta, double* alpha,
+                  uint64_t* failures);
+/* ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157). */
+int mc_tsl_total(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
+                 uint64_t n, double* xs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIMC_GB300_H */

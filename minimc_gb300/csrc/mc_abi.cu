@@ -1,0 +1,895 @@
+// C ABI (include/minimc_gb300.h): context, world upload and the solvers.
+#include "../../include/minimc_gb300.h"
+#include "mc_kernels.cuh"
+#include "mc_model.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+using mcd::DevCounters;
+using mcd::DevWorld;
+using mcd::RunParams;
+using mcd::Site;
+
+static_assert(sizeof(mc_site) == sizeof(Site), "mc_site layout");
+
+struct DevBuffer {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct mc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  bool loaded = false;
+  mc::Model model;
+  std::vector<void*> world_allocs;
+  DevWorld dw{};
+  int32_t geometry_mode = MC_GEOMETRY_ROBUST;
+  uint32_t max_yield = 1;
+  uint64_t total_bins = 0;
+  DevCounters* d_ctr = nullptr;
+  double* d_sum = nullptr;
+  double* d_sq = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint64_t launches = 0;
+  // scratch, grown on demand
+  DevBuffer scratch[12];
+  // k-eigenvalue state
+  struct {
+    bool active = false;
+    uint64_t n = 0, seed = 1;
+    uint32_t inactive = 0, act = 0, cycle = 0;
+    int rng = 0, fast = 0, block = 256;
+    uint32_t max_events = 1000000;
+    std::vector<double> k, ktl;
+    std::vector<uint64_t> bank;
+    double transport_ms = 0;
+    uint64_t events = 0, lost = 0, capped = 0, overflow = 0;
+    uint64_t launches0 = 0;
+  } keig;
+};
+
+namespace {
+
+enum ScratchSlot {
+  kSrc = 0,
+  kSlots,
+  kCount,
+  kOffsets,
+  kScanSums,
+  kTotal,
+  kBank,
+  kHistEvents,
+  kHistFate,
+  kProbeIn,
+  kProbeIn2,
+  kProbeOut,
+};
+
+int fail(mc_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CUDA_TRY(ctx, expr)                                                               \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess) return fail((ctx), MC_ERR_DEVICE, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int upload(mc_ctx* c, const std::vector<T>& v, const T** out) {
+  const size_t bytes = std::max<size_t>(1, v.size()) * sizeof(T);
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc failed for world tables");
+  c->world_allocs.push_back(p);
+  if (!v.empty()) CUDA_TRY(c, cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *out = static_cast<const T*>(p);
+  return MC_OK;
+}
+
+void* scratch(mc_ctx* c, int slot, size_t bytes) {
+  DevBuffer& b = c->scratch[slot];
+  if (b.bytes >= bytes && b.p) return b.p;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (cudaMalloc(&b.p, std::max<size_t>(bytes, 256)) != cudaSuccess) {
+    b.p = nullptr;
+    return nullptr;
+  }
+  b.bytes = std::max<size_t>(bytes, 256);
+  return b.p;
+}
+
+void free_world(mc_ctx* c) {
+  for (void* p : c->world_allocs) cudaFree(p);
+  c->world_allocs.clear();
+  c->loaded = false;
+}
+
+// Builds the flat device tables from the model (see mc_device.cuh for the
+// layout).  Running sums are formed in the reference's summation order so
+// that a table lookup equals the on-the-fly sum bit-for-bit.
+int build_world(mc_ctx* c) {
+  const mc::Model& m = c->model;
+  DevWorld& w = c->dw;
+  w = DevWorld{};
+  w.n_surfaces = static_cast<int32_t>(m.surfaces.size());
+  w.n_cells = static_cast<int32_t>(m.cells.size());
+  w.n_materials = static_cast<int32_t>(m.materials.size());
+  w.n_nuclides = static_cast<int32_t>(m.nuclides.size());
+  w.n_types = 2;
+  w.energy_mode = m.energy_mode;
+  w.tracking = m.tracking;
+  w.quirks = c->geometry_mode;
+  w.G = static_cast<int32_t>(m.energy_mode == mc::kMultigroup ? m.groups : 0);
+
+  std::vector<int32_t> surf_kind, surf_refl;
+  std::vector<double> surf_p;
+  for (const auto& s : m.surfaces) {
+    surf_kind.push_back(s.kind);
+    surf_refl.push_back(s.reflective);
+    for (double v : s.p) surf_p.push_back(v);
+  }
+  std::vector<int32_t> cell_begin{0}, cell_surf, cell_mat, cell_field;
+  std::vector<uint8_t> cell_within;
+  for (const auto& cl : m.cells) {
+    for (size_t k = 0; k < cl.surfaces.size(); k++) {
+      cell_surf.push_back(cl.surfaces[k]);
+      cell_within.push_back(cl.within[k]);
+    }
+    cell_begin.push_back(static_cast<int32_t>(cell_surf.size()));
+    cell_mat.push_back(cl.material);
+    cell_field.push_back(cl.temperature);
+  }
+  std::vector<double> field;
+  for (const auto& f : m.fields) {
+    const double v[8] = {static_cast<double>(f.linear), f.c, f.g[0], f.g[1], f.g[2], f.b, f.upper, f.lower};
+    field.insert(field.end(), v, v + 8);
+  }
+  std::vector<double> mat_density, mat_afrac;
+  std::vector<int32_t> mat_begin{0}, mat_nuc;
+  int32_t max_nuc = 1;
+  for (const auto& mt : m.materials) {
+    mat_density.push_back(mt.number_density);
+    for (size_t k = 0; k < mt.nuclides.size(); k++) {
+      mat_nuc.push_back(mt.nuclides[k]);
+      mat_afrac.push_back(mt.afrac[k]);
+    }
+    mat_begin.push_back(static_cast<int32_t>(mat_nuc.size()));
+    max_nuc = std::max<int32_t>(max_nuc, static_cast<int32_t>(mt.nuclides.size()));
+  }
+  w.max_mat_nuc = max_nuc;
+
+  int rc;
+#define UP(vec, field_)                                  \
+  if ((rc = upload(c, vec, &w.field_)) != MC_OK) return rc;
+  UP(surf_kind, surf_kind)
+  UP(surf_refl, surf_refl)
+  UP(surf_p, surf_p)
+  UP(cell_begin, cell_begin)
+  UP(cell_surf, cell_surf)
+  UP(cell_within, cell_within)
+  UP(cell_mat, cell_mat)
+  UP(cell_field, cell_field)
+  UP(field, field)
+  UP(mat_density, mat_density)
+  UP(mat_begin, mat_begin)
+  UP(mat_nuc, mat_nuc)
+  UP(mat_afrac, mat_afrac)
+
+  c->max_yield = 1;
+  if (m.energy_mode == mc::kMultigroup) {
+    const size_t G = m.groups, N = m.nuclides.size(), M = m.materials.size(), T = 2;
+    std::vector<double> total(T * N * G, 0), rx(T * N * G * 3, 0), scat(T * N * G * G, 0), nubar(T * N * G, 0),
+        chi(T * N * G * G, 0), nusigf(T * N * G, 0);
+    double max_nubar = 0;
+    for (size_t t = 0; t < T; t++) {
+      for (size_t n = 0; n < N; n++) {
+        const auto& nuc = m.nuclides[n];
+        if (!nuc.present[t]) continue;
+        const mc::MGData& d = nuc.mg[t];
+        for (size_t g = 0; g < G; g++) {
+          const size_t i = (t * N + n) * G + g;
+          total[i] = d.total[g];
+          double acc = 0;
+          if (d.has_capture) acc = acc + d.capture[g];
+          rx[i * 3 + 0] = acc;
+          if (d.has_scatter) acc = acc + d.scatter[g];
+          rx[i * 3 + 1] = acc;
+          if (d.has_fission) acc = acc + d.fission[g];
+          rx[i * 3 + 2] = acc;
+          if (d.has_scatter) {
+            double a = 0;
+            for (size_t go = 0; go < G; go++) {
+              a = a + d.scatter_prob[g * G + go];
+              scat[i * G + go] = a;
+            }
+          }
+          if (d.has_fission) {
+            nubar[i] = d.nubar[g];
+            nusigf[i] = d.nubar[g] * d.fission[g];
+            max_nubar = std::max(max_nubar, d.nubar[g]);
+            double a = 0;
+            for (size_t go = 0; go < G; go++) {
+              a = a + d.chi[g * G + go];
+              chi[i * G + go] = a;
+            }
+          }
+        }
+      }
+    }
+    c->max_yield = static_cast<uint32_t>(std::floor(max_nubar)) + 1;
+    std::vector<double> mtot(T * M * G, 0), mcdf(T * M * G * max_nuc, 0), mnsf(T * M * G, 0);
+    for (size_t t = 0; t < T; t++) {
+      for (size_t mi = 0; mi < M; mi++) {
+        const auto& mt = m.materials[mi];
+        for (size_t g = 0; g < G; g++) {
+          // Material::GetMicroscopicTotal: accumulate afrac * sigma_t
+          double acc = 0, nsf = 0;
+          for (size_t k = 0; k < mt.nuclides.size(); k++) {
+            const size_t i = (t * N + mt.nuclides[k]) * G + g;
+            acc = acc + mt.afrac[k] * total[i];
+            mcdf[((t * M + mi) * G + g) * max_nuc + k] = acc;
+            nsf = nsf + mt.afrac[k] * nusigf[i];
+          }
+          mtot[(t * M + mi) * G + g] = acc;
+          mnsf[(t * M + mi) * G + g] = nsf;
+        }
+      }
+    }
+    UP(total, mg_total)
+    UP(rx, mg_rx_cdf)
+    UP(scat, mg_scat_cdf)
+    UP(nubar, mg_nubar)
+    UP(chi, mg_chi_cdf)
+    UP(nusigf, mg_nusigf)
+    UP(mtot, mat_mg_total)
+    UP(mcdf, mat_mg_nuc_cdf)
+    UP(mnsf, mat_mg_nusigf)
+  }
+
+  // estimators
+  std::vector<int32_t> est_kind, est_target, est_has_cos, est_bin_kind;
+  std::vector<uint64_t> est_offset, est_bound_off;
+  std::vector<double> est_cos_dir, est_bin_par, est_bounds;
+  uint64_t off = 0;
+  for (const auto& e : m.estimators) {
+    est_kind.push_back(e.kind);
+    est_target.push_back(e.kind == mc::kCurrent ? e.surface : e.cell);
+    est_offset.push_back(off);
+    off += e.size();
+    est_has_cos.push_back(e.has_cosine ? 1 : 0);
+    for (double v : e.cosine_dir) est_cos_dir.push_back(v);
+    for (const mc::Bins1D* b : {&e.cosine, &e.energy}) {
+      est_bin_kind.push_back(b->kind);
+      const bool lin = b->kind == mc::kLinspace;
+      const double par[6] = {static_cast<double>(b->n_bins), lin ? b->lower : b->log_lower,
+                             lin ? b->upper : b->log_upper, lin ? b->width : b->log_width, b->base,
+                             static_cast<double>(b->boundaries.size())};
+      est_bin_par.insert(est_bin_par.end(), par, par + 6);
+      est_bound_off.push_back(est_bounds.size());
+      est_bounds.insert(est_bounds.end(), b->boundaries.begin(), b->boundaries.end());
+    }
+  }
+  c->total_bins = off;
+  w.n_est = static_cast<int32_t>(m.estimators.size());
+  UP(est_kind, est_kind)
+  UP(est_target, est_target)
+  UP(est_offset, est_offset)
+  UP(est_has_cos, est_has_cos)
+  UP(est_cos_dir, est_cos_dir)
+  UP(est_bin_kind, est_bin_kind)
+  UP(est_bin_par, est_bin_par)
+  UP(est_bound_off, est_bound_off)
+  UP(est_bounds, est_bounds)
+#undef UP
+
+  for (int i = 0; i < 3; i++) {
+    w.src_pos[i] = m.source.position[i];
+    w.src_dir[i] = m.source.dir[i];
+  }
+  w.src_dir_kind = m.source.direction;
+  w.src_type = m.source.type;
+  w.src_energy = m.energy_mode == mc::kMultigroup ? static_cast<double>(m.source.group) : m.source.energy;
+
+  // run buffers
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(DevCounters)) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc counters");
+  c->world_allocs.push_back(p);
+  c->d_ctr = static_cast<DevCounters*>(p);
+  const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
+  if (cudaMalloc(&p, tb) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc tallies");
+  c->world_allocs.push_back(p);
+  c->d_sum = static_cast<double*>(p);
+  if (cudaMalloc(&p, tb) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc tallies");
+  c->world_allocs.push_back(p);
+  c->d_sq = static_cast<double*>(p);
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+bool check_ctx(mc_ctx* c, bool need_world = true) {
+  if (!c) return false;
+  if (need_world && !c->loaded) {
+    c->err = "no problem loaded (call mc_load_xml first)";
+    return false;
+  }
+  return true;
+}
+
+int pick_block(const mc_run_opts* o) {
+  const int b = o && o->block_size > 0 ? o->block_size : 256;
+  return std::min(256, std::max(32, (b / 32) * 32));
+}
+
+int grid_for(mc_ctx* c, int energy_mode, int rng, int block, bool keig, bool fast) {
+  int per_sm = mcd::history_blocks_per_sm(energy_mode, rng, block, keig, fast);
+  if (per_sm < 1) per_sm = 1;
+  return per_sm * c->num_sms;
+}
+
+unsigned long long run_key(uint64_t seed, uint64_t cycle, uint64_t salt) {
+  return mcd::splitmix64(seed * 0x9E3779B97F4A7C15ull + cycle * 0xD1B54A32D192ED03ull + salt);
+}
+
+// outcome of a run's counters as a status code
+int counters_status(mc_ctx* c, const DevCounters& h) {
+  if (h.lost) {
+    char buf[256];
+    std::snprintf(buf, sizeof buf,
+                  "Point does not belong to any Cell. Please check that all space is either assigned a material "
+                  "or void. (%llu particles lost; last at %.17g %.17g %.17g, cell %lld, history %llu)",
+                  h.lost, h.lost_xyz[0], h.lost_xyz[1], h.lost_xyz[2], static_cast<long long>(h.pad[0]) - 1,
+                  h.pad[1]);
+    return fail(c, MC_ERR_LOST, buf);
+  }
+  if (h.overflow) return fail(c, MC_ERR_OVERFLOW, std::to_string(h.overflow) + " bank/stack/tally overflows");
+  if (h.resample)
+    return fail(c, MC_ERR_RESAMPLE, "Number of thermal scattering resamples exceeded limit: 10 (" +
+                                         std::to_string(h.resample) + " times)");
+  if (h.capped) return fail(c, MC_ERR_EVENT_CAP, std::to_string(h.capped) + " particles reached the event cap");
+  return MC_OK;
+}
+
+// one transport launch over rp.n particles; returns elapsed device ms
+int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms) {
+  CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
+  rp.ctr = c->d_ctr;
+  rp.tally_sum = c->d_sum;
+  rp.tally_sq = c->d_sq;
+  rp.total_bins = c->total_bins;
+  const bool keig = rp.keig != 0;
+  const int grid = grid_for(c, c->model.energy_mode, rng, block, keig, rp.fast != 0);
+  CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+  cudaError_t e;
+  if (c->model.energy_mode == mc::kMultigroup) e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream);
+  else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream);
+  if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
+  c->launches++;
+  CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+  if (ms) {
+    CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+    float f = 0;
+    CUDA_TRY(c, cudaEventElapsedTime(&f, c->ev0, c->ev1));
+    *ms = f;
+  }
+  return MC_OK;
+}
+
+// scan + compact the per-history fission slots; returns the bank size
+int compact_bank(mc_ctx* c, uint64_t n, Site** bank_out, uint64_t* m_out) {
+  auto* slots = static_cast<Site*>(c->scratch[kSlots].p);
+  auto* count = static_cast<uint32_t*>(c->scratch[kCount].p);
+  auto* offsets = static_cast<unsigned long long*>(scratch(c, kOffsets, n * 8));
+  auto* sums = static_cast<unsigned long long*>(scratch(c, kScanSums, ((n + 1023) / 1024 + 1) * 8));
+  auto* total = static_cast<unsigned long long*>(scratch(c, kTotal, 8));
+  auto* bank = static_cast<Site*>(scratch(c, kBank, n * c->max_yield * sizeof(Site)));
+  if (!offsets || !sums || !total || !bank) return fail(c, MC_ERR_OOM, "bank scratch allocation failed");
+  CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
+  CUDA_TRY(c, mcd::launch_bank_compact(slots, count, offsets, n, c->max_yield, bank, c->stream));
+  c->launches += 4;
+  unsigned long long m = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&m, total, 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *bank_out = bank;
+  *m_out = m;
+  return MC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mc_version(void) { return 1; }
+
+int mc_create(mc_ctx** out, int device) {
+  if (!out) return MC_ERR_INPUT;
+  *out = nullptr;
+  auto* c = new (std::nothrow) mc_ctx();
+  if (!c) return MC_ERR_OOM;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return MC_ERR_DEVICE;
+  }
+  c->own_stream = true;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  *out = c;
+  return MC_OK;
+}
+
+void mc_destroy(mc_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_world(c);
+  for (auto& b : c->scratch)
+    if (b.p) cudaFree(b.p);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int mc_last_error(const mc_ctx* c, char* buf, size_t n) {
+  if (!c || !buf || n == 0) return MC_ERR_INPUT;
+  std::strncpy(buf, c->err.c_str(), n - 1);
+  buf[n - 1] = 0;
+  return MC_OK;
+}
+
+int mc_set_stream(mc_ctx* c, void* s) {
+  if (!c) return MC_ERR_INPUT;
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  c->own_stream = false;
+  c->stream = static_cast<cudaStream_t>(s);
+  return MC_OK;
+}
+
+int mc_load_xml(mc_ctx* c, const char* xml_text, const char* base_dir) {
+  if (!c || !xml_text) return MC_ERR_INPUT;
+  cudaSetDevice(c->device);
+  free_world(c);
+  try {
+    c->model = mc::load_model(xml_text, base_dir ? base_dir : "");
+  }
+  catch (const std::exception& e) {
+    return fail(c, MC_ERR_INPUT, e.what());
+  }
+  if (c->model.has_perturbations)
+    return fail(c, MC_ERR_INPUT, "perturbations and sensitivities are not supported by the GPU engine");
+  if (c->model.energy_mode == mc::kContinuous) return fail(c, MC_ERR_INPUT, "continuous-energy data: not yet supported");
+  const int rc = build_world(c);
+  if (rc != MC_OK) {
+    free_world(c);
+    return rc;
+  }
+  c->loaded = true;
+  return MC_OK;
+}
+
+int mc_set_geometry_mode(mc_ctx* c, int32_t mode) {
+  if (!c) return MC_ERR_INPUT;
+  if (mode != MC_GEOMETRY_ROBUST && mode != MC_GEOMETRY_REFERENCE) return fail(c, MC_ERR_INPUT, "unknown geometry mode");
+  c->geometry_mode = mode;
+  c->dw.quirks = mode;
+  return MC_OK;
+}
+
+int mc_problem_info_get(mc_ctx* c, mc_problem_info* out) {
+  if (!check_ctx(c) || !out) return MC_ERR_STATE;
+  const mc::Model& m = c->model;
+  std::memset(out, 0, sizeof *out);
+  out->problem = m.problem;
+  out->energy_mode = m.energy_mode;
+  out->tracking = m.tracking;
+  out->n_cells = static_cast<int32_t>(m.cells.size());
+  out->n_surfaces = static_cast<int32_t>(m.surfaces.size());
+  out->n_materials = static_cast<int32_t>(m.materials.size());
+  out->n_nuclides = static_cast<int32_t>(m.nuclides.size());
+  out->groups = static_cast<int32_t>(m.groups);
+  out->n_estimators = static_cast<int32_t>(m.estimators.size());
+  out->n_tsl = static_cast<int32_t>(m.tsl.size());
+  out->histories = m.histories;
+  out->seed = m.seed;
+  out->inactive = static_cast<uint32_t>(m.inactive);
+  out->active = static_cast<uint32_t>(m.active);
+  out->total_bins = c->total_bins;
+  out->max_yield = c->max_yield;
+  return MC_OK;
+}
+
+int mc_estimator_info_get(mc_ctx* c, int32_t index, mc_estimator_info* out) {
+  if (!check_ctx(c) || !out) return MC_ERR_STATE;
+  if (index < 0 || index >= static_cast<int32_t>(c->model.estimators.size()))
+    return fail(c, MC_ERR_INPUT, "estimator index out of range");
+  std::memset(out, 0, sizeof *out);
+  uint64_t off = 0;
+  for (int32_t i = 0; i < index; i++) off += c->model.estimators[i].size();
+  const auto& e = c->model.estimators[index];
+  std::strncpy(out->name, e.name.c_str(), sizeof(out->name) - 1);
+  out->kind = e.kind;
+  out->target = e.kind == mc::kCurrent ? e.surface : e.cell;
+  out->offset = off;
+  out->n_bins = e.size();
+  out->cosine_bins = e.cosine.size();
+  out->energy_bins = e.energy.size();
+  return MC_OK;
+}
+
+int mc_object_name(mc_ctx* c, int32_t kind, int32_t index, char* buf, size_t n) {
+  if (!check_ctx(c) || !buf || n == 0) return MC_ERR_STATE;
+  const mc::Model& m = c->model;
+  std::string s;
+  try {
+    if (kind == 0) s = m.cells.at(index).name;
+    else if (kind == 1) s = m.surfaces.at(index).name;
+    else if (kind == 2) s = m.materials.at(index).name;
+    else if (kind == 3) s = m.nuclides.at(index).name;
+    else return fail(c, MC_ERR_INPUT, "unknown object kind");
+  }
+  catch (const std::exception&) {
+    return fail(c, MC_ERR_INPUT, "object index out of range");
+  }
+  std::strncpy(buf, s.c_str(), n - 1);
+  buf[n - 1] = 0;
+  return MC_OK;
+}
+
+int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  cudaSetDevice(c->device);
+  const uint64_t n = o && o->histories ? o->histories : c->model.histories;
+  const uint64_t seed = o && o->seed ? o->seed : c->model.seed;
+  const int rng = o ? o->rng : 0;
+  if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
+  const int block = pick_block(o);
+  RunParams rp{};
+  rp.n = n;
+  rp.seed = seed;
+  rp.run_key = run_key(seed, 0, 0x46495845ull);
+  rp.max_events = o && o->max_events ? o->max_events : 1000000u;
+  rp.keig = 0;
+  rp.score = 1;
+  rp.fast = (o && o->fast_math && rng == MC_RNG_PHILOX) ? 1 : 0;
+  rp.from_bank = 0;
+  rp.ref_source_seeds = 1;
+  rp.max_yield = c->max_yield;
+  if (out && out->history_events) {
+    rp.hist_events = static_cast<uint32_t*>(scratch(c, kHistEvents, n * 4));
+    if (!rp.hist_events) return fail(c, MC_ERR_OOM, "history buffer");
+  }
+  if (out && out->history_fate) {
+    rp.hist_fate = static_cast<int8_t*>(scratch(c, kHistFate, n));
+    if (!rp.hist_fate) return fail(c, MC_ERR_OOM, "history buffer");
+  }
+  const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
+  double ms = 0;
+  const uint64_t l0 = c->launches;
+  int rc = run_transport(c, rp, rng, block, &ms);
+  if (rc != MC_OK) return rc;
+  DevCounters h{};
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  if (out) {
+    if (out->sum) CUDA_TRY(c, cudaMemcpyAsync(out->sum, c->d_sum, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (out->sum_sq) CUDA_TRY(c, cudaMemcpyAsync(out->sum_sq, c->d_sq, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (out->history_events)
+      CUDA_TRY(c, cudaMemcpyAsync(out->history_events, rp.hist_events, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (out->history_fate)
+      CUDA_TRY(c, cudaMemcpyAsync(out->history_fate, rp.hist_fate, n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (out) {
+    out->histories = n;
+    out->events = h.events;
+    out->secondaries = h.secondaries;
+    out->lost = h.lost;
+    out->capped = h.capped;
+    out->overflow = h.overflow;
+    out->resample_failures = h.resample;
+    out->transport_ms = ms;
+    out->launches = c->launches - l0;
+  }
+  return counters_status(c, h);
+}
+
+int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  cudaSetDevice(c->device);
+  auto& k = c->keig;
+  k = decltype(c->keig){};
+  k.n = o && o->histories ? o->histories : c->model.histories;
+  k.seed = o && o->seed ? o->seed : c->model.seed;
+  k.inactive = o && (o->inactive || o->active) ? o->inactive : static_cast<uint32_t>(c->model.inactive);
+  k.act = o && (o->inactive || o->active) ? o->active : static_cast<uint32_t>(c->model.active);
+  k.rng = o ? o->rng : 0;
+  k.fast = (o && o->fast_math && k.rng == MC_RNG_PHILOX) ? 1 : 0;
+  k.block = pick_block(o);
+  k.max_events = o && o->max_events ? o->max_events : 1000000u;
+  k.launches0 = c->launches;
+  if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
+  if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
+  if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
+      !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
+    return fail(c, MC_ERR_OOM, "k-eigenvalue bank allocation failed");
+  const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
+  k.active = true;
+  return MC_OK;
+}
+
+int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
+  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
+  auto& k = c->keig;
+  RunParams rp{};
+  rp.n = k.n;
+  rp.seed = k.seed;
+  rp.cycle = k.cycle;
+  rp.run_key = run_key(k.seed, k.cycle, 0x4b454947ull);
+  rp.max_events = k.max_events;
+  rp.keig = 1;
+  rp.score = active ? 1 : 0;
+  rp.fast = k.fast;
+  rp.from_bank = k.cycle > 0 ? 1 : 0;
+  rp.ref_source_seeds = 0;  // cycle 0: Source::Sample(1..N) (src/KEigenvalue.cpp:31-33)
+  rp.minstd_base = k.seed + static_cast<unsigned long long>(k.cycle) * k.n;
+  rp.max_yield = c->max_yield;
+  rp.src = static_cast<const Site*>(c->scratch[kSrc].p);
+  rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
+  rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
+  double ms = 0;
+  int rc = run_transport(c, rp, k.rng, k.block, &ms);
+  if (rc != MC_OK) return rc;
+  k.transport_ms += ms;
+  Site* bank = nullptr;
+  uint64_t m = 0;
+  rc = compact_bank(c, k.n, &bank, &m);
+  if (rc != MC_OK) return rc;
+  DevCounters h{};
+  CUDA_TRY(c, cudaMemcpy(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost));
+  k.events += h.events;
+  k.lost += h.lost;
+  k.capped += h.capped;
+  k.overflow += h.overflow;
+  const double kc = static_cast<double>(m) / static_cast<double>(k.n);
+  k.k.push_back(kc);
+  k.ktl.push_back(h.k_tracklength / static_cast<double>(k.n));
+  k.bank.push_back(m);
+  if (kout) *kout = kc;
+  if (m == 0) return fail(c, MC_ERR_INPUT, "fission bank is empty: the source died out");
+  // next cycle's source
+  CUDA_TRY(c, mcd::launch_resample(bank, static_cast<unsigned long long*>(c->scratch[kTotal].p), k.n,
+                                   run_key(k.seed, k.cycle, 0x52455341ull), static_cast<Site*>(c->scratch[kSrc].p),
+                                   c->stream));
+  c->launches++;
+  k.cycle++;
+  return counters_status(c, h);
+}
+
+int mc_keig_status(mc_ctx* c, mc_keig_out* out) {
+  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
+  auto& k = c->keig;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (out) {
+    const size_t nc = k.k.size();
+    if (out->k_cycle) std::copy(k.k.begin(), k.k.end(), out->k_cycle);
+    if (out->bank_size) std::copy(k.bank.begin(), k.bank.end(), out->bank_size);
+    if (out->sum) CUDA_TRY(c, cudaMemcpy(out->sum, c->d_sum, c->total_bins * 8, cudaMemcpyDeviceToHost));
+    if (out->sum_sq) CUDA_TRY(c, cudaMemcpy(out->sum_sq, c->d_sq, c->total_bins * 8, cudaMemcpyDeviceToHost));
+    double s = 0, s2 = 0, st = 0;
+    size_t na = 0;
+    for (size_t i = k.inactive; i < nc; i++) {
+      s += k.k[i];
+      s2 += k.k[i] * k.k[i];
+      st += k.ktl[i];
+      na++;
+    }
+    out->k_mean = na ? s / na : 0;
+    out->k_std = na > 1 ? std::sqrt(std::max(0.0, (s2 - s * s / na) / (na - 1)) / na) : 0;
+    out->k_tracklength_mean = na ? st / na : 0;
+    out->events = k.events;
+    out->lost = k.lost;
+    out->capped = k.capped;
+    out->overflow = k.overflow;
+    out->transport_ms = k.transport_ms;
+    out->launches = c->launches - k.launches0;
+  }
+  return MC_OK;
+}
+
+int mc_keig_end(mc_ctx* c, mc_keig_out* out) {
+  const int rc = mc_keig_status(c, out);
+  if (rc != MC_OK) return rc;
+  c->keig.active = false;
+  return MC_OK;
+}
+
+int mc_run_keigenvalue(mc_ctx* c, const mc_run_opts* o, mc_keig_out* out) {
+  int rc = mc_keig_begin(c, o);
+  if (rc != MC_OK) return rc;
+  const uint32_t total = c->keig.inactive + c->keig.act;
+  int status = MC_OK;
+  for (uint32_t i = 0; i < total; i++) {
+    rc = mc_keig_cycle(c, i >= c->keig.inactive ? 1 : 0, nullptr);
+    if (rc == MC_ERR_DEVICE || rc == MC_ERR_OOM || rc == MC_ERR_STATE || (rc == MC_ERR_INPUT)) {
+      mc_keig_end(c, out);
+      return rc;
+    }
+    if (rc != MC_OK && status == MC_OK) status = rc;
+  }
+  rc = mc_keig_end(c, out);
+  return rc != MC_OK ? rc : status;
+}
+
+int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, int32_t rng, mc_site* fission_sites, uint64_t cap,
+                      uint64_t* n_out) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n == 0) {
+    if (n_out) *n_out = 0;
+    return MC_OK;
+  }
+  if (!sites) return fail(c, MC_ERR_INPUT, "sites is NULL");
+  cudaSetDevice(c->device);
+  auto* src = static_cast<Site*>(scratch(c, kSrc, n * sizeof(Site)));
+  if (!src || !scratch(c, kSlots, n * c->max_yield * sizeof(Site)) || !scratch(c, kCount, n * 4))
+    return fail(c, MC_ERR_OOM, "bank allocation failed");
+  CUDA_TRY(c, cudaMemcpyAsync(src, sites, n * sizeof(Site), cudaMemcpyHostToDevice, c->stream));
+  RunParams rp{};
+  rp.n = n;
+  rp.seed = c->model.seed;
+  rp.run_key = run_key(c->model.seed, 0, 0x42414e4bull);
+  rp.max_events = 1000000u;
+  rp.keig = 1;
+  rp.score = 1;
+  rp.from_bank = 1;
+  rp.minstd_base = 0;  // each site's own key seeds its stream
+  rp.max_yield = c->max_yield;
+  rp.src = src;
+  rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
+  rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
+  int rc = run_transport(c, rp, rng, 256, nullptr);
+  if (rc != MC_OK) return rc;
+  Site* bank = nullptr;
+  uint64_t m = 0;
+  rc = compact_bank(c, n, &bank, &m);
+  if (rc != MC_OK) return rc;
+  if (fission_sites && cap)
+    CUDA_TRY(c, cudaMemcpyAsync(fission_sites, bank, std::min(m, cap) * sizeof(Site), cudaMemcpyDeviceToHost, c->stream));
+  DevCounters h{};
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (n_out) *n_out = m;
+  if (m > cap) return fail(c, MC_ERR_OVERFLOW, "fission bank larger than the output capacity");
+  return counters_status(c, h);
+}
+
+int mc_tallies_reset(mc_ctx* c) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_tallies_get(mc_ctx* c, double* sum, double* sum_sq) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (sum) CUDA_TRY(c, cudaMemcpyAsync(sum, c->d_sum, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (sum_sq) CUDA_TRY(c, cudaMemcpyAsync(sum_sq, c->d_sq, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+// ---- probes --------------------------------------------------------------
+
+int mc_find_cell(mc_ctx* c, const double* xyz, uint64_t n, int32_t* cell) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n == 0) return MC_OK;
+  if (!xyz || !cell) return fail(c, MC_ERR_INPUT, "null argument");
+  auto* dx = static_cast<double*>(scratch(c, kProbeIn, n * 24));
+  auto* dc = static_cast<int32_t*>(scratch(c, kProbeOut, n * 4));
+  if (!dx || !dc) return fail(c, MC_ERR_OOM, "probe buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(dx, xyz, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_find_cell(c->dw, dx, n, dc, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(cell, dc, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_nearest_surface(mc_ctx* c, const int32_t* cell, const double* xyz, const double* uvw, uint64_t n,
+                       int32_t* surf, double* dist) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n == 0) return MC_OK;
+  if (!cell || !xyz || !uvw || !surf || !dist) return fail(c, MC_ERR_INPUT, "null argument");
+  auto* in = static_cast<char*>(scratch(c, kProbeIn, n * (24 + 24 + 4)));
+  auto* outp = static_cast<char*>(scratch(c, kProbeOut, n * (4 + 8)));
+  if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
+  auto* dxyz = reinterpret_cast<double*>(in);
+  auto* duvw = reinterpret_cast<double*>(in + n * 24);
+  auto* dcell = reinterpret_cast<int32_t*>(in + n * 48);
+  auto* ddist = reinterpret_cast<double*>(outp);
+  auto* dsurf = reinterpret_cast<int32_t*>(outp + n * 8);
+  CUDA_TRY(c, cudaMemcpyAsync(dxyz, xyz, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(duvw, uvw, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dcell, cell, n * 4, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_nearest_surface(c->dw, dcell, dxyz, duvw, n, dsurf, ddist, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(surf, dsurf, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dist, ddist, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_surface_distance(mc_ctx* c, int32_t s, const double* xyz, const double* uvw, uint64_t n, double* dist) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (s < 0 || s >= c->dw.n_surfaces) return fail(c, MC_ERR_INPUT, "surface index out of range");
+  if (n == 0) return MC_OK;
+  if (!xyz || !uvw || !dist) return fail(c, MC_ERR_INPUT, "null argument");
+  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * 48));
+  auto* outp = static_cast<double*>(scratch(c, kProbeOut, n * 8));
+  if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(in, xyz, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(in + 3 * n, uvw, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_surface_distance(c->dw, s, in, in + 3 * n, n, outp, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(dist, outp, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_surface_contains(mc_ctx* c, int32_t s, const double* xyz, uint64_t n, int8_t* contains) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (s < 0 || s >= c->dw.n_surfaces) return fail(c, MC_ERR_INPUT, "surface index out of range");
+  if (n == 0) return MC_OK;
+  if (!xyz || !contains) return fail(c, MC_ERR_INPUT, "null argument");
+  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * 24));
+  auto* outp = static_cast<int8_t*>(scratch(c, kProbeOut, n));
+  if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(in, xyz, n * 24, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_surface_contains(c->dw, s, in, n, outp, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(contains, outp, n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_material_xs(mc_ctx* c, int32_t, const double*, const double*, uint64_t, double*, double*) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  return fail(c, MC_ERR_INPUT, "mc_material_xs: not yet implemented");
+}
+
+int mc_energy_index(mc_ctx* c, int32_t, const double*, uint64_t, int64_t*) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  return fail(c, MC_ERR_INPUT, "mc_energy_index: not yet implemented");
+}
+
+int mc_sample_tsl(mc_ctx* c, int32_t, const double*, const double*, uint64_t, uint64_t, int32_t, double*, double*,
+                  uint64_t*) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  return fail(c, MC_ERR_INPUT, "mc_sample_tsl: not yet implemented");
+}
+
+int mc_tsl_total(mc_ctx* c, int32_t, const double*, const double*, uint64_t, double*) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  return fail(c, MC_ERR_INPUT, "mc_tsl_total: not yet implemented");
+}
+
+}  // extern "C"

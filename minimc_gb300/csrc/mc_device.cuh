@@ -1,0 +1,518 @@
+// Device-side world tables, geometry, random streams and physics.
+//
+// Geometry and anything a parity check compares bit-for-bit is written with
+// explicit round-to-nearest intrinsics (__dadd_rn/__dmul_rn/__ddiv_rn), so
+// the compiler cannot contract a*b+c into an FMA: the reference, built for
+// x86-64 without FMA, rounds every product and sum separately.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+namespace mcd {
+
+// ---------------------------------------------------------------------------
+// constants (src/Constants.hpp)
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kNudge = 10 * 2.220446049250313080847e-16;  // 10 * DBL_EPSILON
+constexpr double kOnAxisTolerance = 0.9;
+constexpr double kBoltzmann = 8.617333262145e-11;
+constexpr double kNeutronMass = 1.045354912280858e-18;
+constexpr int kResampleLimit = 10;
+
+// Particle::Event (src/Particle.hpp:36-44) plus the reflection extension
+enum Event : int32_t {
+  kBirth = 0,
+  kScatter = 1,
+  kCapture = 2,
+  kFission = 3,
+  kSurfaceCross = 4,
+  kLeak = 5,
+  kVirtualCollision = 6,
+  kReflect = 7,
+  kLostEvent = 8,
+};
+
+enum SurfKind : int32_t { kSphere = 0, kPlaneX = 1, kPlaneY = 2, kPlaneZ = 3, kCylX = 4, kCylY = 5, kCylZ = 6 };
+
+// error / counter slots shared by all kernels of a run
+struct DevCounters {
+  unsigned long long next;       // queue head for dynamic history assignment
+  unsigned long long events;
+  unsigned long long secondaries;
+  unsigned long long lost;
+  unsigned long long capped;
+  unsigned long long overflow;
+  unsigned long long resample;
+  unsigned long long banked;     // fission sites banked (k-eigenvalue)
+  double k_tracklength;          // sum of nu*Sigma_f*d over the cycle
+  double lost_xyz[3];
+  unsigned long long pad[4];
+};
+
+// Flattened world, passed to kernels by value.
+struct DevWorld {
+  int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
+  int32_t energy_mode, tracking, quirks, G, max_mat_nuc;
+  // surfaces
+  const int32_t* surf_kind;
+  const int32_t* surf_refl;
+  const double* surf_p;  // [n][4]
+  // cells
+  const int32_t* cell_begin;  // [n_cells+1]
+  const int32_t* cell_surf;
+  const uint8_t* cell_within;
+  const int32_t* cell_mat;
+  const int32_t* cell_field;
+  const double* field;  // [nf][8]: linear, c, g0, g1, g2, b, upper, lower
+  // materials
+  const double* mat_density;
+  const int32_t* mat_begin;
+  const int32_t* mat_nuc;
+  const double* mat_afrac;
+  // multigroup tables, all indexed by particle type first
+  const double* mg_total;     // [T][N][G]
+  const double* mg_rx_cdf;    // [T][N][G][3] running sums capture, scatter, fission
+  const double* mg_scat_cdf;  // [T][N][G][G] running sums over outgoing group
+  const double* mg_nubar;     // [T][N][G]
+  const double* mg_chi_cdf;   // [T][N][G][G]
+  const double* mg_nusigf;    // [T][N][G] nubar * fission (track-length k)
+  const double* mat_mg_total;    // [T][M][G]  Σ afrac * total, reference order
+  const double* mat_mg_nuc_cdf;  // [T][M][G][max_mat_nuc] running sums
+  const double* mat_mg_nusigf;   // [T][M][G]  Σ afrac * nu * sigma_f
+  // estimators
+  int32_t n_est;
+  const int32_t* est_kind;     // 0 current, 1 track length
+  const int32_t* est_target;   // surface or cell
+  const uint64_t* est_offset;  // first bin
+  const int32_t* est_has_cos;
+  const double* est_cos_dir;   // [n_est][3]
+  const int32_t* est_bin_kind; // [n_est][2] cosine, energy
+  const double* est_bin_par;   // [n_est][2][6]: n_bins, lower/log_lower, upper/log_upper, width/log_width, base, nbounds
+  const uint64_t* est_bound_off;  // [n_est][2] offset into est_bounds
+  const double* est_bounds;
+  uint64_t est_stride_dummy;
+  // source (src/Source.cpp)
+  double src_pos[3];
+  double src_dir[3];
+  int32_t src_dir_kind;  // 0 constant, 1 isotropic, 2 isotropic flux
+  int32_t src_type;
+  double src_energy;     // MeV or group
+};
+
+// ---------------------------------------------------------------------------
+// arithmetic without contraction
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// Point::Dot (src/Point.cpp:51-53): (x*rx + y*ry) + z*rz
+__device__ __forceinline__ double dot3(double x, double y, double z, double a, double b, double c) {
+  return dadd(dadd(dmul(x, a), dmul(y, b)), dmul(z, c));
+}
+
+// ---------------------------------------------------------------------------
+// random streams
+
+// std::minstd_rand (a = 48271, m = 2^31 - 1) consumed through the C++
+// standard's generate_canonical<double, 53>: two draws, S = g1' + g2'*R,
+// result S / R^2 with R = 2^31 - 2 and g' = g - 1.
+struct MinstdRng {
+  uint32_t x;
+  __device__ __forceinline__ static uint32_t seed_state(unsigned long long s) {
+    const uint32_t r = static_cast<uint32_t>(s % 2147483647ull);
+    return r == 0 ? 1u : r;
+  }
+  __device__ __forceinline__ void seed(unsigned long long s) { x = seed_state(s); }
+  __device__ __forceinline__ uint32_t next() {
+    x = static_cast<uint32_t>((static_cast<unsigned long long>(x) * 48271ull) % 2147483647ull);
+    return x;
+  }
+  __device__ __forceinline__ double u01() {
+    const double r = 2147483646.0;
+    double sum = static_cast<double>(next() - 1u);
+    sum = dadd(sum, dmul(static_cast<double>(next() - 1u), r));
+    const double tmp = dmul(r, r);
+    double ret = ddiv(sum, tmp);
+    if (ret >= 1.0) ret = 0.99999999999999988898;  // nextafter(1, 0)
+    return ret;
+  }
+  __device__ __forceinline__ float u01f() { return static_cast<float>(u01()); }
+  // key for a child particle: the reference seeds secondaries with rng()
+  __device__ __forceinline__ unsigned long long child_key() { return next(); }
+};
+
+// Philox4x32-10 round function (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11): 10 rounds over a 4x32 counter with a
+// 2x32 key; multipliers and Weyl key increments from that paper.
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const unsigned long long p0 = 0xD2511F53ull * c[0];
+    const unsigned long long p1 = 0xCD9E8D57ull * c[2];
+    const uint32_t hi0 = static_cast<uint32_t>(p0 >> 32), lo0 = static_cast<uint32_t>(p0);
+    const uint32_t hi1 = static_cast<uint32_t>(p1 >> 32), lo1 = static_cast<uint32_t>(p1);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Counter-based stream of one particle: key = the run (seed, cycle), counter
+// = (block index, particle id lo, particle id hi, tag).  Primaries use
+// their history index as id and tag 0; secondaries use 64 bits drawn from
+// their parent and tag 1.
+struct PhiloxRng {
+  uint32_t k0, k1, h0, h1, tag;
+  uint32_t ctr;
+  uint32_t buf[4];
+  int32_t idx;
+  __device__ __forceinline__ void init(unsigned long long run_key, unsigned long long id, uint32_t t) {
+    k0 = static_cast<uint32_t>(run_key);
+    k1 = static_cast<uint32_t>(run_key >> 32);
+    h0 = static_cast<uint32_t>(id);
+    h1 = static_cast<uint32_t>(id >> 32);
+    tag = t;
+    ctr = 0;
+    idx = 4;
+  }
+  __device__ __forceinline__ void refill() {
+    uint32_t c[4] = {ctr++, h0, h1, tag};
+    philox4x32_10(c, k0, k1);
+    buf[0] = c[0];
+    buf[1] = c[1];
+    buf[2] = c[2];
+    buf[3] = c[3];
+    idx = 0;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (idx >= 4) refill();
+    return buf[idx++];
+  }
+  // 53-bit uniform in [0, 1)
+  __device__ __forceinline__ double u01() {
+    const uint32_t a = next() >> 5, b = next() >> 6;
+    return (a * 67108864.0 + b) * (1.0 / 9007199254740992.0);
+  }
+  // 24-bit uniform in (0, 1)
+  __device__ __forceinline__ float u01f() { return (static_cast<float>(next() >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+  __device__ __forceinline__ unsigned long long child_key() {
+    const unsigned long long lo = next();
+    return lo | (static_cast<unsigned long long>(next()) << 32);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// surfaces (src/CSGSurface.cpp)
+
+// CSGSurface::SolveQuadratic (src/CSGSurface.cpp:71-97)
+__device__ __forceinline__ double solve_quadratic(double a, double b, double c) {
+  const double disc = dsub(dmul(b, b), dmul(dmul(4.0, a), c));
+  if (disc <= 0) return CUDART_INF;
+  const double sq = __dsqrt_rn(disc);
+  const double two_a = dmul(2.0, a), two_c = dmul(2.0, c);
+  const double lesser = b > 0 ? ddiv(dsub(-b, sq), two_a) : ddiv(two_c, dadd(-b, sq));
+  const double greater = b > 0 ? ddiv(two_c, dsub(-b, sq)) : ddiv(dadd(-b, sq), two_a);
+  if (lesser > 0) return lesser;
+  if (greater > 0) return greater;
+  return CUDART_INF;
+}
+
+// Distance to the cylinder r^2 = |p|^2 - (p.w)^2 about a coordinate axis.
+// (CylinderX::Distance, src/CSGSurface.cpp:148-162; y/z axes by symmetry)
+__device__ __forceinline__ double cylinder_distance(double px, double py, double pz, double dx, double dy, double dz,
+                                                    int axis, double r) {
+  const double pp = dot3(px, py, pz, px, py, pz);
+  const double ax = axis == 0, ay = axis == 1, az = axis == 2;
+  const double pw = dot3(px, py, pz, ax, ay, az);
+  const double dw = dot3(dx, dy, dz, ax, ay, az);
+  const double pd = dot3(px, py, pz, dx, dy, dz);
+  return solve_quadratic(dsub(1.0, dmul(dw, dw)), dmul(2.0, dsub(pd, dmul(pw, dw))),
+                         dsub(dsub(pp, dmul(pw, pw)), dmul(r, r)));
+}
+
+__device__ __forceinline__ double plane_distance(double pos, double dir, double c) {
+  // PlaneX::Distance (src/CSGSurface.cpp:125-134): v = c - p.x, d = v / u
+  const double d = ddiv(dsub(c, pos), dir);
+  return d > 0 ? d : CUDART_INF;
+}
+
+__device__ __forceinline__ double surface_distance(const DevWorld& w, int s, double x, double y, double z, double u,
+                                                   double v, double ww) {
+  const double* p = w.surf_p + 4 * s;
+  switch (__ldg(w.surf_kind + s)) {
+  case kPlaneX: return plane_distance(x, u, __ldg(p));
+  case kPlaneY: return plane_distance(y, v, __ldg(p));
+  case kPlaneZ: return plane_distance(z, ww, __ldg(p));
+  case kSphere: {
+    // Sphere::Distance (src/CSGSurface.cpp:107-111)
+    const double ox = dsub(x, __ldg(p)), oy = dsub(y, __ldg(p + 1)), oz = dsub(z, __ldg(p + 2));
+    const double r = __ldg(p + 3);
+    return solve_quadratic(1.0, dmul(2.0, dot3(ox, oy, oz, u, v, ww)), dsub(dot3(ox, oy, oz, ox, oy, oz), dmul(r, r)));
+  }
+  case kCylX: return cylinder_distance(x, y, z, u, v, ww, 0, __ldg(p));
+  case kCylY: return cylinder_distance(x, y, z, u, v, ww, 1, __ldg(p));
+  default: return cylinder_distance(x, y, z, u, v, ww, 2, __ldg(p));
+  }
+}
+
+// CSGSurface::Contains: true on the negative side; on-surface is positive.
+__device__ __forceinline__ bool surface_contains(const DevWorld& w, int s, double x, double y, double z) {
+  const double* p = w.surf_p + 4 * s;
+  switch (__ldg(w.surf_kind + s)) {
+  case kPlaneX: return x < __ldg(p);
+  case kPlaneY: return y < __ldg(p);
+  case kPlaneZ: return z < __ldg(p);
+  case kSphere: {
+    const double ox = dsub(x, __ldg(p)), oy = dsub(y, __ldg(p + 1)), oz = dsub(z, __ldg(p + 2));
+    const double r = __ldg(p + 3);
+    return dot3(ox, oy, oz, ox, oy, oz) < dmul(r, r);
+  }
+  default: {
+    const int axis = __ldg(w.surf_kind + s) - kCylX;
+    const double pp = dot3(x, y, z, x, y, z);
+    const double pw = dot3(x, y, z, axis == 0, axis == 1, axis == 2);
+    const double r = __ldg(p);
+    const double rho2 = dsub(pp, dmul(pw, pw));
+    // CylinderX::Contains (src/CSGSurface.cpp:164-174) compares sqrt(rho^2)
+    // with r^2; quirks=1 keeps that, quirks=0 compares rho^2 with r^2.
+    return w.quirks ? __dsqrt_rn(rho2) < dmul(r, r) : rho2 < dmul(r, r);
+  }
+  }
+}
+
+// Cell::Contains (src/Cell.cpp:27-35)
+__device__ __forceinline__ bool cell_contains(const DevWorld& w, int c, double x, double y, double z) {
+  const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
+  for (int k = b; k < e; k++) {
+    const bool inside = surface_contains(w, __ldg(w.cell_surf + k), x, y, z);
+    if (inside != (__ldg(w.cell_within + k) != 0)) return false;
+  }
+  return true;
+}
+
+// World::FindCellContaining (src/World.cpp:26-37): first match in XML order
+__device__ __forceinline__ int find_cell(const DevWorld& w, double x, double y, double z) {
+  for (int c = 0; c < w.n_cells; c++)
+    if (cell_contains(w, c, x, y, z)) return c;
+  return -1;
+}
+
+// Cell::NearestSurface (src/Cell.cpp:37-51): first surface (in the cell's
+// surface order) with the least distance.  `skip` (robust crossing, see
+// below) is a surface the particle has just left and is moving away from;
+// it is treated as infinitely far.
+__device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
+                                               double v, double ww, double& dist, int skip = -1) {
+  const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
+  int best = -1;
+  double bd = CUDART_INF;
+  for (int k = b; k < e; k++) {
+    const int s = __ldg(w.cell_surf + k);
+    const double d = s == skip ? CUDART_INF : surface_distance(w, s, x, y, z, u, v, ww);
+    if (best < 0 || d < bd) {
+      best = s;
+      bd = d;
+    }
+  }
+  dist = bd;
+  return best;
+}
+
+// Robust crossing.  The reference relocates a particle after a crossing by
+// moving it a fixed 10*DBL_EPSILON cm past the surface and testing the point
+// (src/TransportMethod.cpp:68-72).  Where a coordinate's ulp exceeds that
+// nudge times the direction component, the point stays on (or before) the
+// surface, the particle is put back into the cell it was leaving, and the
+// surface then reads as infinitely far, so the particle can leave the
+// geometry without ever crossing.  In robust mode the crossed surface's side
+// is taken from the direction of travel instead of the point test, and the
+// surface is skipped until the next collision.
+
+// true if moving along (u,v,w) at (x,y,z) goes to the positive side of s
+__device__ __forceinline__ bool moving_positive(const DevWorld& w, int s, double x, double y, double z, double u,
+                                                double v, double ww) {
+  const double* p = w.surf_p + 4 * s;
+  switch (__ldg(w.surf_kind + s)) {
+  case kPlaneX: return u > 0;
+  case kPlaneY: return v > 0;
+  case kPlaneZ: return ww > 0;
+  case kSphere: return dot3(dsub(x, __ldg(p)), dsub(y, __ldg(p + 1)), dsub(z, __ldg(p + 2)), u, v, ww) > 0;
+  case kCylX: return dadd(dmul(y, v), dmul(z, ww)) > 0;
+  case kCylY: return dadd(dmul(x, u), dmul(z, ww)) > 0;
+  default: return dadd(dmul(x, u), dmul(y, v)) > 0;
+  }
+}
+
+// World::FindCellContaining with the crossed surface's side forced
+__device__ __forceinline__ int find_cell_crossing(const DevWorld& w, double x, double y, double z, int crossed,
+                                                  bool to_positive) {
+  for (int c = 0; c < w.n_cells; c++) {
+    const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
+    bool in = true;
+    for (int k = b; k < e && in; k++) {
+      const int s = __ldg(w.cell_surf + k);
+      const bool inside = s == crossed ? !to_positive : surface_contains(w, s, x, y, z);
+      in = inside == (__ldg(w.cell_within + k) != 0);
+    }
+    if (in) return c;
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// directions (src/Point.cpp:90-121)
+
+// Direction(RNG&): mu = U(-1, 1), phi = U(0, 2 pi)
+template <class Rng>
+__device__ __forceinline__ void isotropic(Rng& rng, double& u, double& v, double& w) {
+  u = dadd(dmul(rng.u01(), 2.0), -1.0);
+  const double st = __dsqrt_rn(dsub(1.0, dmul(u, u)));
+  const double phi = dadd(dmul(rng.u01(), 2 * kPi), 0.0);
+  double s, c;
+  sincos(phi, &s, &c);
+  v = dmul(st, c);
+  w = dmul(st, s);
+}
+
+// isotropic direction with FP32 trigonometry, renormalized in FP64 by one
+// Newton step (fast-math streams only)
+template <class Rng>
+__device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, double& w) {
+  const float mu = 2.0f * rng.u01f() - 1.0f;
+  float s, c;
+  sincospif(2.0f * rng.u01f(), &s, &c);
+  const float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+  u = mu;
+  v = st * c;
+  w = st * s;
+  const double n2 = u * u + v * v + w * w;
+  const double f = 1.5 - 0.5 * n2;
+  u *= f;
+  v *= f;
+  w *= f;
+}
+
+// Direction(d, mu, phi) (src/Point.cpp:98-121), normalized on assignment
+__device__ __forceinline__ void rotate(double& dx, double& dy, double& dz, double mu, double phi) {
+  const bool off_x = dx <= kOnAxisTolerance && dx > -kOnAxisTolerance;
+  const double ax = off_x ? 1.0 : 0.0, ay = off_x ? 0.0 : 1.0, az = 0.0;
+  // u = normalize(d x axis)
+  double ux = dsub(dmul(dy, az), dmul(dz, ay));
+  double uy = dsub(dmul(dz, ax), dmul(dx, az));
+  double uz = dsub(dmul(dx, ay), dmul(dy, ax));
+  double n = __dsqrt_rn(dot3(ux, uy, uz, ux, uy, uz));
+  ux = ddiv(ux, n);
+  uy = ddiv(uy, n);
+  uz = ddiv(uz, n);
+  // v = normalize(d x u)
+  double vx = dsub(dmul(dy, uz), dmul(dz, uy));
+  double vy = dsub(dmul(dz, ux), dmul(dx, uz));
+  double vz = dsub(dmul(dx, uy), dmul(dy, ux));
+  n = __dsqrt_rn(dot3(vx, vy, vz, vx, vy, vz));
+  vx = ddiv(vx, n);
+  vy = ddiv(vy, n);
+  vz = ddiv(vz, n);
+  const double smu = __dsqrt_rn(dsub(1.0, dmul(mu, mu)));
+  double sp, cp;
+  sincos(phi, &sp, &cp);
+  const double a = dmul(smu, cp), bb = dmul(smu, sp);
+  double rx = dadd(dadd(dmul(a, ux), dmul(bb, vx)), dmul(mu, dx));
+  double ry = dadd(dadd(dmul(a, uy), dmul(bb, vy)), dmul(mu, dy));
+  double rz = dadd(dadd(dmul(a, uz), dmul(bb, vz)), dmul(mu, dz));
+  n = __dsqrt_rn(dot3(rx, ry, rz, rx, ry, rz));
+  dx = ddiv(rx, n);
+  dy = ddiv(ry, n);
+  dz = ddiv(rz, n);
+}
+
+// ---------------------------------------------------------------------------
+// bins (src/Bins.cpp)
+__device__ __forceinline__ uint64_t bin_index(const DevWorld& w, int e, int dim, double val) {
+  const int kind = __ldg(w.est_bin_kind + 2 * e + dim);
+  const double* par = w.est_bin_par + (2 * e + dim) * 6;
+  if (kind == 1) {  // linspace
+    const double lo = __ldg(par + 1), hi = __ldg(par + 2), width = __ldg(par + 3);
+    const uint64_t nb = static_cast<uint64_t>(__ldg(par));
+    if (val < lo) return 0;
+    if (val >= hi) return nb - 1;
+    return static_cast<uint64_t>(dadd(ddiv(dsub(val, lo), width), 1.0));
+  }
+  if (kind == 2) {  // logspace
+    const double lo = __ldg(par + 1), hi = __ldg(par + 2), width = __ldg(par + 3), base = __ldg(par + 4);
+    const uint64_t nb = static_cast<uint64_t>(__ldg(par));
+    const double lv = ddiv(log(val), log(base));
+    if (lv < lo) return 0;
+    if (lv >= hi) return nb - 1;
+    return static_cast<uint64_t>(dadd(ddiv(dsub(lv, lo), width), 1.0));
+  }
+  if (kind == 3) {  // boundaries: upper_bound
+    const double* bnd = w.est_bounds + __ldg(w.est_bound_off + 2 * e + dim);
+    uint64_t lo = 0, n = static_cast<uint64_t>(__ldg(par + 5));
+    while (n > 0) {
+      const uint64_t half = n >> 1;
+      if (!(val < __ldg(bnd + lo + half))) {
+        lo += half + 1;
+        n -= half + 1;
+      }
+      else {
+        n = half;
+      }
+    }
+    return lo;
+  }
+  return 0;
+}
+
+// ParticleBins::GetIndex (src/Bins.cpp:196-204)
+__device__ __forceinline__ uint64_t particle_bin(const DevWorld& w, int e, double u, double v, double ww,
+                                                 double energy) {
+  uint64_t ci = 0;
+  if (__ldg(w.est_has_cos + e)) {
+    const double* d = w.est_cos_dir + 3 * e;
+    ci = bin_index(w, e, 0, dot3(__ldg(d), __ldg(d + 1), __ldg(d + 2), u, v, ww));
+  }
+  const uint64_t ei = bin_index(w, e, 1, energy);
+  const double* epar = w.est_bin_par + (2 * e + 1) * 6;
+  const int ek = __ldg(w.est_bin_kind + 2 * e + 1);
+  const uint64_t esize = ek == 0 ? 1 : (ek == 3 ? static_cast<uint64_t>(__ldg(epar + 5)) + 1 : static_cast<uint64_t>(__ldg(epar)));
+  return esize * ci + ei;
+}
+
+// Per-history pending scores (ScorableProxy::pending_scores,
+// src/Scorable.hpp:82-86): a short list of (bin, score).
+template <int N>
+struct Pending {
+  uint32_t bin[N];
+  double score[N];
+  int n;
+  bool overflow;
+  __device__ __forceinline__ void clear() {
+    n = 0;
+    overflow = false;
+  }
+  __device__ __forceinline__ void add(uint32_t b, double s) {
+    for (int i = 0; i < n; i++) {
+      if (bin[i] == b) {
+        score[i] += s;
+        return;
+      }
+    }
+    if (n < N) {
+      bin[n] = b;
+      score[n] = s;
+      n++;
+    }
+    else {
+      overflow = true;
+    }
+  }
+};
+
+}  // namespace mcd

@@ -1,0 +1,71 @@
+// Kernel launch interface shared by the transport kernels and the C ABI.
+#pragma once
+
+#include "mc_device.cuh"
+
+namespace mcd {
+
+// mc_site layout (include/minimc_gb300.h)
+struct Site {
+  double x, y, z, u, v, w, energy;
+  unsigned long long key;
+};
+
+struct RunParams {
+  unsigned long long n;        // source particles (histories)
+  unsigned long long seed;     // run seed
+  unsigned long long run_key;  // Philox key of this run/cycle
+  unsigned long long minstd_base;  // k-eigenvalue: minstd seed of source 0 of the cycle
+  uint32_t cycle;
+  uint32_t max_events;
+  int32_t keig;        // 1: bank fission sites and end the history
+  int32_t score;       // 1: accumulate estimator scores
+  int32_t fast;        // 1: FP32 sampling arithmetic
+  int32_t from_bank;   // 1: particles come from src[]; 0: sampled from Source
+  int32_t ref_source_seeds;  // 1: source i uses Source::Sample(seed + i)
+  uint32_t max_yield;
+  const Site* src;
+  Site* bank;          // k-eigenvalue: [n * max_yield] per-history slots
+  uint32_t* bank_count;  // [n]
+  double* tally_sum;
+  double* tally_sq;
+  unsigned long long total_bins;
+  uint32_t* hist_events;
+  int8_t* hist_fate;
+  DevCounters* ctr;
+};
+
+// launches (mc_transport.cu)
+cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
+                              cudaStream_t stream);
+cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
+                              cudaStream_t stream);
+int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast);
+
+// bank compaction and resampling (mc_transport.cu)
+cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
+                             unsigned long long* scratch_sums, unsigned long long* total, cudaStream_t stream);
+cudaError_t launch_bank_compact(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
+                                unsigned long long n, uint32_t max_yield, Site* out, cudaStream_t stream);
+cudaError_t launch_resample(const Site* bank, const unsigned long long* total, unsigned long long n,
+                            unsigned long long key, Site* next, cudaStream_t stream);
+
+// parity probes (mc_probe.cu)
+cudaError_t launch_find_cell(const DevWorld& w, const double* xyz, unsigned long long n, int32_t* cell,
+                             cudaStream_t stream);
+cudaError_t launch_nearest_surface(const DevWorld& w, const int32_t* cell, const double* xyz, const double* uvw,
+                                   unsigned long long n, int32_t* surf, double* dist, cudaStream_t stream);
+cudaError_t launch_surface_distance(const DevWorld& w, int32_t s, const double* xyz, const double* uvw,
+                                    unsigned long long n, double* dist, cudaStream_t stream);
+cudaError_t launch_surface_contains(const DevWorld& w, int32_t s, const double* xyz, unsigned long long n,
+                                    int8_t* out, cudaStream_t stream);
+
+// Philox helper shared with the host-side resampler description
+__host__ __device__ inline unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace mcd

@@ -1,0 +1,79 @@
+// Deterministic geometry kernels exposed through the C ABI so that parity
+// tests can compare them bit-for-bit with the CPU oracle:
+// World::FindCellContaining, Cell::NearestSurface, CSGSurface::Distance and
+// CSGSurface::Contains, one query per thread.
+#include "mc_kernels.cuh"
+
+namespace mcd {
+
+namespace {
+
+__global__ void k_find_cell(const DevWorld w, const double* xyz, unsigned long long n, int32_t* cell) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cell[i] = find_cell(w, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+}
+
+__global__ void k_nearest_surface(const DevWorld w, const int32_t* cell, const double* xyz, const double* uvw,
+                                  unsigned long long n, int32_t* surf, double* dist) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell[i];
+  if (c < 0 || c >= w.n_cells) {
+    surf[i] = -1;
+    dist[i] = CUDART_INF;
+    return;
+  }
+  double d;
+  surf[i] = nearest_surface(w, c, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], uvw[3 * i], uvw[3 * i + 1],
+                            uvw[3 * i + 2], d);
+  dist[i] = d;
+}
+
+__global__ void k_surface_distance(const DevWorld w, int32_t s, const double* xyz, const double* uvw,
+                                   unsigned long long n, double* dist) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dist[i] = surface_distance(w, s, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], uvw[3 * i], uvw[3 * i + 1],
+                             uvw[3 * i + 2]);
+}
+
+__global__ void k_surface_contains(const DevWorld w, int32_t s, const double* xyz, unsigned long long n, int8_t* out) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = surface_contains(w, s, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) ? 1 : 0;
+}
+
+unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
+
+}  // namespace
+
+cudaError_t launch_find_cell(const DevWorld& w, const double* xyz, unsigned long long n, int32_t* cell,
+                             cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_find_cell<<<blocks_for(n), 256, 0, stream>>>(w, xyz, n, cell);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nearest_surface(const DevWorld& w, const int32_t* cell, const double* xyz, const double* uvw,
+                                   unsigned long long n, int32_t* surf, double* dist, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_nearest_surface<<<blocks_for(n), 256, 0, stream>>>(w, cell, xyz, uvw, n, surf, dist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_surface_distance(const DevWorld& w, int32_t s, const double* xyz, const double* uvw,
+                                    unsigned long long n, double* dist, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_surface_distance<<<blocks_for(n), 256, 0, stream>>>(w, s, xyz, uvw, n, dist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_surface_contains(const DevWorld& w, int32_t s, const double* xyz, unsigned long long n,
+                                    int8_t* out, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_surface_contains<<<blocks_for(n), 256, 0, stream>>>(w, s, xyz, n, out);
+  return cudaGetLastError();
+}
+
+}  // namespace mcd

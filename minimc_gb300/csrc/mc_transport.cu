@@ -1,0 +1,651 @@
+// Transport kernels: the particle-history loop of
+//   FixedSource::StartWorker (src/FixedSource.cpp:40-77)
+//   -> Particle::Transport -> SurfaceTracking / CellDeltaTracking::Transport
+//      (src/TransportMethod.cpp:52-127)
+// recast for the GPU.
+//
+// History schedule ("fused"): a persistent grid, one particle per thread.
+// Every loop trip each live lane performs exactly one event; lanes whose
+// history ended take the next history index from a global queue with one
+// atomic per warp, so warps stay full until the queue drains.  Particle
+// state lives in registers; HBM traffic is the source bank, the fission bank
+// and the tallies.
+#include "mc_kernels.cuh"
+
+#include <type_traits>
+
+namespace mcd {
+
+namespace {
+
+constexpr int kStack = 32;    // fixed-source secondaries per history in flight
+constexpr int kPending = 24;  // distinct tally bins per history
+
+template <class Rng>
+struct Particle {
+  double x, y, z, u, v, w;
+  int g;          // multigroup group, 0-based
+  double E;       // continuous energy, MeV
+  int cell;
+  int surf;       // last surface crossed (current estimator)
+  int skip;       // robust crossing: surface just left, ignored until the next collision
+  int event;
+  int type;
+  uint32_t nev;
+  Rng rng;
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// start a particle from the problem's Source (src/Source.cpp:143-154)
+template <class Rng>
+__device__ __forceinline__ void sample_source(const DevWorld& w, const RunParams& rp, unsigned long long i,
+                                              Particle<Rng>& p) {
+  p.x = w.src_pos[0];
+  p.y = w.src_pos[1];
+  p.z = w.src_pos[2];
+  p.type = w.src_type;
+  if constexpr (std::is_same_v<Rng, MinstdRng>) {
+    // Source::Sample(seed): a fresh RNG{seed} samples position, direction,
+    // energy and type in that order, then the particle is seeded with rng()
+    MinstdRng s;
+    s.seed(rp.ref_source_seeds ? rp.seed + i : i + 1);
+    if (w.src_dir_kind == 0) {
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+    }
+    else if (w.src_dir_kind == 1) {
+      isotropic(s, p.u, p.v, p.w);
+    }
+    else {
+      // IsotropicFlux::Sample (src/Source.cpp:113-120)
+      const double mu = __dsqrt_rn(s.u01());
+      const double phi = dadd(dmul(s.u01(), 2 * kPi), 0.0);
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+      rotate(p.u, p.v, p.w, mu, phi);
+    }
+    p.rng.seed(s.next());
+  }
+  else {
+    p.rng.init(rp.run_key, i, 0);
+    if (w.src_dir_kind == 0) {
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+    }
+    else if (w.src_dir_kind == 1) {
+      if (rp.fast) isotropic_fast(p.rng, p.u, p.v, p.w);
+      else isotropic(p.rng, p.u, p.v, p.w);
+    }
+    else {
+      const double mu = sqrt(p.rng.u01());
+      const double phi = 2 * kPi * p.rng.u01();
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+      rotate(p.u, p.v, p.w, mu, phi);
+    }
+  }
+  if (w.energy_mode == 0) p.g = static_cast<int>(w.src_energy) - 1;
+  else p.E = w.src_energy;
+}
+
+template <class Rng>
+__device__ __forceinline__ void start_from_site(const RunParams& rp, unsigned long long i, const Site& s,
+                                                Particle<Rng>& p, int energy_mode) {
+  p.x = s.x;
+  p.y = s.y;
+  p.z = s.z;
+  p.u = s.u;
+  p.v = s.v;
+  p.w = s.w;
+  if (energy_mode == 0) p.g = static_cast<int>(s.energy) - 1;
+  else p.E = s.energy;
+  p.type = 0;
+  if constexpr (std::is_same_v<Rng, MinstdRng>) {
+    // k-eigenvalue sources: particle i of a cycle is seeded with base + i;
+    // mc_transport_bank passes the site's own key
+    p.rng.seed(rp.minstd_base ? rp.minstd_base + i : s.key);
+  }
+  else {
+    if (rp.minstd_base) p.rng.init(rp.run_key, i, 0);
+    else p.rng.init(rp.run_key, s.key, 1);
+  }
+}
+
+template <class Rng>
+__device__ __forceinline__ double uniform(Rng& rng, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return static_cast<double>(rng.u01f());
+  }
+  return rng.u01();
+}
+
+// exponential_distribution{sigma}: -log(1 - U) / sigma
+template <class Rng>
+__device__ __forceinline__ double sample_flight(Rng& rng, double sigma, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return static_cast<double>(-__logf(rng.u01f()) / static_cast<float>(sigma));
+  }
+  return ddiv(-log(dsub(1.0, rng.u01())), sigma);
+}
+
+template <class Rng>
+__device__ __forceinline__ void sample_isotropic(Rng& rng, double& u, double& v, double& w, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) {
+      isotropic_fast(rng, u, v, w);
+      return;
+    }
+  }
+  isotropic(rng, u, v, w);
+}
+
+// first index k in [0, n) with cdf[k] > threshold, or -1
+__device__ __forceinline__ int cdf_search(const double* cdf, int n, int stride, double threshold) {
+  for (int k = 0; k < n; k++)
+    if (__ldg(cdf + k * stride) > threshold) return k;
+  return -1;
+}
+
+// score helpers -----------------------------------------------------------
+
+template <class Rng>
+__device__ __forceinline__ double energy_value(const DevWorld& w, const Particle<Rng>& p) {
+  // ParticleBins::VisitEnergy: group number or energy
+  return w.energy_mode == 0 ? static_cast<double>(p.g + 1) : p.E;
+}
+
+// EstimatorSetProxy::Score (src/Estimator.cpp:247-251) for the current
+// estimator (src/Estimator.cpp:142-151): 1 on a crossing of its surface
+template <class Rng>
+__device__ __forceinline__ void score_event(const DevWorld& w, const Particle<Rng>& p, Pending<kPending>& pend) {
+  if (p.event != kSurfaceCross && p.event != kLeak) return;
+  for (int e = 0; e < w.n_est; e++) {
+    if (__ldg(w.est_kind + e) != 0 || __ldg(w.est_target + e) != p.surf) continue;
+    const uint64_t b = __ldg(w.est_offset + e) + particle_bin(w, e, p.u, p.v, p.w, energy_value(w, p));
+    pend.add(static_cast<uint32_t>(b), 1.0);
+  }
+}
+
+// track-length estimator (extension): flight length inside the cell
+template <class Rng>
+__device__ __forceinline__ void score_track(const DevWorld& w, const Particle<Rng>& p, double d,
+                                            Pending<kPending>& pend) {
+  for (int e = 0; e < w.n_est; e++) {
+    if (__ldg(w.est_kind + e) != 1 || __ldg(w.est_target + e) != p.cell) continue;
+    const uint64_t b = __ldg(w.est_offset + e) + particle_bin(w, e, p.u, p.v, p.w, energy_value(w, p));
+    pend.add(static_cast<uint32_t>(b), d);
+  }
+}
+
+__device__ __forceinline__ void stream(double& x, double& y, double& z, double u, double v, double w, double d) {
+  // Particle::Stream (src/Particle.cpp:46-53): position += direction * d
+  x = dadd(x, dmul(u, d));
+  y = dadd(y, dmul(v, d));
+  z = dadd(z, dmul(w, d));
+}
+
+// block-shared tally cache for problems with few bins
+constexpr int kSharedBins = 512;
+
+struct TallySink {
+  double* ssum;  // shared or nullptr
+  double* ssq;
+  double* gsum;
+  double* gsq;
+  __device__ __forceinline__ void commit(const Pending<kPending>& pend) {
+    for (int i = 0; i < pend.n; i++) {
+      const double s = pend.score[i];
+      const uint32_t b = pend.bin[i];
+      if (ssum) {
+        atomicAdd(ssum + b, s);
+        atomicAdd(ssq + b, s * s);
+      }
+      else {
+        atomicAdd(gsum + b, s);
+        atomicAdd(gsq + b, s * s);
+      }
+    }
+  }
+};
+
+// fission: Multigroup::Fission (src/Multigroup.cpp:267-286).  The number of
+// secondaries is floor(nubar + U); each draws its group from chi (incident
+// group column) and an isotropic direction, then is seeded with rng()
+// (Particle::BankSecondaries, src/Particle.cpp:96-100).
+template <class Rng, class Emit>
+__device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, int t, int nuc, bool fast,
+                                           Emit&& emit) {
+  const int G = w.G;
+  const size_t base = (static_cast<size_t>(t) * w.n_nuclides + nuc) * G;
+  const double nubar = __ldg(w.mg_nubar + base + p.g);
+  const unsigned yield = static_cast<unsigned>(dadd(nubar, uniform(p.rng, fast)));
+  const double* chi = w.mg_chi_cdf + (base + p.g) * G;
+  for (unsigned i = 0; i < yield; i++) {
+    const double thr = uniform(p.rng, fast);
+    const int go = cdf_search(chi, G, 1, thr);
+    if (go < 0) continue;
+    Site s;
+    sample_isotropic(p.rng, s.u, s.v, s.w, fast);
+    s.x = p.x;
+    s.y = p.y;
+    s.z = p.z;
+    s.energy = static_cast<double>(go + 1);
+    s.key = p.rng.child_key();
+    emit(s);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// multigroup history kernel
+template <class Rng, bool KEIG>
+__global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunParams rp) {
+  extern __shared__ double smem[];
+  const bool use_smem = rp.total_bins <= kSharedBins && rp.score;
+  TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
+  if (use_smem) {
+    for (int i = threadIdx.x; i < 2 * kSharedBins; i += blockDim.x) smem[i] = 0;
+    __syncthreads();
+  }
+  const unsigned lane = lane_id();
+  const bool fast = rp.fast != 0;
+  Particle<Rng> p;
+  Pending<kPending> pend;
+  pend.clear();
+  Site stack[KEIG ? 1 : kStack];
+  int sp = 0;
+  bool alive = false, done = false;
+  unsigned long long hist = 0;
+  unsigned long long my_events = 0, my_lost = 0, my_capped = 0, my_overflow = 0, my_sec = 0;
+  double my_ktl = 0;
+  uint32_t hist_nev = 0;
+  int8_t fate = 0;
+  uint32_t nbank = 0;
+
+  // history complete: ScorableProxy::CommitHistory (src/Scorable.cpp:101-106)
+  auto finish_history = [&]() {
+    if (rp.score) {
+      sink.commit(pend);
+      if (pend.overflow) my_overflow++;
+    }
+    pend.clear();
+    if constexpr (KEIG) rp.bank_count[hist] = nbank;
+    if (rp.hist_events) rp.hist_events[hist] = hist_nev;
+    if (rp.hist_fate) rp.hist_fate[hist] = fate;
+  };
+
+  for (;;) {
+    // ---- refill: lanes without a live particle take the next history
+    const bool want = !alive && !done;
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (mask) {
+      const int leader = __ffs(mask) - 1;
+      unsigned long long base = 0;
+      if (lane == static_cast<unsigned>(leader)) base = atomicAdd(&rp.ctr->next, static_cast<unsigned long long>(__popc(mask)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (want) {
+        hist = base + __popc(mask & ((1u << lane) - 1u));
+        if (hist >= rp.n) {
+          done = true;
+        }
+        else {
+          if (rp.from_bank) start_from_site(rp, hist, rp.src[hist], p, 0);
+          else sample_source(w, rp, hist, p);
+          p.cell = find_cell(w, p.x, p.y, p.z);
+          p.event = kBirth;
+          p.surf = -1;
+          p.skip = -1;
+          p.nev = 0;
+          hist_nev = 0;
+          fate = kBirth;
+          nbank = 0;
+          alive = true;
+          if (p.cell < 0 || __ldg(w.cell_mat + p.cell) < 0) {
+            // the reference throws (src/World.cpp:34-36) or dereferences a
+            // void material; the GPU counts the particle as lost
+            alive = false;
+            my_lost++;
+            p.event = kLostEvent;
+            fate = kLostEvent;
+            rp.ctr->lost_xyz[0] = p.x;
+            rp.ctr->lost_xyz[1] = p.y;
+            rp.ctr->lost_xyz[2] = p.z;
+            rp.ctr->pad[0] = static_cast<unsigned long long>(p.cell + 1);
+            rp.ctr->pad[1] = hist;
+            finish_history();
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+
+    if (alive) {
+      // ---- one event (SurfaceTracking::Transport body, src/TransportMethod.cpp:56-75)
+      const int t = p.type;
+      const int m = __ldg(w.cell_mat + p.cell);
+      const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * w.G + p.g;
+      const double micro = __ldg(w.mat_mg_total + mg);
+      const double sigma = dmul(__ldg(w.mat_density + m), micro);
+      const double dcol = sample_flight(p.rng, sigma, fast);
+      double dsurf;
+      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
+      const bool delta = w.tracking == 1;
+      const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
+      if (collide) {
+        if (rp.score) score_track(w, p, dcol, pend);
+        if (KEIG) my_ktl += dcol * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+        stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
+        p.skip = -1;
+        // multigroup majorant == total, so CellDeltaTracking's rejection
+        // (src/TransportMethod.cpp:106-108) always accepts; it still draws
+        if (delta) (void)uniform(p.rng, fast);
+        // Particle::SampleNuclide (src/Particle.cpp:110-124)
+        const double thr_n = dmul(micro, uniform(p.rng, fast));
+        const double* ncdf = w.mat_mg_nuc_cdf + mg * w.max_mat_nuc;
+        const int nb = __ldg(w.mat_begin + m), ne = __ldg(w.mat_begin + m + 1);
+        int k = cdf_search(ncdf, ne - nb, 1, thr_n);
+        if (k < 0) k = ne - nb - 1;  // unreachable in the reference (assert)
+        const int nuc = __ldg(w.mat_nuc + nb + k);
+        // Multigroup::Interact (src/Multigroup.cpp:49-73)
+        const size_t ng = (static_cast<size_t>(t) * w.n_nuclides + nuc) * w.G + p.g;
+        const double thr_r = dmul(uniform(p.rng, fast), __ldg(w.mg_total + ng));
+        const int rx = cdf_search(w.mg_rx_cdf + ng * 3, 3, 1, thr_r);
+        if (rx == 0) {
+          p.event = kCapture;
+        }
+        else if (rx == 1) {
+          // Multigroup::Scatter (src/Multigroup.cpp:249-265)
+          p.event = kScatter;
+          const double thr = uniform(p.rng, fast);
+          const int go = cdf_search(w.mg_scat_cdf + ng * w.G, w.G, 1, thr);
+          if (go >= 0) {
+            p.g = go;
+            sample_isotropic(p.rng, p.u, p.v, p.w, fast);
+          }
+        }
+        else if (rx == 2) {
+          p.event = kFission;
+          if constexpr (KEIG) {
+            Site* slots = rp.bank + hist * rp.max_yield;
+            mg_fission(w, p, t, nuc, fast, [&](const Site& st) {
+              if (nbank < rp.max_yield) slots[nbank++] = st;
+              else my_overflow++;
+            });
+          }
+          else {
+            mg_fission(w, p, t, nuc, fast, [&](const Site& st) {
+              if (sp < kStack) stack[sp++] = st;
+              else my_overflow++;
+              my_sec++;
+            });
+          }
+        }
+      }
+      else {
+        const bool refl = __ldg(w.surf_refl + s) != 0;
+        if (refl) {
+          // reflective boundary (extension): stop on the plane, mirror the
+          // normal component, stay in the cell
+          if (rp.score) score_track(w, p, dsurf, pend);
+          if (KEIG) my_ktl += dsurf * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+          stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
+          const int kind = __ldg(w.surf_kind + s);
+          if (kind == kPlaneX) p.u = -p.u;
+          else if (kind == kPlaneY) p.v = -p.v;
+          else p.w = -p.w;
+          p.event = kReflect;
+          p.surf = s;
+          p.skip = s;
+        }
+        else {
+          const double d = dadd(dsurf, kNudge);
+          if (rp.score) score_track(w, p, d, pend);
+          if (KEIG) my_ktl += d * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+          stream(p.x, p.y, p.z, p.u, p.v, p.w, d);
+          if (w.quirks) {
+            p.cell = find_cell(w, p.x, p.y, p.z);
+          }
+          else {
+            p.cell = find_cell_crossing(w, p.x, p.y, p.z, s, moving_positive(w, s, p.x, p.y, p.z, p.u, p.v, p.w));
+            p.skip = s;
+          }
+          p.surf = s;
+          if (p.cell < 0) {
+            p.event = kLostEvent;
+            my_lost++;
+            rp.ctr->lost_xyz[0] = p.x;
+            rp.ctr->lost_xyz[1] = p.y;
+            rp.ctr->lost_xyz[2] = p.z;
+          }
+          else {
+            p.event = __ldg(w.cell_mat + p.cell) >= 0 ? kSurfaceCross : kLeak;
+          }
+        }
+      }
+      if (rp.score) score_event(w, p, pend);
+      p.nev++;
+      hist_nev++;
+      my_events++;
+      const bool dead = p.event == kCapture || p.event == kLeak || p.event == kFission || p.event == kLostEvent;
+      if (!dead && p.nev >= rp.max_events) {
+        my_capped++;
+        p.event = kLostEvent;
+      }
+      if (dead || p.event == kLostEvent) {
+        if (fate == kBirth) fate = static_cast<int8_t>(p.event);
+        alive = false;
+        if (!KEIG && sp > 0) {
+          // next particle of the same history (FixedSource bank loop,
+          // src/FixedSource.cpp:63-72)
+          const Site st = stack[--sp];
+          p.x = st.x;
+          p.y = st.y;
+          p.z = st.z;
+          p.u = st.u;
+          p.v = st.v;
+          p.w = st.w;
+          p.g = static_cast<int>(st.energy) - 1;
+          p.type = 0;  // BankSecondaries creates neutrons
+          if constexpr (std::is_same_v<Rng, PhiloxRng>) p.rng.init(rp.run_key, st.key, 1);
+          else p.rng.seed(st.key);
+          p.cell = find_cell(w, p.x, p.y, p.z);
+          p.event = kBirth;
+          p.surf = -1;
+          p.skip = -1;
+          p.nev = 0;
+          alive = p.cell >= 0 && __ldg(w.cell_mat + p.cell) >= 0;
+          if (!alive) my_lost++;
+        }
+        if (!alive) finish_history();
+      }
+    }
+  }
+
+  // ---- counters: warp reduce, one atomic per warp
+  for (int off = 16; off > 0; off >>= 1) {
+    my_events += __shfl_down_sync(0xffffffffu, my_events, off);
+    my_lost += __shfl_down_sync(0xffffffffu, my_lost, off);
+    my_capped += __shfl_down_sync(0xffffffffu, my_capped, off);
+    my_overflow += __shfl_down_sync(0xffffffffu, my_overflow, off);
+    my_sec += __shfl_down_sync(0xffffffffu, my_sec, off);
+    my_ktl += __shfl_down_sync(0xffffffffu, my_ktl, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&rp.ctr->events, my_events);
+    if (my_lost) atomicAdd(&rp.ctr->lost, my_lost);
+    if (my_capped) atomicAdd(&rp.ctr->capped, my_capped);
+    if (my_overflow) atomicAdd(&rp.ctr->overflow, my_overflow);
+    if (my_sec) atomicAdd(&rp.ctr->secondaries, my_sec);
+    if (KEIG) atomicAdd(&rp.ctr->k_tracklength, my_ktl);
+  }
+  if (use_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < static_cast<int>(rp.total_bins); i += blockDim.x) {
+      if (smem[i] != 0) atomicAdd(rp.tally_sum + i, smem[i]);
+      if (smem[kSharedBins + i] != 0) atomicAdd(rp.tally_sq + i, smem[kSharedBins + i]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launches
+
+namespace {
+template <class K>
+int occupancy(K kernel, int block, size_t smem) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem);
+  return n;
+}
+}  // namespace
+
+int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast) {
+  (void)fast;
+  const size_t smem = 2 * kSharedBins * sizeof(double);
+  if (energy_mode == 0) {
+    if (rng_mode == 1) return keig ? occupancy(k_history_mg<MinstdRng, true>, block, smem)
+                                   : occupancy(k_history_mg<MinstdRng, false>, block, smem);
+    return keig ? occupancy(k_history_mg<PhiloxRng, true>, block, smem)
+                : occupancy(k_history_mg<PhiloxRng, false>, block, smem);
+  }
+  return 1;
+}
+
+cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
+                              cudaStream_t stream) {
+  const size_t smem = 2 * kSharedBins * sizeof(double);
+  if (rng_mode == 1) {
+    if (rp.keig) k_history_mg<MinstdRng, true><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_mg<MinstdRng, false><<<grid, block, smem, stream>>>(w, rp);
+  }
+  else {
+    if (rp.keig) k_history_mg<PhiloxRng, true><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_mg<PhiloxRng, false><<<grid, block, smem, stream>>>(w, rp);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// fission bank: exclusive scan of per-history counts (three-phase block
+// scan), compaction in history order, uniform resampling
+
+namespace {
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
+                              unsigned long long* block_sums) {
+  __shared__ unsigned long long warp_sums[32];
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
+  unsigned long long v = i < n ? count[i] : 0;
+  // inclusive warp scan
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long x = v;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= static_cast<unsigned>(off)) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long s = warp_sums[lane];
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, s, off);
+      if (lane >= static_cast<unsigned>(off)) s += y;
+    }
+    warp_sums[lane] = s;
+  }
+  __syncthreads();
+  const unsigned long long warp_base = wid ? warp_sums[wid - 1] : 0;
+  if (i < n) offsets[i] = warp_base + x - v;
+  if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = warp_base + x;
+}
+
+__global__ void k_scan_sums(unsigned long long* block_sums, unsigned long long nb, unsigned long long* total) {
+  // single block; nb is small (n / 1024)
+  __shared__ unsigned long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (unsigned long long base = 0; base < nb; base += blockDim.x) {
+    const unsigned long long i = base + threadIdx.x;
+    const unsigned long long v = i < nb ? block_sums[i] : 0;
+    __shared__ unsigned long long buf[1024];
+    buf[threadIdx.x] = v;
+    __syncthreads();
+    for (unsigned off = 1; off < blockDim.x; off <<= 1) {
+      const unsigned long long y = threadIdx.x >= off ? buf[threadIdx.x - off] : 0;
+      __syncthreads();
+      buf[threadIdx.x] += y;
+      __syncthreads();
+    }
+    if (i < nb) block_sums[i] = carry + buf[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += buf[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(unsigned long long* offsets, unsigned long long n, const unsigned long long* block_sums) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
+  if (i < n) offsets[i] += block_sums[blockIdx.x];
+}
+
+__global__ void k_compact(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
+                          unsigned long long n, uint32_t max_yield, Site* out) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t c = count[i];
+  const unsigned long long o = offsets[i];
+  for (uint32_t k = 0; k < c; k++) out[o + k] = slots[i * max_yield + k];
+}
+
+// next source j = bank[floor(U_j * M)], U_j from Philox(key, counter j)
+__global__ void k_resample(const Site* bank, const unsigned long long* total, unsigned long long n,
+                           unsigned long long key, Site* next) {
+  const unsigned long long j = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const unsigned long long m = *total;
+  if (m == 0) return;
+  uint32_t c[4] = {static_cast<uint32_t>(j), static_cast<uint32_t>(j >> 32), 0x72657361u, 0};
+  philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
+  const double u = ((c[0] >> 5) * 67108864.0 + (c[1] >> 6)) * (1.0 / 9007199254740992.0);
+  unsigned long long idx = static_cast<unsigned long long>(u * static_cast<double>(m));
+  if (idx >= m) idx = m - 1;
+  next[j] = bank[idx];
+}
+}  // namespace
+
+cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
+                             unsigned long long* scratch_sums, unsigned long long* total, cudaStream_t stream) {
+  const unsigned long long nb = (n + kScanBlock - 1) / kScanBlock;
+  k_scan_blocks<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(count, n, offsets, scratch_sums);
+  k_scan_sums<<<1, 1024, 0, stream>>>(scratch_sums, nb, total);
+  k_scan_add<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(offsets, n, scratch_sums);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bank_compact(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
+                                unsigned long long n, uint32_t max_yield, Site* out, cudaStream_t stream) {
+  const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+  k_compact<<<blocks, 256, 0, stream>>>(slots, count, offsets, n, max_yield, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resample(const Site* bank, const unsigned long long* total, unsigned long long n,
+                            unsigned long long key, Site* next, cudaStream_t stream) {
+  const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+  k_resample<<<blocks, 256, 0, stream>>>(bank, total, n, key, next);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_history_ce(const DevWorld&, const RunParams&, int, int, int, cudaStream_t) {
+  return cudaErrorNotSupported;
+}
+
+}  // namespace mcd

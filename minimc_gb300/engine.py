@@ -1,0 +1,465 @@
+"""ctypes binding of the C ABI (include/minimc_gb300.h) and a thin host-side
+mirror of minimc's driver interface.
+
+The reference is driven as ``Driver::Create(path)->Solve()``
+(src/minimc.cpp:16-21, src/Driver.cpp:18-35), returning an ``EstimatorSet``
+whose estimators report ``mean`` and ``std dev`` per bin
+(src/Scorable.cpp:51-70).  ``Driver.create`` / ``Driver.solve`` below do the
+same through the GPU library; ``World`` exposes the deterministic queries
+(``find_cell_containing``, ``nearest_surface``) that the reference's unit
+tests exercise.
+
+The library is the CUDA build in ``minimc_gb300/_lib``; there is no CPU
+fallback: loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libminimc_gb300.so"
+
+MC_OK = 0
+ERRORS = {
+    -1: "MC_ERR_INPUT", -2: "MC_ERR_OOM", -3: "MC_ERR_DEVICE", -4: "MC_ERR_TIMEOUT",
+    -5: "MC_ERR_LOST", -6: "MC_ERR_RESAMPLE", -7: "MC_ERR_STATE", -8: "MC_ERR_OVERFLOW",
+    -9: "MC_ERR_EVENT_CAP",
+}
+RNG_PHILOX, RNG_MINSTD = 0, 1
+SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT = 0, 1, 2
+TSL_POD, TSL_MLP = 0, 1
+GEOMETRY_ROBUST, GEOMETRY_REFERENCE = 0, 1
+
+# Particle::Event order (src/Particle.hpp:36-44) plus extensions
+EVENTS = ["birth", "scatter", "capture", "fission", "surface_cross", "leak", "virtual_collision",
+          "reflect", "lost"]
+
+
+class MCError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {message}")
+        self.code = code
+        self.message = message
+
+
+class RunOpts(C.Structure):
+    _fields_ = [("histories", C.c_uint64), ("seed", C.c_uint64), ("inactive", C.c_uint32),
+                ("active", C.c_uint32), ("rng", C.c_int32), ("schedule", C.c_int32),
+                ("max_events", C.c_uint32), ("block_size", C.c_int32), ("fast_math", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
+
+
+class Site(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("u", C.c_double),
+                ("v", C.c_double), ("w", C.c_double), ("energy", C.c_double), ("key", C.c_uint64)]
+
+
+SITE_DTYPE = np.dtype([("x", "f8"), ("y", "f8"), ("z", "f8"), ("u", "f8"), ("v", "f8"), ("w", "f8"),
+                       ("energy", "f8"), ("key", "u8")])
+
+
+class ProblemInfo(C.Structure):
+    _fields_ = [("problem", C.c_int32), ("energy_mode", C.c_int32), ("tracking", C.c_int32),
+                ("n_cells", C.c_int32), ("n_surfaces", C.c_int32), ("n_materials", C.c_int32),
+                ("n_nuclides", C.c_int32), ("groups", C.c_int32), ("n_estimators", C.c_int32),
+                ("n_tsl", C.c_int32), ("histories", C.c_uint64), ("seed", C.c_uint64),
+                ("inactive", C.c_uint32), ("active", C.c_uint32), ("total_bins", C.c_uint64),
+                ("max_yield", C.c_uint32), ("reserved", C.c_int32 * 7)]
+
+
+class EstimatorInfo(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("kind", C.c_int32), ("target", C.c_int32),
+                ("offset", C.c_uint64), ("n_bins", C.c_uint64), ("cosine_bins", C.c_uint64),
+                ("energy_bins", C.c_uint64)]
+
+
+class TallyOut(C.Structure):
+    _fields_ = [("sum", C.POINTER(C.c_double)), ("sum_sq", C.POINTER(C.c_double)),
+                ("history_events", C.POINTER(C.c_uint32)), ("history_fate", C.POINTER(C.c_int8)),
+                ("histories", C.c_uint64), ("events", C.c_uint64), ("secondaries", C.c_uint64),
+                ("lost", C.c_uint64), ("capped", C.c_uint64), ("overflow", C.c_uint64),
+                ("resample_failures", C.c_uint64), ("transport_ms", C.c_double),
+                ("launches", C.c_uint64), ("reserved", C.c_double * 4)]
+
+
+class KeigOut(C.Structure):
+    _fields_ = [("k_cycle", C.POINTER(C.c_double)), ("bank_size", C.POINTER(C.c_uint64)),
+                ("sum", C.POINTER(C.c_double)), ("sum_sq", C.POINTER(C.c_double)),
+                ("k_mean", C.c_double), ("k_std", C.c_double), ("k_tracklength_mean", C.c_double),
+                ("events", C.c_uint64), ("lost", C.c_uint64), ("capped", C.c_uint64),
+                ("overflow", C.c_uint64), ("transport_ms", C.c_double), ("launches", C.c_uint64),
+                ("reserved", C.c_double * 4)]
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_SIGNATURES = {
+    "mc_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "mc_destroy": (None, [_P]),
+    "mc_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
+    "mc_set_stream": (C.c_int, [_P, _P]),
+    "mc_version": (C.c_int, []),
+    "mc_load_xml": (C.c_int, [_P, C.c_char_p, C.c_char_p]),
+    "mc_problem_info_get": (C.c_int, [_P, C.POINTER(ProblemInfo)]),
+    "mc_set_geometry_mode": (C.c_int, [_P, C.c_int32]),
+    "mc_estimator_info_get": (C.c_int, [_P, C.c_int32, C.POINTER(EstimatorInfo)]),
+    "mc_object_name": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]),
+    "mc_run_fixed_source": (C.c_int, [_P, C.POINTER(RunOpts), C.POINTER(TallyOut)]),
+    "mc_run_keigenvalue": (C.c_int, [_P, C.POINTER(RunOpts), C.POINTER(KeigOut)]),
+    "mc_keig_begin": (C.c_int, [_P, C.POINTER(RunOpts)]),
+    "mc_keig_cycle": (C.c_int, [_P, C.c_int32, _D]),
+    "mc_keig_end": (C.c_int, [_P, C.POINTER(KeigOut)]),
+    "mc_keig_status": (C.c_int, [_P, C.POINTER(KeigOut)]),
+    "mc_transport_bank": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "mc_tallies_reset": (C.c_int, [_P]),
+    "mc_tallies_get": (C.c_int, [_P, _D, _D]),
+    "mc_find_cell": (C.c_int, [_P, _D, C.c_uint64, C.POINTER(C.c_int32)]),
+    "mc_nearest_surface": (C.c_int, [_P, C.POINTER(C.c_int32), _D, _D, C.c_uint64, C.POINTER(C.c_int32), _D]),
+    "mc_surface_distance": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+    "mc_surface_contains": (C.c_int, [_P, C.c_int32, _D, C.c_uint64, C.POINTER(C.c_int8)]),
+    "mc_material_xs": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D, _D]),
+    "mc_energy_index": (C.c_int, [_P, C.c_int32, _D, C.c_uint64, C.POINTER(C.c_int64)]),
+    "mc_sample_tsl": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, C.c_uint64, C.c_int32, _D, _D,
+                                C.POINTER(C.c_uint64)]),
+    "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def load_library() -> C.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        raise RuntimeError(f"minimc_gb300 CUDA library not built: {_LIB_PATH} (run __graft_entry__.build())")
+    lib = C.CDLL(str(_LIB_PATH))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _arr(a, dtype) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class Context:
+    """One device context (mc_ctx): owns the device copy of one problem."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.mc_create(C.byref(h), device)
+        if rc != MC_OK:
+            raise MCError(rc, "mc_create failed (no usable CUDA device?)")
+        self.h = h
+        self.info: ProblemInfo | None = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self.lib.mc_last_error(self.h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def check(self, rc: int, allow=()):
+        if rc != MC_OK and rc not in allow:
+            raise MCError(rc, self.error())
+        return rc
+
+    def set_stream(self, stream_handle: int):
+        self.check(self.lib.mc_set_stream(self.h, _P(stream_handle)))
+
+    def set_geometry_mode(self, mode: int):
+        """GEOMETRY_ROBUST (default) or GEOMETRY_REFERENCE (include/minimc_gb300.h)."""
+        self.check(self.lib.mc_set_geometry_mode(self.h, mode))
+
+    def load_xml(self, xml_text: str, base_dir: str | os.PathLike | None = None):
+        self.check(self.lib.mc_load_xml(self.h, xml_text.encode(), str(base_dir or "").encode()))
+        info = ProblemInfo()
+        self.check(self.lib.mc_problem_info_get(self.h, C.byref(info)))
+        self.info = info
+        return info
+
+    def estimators(self) -> list[EstimatorInfo]:
+        out = []
+        for i in range(self.info.n_estimators):
+            e = EstimatorInfo()
+            self.check(self.lib.mc_estimator_info_get(self.h, i, C.byref(e)))
+            out.append(e)
+        return out
+
+    def object_name(self, kind: int, index: int) -> str:
+        buf = C.create_string_buffer(256)
+        self.check(self.lib.mc_object_name(self.h, kind, index, buf, 256))
+        return buf.value.decode()
+
+    # -- solvers -------------------------------------------------------------
+    @staticmethod
+    def opts(**kw) -> RunOpts:
+        o = RunOpts()
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    def run_fixed_source(self, per_history: bool = False, allow=(), **kw):
+        nb = max(1, self.info.total_bins)
+        s = np.zeros(nb)
+        s2 = np.zeros(nb)
+        out = TallyOut()
+        out.sum = _dptr(s)
+        out.sum_sq = _dptr(s2)
+        n = kw.get("histories") or self.info.histories
+        ev = fate = None
+        if per_history:
+            ev = np.zeros(n, np.uint32)
+            fate = np.zeros(n, np.int8)
+            out.history_events = ev.ctypes.data_as(C.POINTER(C.c_uint32))
+            out.history_fate = fate.ctypes.data_as(C.POINTER(C.c_int8))
+        o = self.opts(**kw)
+        rc = self.check(self.lib.mc_run_fixed_source(self.h, C.byref(o), C.byref(out)), allow)
+        return FixedSourceResult(rc, s[: self.info.total_bins], s2[: self.info.total_bins], out, ev, fate)
+
+    def run_keigenvalue(self, allow=(), **kw):
+        o = self.opts(**kw)
+        inactive = o.inactive if (o.inactive or o.active) else self.info.inactive
+        active = o.active if (o.inactive or o.active) else self.info.active
+        ncyc = inactive + active
+        k = np.zeros(ncyc)
+        bank = np.zeros(ncyc, np.uint64)
+        nb = max(1, self.info.total_bins)
+        s = np.zeros(nb)
+        s2 = np.zeros(nb)
+        out = KeigOut()
+        out.k_cycle = _dptr(k)
+        out.bank_size = bank.ctypes.data_as(C.POINTER(C.c_uint64))
+        out.sum = _dptr(s)
+        out.sum_sq = _dptr(s2)
+        rc = self.check(self.lib.mc_run_keigenvalue(self.h, C.byref(o), C.byref(out)), allow)
+        return KeigResult(rc, k, bank, s[: self.info.total_bins], s2[: self.info.total_bins], out,
+                          inactive, active)
+
+    def keig_begin(self, **kw):
+        o = self.opts(**kw)
+        self.check(self.lib.mc_keig_begin(self.h, C.byref(o)))
+
+    def keig_cycle(self, active: bool) -> float:
+        k = C.c_double()
+        self.check(self.lib.mc_keig_cycle(self.h, int(active), C.byref(k)))
+        return k.value
+
+    def keig_status(self) -> KeigOut:
+        out = KeigOut()
+        self.check(self.lib.mc_keig_status(self.h, C.byref(out)))
+        return out
+
+    def keig_end(self) -> KeigOut:
+        out = KeigOut()
+        self.check(self.lib.mc_keig_end(self.h, C.byref(out)))
+        return out
+
+    def transport_bank(self, sites: np.ndarray, rng: int = RNG_PHILOX, cap: int | None = None):
+        sites = np.ascontiguousarray(sites, dtype=SITE_DTYPE)
+        cap = cap if cap is not None else len(sites) * max(1, self.info.max_yield)
+        out = np.zeros(cap, SITE_DTYPE)
+        n_out = C.c_uint64()
+        self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), rng,
+                                              out.ctypes.data_as(_P), cap, C.byref(n_out)))
+        return out[: n_out.value]
+
+    def transport_bank_into(self, sites: np.ndarray, out: np.ndarray, rng: int = RNG_PHILOX) -> int:
+        """Like transport_bank, with caller-owned (e.g. pinned) site arrays;
+        returns the number of fission sites written to ``out``."""
+        assert sites.dtype == SITE_DTYPE and out.dtype == SITE_DTYPE
+        n_out = C.c_uint64()
+        self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), rng,
+                                              out.ctypes.data_as(_P), len(out), C.byref(n_out)))
+        return int(n_out.value)
+
+    def tallies(self):
+        nb = max(1, self.info.total_bins)
+        s = np.zeros(nb)
+        s2 = np.zeros(nb)
+        self.check(self.lib.mc_tallies_get(self.h, _dptr(s), _dptr(s2)))
+        return s[: self.info.total_bins], s2[: self.info.total_bins]
+
+    def tallies_reset(self):
+        self.check(self.lib.mc_tallies_reset(self.h))
+
+    # -- deterministic queries ------------------------------------------------
+    def find_cell(self, xyz) -> np.ndarray:
+        xyz = _arr(xyz, np.float64).reshape(-1, 3)
+        out = np.zeros(len(xyz), np.int32)
+        self.check(self.lib.mc_find_cell(self.h, _dptr(xyz), len(xyz), out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def nearest_surface(self, cell, xyz, uvw):
+        xyz = _arr(xyz, np.float64).reshape(-1, 3)
+        uvw = _arr(uvw, np.float64).reshape(-1, 3)
+        cell = _arr(np.broadcast_to(cell, (len(xyz),)), np.int32)
+        surf = np.zeros(len(xyz), np.int32)
+        dist = np.zeros(len(xyz))
+        self.check(self.lib.mc_nearest_surface(self.h, cell.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(xyz),
+                                               _dptr(uvw), len(xyz), surf.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               _dptr(dist)))
+        return surf, dist
+
+    def surface_distance(self, surface: int, xyz, uvw) -> np.ndarray:
+        xyz = _arr(xyz, np.float64).reshape(-1, 3)
+        uvw = _arr(uvw, np.float64).reshape(-1, 3)
+        out = np.zeros(len(xyz))
+        self.check(self.lib.mc_surface_distance(self.h, surface, _dptr(xyz), _dptr(uvw), len(xyz), _dptr(out)))
+        return out
+
+    def surface_contains(self, surface: int, xyz) -> np.ndarray:
+        xyz = _arr(xyz, np.float64).reshape(-1, 3)
+        out = np.zeros(len(xyz), np.int8)
+        self.check(self.lib.mc_surface_contains(self.h, surface, _dptr(xyz), len(xyz),
+                                                out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out.astype(bool)
+
+
+@dataclass
+class FixedSourceResult:
+    status: int
+    sum: np.ndarray
+    sum_sq: np.ndarray
+    raw: TallyOut
+    history_events: np.ndarray | None = None
+    history_fate: np.ndarray | None = None
+
+    @property
+    def histories(self) -> int:
+        return int(self.raw.histories)
+
+    def mean(self) -> np.ndarray:
+        """Scorable mean: S / N (src/Scorable.cpp:51-58)."""
+        return self.sum / self.histories
+
+    def std(self) -> np.ndarray:
+        """Scorable std dev: sqrt(S2 - S^2/N) / N (src/Scorable.cpp:59-68)."""
+        n = self.histories
+        return np.sqrt(np.maximum(self.sum_sq - self.sum * self.sum / n, 0.0)) / n
+
+
+@dataclass
+class KeigResult:
+    status: int
+    k_cycle: np.ndarray
+    bank_size: np.ndarray
+    sum: np.ndarray
+    sum_sq: np.ndarray
+    raw: KeigOut
+    inactive: int
+    active: int
+
+    @property
+    def k_mean(self) -> float:
+        return float(self.raw.k_mean)
+
+    @property
+    def k_std(self) -> float:
+        return float(self.raw.k_std)
+
+
+class World:
+    """Deterministic queries of a loaded problem (World/Cell/CSGSurface)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.cells = [ctx.object_name(0, i) for i in range(ctx.info.n_cells)]
+        self.surfaces = [ctx.object_name(1, i) for i in range(ctx.info.n_surfaces)]
+
+    def find_cell_containing(self, point) -> str:
+        """World::FindCellContaining (src/World.cpp:26-37)."""
+        c = int(self.ctx.find_cell(np.asarray(point, dtype=np.float64).reshape(1, 3))[0])
+        if c < 0:
+            raise RuntimeError("Point does not belong to any Cell. Please check"
+                               "that all space is either assigned a material or void.")
+        return self.cells[c]
+
+    def nearest_surface(self, cell: str, point, direction) -> tuple[str, float]:
+        """Cell::NearestSurface (src/Cell.cpp:37-51)."""
+        ci = self.cells.index(cell)
+        s, d = self.ctx.nearest_surface(ci, np.asarray(point, float).reshape(1, 3),
+                                        np.asarray(direction, float).reshape(1, 3))
+        return self.surfaces[int(s[0])], float(d[0])
+
+
+class Driver:
+    """``Driver::Create(path)`` + ``Solve()`` (src/Driver.cpp:18-35)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.world = World(ctx)
+
+    @classmethod
+    def create(cls, xml_path: str | os.PathLike, device: int = 0) -> "Driver":
+        p = Path(xml_path)
+        ctx = Context(device)
+        ctx.load_xml(p.read_text(), p.parent)
+        return cls(ctx)
+
+    @classmethod
+    def from_text(cls, xml_text: str, base_dir=None, device: int = 0) -> "Driver":
+        ctx = Context(device)
+        ctx.load_xml(xml_text, base_dir)
+        return cls(ctx)
+
+    @property
+    def batchsize(self) -> int:
+        return int(self.ctx.info.histories)
+
+    def solve(self, **kw):
+        if self.ctx.info.problem == 0:
+            return self.ctx.run_fixed_source(**kw)
+        return self.ctx.run_keigenvalue(**kw)
+
+    def estimator_results(self, result) -> dict[str, dict]:
+        """Estimator means and std devs by name, normalized per history (fixed
+        source: histories; k-eigenvalue: histories per cycle x active cycles)."""
+        if isinstance(result, KeigResult):
+            n = self.ctx.info.histories * result.active
+        else:
+            n = result.histories
+        out = {}
+        for e in self.ctx.estimators():
+            sl = slice(e.offset, e.offset + e.n_bins)
+            s, s2 = result.sum[sl], result.sum_sq[sl]
+            out[e.name.decode()] = {
+                "mean": s / n,
+                "std": np.sqrt(np.maximum(s2 - s * s / n, 0.0)) / n,
+                "cosine_bins": int(e.cosine_bins),
+                "energy_bins": int(e.energy_bins),
+            }
+        return out
