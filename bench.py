@@ -173,7 +173,7 @@ def run_gpu(args) -> None:
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.load_xml(xml)
-    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block)
+    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block, schedule=args.schedule)
 
     def barrier():
         if dist is not None:
@@ -299,6 +299,7 @@ def main():
     ap.add_argument("--histories", type=int, default=1_000_000)
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--fast", type=int, default=0)
+    ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 history, 2 event")
     ap.add_argument("--cpu-histories", type=int, default=1_000_000)
     ap.add_argument("--cpu-cycles", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")

@@ -22,7 +22,7 @@ OBJ_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libminimc_gb300.so"
 
 HOST_SOURCES = ["mc_xml.cpp", "mc_model.cpp"]
-CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_probe.cu"]
+CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_event.cu", "mc_probe.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -1,5 +1,6 @@
 // C ABI (include/minimc_gb300.h): context, world upload and the solvers.
 #include "../../include/minimc_gb300.h"
+#include "mc_event.cuh"
 #include "mc_kernels.cuh"
 #include "mc_model.hpp"
 
@@ -41,13 +42,14 @@ struct mc_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   uint64_t launches = 0;
   // scratch, grown on demand
-  DevBuffer scratch[12];
+  DevBuffer scratch[20];
+  int last_schedule = MC_SCHEDULE_HISTORY;
   // k-eigenvalue state
   struct {
     bool active = false;
     uint64_t n = 0, seed = 1;
     uint32_t inactive = 0, act = 0, cycle = 0;
-    int rng = 0, fast = 0, block = 256;
+    int rng = 0, fast = 0, block = 256, schedule = 0;
     uint32_t max_events = 1000000;
     std::vector<double> k, ktl;
     std::vector<uint64_t> bank;
@@ -72,6 +74,11 @@ enum ScratchSlot {
   kProbeIn,
   kProbeIn2,
   kProbeOut,
+  kEvState,
+  kEvQueues,
+  kEvCnt,
+  kEvPend,
+  kEvFis,
 };
 
 int fail(mc_ctx* c, int code, const std::string& msg) {
@@ -229,7 +236,7 @@ int build_world(mc_ctx* c) {
       }
     }
     c->max_yield = static_cast<uint32_t>(std::floor(max_nubar)) + 1;
-    std::vector<double> mtot(T * M * G, 0), mcdf(T * M * G * max_nuc, 0), mnsf(T * M * G, 0);
+    std::vector<double> mtot(T * M * G, 0), mcdf(T * M * G * max_nuc, 0), mnsf(T * M * G, 0), msig(T * M * G, 0);
     for (size_t t = 0; t < T; t++) {
       for (size_t mi = 0; mi < M; mi++) {
         const auto& mt = m.materials[mi];
@@ -243,10 +250,13 @@ int build_world(mc_ctx* c) {
             nsf = nsf + mt.afrac[k] * nusigf[i];
           }
           mtot[(t * M + mi) * G + g] = acc;
-          mnsf[(t * M + mi) * G + g] = nsf;
+          // SurfaceTracking: number_density * GetCollisionProbabilityDensity
+          msig[(t * M + mi) * G + g] = mt.number_density * acc;
+          mnsf[(t * M + mi) * G + g] = mt.number_density * nsf;
         }
       }
     }
+    UP(msig, mat_mg_sigma)
     UP(total, mg_total)
     UP(rx, mg_rx_cdf)
     UP(scat, mg_scat_cdf)
@@ -283,6 +293,56 @@ int build_world(mc_ctx* c) {
   }
   c->total_bins = off;
   w.n_est = static_cast<int32_t>(m.estimators.size());
+  // multigroup: energy bin of each group number, by the reference formulas
+  std::vector<int32_t> est_ebin_mg;
+  std::vector<uint64_t> est_esize;
+  for (const auto& e : m.estimators) {
+    est_esize.push_back(e.energy.size());
+    for (uint64_t g = 1; g <= std::max<uint64_t>(1, m.groups); g++)
+      est_ebin_mg.push_back(static_cast<int32_t>(e.energy.index(static_cast<double>(g))));
+  }
+  UP(est_ebin_mg, est_ebin_mg)
+  UP(est_esize, est_esize)
+  // plane keys and box cells (exact fast paths, mc_device.cuh)
+  std::vector<long long> surf_key;
+  for (const auto& s : m.surfaces)
+    surf_key.push_back(s.kind == mc::kPlaneX || s.kind == mc::kPlaneY || s.kind == mc::kPlaneZ ? mcd::dkey(s.p[0]) : 0);
+  UP(surf_key, surf_key)
+  std::vector<int32_t> cell_box;
+  std::vector<mcd::BoxCell> boxes;
+  for (const auto& cl : m.cells) {
+    mcd::BoxCell bx{};
+    bool ok = cl.surfaces.size() == 6;
+    int seen[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t k = 0; ok && k < cl.surfaces.size(); k++) {
+      const mc::Surface& s = m.surfaces[cl.surfaces[k]];
+      const int axis = s.kind == mc::kPlaneX ? 0 : s.kind == mc::kPlaneY ? 1 : s.kind == mc::kPlaneZ ? 2 : -1;
+      if (axis < 0) {
+        ok = false;
+        break;
+      }
+      // sense +1 (within = 0): the cell is above the plane -> low plane
+      const int j = 2 * axis + (cl.within[k] ? 1 : 0);
+      if (seen[j]++) ok = false;
+      bx.c[j] = s.p[0];
+      bx.s[j] = cl.surfaces[k];
+      bx.order[j] = static_cast<int32_t>(k);
+    }
+    for (int a = 0; ok && a < 3; a++) ok = bx.c[2 * a] < bx.c[2 * a + 1];
+    if (ok) {
+      cell_box.push_back(static_cast<int32_t>(boxes.size()));
+      boxes.push_back(bx);
+    }
+    else {
+      cell_box.push_back(-1);
+    }
+  }
+  UP(cell_box, cell_box)
+  {
+    const mcd::BoxCell* dp = nullptr;
+    if ((rc = upload(c, boxes, &dp)) != MC_OK) return rc;
+    w.boxes = dp;
+  }
   UP(est_kind, est_kind)
   UP(est_target, est_target)
   UP(est_offset, est_offset)
@@ -363,21 +423,131 @@ int counters_status(mc_ctx* c, const DevCounters& h) {
   return MC_OK;
 }
 
+// resolves MC_SCHEDULE_AUTO.  Measured on the 8-group two-zone problem the
+// fused history schedule is faster than the event queues (the event kernels
+// pay a launch and a state round trip per event), so AUTO picks it; the
+// event schedule runs multigroup problems whose estimators fit the dense
+// per-history scores when asked for.
+int resolve_schedule(mc_ctx* c, int requested) {
+  const bool event_ok = c->model.energy_mode == mc::kMultigroup && c->total_bins <= mcd::kEvDenseBins;
+  if (requested == MC_SCHEDULE_EVENT) return event_ok ? MC_SCHEDULE_EVENT : -1;
+  return MC_SCHEDULE_HISTORY;
+}
+
+void count_launches(void* ctx, int n) { static_cast<mc_ctx*>(ctx)->launches += n; }
+
+// event schedule: SoA store, queues, pending scores, fission records.
+// Fixed-source secondaries take new store slots; when a chain needs more
+// slots than the store holds the run is repeated with a larger store (every
+// particle's stream is keyed by its own identity, not its slot, so the
+// repeat draws the same numbers).
+int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap);
+
+int run_event(mc_ctx* c, RunParams& rp, int rng) {
+  uint64_t cap = rp.keig ? rp.n : rp.n * 4 + 65536;
+  for (int attempt = 0;; attempt++) {
+    const int rc = run_event_once(c, rp, rng, cap);
+    if (rc != MC_OK) return rc;
+    if (rp.keig || attempt == 3) return MC_OK;
+    unsigned long long overflow = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&overflow, &c->d_ctr->overflow, sizeof overflow, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (!overflow) return MC_OK;
+    cap *= 4;
+    CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
+    if (rp.pend) CUDA_TRY(c, cudaMemsetAsync(rp.pend, 0, rp.n * rp.nb * sizeof(double), c->stream));
+  }
+}
+
+int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap) {
+  const uint64_t n = rp.n;
+  mcd::EvParams ep{};
+  ep.rp = rp;
+  ep.capacity = static_cast<unsigned>(std::min<uint64_t>(cap, 0xffffffffull));
+  if (cap >= 0x7fffffffull) return fail(c, MC_ERR_INPUT, "too many particles for the event schedule");
+  // one allocation for the particle store: 6 f64 + E + 6 x u32 + u64 + u8
+  const size_t bytes = cap * (8 * 7 + 4 * 6 + 8 + 1) + 256 * 16;
+  char* base = static_cast<char*>(scratch(c, kEvState, bytes));
+  auto* q = static_cast<int32_t*>(scratch(c, kEvQueues, cap * 3 * sizeof(int32_t)));
+  auto* cnt = static_cast<unsigned*>(scratch(c, kEvCnt, 64));
+  if (!base || !q || !cnt) return fail(c, MC_ERR_OOM, "event-schedule buffers");
+  size_t off = 0;
+  auto take = [&](size_t each) {
+    char* p = base + off;
+    off += (cap * each + 255) / 256 * 256;
+    return p;
+  };
+  ep.st.x = reinterpret_cast<double*>(take(8));
+  ep.st.y = reinterpret_cast<double*>(take(8));
+  ep.st.z = reinterpret_cast<double*>(take(8));
+  ep.st.u = reinterpret_cast<double*>(take(8));
+  ep.st.v = reinterpret_cast<double*>(take(8));
+  ep.st.w = reinterpret_cast<double*>(take(8));
+  ep.st.E = reinterpret_cast<double*>(take(8));
+  ep.st.g = reinterpret_cast<int32_t*>(take(4));
+  ep.st.cell = reinterpret_cast<int32_t*>(take(4));
+  ep.st.skip = reinterpret_cast<int32_t*>(take(4));
+  ep.st.nev = reinterpret_cast<uint32_t*>(take(4));
+  ep.st.hist = reinterpret_cast<uint32_t*>(take(4));
+  ep.st.rng = reinterpret_cast<uint32_t*>(take(4));
+  ep.st.id = reinterpret_cast<unsigned long long*>(take(8));
+  ep.st.tag = reinterpret_cast<uint8_t*>(take(1));
+  ep.q_in = q;
+  ep.q_out = q + cap;
+  ep.q_coll = q + 2 * cap;
+  ep.cnt = cnt;
+  if (rp.hist_events) CUDA_TRY(c, cudaMemsetAsync(rp.hist_events, 0, n * 4, c->stream));
+  mcd::EvLaunch L{};
+  L.grid = c->num_sms * 8;
+  L.check_every = 8;
+  L.max_iterations = ((rp.max_events + 64) / L.check_every + 1) * L.check_every;
+  const cudaError_t e = mcd::launch_event_mg(c->dw, ep, L, rng, c->stream, count_launches, c);
+  if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("event transport: ") + cudaGetErrorString(e));
+  return MC_OK;
+}
+
 // one transport launch over rp.n particles; returns elapsed device ms
-int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms) {
+int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int schedule = MC_SCHEDULE_AUTO) {
   CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
   rp.ctr = c->d_ctr;
   rp.tally_sum = c->d_sum;
   rp.tally_sq = c->d_sq;
   rp.total_bins = c->total_bins;
   const bool keig = rp.keig != 0;
-  const int grid = grid_for(c, c->model.energy_mode, rng, block, keig, rp.fast != 0);
+  const int sched = resolve_schedule(c, schedule);
+  if (sched < 0) return fail(c, MC_ERR_INPUT, "the event schedule supports multigroup problems with at most 64 tally bins");
+  c->last_schedule = sched;
+  // dense per-history scores when the estimators are small, fission records
+  // for k-eigenvalue cycles
+  const uint64_t n = rp.n;
+  rp.nb = (rp.score && c->total_bins > 0 && c->total_bins <= static_cast<uint64_t>(mcd::kDenseBins))
+              ? static_cast<int32_t>(c->total_bins)
+              : 0;
+  rp.pend = rp.nb ? static_cast<double*>(scratch(c, kEvPend, n * rp.nb * sizeof(double))) : nullptr;
+  rp.fis = keig ? static_cast<mcd::FissionRec*>(scratch(c, kEvFis, n * sizeof(mcd::FissionRec))) : nullptr;
+  if ((rp.nb && !rp.pend) || (keig && !rp.fis)) return fail(c, MC_ERR_OOM, "score/fission buffers");
   CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-  cudaError_t e;
-  if (c->model.energy_mode == mc::kMultigroup) e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream);
-  else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream);
-  if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
-  c->launches++;
+  if (rp.pend) CUDA_TRY(c, cudaMemsetAsync(rp.pend, 0, n * rp.nb * sizeof(double), c->stream));
+  if (sched == MC_SCHEDULE_EVENT) {
+    const int rc = run_event(c, rp, rng);
+    if (rc != MC_OK) return rc;
+  }
+  else {
+    const int grid = grid_for(c, c->model.energy_mode, rng, block, keig, rp.fast != 0);
+    cudaError_t e;
+    if (c->model.energy_mode == mc::kMultigroup) e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream);
+    else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream);
+    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
+    c->launches++;
+  }
+  if (keig && c->model.energy_mode == mc::kMultigroup) {
+    CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
+    c->launches++;
+  }
+  if (rp.nb) {
+    CUDA_TRY(c, mcd::launch_commit_dense(rp, c->num_sms * 8, c->stream));
+    c->launches++;
+  }
   CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
   if (ms) {
     CUDA_TRY(c, cudaEventSynchronize(c->ev1));
@@ -582,7 +752,7 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
   CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
   double ms = 0;
   const uint64_t l0 = c->launches;
-  int rc = run_transport(c, rp, rng, block, &ms);
+  int rc = run_transport(c, rp, rng, block, &ms, o ? o->schedule : 0);
   if (rc != MC_OK) return rc;
   DevCounters h{};
   CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost, c->stream));
@@ -621,6 +791,7 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   k.rng = o ? o->rng : 0;
   k.fast = (o && o->fast_math && k.rng == MC_RNG_PHILOX) ? 1 : 0;
   k.block = pick_block(o);
+  k.schedule = o ? o->schedule : 0;
   k.max_events = o && o->max_events ? o->max_events : 1000000u;
   k.launches0 = c->launches;
   if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
@@ -655,7 +826,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
   double ms = 0;
-  int rc = run_transport(c, rp, k.rng, k.block, &ms);
+  int rc = run_transport(c, rp, k.rng, k.block, &ms, k.schedule);
   if (rc != MC_OK) return rc;
   k.transport_ms += ms;
   Site* bank = nullptr;
@@ -871,9 +1042,24 @@ int mc_surface_contains(mc_ctx* c, int32_t s, const double* xyz, uint64_t n, int
   return MC_OK;
 }
 
-int mc_material_xs(mc_ctx* c, int32_t, const double*, const double*, uint64_t, double*, double*) {
+int mc_material_xs(mc_ctx* c, int32_t cell, const double* xyz, const double* energy, uint64_t n, double* total,
+                   double* majorant) {
   if (!check_ctx(c)) return MC_ERR_STATE;
-  return fail(c, MC_ERR_INPUT, "mc_material_xs: not yet implemented");
+  if (cell < 0 || cell >= c->dw.n_cells) return fail(c, MC_ERR_INPUT, "cell index out of range");
+  if (n == 0) return MC_OK;
+  if (!energy || !total || !majorant) return fail(c, MC_ERR_INPUT, "null argument");
+  (void)xyz;  // multigroup cross sections do not depend on position
+  if (c->model.energy_mode != mc::kMultigroup) return fail(c, MC_ERR_INPUT, "continuous-energy data: not yet supported");
+  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * 8));
+  auto* outp = static_cast<double*>(scratch(c, kProbeOut, n * 16));
+  if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(in, energy, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_material_xs_mg(c->dw, cell, in, n, outp, outp + n, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(total, outp, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(majorant, outp + n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
 }
 
 int mc_energy_index(mc_ctx* c, int32_t, const double*, uint64_t, int64_t*) {

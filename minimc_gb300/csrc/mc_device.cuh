@@ -51,6 +51,15 @@ struct DevCounters {
   unsigned long long pad[4];
 };
 
+// A cell bounded by exactly one low and one high axis-aligned plane per axis.
+// Per axis at most one of the two planes can be ahead of the particle, so
+// Cell::NearestSurface needs three distances instead of six.
+struct BoxCell {
+  double c[6];      // plane positions: x lo, x hi, y lo, y hi, z lo, z hi
+  int32_t s[6];     // surface indices
+  int32_t order[6]; // position of each plane in the cell's surface list
+};
+
 // Flattened world, passed to kernels by value.
 struct DevWorld {
   int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
@@ -80,7 +89,7 @@ struct DevWorld {
   const double* mg_nusigf;    // [T][N][G] nubar * fission (track-length k)
   const double* mat_mg_total;    // [T][M][G]  Σ afrac * total, reference order
   const double* mat_mg_nuc_cdf;  // [T][M][G][max_mat_nuc] running sums
-  const double* mat_mg_nusigf;   // [T][M][G]  Σ afrac * nu * sigma_f
+  const double* mat_mg_nusigf;   // [T][M][G]  N * Σ afrac * nu * sigma_f (macroscopic)
   // estimators
   int32_t n_est;
   const int32_t* est_kind;     // 0 current, 1 track length
@@ -92,7 +101,13 @@ struct DevWorld {
   const double* est_bin_par;   // [n_est][2][6]: n_bins, lower/log_lower, upper/log_upper, width/log_width, base, nbounds
   const uint64_t* est_bound_off;  // [n_est][2] offset into est_bounds
   const double* est_bounds;
-  uint64_t est_stride_dummy;
+  const int32_t* est_ebin_mg;     // [n_est][G] energy bin of each group (multigroup)
+  const uint64_t* est_esize;      // [n_est] number of energy bins
+  // fast paths (all exact)
+  const long long* surf_key;      // [n] order-preserving integer key of a plane's position
+  const int32_t* cell_box;        // [n_cells] index into boxes, or -1
+  const struct BoxCell* boxes;
+  const double* mat_mg_sigma;     // [T][M][G] number_density * microscopic total
   // source (src/Source.cpp)
   double src_pos[3];
   double src_dir[3];
@@ -112,6 +127,25 @@ __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a,
 __device__ __forceinline__ double dot3(double x, double y, double z, double a, double b, double c) {
   return dadd(dadd(dmul(x, a), dmul(y, b)), dmul(z, c));
 }
+
+// Order-preserving integer key of a double: for non-NaN a, b,
+// a < b  <=>  dkey(a) < dkey(b) (signed).  -0.0 maps to the key of +0.0, so
+// equal values get equal keys.  Comparing keys runs on the integer pipe,
+// which on this part issues 32x more operations per clock than FP64.
+__host__ __device__ __forceinline__ long long dkey(double v) {
+#ifdef __CUDA_ARCH__
+  long long b = __double_as_longlong(v);
+#else
+  long long b;
+  __builtin_memcpy(&b, &v, sizeof b);
+#endif
+  if (b == static_cast<long long>(0x8000000000000000ull)) b = 0;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
+// threshold comparisons of non-negative doubles (running sums of cross
+// sections and probabilities): the IEEE bit patterns order like the values
+__device__ __forceinline__ long long nonneg_bits(double v) { return __double_as_longlong(v); }
 
 // ---------------------------------------------------------------------------
 // random streams
@@ -142,6 +176,10 @@ struct MinstdRng {
   __device__ __forceinline__ float u01f() { return static_cast<float>(u01()); }
   // key for a child particle: the reference seeds secondaries with rng()
   __device__ __forceinline__ unsigned long long child_key() { return next(); }
+  __device__ __forceinline__ uint32_t save() const { return x; }
+  __device__ __forceinline__ void restore(unsigned long long, unsigned long long, uint32_t, uint32_t packed) {
+    x = packed;
+  }
 };
 
 // Philox4x32-10 round function (Salmon, Moraes, Dror, Shaw, "Parallel random
@@ -195,16 +233,36 @@ struct PhiloxRng {
     if (idx >= 4) refill();
     return buf[idx++];
   }
-  // 53-bit uniform in [0, 1)
+  // uniform in [0, 1) on the 2^-52 lattice: 52 random mantissa bits under
+  // the exponent of 1.0 give [1, 2); one FP64 subtraction shifts it down
   __device__ __forceinline__ double u01() {
-    const uint32_t a = next() >> 5, b = next() >> 6;
-    return (a * 67108864.0 + b) * (1.0 / 9007199254740992.0);
+    const uint32_t hi = next(), lo = next();
+    return __hiloint2double(static_cast<int>(0x3FF00000u | (hi >> 12)), static_cast<int>(lo)) - 1.0;
   }
-  // 24-bit uniform in (0, 1)
-  __device__ __forceinline__ float u01f() { return (static_cast<float>(next() >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+  // uniform in [2^-24, 1 - 2^-24]: 23 random bits plus a half step, exact in
+  // FP32 (24 bits plus the half step would round the top value up to 1.0)
+  __device__ __forceinline__ float u01f() { return (static_cast<float>(next() >> 9) + 0.5f) * (1.0f / 8388608.0f); }
   __device__ __forceinline__ unsigned long long child_key() {
     const unsigned long long lo = next();
     return lo | (static_cast<unsigned long long>(next()) << 32);
+  }
+  // Position in the stream as one word (block counter, index in block), so
+  // that a particle resumed in another kernel draws exactly the numbers it
+  // would have drawn without the break.
+  __device__ __forceinline__ uint32_t save() const { return (ctr << 3) | static_cast<uint32_t>(idx); }
+  __device__ __forceinline__ void restore(unsigned long long run_key, unsigned long long id, uint32_t t,
+                                          uint32_t packed) {
+    init(run_key, id, t);
+    ctr = packed >> 3;
+    idx = static_cast<int32_t>(packed & 7u);
+    if (idx < 4) {
+      uint32_t c[4] = {ctr - 1, h0, h1, tag};
+      philox4x32_10(c, k0, k1);
+      buf[0] = c[0];
+      buf[1] = c[1];
+      buf[2] = c[2];
+      buf[3] = c[3];
+    }
   }
 };
 
@@ -262,13 +320,23 @@ __device__ __forceinline__ double surface_distance(const DevWorld& w, int s, dou
   }
 }
 
+// a point with the order-preserving keys of its coordinates
+struct PointK {
+  double x, y, z;
+  long long kx, ky, kz;
+  __device__ __forceinline__ PointK(double x_, double y_, double z_)
+      : x(x_), y(y_), z(z_), kx(dkey(x_)), ky(dkey(y_)), kz(dkey(z_)) {}
+};
+
 // CSGSurface::Contains: true on the negative side; on-surface is positive.
-__device__ __forceinline__ bool surface_contains(const DevWorld& w, int s, double x, double y, double z) {
+// Planes compare integer keys (x < c  <=>  key(x) < key(c)).
+__device__ __forceinline__ bool surface_contains(const DevWorld& w, int s, const PointK& q) {
   const double* p = w.surf_p + 4 * s;
+  const double x = q.x, y = q.y, z = q.z;
   switch (__ldg(w.surf_kind + s)) {
-  case kPlaneX: return x < __ldg(p);
-  case kPlaneY: return y < __ldg(p);
-  case kPlaneZ: return z < __ldg(p);
+  case kPlaneX: return q.kx < __ldg(w.surf_key + s);
+  case kPlaneY: return q.ky < __ldg(w.surf_key + s);
+  case kPlaneZ: return q.kz < __ldg(w.surf_key + s);
   case kSphere: {
     const double ox = dsub(x, __ldg(p)), oy = dsub(y, __ldg(p + 1)), oz = dsub(z, __ldg(p + 2));
     const double r = __ldg(p + 3);
@@ -287,11 +355,15 @@ __device__ __forceinline__ bool surface_contains(const DevWorld& w, int s, doubl
   }
 }
 
+__device__ __forceinline__ bool surface_contains(const DevWorld& w, int s, double x, double y, double z) {
+  return surface_contains(w, s, PointK(x, y, z));
+}
+
 // Cell::Contains (src/Cell.cpp:27-35)
-__device__ __forceinline__ bool cell_contains(const DevWorld& w, int c, double x, double y, double z) {
+__device__ __forceinline__ bool cell_contains(const DevWorld& w, int c, const PointK& q) {
   const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
   for (int k = b; k < e; k++) {
-    const bool inside = surface_contains(w, __ldg(w.cell_surf + k), x, y, z);
+    const bool inside = surface_contains(w, __ldg(w.cell_surf + k), q);
     if (inside != (__ldg(w.cell_within + k) != 0)) return false;
   }
   return true;
@@ -299,9 +371,44 @@ __device__ __forceinline__ bool cell_contains(const DevWorld& w, int c, double x
 
 // World::FindCellContaining (src/World.cpp:26-37): first match in XML order
 __device__ __forceinline__ int find_cell(const DevWorld& w, double x, double y, double z) {
+  const PointK q(x, y, z);
   for (int c = 0; c < w.n_cells; c++)
-    if (cell_contains(w, c, x, y, z)) return c;
+    if (cell_contains(w, c, q)) return c;
   return -1;
+}
+
+// Cell::NearestSurface for a box cell: per axis only the plane ahead can have
+// a positive distance -- the high plane when moving up (the low one if the
+// point is below it), the low plane when moving down (the high one if above
+// it) -- so one exact division per axis.  Ties keep the reference's order:
+// the earliest surface in the cell's list wins, and with every distance
+// infinite the cell's first surface is returned.
+__device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, int c, const double* pos,
+                                                   const double* dir, double& dist, int skip) {
+  const BoxCell& B = w.boxes[box];
+  int best_s = __ldg(w.cell_surf + __ldg(w.cell_begin + c));
+  int best_o = 0x7fffffff;
+  double bd = CUDART_INF;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double p = pos[a], d = dir[a];
+    const double clo = __ldg(&B.c[2 * a]), chi = __ldg(&B.c[2 * a + 1]);
+    const bool hi = d > 0 ? !(p < clo) : (p > chi);
+    int j = 2 * a + (hi ? 1 : 0);
+    // the skipped surface reads as infinitely far; the axis' other plane
+    // then is the only candidate
+    if (__ldg(&B.s[j]) == skip) j ^= 1;
+    const int s = __ldg(&B.s[j]);
+    const int o = __ldg(&B.order[j]);
+    const double t = s == skip ? CUDART_INF : plane_distance(p, d, __ldg(&B.c[j]));
+    if (t < bd || (t == bd && t != CUDART_INF && o < best_o)) {
+      bd = t;
+      best_s = s;
+      best_o = o;
+    }
+  }
+  dist = bd;
+  return best_s;
 }
 
 // Cell::NearestSurface (src/Cell.cpp:37-51): first surface (in the cell's
@@ -310,6 +417,11 @@ __device__ __forceinline__ int find_cell(const DevWorld& w, double x, double y, 
 // it is treated as infinitely far.
 __device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
                                                double v, double ww, double& dist, int skip = -1) {
+  const int box = __ldg(w.cell_box + c);
+  if (box >= 0) {
+    const double pos[3] = {x, y, z}, dir[3] = {u, v, ww};
+    return nearest_surface_box(w, box, c, pos, dir, dist, skip);
+  }
   const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
   int best = -1;
   double bd = CUDART_INF;
@@ -353,12 +465,13 @@ __device__ __forceinline__ bool moving_positive(const DevWorld& w, int s, double
 // World::FindCellContaining with the crossed surface's side forced
 __device__ __forceinline__ int find_cell_crossing(const DevWorld& w, double x, double y, double z, int crossed,
                                                   bool to_positive) {
+  const PointK q(x, y, z);
   for (int c = 0; c < w.n_cells; c++) {
     const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
     bool in = true;
     for (int k = b; k < e && in; k++) {
       const int s = __ldg(w.cell_surf + k);
-      const bool inside = s == crossed ? !to_positive : surface_contains(w, s, x, y, z);
+      const bool inside = s == crossed ? !to_positive : surface_contains(w, s, q);
       in = inside == (__ldg(w.cell_within + k) != 0);
     }
     if (in) return c;
@@ -383,20 +496,36 @@ __device__ __forceinline__ void isotropic(Rng& rng, double& u, double& v, double
 
 // isotropic direction with FP32 trigonometry, renormalized in FP64 by one
 // Newton step (fast-math streams only)
+// Every FP32 operation is an explicit round-to-nearest intrinsic or a
+// hardware approximation (__sincosf), so the result is the same in every
+// kernel that inlines it whatever the compiler contracts elsewhere.
 template <class Rng>
 __device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, double& w) {
-  const float mu = 2.0f * rng.u01f() - 1.0f;
+  const float mu = __fmaf_rn(2.0f, rng.u01f(), -1.0f);
   float s, c;
-  sincospif(2.0f * rng.u01f(), &s, &c);
-  const float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+  // phi in [-pi, pi): the hardware sine/cosine is accurate to ~2^-21 there
+  __sincosf(__fmul_rn(__fsub_rn(rng.u01f(), 0.5f), 6.28318530717958647692f), &s, &c);
+  const float st = __fsqrt_rn(fmaxf(0.0f, __fmaf_rn(-mu, mu, 1.0f)));
+  // unit to FP32 precision (|d|^2 = 1 +- 1e-7); plane distances do not
+  // depend on the norm and the robust crossing tolerates the ~1e-7 relative
+  // path-length error on curved surfaces
   u = mu;
-  v = st * c;
-  w = st * s;
-  const double n2 = u * u + v * v + w * w;
-  const double f = 1.5 - 0.5 * n2;
-  u *= f;
-  v *= f;
-  w *= f;
+  v = __fmul_rn(st, c);
+  w = __fmul_rn(st, s);
+}
+
+// exponential flight length in FP32: -log(U) / sigma (U in (0,1))
+__device__ __forceinline__ double flight_fast(float u, double sigma) {
+  return static_cast<double>(__fdiv_rn(-__logf(u), __double2float_rn(sigma)));
+}
+
+// first k in [0, n) with cdf[k] > threshold (both non-negative), or -1;
+// the comparison runs on the integer pipe (IEEE order of non-negative values)
+__device__ __forceinline__ int cdf_first_above(const double* cdf, int n, double threshold) {
+  const long long t = nonneg_bits(threshold);
+  for (int k = 0; k < n; k++)
+    if (__double_as_longlong(__ldg(cdf + k)) > t) return k;
+  return -1;
 }
 
 // Direction(d, mu, phi) (src/Point.cpp:98-121), normalized on assignment
@@ -483,6 +612,17 @@ __device__ __forceinline__ uint64_t particle_bin(const DevWorld& w, int e, doubl
   const int ek = __ldg(w.est_bin_kind + 2 * e + 1);
   const uint64_t esize = ek == 0 ? 1 : (ek == 3 ? static_cast<uint64_t>(__ldg(epar + 5)) + 1 : static_cast<uint64_t>(__ldg(epar)));
   return esize * ci + ei;
+}
+
+// multigroup form: the energy value is the group number, whose bin is
+// tabulated per group on the host with the same formulas
+__device__ __forceinline__ uint64_t particle_bin_mg(const DevWorld& w, int e, double u, double v, double ww, int g) {
+  uint64_t ci = 0;
+  if (__ldg(w.est_has_cos + e)) {
+    const double* d = w.est_cos_dir + 3 * e;
+    ci = bin_index(w, e, 0, dot3(__ldg(d), __ldg(d + 1), __ldg(d + 2), u, v, ww));
+  }
+  return __ldg(w.est_esize + e) * ci + static_cast<uint64_t>(__ldg(w.est_ebin_mg + e * w.G + g));
 }
 
 // Per-history pending scores (ScorableProxy::pending_scores,

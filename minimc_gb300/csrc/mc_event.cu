@@ -1,0 +1,617 @@
+// Event schedule: the particle-history loop split into event kernels over
+// compacted queues (SoA particle state in HBM).
+//
+//   init     : one thread per history; source sampling or bank load, cell
+//              search; live particles enter the active queue
+//   advance  : per active particle: Sigma_t lookup, distance to collision
+//              (exponential_distribution), Cell::NearestSurface, classify;
+//              crossings are relocated and scored here and re-queued,
+//              collisions go to the collision queue
+//              (SurfaceTracking::Transport, src/TransportMethod.cpp:56-75)
+//   collide  : per collision: Particle::SampleNuclide, Multigroup::Interact
+//              (src/Multigroup.cpp:49-73); survivors re-queued; fixed-source
+//              fission secondaries get new slots and join the queue;
+//              k-eigenvalue fissions are recorded for the site kernel
+//   sites    : k-eigenvalue fission sites generated from the recorded
+//              stream position (Multigroup::Fission, src/Multigroup.cpp:267-286)
+//   commit   : per-history pending scores -> sums and sums of squares
+//              (ScorableProxy::CommitHistory, src/Scorable.cpp:101-106)
+//
+// Queue slots are appended with one atomic per warp (ballot + popc).  Every
+// particle's random stream is saved as one word between kernels and resumed
+// exactly, so the event and history schedules draw identical numbers and give
+// identical results for the same seed.
+#include "mc_event.cuh"
+
+#include <type_traits>
+
+namespace mcd {
+
+namespace {
+
+constexpr int kMaxSec = 8;  // fixed-source secondaries per fission kept in registers
+
+__device__ __forceinline__ unsigned lane() { return threadIdx.x & 31u; }
+
+// warp-aggregated append of `want` lanes to a queue; returns the slot
+__device__ __forceinline__ unsigned queue_slot(unsigned* counter, bool want) {
+  const unsigned active = __activemask();
+  const unsigned mask = __ballot_sync(active, want);
+  if (!mask) return 0;
+  const int leader = __ffs(mask) - 1;
+  unsigned base = 0;
+  if (lane() == static_cast<unsigned>(leader)) base = atomicAdd(counter, static_cast<unsigned>(__popc(mask)));
+  base = __shfl_sync(active, base, leader);
+  return base + __popc(mask & ((1u << lane()) - 1u));
+}
+
+template <class Rng>
+__device__ __forceinline__ void load_rng(const EvParams& ep, unsigned i, Rng& rng) {
+  rng.restore(ep.rp.run_key, ep.st.id[i], ep.st.tag[i] & 1u, ep.st.rng[i]);
+}
+
+template <class Rng>
+__device__ __forceinline__ double uni(Rng& rng, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return static_cast<double>(rng.u01f());
+  }
+  return rng.u01();
+}
+
+template <class Rng>
+__device__ __forceinline__ void iso(Rng& rng, double& u, double& v, double& w, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) {
+      isotropic_fast(rng, u, v, w);
+      return;
+    }
+  }
+  isotropic(rng, u, v, w);
+}
+
+__device__ __forceinline__ int first_above(const double* cdf, int n, double threshold) {
+  return cdf_first_above(cdf, n, threshold);
+}
+
+// particle death bookkeeping shared by all kernels
+__device__ __forceinline__ void particle_died(const EvParams& ep, unsigned i, int event) {
+  const unsigned h = ep.st.hist[i];
+  if (ep.rp.hist_events) atomicAdd(ep.rp.hist_events + h, ep.st.nev[i]);
+  if (ep.rp.hist_fate && !(ep.st.tag[i] & 1u)) ep.rp.hist_fate[h] = static_cast<int8_t>(event);
+}
+
+__device__ __forceinline__ void pend_add(const EvParams& ep, unsigned h, uint64_t bin, double s) {
+  atomicAdd(ep.rp.pend + static_cast<size_t>(h) * ep.rp.nb + bin, s);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+template <class Rng>
+__global__ void __launch_bounds__(256) k_ev_init(const DevWorld w, const EvParams ep) {
+  const unsigned long long n = ep.rp.n;
+  const bool fast = ep.rp.fast != 0;
+  unsigned long long lost = 0;
+  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    double x, y, z, u, v, ww;
+    int g = 0;
+    Rng rng;
+    unsigned long long id = i;
+    uint8_t tag = 0;
+    if (ep.rp.from_bank) {
+      const Site& s = ep.rp.src[i];
+      x = s.x; y = s.y; z = s.z; u = s.u; v = s.v; ww = s.w;
+      g = static_cast<int>(s.energy) - 1;
+      if constexpr (std::is_same_v<Rng, MinstdRng>) {
+        rng.seed(ep.rp.minstd_base ? ep.rp.minstd_base + i : s.key);
+      }
+      else {
+        if (!ep.rp.minstd_base) {
+          id = s.key;
+          tag = 1;
+        }
+        rng.init(ep.rp.run_key, id, tag);
+      }
+    }
+    else {
+      x = w.src_pos[0]; y = w.src_pos[1]; z = w.src_pos[2];
+      tag = w.src_type == 1 ? 2 : 0;
+      if constexpr (std::is_same_v<Rng, MinstdRng>) {
+        MinstdRng s;
+        s.seed(ep.rp.ref_source_seeds ? ep.rp.seed + i : i + 1);
+        if (w.src_dir_kind == 0) { u = w.src_dir[0]; v = w.src_dir[1]; ww = w.src_dir[2]; }
+        else if (w.src_dir_kind == 1) isotropic(s, u, v, ww);
+        else {
+          const double mu = __dsqrt_rn(s.u01());
+          const double phi = dadd(dmul(s.u01(), 2 * kPi), 0.0);
+          u = w.src_dir[0]; v = w.src_dir[1]; ww = w.src_dir[2];
+          rotate(u, v, ww, mu, phi);
+        }
+        rng.seed(s.next());
+      }
+      else {
+        rng.init(ep.rp.run_key, i, 0);
+        if (w.src_dir_kind == 0) { u = w.src_dir[0]; v = w.src_dir[1]; ww = w.src_dir[2]; }
+        else if (w.src_dir_kind == 1) iso(rng, u, v, ww, fast);
+        else {
+          const double mu = sqrt(rng.u01());
+          const double phi = 2 * kPi * rng.u01();
+          u = w.src_dir[0]; v = w.src_dir[1]; ww = w.src_dir[2];
+          rotate(u, v, ww, mu, phi);
+        }
+      }
+      g = static_cast<int>(w.src_energy) - 1;
+    }
+    const int cell = find_cell(w, x, y, z);
+    const unsigned slot = static_cast<unsigned>(i);
+    ep.st.x[slot] = x; ep.st.y[slot] = y; ep.st.z[slot] = z;
+    ep.st.u[slot] = u; ep.st.v[slot] = v; ep.st.w[slot] = ww;
+    ep.st.g[slot] = g;
+    ep.st.cell[slot] = cell;
+    ep.st.skip[slot] = -1;
+    ep.st.nev[slot] = 0;
+    ep.st.hist[slot] = slot;
+    ep.st.id[slot] = id;
+    ep.st.tag[slot] = tag;
+    ep.st.rng[slot] = rng.save();
+    if (ep.rp.keig) ep.rp.fis[slot].n = 0;
+    const bool ok = cell >= 0 && __ldg(w.cell_mat + cell) >= 0;
+    if (!ok) {
+      lost++;
+      ep.rp.ctr->lost_xyz[0] = x;
+      ep.rp.ctr->lost_xyz[1] = y;
+      ep.rp.ctr->lost_xyz[2] = z;
+      if (ep.rp.hist_fate) ep.rp.hist_fate[slot] = kLostEvent;
+      if (ep.rp.hist_events) ep.rp.hist_events[slot] = 0;
+    }
+    else if (ep.rp.hist_events) {
+      ep.rp.hist_events[slot] = 0;
+    }
+    const unsigned q = queue_slot(ep.cnt + 1, ok);
+    if (ok) ep.q_out[q] = static_cast<int32_t>(slot);
+  }
+  if (lost) atomicAdd(&ep.rp.ctr->lost, lost);
+}
+
+// ---------------------------------------------------------------------------
+template <class Rng>
+__global__ void __launch_bounds__(256) k_ev_advance_mg(const DevWorld w, const EvParams ep) {
+  const unsigned n_in = ep.cnt[0];
+  const bool fast = ep.rp.fast != 0;
+  unsigned long long my_events = 0, my_lost = 0, my_capped = 0;
+  double my_ktl = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
+    if (__all_sync(0xffffffffu, k >= n_in)) break;
+    const int32_t qi = k < n_in ? ep.q_in[k] : -1;  // -1: slot lost to an overflow
+    const bool have = qi >= 0;
+    bool to_coll = false, to_next = false;
+    unsigned i = 0;
+    if (have) {
+      i = static_cast<unsigned>(qi);
+      Rng rng;
+      load_rng(ep, i, rng);
+      double x = ep.st.x[i], y = ep.st.y[i], z = ep.st.z[i];
+      const double u = ep.st.u[i], v = ep.st.v[i], ww = ep.st.w[i];
+      const int g = ep.st.g[i];
+      int cell = ep.st.cell[i];
+      int skip = ep.st.skip[i];
+      const unsigned h = ep.st.hist[i];
+      const int t = (ep.st.tag[i] >> 1) & 1;
+      const int m = __ldg(w.cell_mat + cell);
+      const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * w.G + g;
+      const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
+      double dcol;
+      if (fast) {
+        if constexpr (std::is_same_v<Rng, PhiloxRng>) dcol = flight_fast(rng.u01f(), sigma);
+        else dcol = flight_fast(static_cast<float>(rng.u01()), sigma);
+      }
+      else dcol = ddiv(-log(dsub(1.0, rng.u01())), sigma);
+      double dsurf;
+      const int s = nearest_surface(w, cell, x, y, z, u, v, ww, dsurf, skip);
+      const bool collide = w.tracking == 1 ? !(dsurf < dcol) : (dcol < dsurf);
+      const bool score = ep.rp.score != 0;
+      auto track = [&](double d) {
+        if (ep.rp.keig) my_ktl += d * __ldg(w.mat_mg_nusigf + mg);
+        if (!score) return;
+        for (int e = 0; e < w.n_est; e++) {
+          if (__ldg(w.est_kind + e) != 1 || __ldg(w.est_target + e) != cell) continue;
+          pend_add(ep, h, __ldg(w.est_offset + e) + particle_bin_mg(w, e, u, v, ww, g), d);
+        }
+      };
+      int event;
+      if (collide) {
+        track(dcol);
+        x = dadd(x, dmul(u, dcol));
+        y = dadd(y, dmul(v, dcol));
+        z = dadd(z, dmul(ww, dcol));
+        skip = -1;
+        to_coll = true;
+        event = kScatter;  // placeholder; the collide kernel decides
+      }
+      else if (__ldg(w.surf_refl + s)) {
+        track(dsurf);
+        x = dadd(x, dmul(u, dsurf));
+        y = dadd(y, dmul(v, dsurf));
+        z = dadd(z, dmul(ww, dsurf));
+        const int kind = __ldg(w.surf_kind + s);
+        double nu = u, nv = v, nw = ww;
+        if (kind == kPlaneX) nu = -u;
+        else if (kind == kPlaneY) nv = -v;
+        else nw = -ww;
+        ep.st.u[i] = nu;
+        ep.st.v[i] = nv;
+        ep.st.w[i] = nw;
+        skip = s;
+        event = kReflect;
+        to_next = true;
+      }
+      else {
+        const double d = dadd(dsurf, kNudge);
+        track(d);
+        x = dadd(x, dmul(u, d));
+        y = dadd(y, dmul(v, d));
+        z = dadd(z, dmul(ww, d));
+        if (w.quirks) {
+          cell = find_cell(w, x, y, z);
+        }
+        else {
+          cell = find_cell_crossing(w, x, y, z, s, moving_positive(w, s, x, y, z, u, v, ww));
+          skip = s;
+        }
+        if (cell < 0) {
+          event = kLostEvent;
+          my_lost++;
+          ep.rp.ctr->lost_xyz[0] = x;
+          ep.rp.ctr->lost_xyz[1] = y;
+          ep.rp.ctr->lost_xyz[2] = z;
+        }
+        else {
+          event = __ldg(w.cell_mat + cell) >= 0 ? kSurfaceCross : kLeak;
+        }
+        if (score && (event == kSurfaceCross || event == kLeak)) {
+          for (int e = 0; e < w.n_est; e++) {
+            if (__ldg(w.est_kind + e) != 0 || __ldg(w.est_target + e) != s) continue;
+            pend_add(ep, h, __ldg(w.est_offset + e) + particle_bin_mg(w, e, u, v, ww, g), 1.0);
+          }
+        }
+        to_next = event == kSurfaceCross;
+      }
+      const uint32_t nev = ep.st.nev[i] + 1;
+      my_events++;
+      ep.st.x[i] = x;
+      ep.st.y[i] = y;
+      ep.st.z[i] = z;
+      ep.st.cell[i] = cell;
+      ep.st.skip[i] = skip;
+      ep.st.nev[i] = nev;
+      ep.st.rng[i] = rng.save();
+      if (!to_coll && !to_next) {
+        particle_died(ep, i, event);
+      }
+      else if (to_next && nev >= ep.rp.max_events) {
+        to_next = false;
+        my_capped++;
+        particle_died(ep, i, kLostEvent);
+      }
+    }
+    const unsigned qc = queue_slot(ep.cnt + 2, to_coll);
+    if (to_coll) ep.q_coll[qc] = static_cast<int32_t>(i);
+    const unsigned qn = queue_slot(ep.cnt + 1, to_next);
+    if (to_next) ep.q_out[qn] = static_cast<int32_t>(i);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    my_events += __shfl_down_sync(0xffffffffu, my_events, off);
+    my_lost += __shfl_down_sync(0xffffffffu, my_lost, off);
+    my_capped += __shfl_down_sync(0xffffffffu, my_capped, off);
+    my_ktl += __shfl_down_sync(0xffffffffu, my_ktl, off);
+  }
+  if (lane() == 0) {
+    if (my_events) atomicAdd(&ep.rp.ctr->events, my_events);
+    if (my_lost) atomicAdd(&ep.rp.ctr->lost, my_lost);
+    if (my_capped) atomicAdd(&ep.rp.ctr->capped, my_capped);
+    if (my_ktl != 0) atomicAdd(&ep.rp.ctr->k_tracklength, my_ktl);
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <class Rng>
+__global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const EvParams ep) {
+  const unsigned n_in = ep.cnt[2];
+  const bool fast = ep.rp.fast != 0;
+  const int G = w.G;
+  unsigned long long my_overflow = 0, my_sec = 0, my_capped = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
+    const bool have = k < n_in;
+    if (__all_sync(0xffffffffu, !have)) break;
+    bool to_next = false;
+    int n_sec = 0;
+    unsigned i = 0;
+    Site sec[kMaxSec];
+    if (have) {
+      i = static_cast<unsigned>(ep.q_coll[k]);
+      Rng rng;
+      load_rng(ep, i, rng);
+      const int t = (ep.st.tag[i] >> 1) & 1;
+      const int cell = ep.st.cell[i];
+      const int m = __ldg(w.cell_mat + cell);
+      int g = ep.st.g[i];
+      const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * G + g;
+      const double micro = __ldg(w.mat_mg_total + mg);
+      // CellDeltaTracking's real/virtual test; multigroup majorant == total
+      if (w.tracking == 1) (void)uni(rng, fast);
+      const double thr_n = dmul(micro, uni(rng, fast));
+      const int nb = __ldg(w.mat_begin + m), ne = __ldg(w.mat_begin + m + 1);
+      int kn = first_above(w.mat_mg_nuc_cdf + mg * w.max_mat_nuc, ne - nb, thr_n);
+      if (kn < 0) kn = ne - nb - 1;
+      const int nuc = __ldg(w.mat_nuc + nb + kn);
+      const size_t ng = (static_cast<size_t>(t) * w.n_nuclides + nuc) * G + g;
+      const double thr_r = dmul(uni(rng, fast), __ldg(w.mg_total + ng));
+      const int rx = first_above(w.mg_rx_cdf + ng * 3, 3, thr_r);
+      int event = kScatter;
+      if (rx < 0) {
+        // no reaction selected (threshold at the top of the CDF): the
+        // reference's Interact falls through without touching the particle
+        // (src/Multigroup.cpp:70-72, assert compiled out), so it flies on
+        to_next = true;
+      }
+      else if (rx == 0) {
+        event = kCapture;
+      }
+      else if (rx == 1) {
+        const double thr = uni(rng, fast);
+        const int go = first_above(w.mg_scat_cdf + ng * G, G, thr);
+        if (go >= 0) {
+          g = go;
+          double u, v, ww;
+          iso(rng, u, v, ww, fast);
+          ep.st.u[i] = u;
+          ep.st.v[i] = v;
+          ep.st.w[i] = ww;
+          ep.st.g[i] = g;
+        }
+        to_next = true;
+      }
+      else if (rx == 2) {
+        event = kFission;
+        const double nubar = __ldg(w.mg_nubar + ng);
+        const unsigned yield = static_cast<unsigned>(dadd(nubar, uni(rng, fast)));
+        if (ep.rp.keig) {
+          FissionRec& f = ep.rp.fis[ep.st.hist[i]];
+          f.x = ep.st.x[i];
+          f.y = ep.st.y[i];
+          f.z = ep.st.z[i];
+          f.g = g;
+          f.n = yield;
+          f.rng = rng.save();
+          f.tag = ep.st.tag[i];
+          f.id = ep.st.id[i];
+          f.chi_index = static_cast<uint32_t>(ng);
+        }
+        else {
+          // secondaries, sampled now in the reference's draw order
+          const double* chi = w.mg_chi_cdf + ng * G;
+          for (unsigned y = 0; y < yield; y++) {
+            const double thr = uni(rng, fast);
+            const int go = first_above(chi, G, thr);
+            if (go < 0) continue;
+            Site s;
+            iso(rng, s.u, s.v, s.w, fast);
+            s.energy = go;
+            s.key = rng.child_key();
+            if (n_sec < kMaxSec) sec[n_sec++] = s;
+            else my_overflow++;
+          }
+        }
+      }
+      ep.st.rng[i] = rng.save();
+      if (!to_next) particle_died(ep, i, event);
+    }
+    const unsigned qn = queue_slot(ep.cnt + 1, to_next);
+    if (to_next) ep.q_out[qn] = static_cast<int32_t>(i);
+    // fixed-source secondaries: new slots, same history, into the next queue
+    const unsigned total_sec = __reduce_add_sync(0xffffffffu, static_cast<unsigned>(n_sec));
+    if (total_sec) {
+      unsigned base = 0;
+      unsigned excl = n_sec;
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned yv = __shfl_up_sync(0xffffffffu, excl, off);
+        if (lane() >= static_cast<unsigned>(off)) excl += yv;
+      }
+      excl -= n_sec;
+      if (lane() == 0) base = atomicAdd(ep.cnt + 3, total_sec);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      unsigned qbase = 0;
+      if (lane() == 0) qbase = atomicAdd(ep.cnt + 1, total_sec);
+      qbase = __shfl_sync(0xffffffffu, qbase, 0);
+      for (int s = 0; s < n_sec; s++) {
+        const unsigned slot = base + excl + s;
+        if (slot >= ep.capacity) {
+          my_overflow++;
+          ep.q_out[qbase + excl + s] = -1;
+          continue;
+        }
+        ep.st.x[slot] = ep.st.x[i];
+        ep.st.y[slot] = ep.st.y[i];
+        ep.st.z[slot] = ep.st.z[i];
+        ep.st.u[slot] = sec[s].u;
+        ep.st.v[slot] = sec[s].v;
+        ep.st.w[slot] = sec[s].w;
+        ep.st.g[slot] = static_cast<int>(sec[s].energy);
+        ep.st.cell[slot] = ep.st.cell[i];
+        ep.st.skip[slot] = -1;
+        ep.st.nev[slot] = 0;
+        ep.st.hist[slot] = ep.st.hist[i];
+        ep.st.tag[slot] = 1;
+        if constexpr (std::is_same_v<Rng, MinstdRng>) {
+          ep.st.id[slot] = 0;
+          ep.st.rng[slot] = MinstdRng::seed_state(sec[s].key);
+        }
+        else {
+          ep.st.id[slot] = sec[s].key;
+          ep.st.rng[slot] = 4u;  // counter 0, buffer empty
+        }
+        ep.q_out[qbase + excl + s] = static_cast<int32_t>(slot);
+        my_sec++;
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    my_overflow += __shfl_down_sync(0xffffffffu, my_overflow, off);
+    my_sec += __shfl_down_sync(0xffffffffu, my_sec, off);
+    my_capped += __shfl_down_sync(0xffffffffu, my_capped, off);
+  }
+  if (lane() == 0) {
+    if (my_overflow) atomicAdd(&ep.rp.ctr->overflow, my_overflow);
+    if (my_sec) atomicAdd(&ep.rp.ctr->secondaries, my_sec);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k-eigenvalue fission sites from the recorded stream positions
+// (Multigroup::Fission, src/Multigroup.cpp:267-286: per site a chi group,
+// an isotropic direction, then rng() seeds the secondary)
+template <class Rng>
+__global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, const RunParams rp) {
+  const unsigned long long n = rp.n;
+  const bool fast = rp.fast != 0;
+  const int G = w.G;
+  unsigned long long my_overflow = 0;
+  for (unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; h < n;
+       h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const FissionRec f = rp.fis[h];
+    uint32_t written = 0;
+    if (f.n) {
+      Rng rng;
+      rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
+      // chi column of the fissioning (type, nuclide, incident group)
+      const double* chi = w.mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
+      Site* slots = rp.bank + h * rp.max_yield;
+      for (uint32_t y = 0; y < f.n; y++) {
+        const double thr = uni(rng, fast);
+        const int go = first_above(chi, G, thr);
+        if (go < 0) continue;
+        Site s;
+        iso(rng, s.u, s.v, s.w, fast);
+        s.x = f.x;
+        s.y = f.y;
+        s.z = f.z;
+        s.energy = static_cast<double>(go + 1);
+        s.key = rng.child_key();
+        if (written < rp.max_yield) slots[written++] = s;
+        else my_overflow++;
+      }
+    }
+    rp.bank_count[h] = written;
+  }
+  if (my_overflow) atomicAdd(&rp.ctr->overflow, my_overflow);
+}
+
+// ---------------------------------------------------------------------------
+// per-history dense scores -> sum, sum of squares
+// (ScorableProxy::CommitHistory, src/Scorable.cpp:101-106), reduced in shared
+// memory per block before one global atomic per bin
+__global__ void __launch_bounds__(256) k_commit_dense(const RunParams rp) {
+  __shared__ double ssum[kDenseBins], ssq[kDenseBins];
+  const int nb = rp.nb;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    ssum[b] = 0;
+    ssq[b] = 0;
+  }
+  __syncthreads();
+  for (unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; h < rp.n;
+       h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const double* p = rp.pend + h * nb;
+    for (int b = 0; b < nb; b++) {
+      const double v = p[b];
+      if (v != 0) {
+        atomicAdd(ssum + b, v);
+        atomicAdd(ssq + b, v * v);
+      }
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    if (ssum[b] != 0) atomicAdd(rp.tally_sum + b, ssum[b]);
+    if (ssq[b] != 0) atomicAdd(rp.tally_sq + b, ssq[b]);
+  }
+}
+
+cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid,
+                                    cudaStream_t stream) {
+  if (rng_mode == 1) k_fission_sites_mg<MinstdRng><<<grid, 256, 0, stream>>>(w, rp);
+  else k_fission_sites_mg<PhiloxRng><<<grid, 256, 0, stream>>>(w, rp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream) {
+  k_commit_dense<<<grid, 256, 0, stream>>>(rp);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// launches
+
+// next-queue count becomes the input count of the following iteration
+__global__ void k_ev_swap(unsigned* cnt) {
+  cnt[0] = cnt[1];
+  cnt[1] = 0;
+  cnt[2] = 0;
+}
+
+__global__ void k_ev_reset(unsigned* cnt, unsigned slots) {
+  cnt[0] = 0;
+  cnt[1] = 0;
+  cnt[2] = 0;
+  cnt[3] = slots;
+}
+
+template <class Rng>
+static cudaError_t launch_all(const DevWorld& w, EvParams ep, const EvLaunch& L, cudaStream_t stream,
+                              EvStepHook hook, void* hook_ctx) {
+  const int block = 256;
+  cudaError_t e;
+  // slots [0, n) hold the histories' primaries; secondaries are appended
+  k_ev_reset<<<1, 1, 0, stream>>>(ep.cnt, static_cast<unsigned>(ep.rp.n));
+  // init appends the live primaries to the queue through cnt[1]
+  int32_t* qa = ep.q_in;
+  int32_t* qb = ep.q_out;
+  ep.q_out = qa;
+  k_ev_init<Rng><<<L.grid, block, 0, stream>>>(w, ep);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (hook) hook(hook_ctx, 2);
+  // qa holds the live set.  Each iteration: swap counts on the device,
+  // advance + collide from qa into qb, swap the queue pointers on the host.
+  // The host reads the queue size only every check_every iterations.
+  unsigned* pinned = nullptr;
+  unsigned host_count = 1;
+  for (unsigned iter = 0; iter < L.max_iterations; iter++) {
+    k_ev_swap<<<1, 1, 0, stream>>>(ep.cnt);
+    ep.q_in = qa;
+    ep.q_out = qb;
+    k_ev_advance_mg<Rng><<<L.grid, block, 0, stream>>>(w, ep);
+    k_ev_collide_mg<Rng><<<L.grid, block, 0, stream>>>(w, ep);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (hook) hook(hook_ctx, 3);
+    std::swap(qa, qb);
+    if ((iter + 1) % L.check_every == 0) {
+      e = cudaMemcpyAsync(&host_count, ep.cnt + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
+      if (e != cudaSuccess) return e;
+      if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+      if (host_count == 0) break;
+    }
+  }
+  (void)pinned;
+  if (host_count != 0) return cudaErrorLaunchTimeout;  // the iteration cap was reached
+  // fission sites and the score commit are launched by the caller, after it
+  // has checked the particle store did not overflow
+  return cudaSuccess;
+}
+
+cudaError_t launch_event_mg(const DevWorld& w, const EvParams& ep, const EvLaunch& L, int rng_mode,
+                            cudaStream_t stream, EvStepHook hook, void* hook_ctx) {
+  if (rng_mode == 1) return launch_all<MinstdRng>(w, ep, L, stream, hook, hook_ctx);
+  return launch_all<PhiloxRng>(w, ep, L, stream, hook, hook_ctx);
+}
+
+}  // namespace mcd

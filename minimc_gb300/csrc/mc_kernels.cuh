@@ -11,6 +11,23 @@ struct Site {
   unsigned long long key;
 };
 
+// a k-eigenvalue fission: where, the incident group and the stream
+// position right after the yield draw, from which the sites are generated
+// by a separate kernel (keeps the per-site sampling out of the transport loop)
+struct FissionRec {
+  double x, y, z;
+  int32_t g;
+  uint32_t n;
+  uint32_t rng;
+  uint32_t tag;
+  unsigned long long id;
+  uint32_t chi_index;  // (type, nuclide, incident group) row of the chi table
+  uint32_t pad;
+};
+
+// most tally bins kept densely per history; more bins use a per-thread list
+constexpr int kDenseBins = 64;
+
 struct RunParams {
   unsigned long long n;        // source particles (histories)
   unsigned long long seed;     // run seed
@@ -33,7 +50,16 @@ struct RunParams {
   uint32_t* hist_events;
   int8_t* hist_fate;
   DevCounters* ctr;
+  double* pend;        // dense per-history scores [n][nb] when nb <= kDenseBins
+  int32_t nb;
+  FissionRec* fis;     // k-eigenvalue fission records [n]
 };
+
+// k-eigenvalue sites from fission records and the per-history commit of
+// dense scores (mc_event.cu)
+cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid,
+                                    cudaStream_t stream);
+cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream);
 
 // launches (mc_transport.cu)
 cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
@@ -59,6 +85,8 @@ cudaError_t launch_surface_distance(const DevWorld& w, int32_t s, const double* 
                                     unsigned long long n, double* dist, cudaStream_t stream);
 cudaError_t launch_surface_contains(const DevWorld& w, int32_t s, const double* xyz, unsigned long long n,
                                     int8_t* out, cudaStream_t stream);
+cudaError_t launch_material_xs_mg(const DevWorld& w, int32_t cell, const double* energy, unsigned long long n,
+                                  double* total, double* majorant, cudaStream_t stream);
 
 // Philox helper shared with the host-side resampler description
 __host__ __device__ inline unsigned long long splitmix64(unsigned long long z) {

@@ -44,6 +44,20 @@ __global__ void k_surface_contains(const DevWorld w, int32_t s, const double* xy
   out[i] = surface_contains(w, s, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) ? 1 : 0;
 }
 
+// Material::GetMicroscopicTotal / GetMicroscopicMajorant for a neutron in
+// `cell` (multigroup: energy holds the group number)
+__global__ void k_material_xs_mg(const DevWorld w, int32_t cell, const double* energy, unsigned long long n,
+                                 double* total, double* majorant) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int m = __ldg(w.cell_mat + cell);
+  const int g = static_cast<int>(energy[i]) - 1;
+  double t = 0;
+  if (m >= 0 && g >= 0 && g < w.G) t = __ldg(w.mat_mg_total + static_cast<size_t>(m) * w.G + g);
+  total[i] = t;
+  majorant[i] = t;  // Multigroup::GetMajorant returns the total
+}
+
 unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
 
 }  // namespace
@@ -73,6 +87,13 @@ cudaError_t launch_surface_contains(const DevWorld& w, int32_t s, const double* 
                                     int8_t* out, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   k_surface_contains<<<blocks_for(n), 256, 0, stream>>>(w, s, xyz, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_material_xs_mg(const DevWorld& w, int32_t cell, const double* energy, unsigned long long n,
+                                  double* total, double* majorant, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_material_xs_mg<<<blocks_for(n), 256, 0, stream>>>(w, cell, energy, n, total, majorant);
   return cudaGetLastError();
 }
 

@@ -128,7 +128,7 @@ __device__ __forceinline__ double uniform(Rng& rng, bool fast) {
 template <class Rng>
 __device__ __forceinline__ double sample_flight(Rng& rng, double sigma, bool fast) {
   if constexpr (std::is_same_v<Rng, PhiloxRng>) {
-    if (fast) return static_cast<double>(-__logf(rng.u01f()) / static_cast<float>(sigma));
+    if (fast) return flight_fast(rng.u01f(), sigma);
   }
   return ddiv(-log(dsub(1.0, rng.u01())), sigma);
 }
@@ -145,10 +145,8 @@ __device__ __forceinline__ void sample_isotropic(Rng& rng, double& u, double& v,
 }
 
 // first index k in [0, n) with cdf[k] > threshold, or -1
-__device__ __forceinline__ int cdf_search(const double* cdf, int n, int stride, double threshold) {
-  for (int k = 0; k < n; k++)
-    if (__ldg(cdf + k * stride) > threshold) return k;
-  return -1;
+__device__ __forceinline__ int cdf_search(const double* cdf, int n, int, double threshold) {
+  return cdf_first_above(cdf, n, threshold);
 }
 
 // score helpers -----------------------------------------------------------
@@ -159,26 +157,36 @@ __device__ __forceinline__ double energy_value(const DevWorld& w, const Particle
   return w.energy_mode == 0 ? static_cast<double>(p.g + 1) : p.E;
 }
 
+// Per-history scores go to the history's row of a dense array (few bins,
+// committed by a separate kernel) or to a per-thread list (many bins).
+struct Scorer {
+  Pending<kPending>* list;
+  double* dense;
+  __device__ __forceinline__ void add(uint32_t b, double s) {
+    if (dense) atomicAdd(dense + b, s);
+    else list->add(b, s);
+  }
+};
+
 // EstimatorSetProxy::Score (src/Estimator.cpp:247-251) for the current
 // estimator (src/Estimator.cpp:142-151): 1 on a crossing of its surface
 template <class Rng>
-__device__ __forceinline__ void score_event(const DevWorld& w, const Particle<Rng>& p, Pending<kPending>& pend) {
+__device__ __forceinline__ void score_event(const DevWorld& w, const Particle<Rng>& p, Scorer& sc) {
   if (p.event != kSurfaceCross && p.event != kLeak) return;
   for (int e = 0; e < w.n_est; e++) {
     if (__ldg(w.est_kind + e) != 0 || __ldg(w.est_target + e) != p.surf) continue;
-    const uint64_t b = __ldg(w.est_offset + e) + particle_bin(w, e, p.u, p.v, p.w, energy_value(w, p));
-    pend.add(static_cast<uint32_t>(b), 1.0);
+    const uint64_t b = __ldg(w.est_offset + e) + particle_bin_mg(w, e, p.u, p.v, p.w, p.g);
+    sc.add(static_cast<uint32_t>(b), 1.0);
   }
 }
 
 // track-length estimator (extension): flight length inside the cell
 template <class Rng>
-__device__ __forceinline__ void score_track(const DevWorld& w, const Particle<Rng>& p, double d,
-                                            Pending<kPending>& pend) {
+__device__ __forceinline__ void score_track(const DevWorld& w, const Particle<Rng>& p, double d, Scorer& sc) {
   for (int e = 0; e < w.n_est; e++) {
     if (__ldg(w.est_kind + e) != 1 || __ldg(w.est_target + e) != p.cell) continue;
-    const uint64_t b = __ldg(w.est_offset + e) + particle_bin(w, e, p.u, p.v, p.w, energy_value(w, p));
-    pend.add(static_cast<uint32_t>(b), d);
+    const uint64_t b = __ldg(w.est_offset + e) + particle_bin_mg(w, e, p.u, p.v, p.w, p.g);
+    sc.add(static_cast<uint32_t>(b), d);
   }
 }
 
@@ -247,7 +255,7 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 template <class Rng, bool KEIG>
 __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunParams rp) {
   extern __shared__ double smem[];
-  const bool use_smem = rp.total_bins <= kSharedBins && rp.score;
+  const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
   if (use_smem) {
     for (int i = threadIdx.x; i < 2 * kSharedBins; i += blockDim.x) smem[i] = 0;
@@ -258,6 +266,7 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
   Particle<Rng> p;
   Pending<kPending> pend;
   pend.clear();
+  Scorer sc{&pend, nullptr};
   Site stack[KEIG ? 1 : kStack];
   int sp = 0;
   bool alive = false, done = false;
@@ -270,12 +279,11 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
 
   // history complete: ScorableProxy::CommitHistory (src/Scorable.cpp:101-106)
   auto finish_history = [&]() {
-    if (rp.score) {
+    if (rp.score && !rp.nb) {
       sink.commit(pend);
       if (pend.overflow) my_overflow++;
     }
     pend.clear();
-    if constexpr (KEIG) rp.bank_count[hist] = nbank;
     if (rp.hist_events) rp.hist_events[hist] = hist_nev;
     if (rp.hist_fate) rp.hist_fate[hist] = fate;
   };
@@ -306,6 +314,8 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
           fate = kBirth;
           nbank = 0;
           alive = true;
+          sc.dense = rp.nb ? rp.pend + hist * rp.nb : nullptr;
+          if constexpr (KEIG) rp.fis[hist].n = 0;
           if (p.cell < 0 || __ldg(w.cell_mat + p.cell) < 0) {
             // the reference throws (src/World.cpp:34-36) or dereferences a
             // void material; the GPU counts the particle as lost
@@ -331,15 +341,15 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
       const int m = __ldg(w.cell_mat + p.cell);
       const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * w.G + p.g;
       const double micro = __ldg(w.mat_mg_total + mg);
-      const double sigma = dmul(__ldg(w.mat_density + m), micro);
+      const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
       const double dcol = sample_flight(p.rng, sigma, fast);
       double dsurf;
       const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
       const bool delta = w.tracking == 1;
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
       if (collide) {
-        if (rp.score) score_track(w, p, dcol, pend);
-        if (KEIG) my_ktl += dcol * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+        if (rp.score) score_track(w, p, dcol, sc);
+        if (KEIG) my_ktl += dcol * __ldg(w.mat_mg_nusigf + mg);
         stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
         p.skip = -1;
         // multigroup majorant == total, so CellDeltaTracking's rejection
@@ -372,11 +382,27 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
         else if (rx == 2) {
           p.event = kFission;
           if constexpr (KEIG) {
-            Site* slots = rp.bank + hist * rp.max_yield;
-            mg_fission(w, p, t, nuc, fast, [&](const Site& st) {
-              if (nbank < rp.max_yield) slots[nbank++] = st;
-              else my_overflow++;
-            });
+            // record the fission; its sites are drawn by the sites kernel
+            // from the stream position after the yield draw
+            const unsigned yield = static_cast<unsigned>(dadd(__ldg(w.mg_nubar + ng), uniform(p.rng, fast)));
+            FissionRec f;
+            f.x = p.x;
+            f.y = p.y;
+            f.z = p.z;
+            f.g = p.g;
+            f.n = yield;
+            f.rng = p.rng.save();
+            if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+              f.tag = p.rng.tag;
+              f.id = static_cast<unsigned long long>(p.rng.h0) | (static_cast<unsigned long long>(p.rng.h1) << 32);
+            }
+            else {
+              f.tag = 0;
+              f.id = 0;
+            }
+            f.chi_index = static_cast<uint32_t>(ng);
+            f.pad = 0;
+            rp.fis[hist] = f;
           }
           else {
             mg_fission(w, p, t, nuc, fast, [&](const Site& st) {
@@ -392,8 +418,8 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
         if (refl) {
           // reflective boundary (extension): stop on the plane, mirror the
           // normal component, stay in the cell
-          if (rp.score) score_track(w, p, dsurf, pend);
-          if (KEIG) my_ktl += dsurf * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+          if (rp.score) score_track(w, p, dsurf, sc);
+          if (KEIG) my_ktl += dsurf * __ldg(w.mat_mg_nusigf + mg);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
           const int kind = __ldg(w.surf_kind + s);
           if (kind == kPlaneX) p.u = -p.u;
@@ -405,8 +431,8 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
         }
         else {
           const double d = dadd(dsurf, kNudge);
-          if (rp.score) score_track(w, p, d, pend);
-          if (KEIG) my_ktl += d * __ldg(w.mat_density + m) * __ldg(w.mat_mg_nusigf + mg);
+          if (rp.score) score_track(w, p, d, sc);
+          if (KEIG) my_ktl += d * __ldg(w.mat_mg_nusigf + mg);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, d);
           if (w.quirks) {
             p.cell = find_cell(w, p.x, p.y, p.z);
@@ -428,7 +454,7 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
           }
         }
       }
-      if (rp.score) score_event(w, p, pend);
+      if (rp.score) score_event(w, p, sc);
       p.nev++;
       hist_nev++;
       my_events++;

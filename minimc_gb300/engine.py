@@ -341,6 +341,15 @@ class Context:
         self.check(self.lib.mc_surface_distance(self.h, surface, _dptr(xyz), _dptr(uvw), len(xyz), _dptr(out)))
         return out
 
+    def material_xs(self, cell: int, energy) -> tuple[np.ndarray, np.ndarray]:
+        """Material::GetMicroscopicTotal / Majorant for neutrons in `cell`."""
+        e = _arr(np.atleast_1d(energy), np.float64)
+        tot = np.zeros(len(e))
+        maj = np.zeros(len(e))
+        xyz = np.zeros((len(e), 3))
+        self.check(self.lib.mc_material_xs(self.h, cell, _dptr(xyz), _dptr(e), len(e), _dptr(tot), _dptr(maj)))
+        return tot, maj
+
     def surface_contains(self, surface: int, xyz) -> np.ndarray:
         xyz = _arr(xyz, np.float64).reshape(-1, 3)
         out = np.zeros(len(xyz), np.int8)

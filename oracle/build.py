@@ -60,6 +60,10 @@ def load() -> C.CDLL:
         lib.orc_surface_contains.argtypes = [C.c_void_p, C.c_int32, _D, C.c_uint64, C.POINTER(C.c_int8)]
         lib.orc_philox.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32]
         lib.orc_minstd_canonical.argtypes = [C.c_uint64, C.c_uint64, _D]
+        lib.orc_rotate.argtypes = [_D, C.c_double, C.c_double, _D]
+        lib.orc_normalize.argtypes = [_D, _D]
+        lib.orc_material_total.restype = C.c_double
+        lib.orc_material_total.argtypes = [C.c_void_p, C.c_int32, C.c_uint64]
         lib.orc_run_fixed_source.restype = C.c_int
         lib.orc_run_fixed_source.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, _D, _D,
                                              C.POINTER(C.c_uint32), C.POINTER(C.c_int8), C.POINTER(OrcStats)]
@@ -92,7 +96,11 @@ class Oracle:
             self.h = None
 
     def set_quirks(self, q: bool):
+        """True: the reference's exact geometry semantics; False: robust."""
         self.lib.orc_set_quirks(self.h, int(q))
+
+    def material_total(self, cell: int, group: int) -> float:
+        return float(self.lib.orc_material_total(self.h, cell, group))
 
     def find_cell(self, xyz):
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
@@ -158,6 +166,20 @@ def philox(counter, key):
     c = (C.c_uint32 * 4)(*counter)
     load().orc_philox(c, key[0], key[1])
     return list(c)
+
+
+def rotate(d, mu: float, phi: float) -> np.ndarray:
+    d = np.ascontiguousarray(d, np.float64)
+    out = np.zeros(3)
+    load().orc_rotate(_d(d), mu, phi, _d(out))
+    return out
+
+
+def normalize(d) -> np.ndarray:
+    d = np.ascontiguousarray(d, np.float64)
+    out = np.zeros(3)
+    load().orc_normalize(_d(d), _d(out))
+    return out
 
 
 def minstd_canonical(seed: int, n: int) -> np.ndarray:

@@ -559,6 +559,31 @@ void orc_surface_contains(void* h, int32_t s, const double* xyz, uint64_t n, int
 
 void orc_philox(uint32_t* c, uint32_t k0, uint32_t k1) { philox(c, k0, k1); }
 
+// Direction(d, mu, phi) and Direction(x, y, z) (src/Point.cpp:98-129)
+void orc_rotate(const double* d, double mu, double phi, double* out) {
+  const Vec r = Rotate(Vec{d[0], d[1], d[2]}, mu, phi);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+}
+void orc_normalize(const double* d, double* out) {
+  const Vec r = Normalized(Vec{d[0], d[1], d[2]});
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+}
+
+// Material::GetMicroscopicTotal of a neutron of group g in cell c
+double orc_material_total(void* h, int32_t cell, uint64_t g) {
+  auto* o = static_cast<Oracle*>(h);
+  const int mat = o->m.cells.at(cell).material;
+  if (mat < 0) return 0;
+  Oracle::P p;
+  p.g = g;
+  p.type = 0;
+  return o->MaterialTotal(mat, p);
+}
+
 // minstd + generate_canonical values for a seed (RNG parity checks)
 void orc_minstd_canonical(uint64_t seed, uint64_t n, double* out) {
   RNG rng{static_cast<RNG::result_type>(seed)};

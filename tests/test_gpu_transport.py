@@ -1,0 +1,162 @@
+"""GPU transport parity, through the C ABI.
+
+* Reference streams (minstd): a GPU history draws the same random numbers as
+  the reference would, so fission banks (k per cycle), per-history event
+  counts and integer tallies equal the CPU oracle's exactly; floating-point
+  tallies agree to the last few ulps (summation order).
+* Philox streams: statistical agreement (k within 3 combined sigma) and
+  run-to-run / schedule-to-schedule reproducibility.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from minimc_gb300 import (GEOMETRY_REFERENCE, RNG_MINSTD, RNG_PHILOX, SCHEDULE_EVENT, SCHEDULE_HISTORY, Context,
+                          MCError, synth)
+from oracle.build import Oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+KA = json.loads((GOLDEN / "reference_known_answers.json").read_text())
+FP_RTOL = 1e-12  # floating-point tallies: summation order only
+
+
+def gpu_ctx(xml, mode=None):
+    ctx = Context(0)
+    if mode is not None:
+        ctx.set_geometry_mode(mode)
+    ctx.load_xml(xml)
+    return ctx
+
+
+@pytest.mark.parametrize("schedule", [SCHEDULE_HISTORY, SCHEDULE_EVENT])
+def test_keig_one_group_cube_identical_to_oracle(schedule, built_library):
+    p = synth.one_group_cube(histories=20000, inactive=5, active=10)
+    xml = p.xml()
+    g = gpu_ctx(xml).run_keigenvalue(rng=RNG_MINSTD, schedule=schedule)
+    o = Oracle(xml).run_keigenvalue(20000, 1, 5, 10, threads=8)
+    assert np.array_equal(g.bank_size, o["bank_size"])
+    assert np.array_equal(g.k_cycle, o["k_cycle"])
+    np.testing.assert_allclose(g.sum, o["sum"], rtol=FP_RTOL)
+    np.testing.assert_allclose(g.sum_sq, o["sum_sq"], rtol=FP_RTOL)
+
+
+def test_keig_two_zone_identical_to_oracle(built_library):
+    p = synth.two_zone_cubes(histories=50000, inactive=3, active=3)
+    xml = p.xml()
+    g = gpu_ctx(xml).run_keigenvalue(rng=RNG_MINSTD)
+    o = Oracle(xml).run_keigenvalue(50000, 1, 3, 3, threads=8)
+    assert np.array_equal(g.bank_size, o["bank_size"])
+    np.testing.assert_allclose(g.sum, o["sum"], rtol=FP_RTOL)
+
+
+@pytest.mark.parametrize("schedule", [SCHEDULE_HISTORY, SCHEDULE_EVENT])
+def test_fixed_source_with_secondaries_per_history(schedule, built_library):
+    """Fixed source in a fissile sphere: secondaries are transported inside
+    their history; per-history events and fates equal the oracle's."""
+    p = synth.one_group_cube(histories=20000)
+    p.problem = "fixedsource"
+    p.nuclides[0].nubar = np.array([0.9])  # subcritical
+    xml = p.xml()
+    n = 20000
+    g = gpu_ctx(xml).run_fixed_source(rng=RNG_MINSTD, per_history=True, histories=n, schedule=schedule)
+    o = Oracle(xml).run_fixed_source(n, 1, threads=8, per_history=True)
+    assert g.raw.secondaries == o["secondaries"] > 0
+    assert np.array_equal(g.history_events, o["history_events"])
+    assert np.array_equal(g.history_fate, o["history_fate"])
+    np.testing.assert_allclose(g.sum, o["sum"], rtol=FP_RTOL)
+
+
+def test_point_source_leakage_reference_test(built_library):
+    """The reference's statistical test (leakage = e^-1 within 3 sigma) on
+    both random streams; with minstd the count equals the oracle's."""
+    ka = KA["point_source_leakage"]
+    xml = (GOLDEN / "point_source_leakage.xml").read_text()
+    p, n = ka["expected"], ka["histories"]
+    o = Oracle(xml).run_fixed_source(n, 1)
+    for rng in (RNG_MINSTD, RNG_PHILOX):
+        r = gpu_ctx(xml).run_fixed_source(rng=rng)
+        est = r.sum[0] / n
+        assert abs(est - p) / p < 3 * math.sqrt((1 - p) / (p * n))
+        if rng == RNG_MINSTD:
+            assert r.sum[0] == o["sum"][0]
+
+
+def test_reference_geometry_mode_fixed_source(built_library):
+    xml = (GOLDEN / "mg_spheres.xml").read_text()
+    n = 50000
+    g = gpu_ctx(xml, GEOMETRY_REFERENCE).run_fixed_source(rng=RNG_MINSTD, per_history=True, histories=n)
+    oc = Oracle(xml)
+    oc.set_quirks(True)
+    o = oc.run_fixed_source(n, 1, threads=8, per_history=True)
+    agree = np.mean((g.history_events == o["history_events"]) & (g.history_fate == o["history_fate"]))
+    assert agree > 0.999  # libm ulps may move a grazing history
+    assert abs(g.sum[0] - o["sum"][0]) <= 0.001 * n
+
+
+def test_philox_keig_matches_oracle_statistically(built_library):
+    p = synth.one_group_cube(histories=20000, inactive=10, active=30)
+    xml = p.xml()
+    for fast in (0, 1):
+        g = gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=fast)
+        o = Oracle(xml).run_keigenvalue(20000, 1, 10, 30, threads=8)
+        kg, ko = g.k_cycle[10:], o["k_cycle"][10:]
+        sig = math.sqrt(kg.var(ddof=1) / len(kg) + ko.var(ddof=1) / len(ko))
+        assert abs(kg.mean() - ko.mean()) < 3 * sig + 1e-4, (fast, kg.mean(), ko.mean(), sig)
+
+
+def test_reflected_box_gives_k_inf(built_library):
+    p = synth.one_group_cube(histories=100000, inactive=5, active=20)
+    p.surfaces = synth.box_planes("cube", 10.0, reflective=True)
+    r = gpu_ctx(p.xml()).run_keigenvalue(rng=RNG_PHILOX, fast_math=1)
+    k = r.k_cycle[5:]
+    assert r.raw.lost == 0
+    assert k.mean() == pytest.approx(5 / 3, abs=4 * k.std(ddof=1) / math.sqrt(len(k)) + 2e-4)
+
+
+def test_philox_reproducible_and_schedule_independent(built_library):
+    p = synth.two_zone_cubes(histories=200000, inactive=2, active=2)
+    xml = p.xml()
+    runs = [gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=1, schedule=s)
+            for s in (SCHEDULE_HISTORY, SCHEDULE_HISTORY, SCHEDULE_EVENT)]
+    for r in runs[1:]:
+        assert np.array_equal(r.bank_size, runs[0].bank_size)
+        np.testing.assert_allclose(r.sum, runs[0].sum, rtol=FP_RTOL)
+
+
+def test_full_size_two_zone_invariants(built_library):
+    """1e6 histories per cycle: no lost particles, fission bank = sum of
+    per-history sites, tallies finite and non-negative, k in range."""
+    p = synth.two_zone_cubes(histories=1_000_000, inactive=2, active=2)
+    r = gpu_ctx(p.xml()).run_keigenvalue(rng=RNG_PHILOX, fast_math=1)
+    assert r.raw.lost == 0 and r.raw.overflow == 0 and r.raw.capped == 0
+    assert np.all(np.isfinite(r.sum)) and np.all(r.sum >= 0) and np.all(r.sum_sq >= 0)
+    assert np.all((r.k_cycle > 0.7) & (r.k_cycle < 1.3))
+    assert r.raw.events > 5 * 4 * 1_000_000
+
+
+def test_event_cap_reports_and_context_survives(built_library):
+    """Per-particle event cap: the run stops those particles, reports
+    MC_ERR_EVENT_CAP, and the context keeps working."""
+    xml = (GOLDEN / "infinite_medium.xml").read_text()
+    ctx = gpu_ctx(xml)
+    with pytest.raises(MCError) as e:
+        ctx.run_fixed_source(rng=RNG_PHILOX, histories=10000, max_events=1)
+    assert e.value.code == -9
+    r = ctx.run_fixed_source(rng=RNG_PHILOX, histories=10000)
+    assert r.raw.capped == 0 and r.raw.lost == 0
+
+
+def test_lost_particle_reported(built_library):
+    """A source outside every cell: the reference throws; the engine reports
+    MC_ERR_LOST with the reference's message."""
+    xml = (GOLDEN / "mg_spheres.xml").read_text().replace(
+        '<void><surface name="outer shell" sense="+1"/></void>', "").replace(
+        '<constant x="0" y="0" z="0"/>', '<constant x="5" y="0" z="0"/>')
+    ctx = gpu_ctx(xml)
+    with pytest.raises(MCError) as e:
+        ctx.run_fixed_source(rng=RNG_PHILOX, histories=100)
+    assert e.value.code == -5 and "Point does not belong to any Cell" in e.value.message
