@@ -189,11 +189,12 @@ def run_gpu(args) -> None:
     clocks = ClockSampler(local)
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    k_steps = []
     barrier()
     t_wall = time.perf_counter()
     for i in range(args.steps):
         ev[i][0].record(stream)
-        ctx.keig_cycle(True)
+        k_steps.append(ctx.keig_cycle(True))
         ev[i][1].record(stream)
         flush.zero_()  # L2 flush between timed steps (outside the event pair)
     barrier()
@@ -202,9 +203,10 @@ def run_gpu(args) -> None:
     st1 = ctx.keig_status()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
+    sched = ctx.schedule_info()
     k_out = ctx.keig_end()
     events = st1.events - st0.events
-    transport_ms = st1.transport_ms - st0.transport_ms
+    kernel_ms = st1.kernel_ms - st0.kernel_ms
     launches = st1.launches - st0.launches
     # max over ranks
     if dist is not None:
@@ -215,12 +217,14 @@ def run_gpu(args) -> None:
     e_h = events / (hist * args.steps)
     peak, peak_kind = peaks()
     alg_bytes = e_h * BYTES_PER_EVENT * hist  # per transport launch (one per step)
-    launch_ms = transport_ms / args.steps
+    launch_ms = kernel_ms / args.steps        # the transport kernel alone, CUDA events
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
-    traffic = None
+    traffic = fp64 = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("k_history_mg_per_launch_bytes")
+        prof = json.loads(tf.read_text())
+        traffic = prof.get("k_history_mg_dram_bytes_per_launch")
+        fp64 = prof.get("k_history_mg_fp64_pipe_active")
 
     # ---- end to end through the host-buffer ABI call
     n_sites = hist
@@ -245,7 +249,7 @@ def run_gpu(args) -> None:
     for i in range(args.warmup + args.steps):
         barrier()
         t0 = time.perf_counter()
-        m = ctx.transport_bank_into(src, bank)
+        m = ctx.transport_bank_into(src, bank, **opts)
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_times.append(t1 - t0)
@@ -270,13 +274,15 @@ def run_gpu(args) -> None:
             "config": {"workload": WORKLOAD, "histories_per_cycle": hist, "groups": 8, "rng": "philox",
                        "fast_math": bool(args.fast), "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas{ws}" if ws > 1 else "single GPU",
-                       "schedule": "history (fused)", "block": args.block},
-            "k_eff_last": float(k_out.k_mean) if k_out.k_mean else None,
+                       "schedule": sched},
+            "k_cycles": [round(k, 6) for k in k_steps],
             "events_per_history": e_h,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_history_mg", "algorithmic_bytes_per_launch": alg_bytes,
-                         "launch_ms": launch_ms},
+                         "launch_ms": launch_ms, "fp64_pipe_active_ncu": fp64,
+                         "note": "state lives in registers, so DRAM traffic is far below the algorithmic "
+                                 "bytes; the limiter is the FP64 pipe (2 ops/clk/SM on this part)"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(d2h_total / max(1, args.steps)),
@@ -297,8 +303,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--histories", type=int, default=1_000_000)
-    ap.add_argument("--block", type=int, default=256)
-    ap.add_argument("--fast", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0, help="0: autotuned")
+    ap.add_argument("--fast", type=int, default=1,
+                    help="FP32 sampling arithmetic (geometry, positions, k and tallies stay FP64)")
     ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 history, 2 event")
     ap.add_argument("--cpu-histories", type=int, default=1_000_000)
     ap.add_argument("--cpu-cycles", type=int, default=6)

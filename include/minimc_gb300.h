@@ -127,7 +127,8 @@ typedef struct {
   uint64_t lost, capped, overflow, resample_failures;
   double transport_ms;       /* device time of the transport kernels       */
   uint64_t launches;         /* kernels launched                           */
-  double reserved[4];
+  double kernel_ms;          /* device time of the main transport kernel    */
+  double reserved[3];
 } mc_tally_out;
 
 /* k-eigenvalue results.  k_cycle: caller-owned [inactive+active]; tallies
@@ -140,9 +141,10 @@ typedef struct {
   double k_mean, k_std;      /* over active cycles                          */
   double k_tracklength_mean; /* track-length estimate over active cycles    */
   uint64_t events, lost, capped, overflow;
-  double transport_ms;
+  double transport_ms;       /* transport kernels + site/score kernels      */
   uint64_t launches;
-  double reserved[4];
+  double kernel_ms;          /* device time of the main transport kernel(s) */
+  double reserved[3];
 } mc_keig_out;
 
 /* ---- context ------------------------------------------------------------ */
@@ -203,14 +205,23 @@ int mc_keig_end(mc_ctx* ctx, mc_keig_out* out);
  * counters); k_cycle/bank_size/sum/sum_sq are filled when non-NULL. */
 int mc_keig_status(mc_ctx* ctx, mc_keig_out* out);
 
+/* What the last transport ran: schedule (MC_SCHEDULE_*), the autotuned
+ * history-kernel variant, grid and block, and the kernel times the tuner
+ * measured per variant (tune_ms: n entries, may be NULL).  The tuner runs
+ * on the first inactive k-eigenvalue cycle unless opts->block_size is set;
+ * it has no counterpart in the reference. */
+int mc_schedule_info(mc_ctx* ctx, int32_t* schedule, int32_t* variant, int32_t* grid, int32_t* block,
+                     double* tune_ms, int32_t n);
+
 /* Batched Particle::Transport (src/Particle.cpp:42-44) over a host bank:
  * copies n sites in, transports each until it dies, and copies the fission
  * sites they banked (Particle::MoveSecondariesTo, src/Particle.cpp:102-104)
  * back, ordered by source index.  *n_out receives the number of sites;
  * MC_ERR_OVERFLOW if it exceeds cap (the first cap sites are returned).
- * keys of the input sites seed each particle's stream.  Tallies are
+ * keys of the input sites seed each particle's stream; opts (may be NULL)
+ * selects rng, fast_math, schedule and max_events.  Tallies are
  * accumulated into the context's estimators (see mc_tallies_get). */
-int mc_transport_bank(mc_ctx* ctx, const mc_site* sites, uint64_t n, int32_t rng,
+int mc_transport_bank(mc_ctx* ctx, const mc_site* sites, uint64_t n, const mc_run_opts* opts,
                       mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
 int mc_tallies_reset(mc_ctx* ctx);
 int mc_tallies_get(mc_ctx* ctx, double* sum, double* sum_sq);

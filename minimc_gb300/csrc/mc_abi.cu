@@ -39,11 +39,19 @@ struct mc_ctx {
   DevCounters* d_ctr = nullptr;
   double* d_sum = nullptr;
   double* d_sq = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  double last_kernel_ms = 0;  // main transport kernel(s) of the last run_transport
+  const double* pend_clean = nullptr;  // dense score array known to be all zero
+  size_t pend_clean_bytes = 0;
   uint64_t launches = 0;
   // scratch, grown on demand
   DevBuffer scratch[20];
   int last_schedule = MC_SCHEDULE_HISTORY;
+  // autotuner: history-kernel variant (occupancy target) chosen by timing
+  int variant = 0;
+  bool tune_pending = false;
+  double tune_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int last_grid = 0, last_block = 0;
   // k-eigenvalue state
   struct {
     bool active = false;
@@ -53,7 +61,7 @@ struct mc_ctx {
     uint32_t max_events = 1000000;
     std::vector<double> k, ktl;
     std::vector<uint64_t> bank;
-    double transport_ms = 0;
+    double transport_ms = 0, kernel_ms = 0;
     uint64_t events = 0, lost = 0, capped = 0, overflow = 0;
     uint64_t launches0 = 0;
   } keig;
@@ -325,6 +333,7 @@ int build_world(mc_ctx* c) {
       const int j = 2 * axis + (cl.within[k] ? 1 : 0);
       if (seen[j]++) ok = false;
       bx.c[j] = s.p[0];
+      bx.key[j] = mcd::dkey(s.p[0]);
       bx.s[j] = cl.surfaces[k];
       bx.order[j] = static_cast<int32_t>(k);
     }
@@ -395,7 +404,7 @@ int pick_block(const mc_run_opts* o) {
 }
 
 int grid_for(mc_ctx* c, int energy_mode, int rng, int block, bool keig, bool fast) {
-  int per_sm = mcd::history_blocks_per_sm(energy_mode, rng, block, keig, fast);
+  int per_sm = mcd::history_blocks_per_sm(energy_mode, rng, block, keig, fast, c->variant);
   if (per_sm < 1) per_sm = 1;
   return per_sm * c->num_sms;
 }
@@ -527,19 +536,34 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   rp.fis = keig ? static_cast<mcd::FissionRec*>(scratch(c, kEvFis, n * sizeof(mcd::FissionRec))) : nullptr;
   if ((rp.nb && !rp.pend) || (keig && !rp.fis)) return fail(c, MC_ERR_OOM, "score/fission buffers");
   CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-  if (rp.pend) CUDA_TRY(c, cudaMemsetAsync(rp.pend, 0, n * rp.nb * sizeof(double), c->stream));
+  // the commit kernel zeroes what it reads, so the dense array only needs a
+  // memset when it is new or a previous run did not reach the commit
+  const size_t pend_bytes = n * rp.nb * sizeof(double);
+  if (rp.pend && (rp.pend != c->pend_clean || c->pend_clean_bytes < pend_bytes)) {
+    const size_t all = c->scratch[kEvPend].bytes;
+    CUDA_TRY(c, cudaMemsetAsync(rp.pend, 0, all, c->stream));
+    c->pend_clean = rp.pend;
+    c->pend_clean_bytes = all;
+  }
+  const double* pend_before = c->pend_clean;
+  c->pend_clean = nullptr;  // dirty until the commit has run
+  CUDA_TRY(c, cudaEventRecord(c->evk0, c->stream));
   if (sched == MC_SCHEDULE_EVENT) {
     const int rc = run_event(c, rp, rng);
     if (rc != MC_OK) return rc;
   }
   else {
     const int grid = grid_for(c, c->model.energy_mode, rng, block, keig, rp.fast != 0);
+    c->last_grid = grid;
+    c->last_block = block;
     cudaError_t e;
-    if (c->model.energy_mode == mc::kMultigroup) e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream);
+    if (c->model.energy_mode == mc::kMultigroup)
+      e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
     else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream);
     if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
     c->launches++;
   }
+  CUDA_TRY(c, cudaEventRecord(c->evk1, c->stream));
   if (keig && c->model.energy_mode == mc::kMultigroup) {
     CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
     c->launches++;
@@ -548,12 +572,15 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     CUDA_TRY(c, mcd::launch_commit_dense(rp, c->num_sms * 8, c->stream));
     c->launches++;
   }
+  c->pend_clean = pend_before;
   CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
   if (ms) {
     CUDA_TRY(c, cudaEventSynchronize(c->ev1));
     float f = 0;
     CUDA_TRY(c, cudaEventElapsedTime(&f, c->ev0, c->ev1));
     *ms = f;
+    CUDA_TRY(c, cudaEventElapsedTime(&f, c->evk0, c->evk1));
+    c->last_kernel_ms = f;
   }
   return MC_OK;
 }
@@ -598,6 +625,8 @@ int mc_create(mc_ctx** out, int device) {
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
+  cudaEventCreate(&c->evk0);
+  cudaEventCreate(&c->evk1);
   *out = c;
   return MC_OK;
 }
@@ -611,6 +640,8 @@ void mc_destroy(mc_ctx* c) {
     if (b.p) cudaFree(b.p);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->evk0) cudaEventDestroy(c->evk0);
+  if (c->evk1) cudaEventDestroy(c->evk1);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -774,6 +805,7 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
     out->overflow = h.overflow;
     out->resample_failures = h.resample;
     out->transport_ms = ms;
+    out->kernel_ms = c->last_kernel_ms;
     out->launches = c->launches - l0;
   }
   return counters_status(c, h);
@@ -794,6 +826,9 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   k.schedule = o ? o->schedule : 0;
   k.max_events = o && o->max_events ? o->max_events : 1000000u;
   k.launches0 = c->launches;
+  // tune the history kernel on the first inactive cycle unless the caller
+  // fixed the block size
+  c->tune_pending = !(o && o->block_size > 0) && k.inactive > 0;
   if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
@@ -826,9 +861,30 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
   double ms = 0;
+  if (!active && c->tune_pending && resolve_schedule(c, k.schedule) == MC_SCHEDULE_HISTORY) {
+    // Autotuner: every variant transports this (inactive, unscored) cycle;
+    // the variants draw the same numbers and give identical results, so
+    // the last run's outputs stand and only the timing differs.
+    c->tune_pending = false;
+    int best = 0;
+    double best_ms = 1e300;
+    for (int v = 0; v < mcd::history_variants() && v < 8; v++) {
+      c->variant = v;
+      double t = 0;
+      const int rc = run_transport(c, rp, k.rng, k.block, &t, k.schedule);
+      if (rc != MC_OK) return rc;
+      c->tune_ms[v] = c->last_kernel_ms;
+      if (c->last_kernel_ms < best_ms) {
+        best_ms = c->last_kernel_ms;
+        best = v;
+      }
+    }
+    c->variant = best;
+  }
   int rc = run_transport(c, rp, k.rng, k.block, &ms, k.schedule);
   if (rc != MC_OK) return rc;
   k.transport_ms += ms;
+  k.kernel_ms += c->last_kernel_ms;
   Site* bank = nullptr;
   uint64_t m = 0;
   rc = compact_bank(c, k.n, &bank, &m);
@@ -880,8 +936,21 @@ int mc_keig_status(mc_ctx* c, mc_keig_out* out) {
     out->capped = k.capped;
     out->overflow = k.overflow;
     out->transport_ms = k.transport_ms;
+    out->kernel_ms = k.kernel_ms;
     out->launches = c->launches - k.launches0;
   }
+  return MC_OK;
+}
+
+int mc_schedule_info(mc_ctx* c, int32_t* schedule, int32_t* variant, int32_t* grid, int32_t* block, double* tune_ms,
+                     int32_t n) {
+  if (!c) return MC_ERR_INPUT;
+  if (schedule) *schedule = c->last_schedule;
+  if (variant) *variant = c->variant;
+  if (grid) *grid = c->last_grid;
+  if (block) *block = c->last_block;
+  if (tune_ms)
+    for (int32_t i = 0; i < n && i < 8; i++) tune_ms[i] = c->tune_ms[i];
   return MC_OK;
 }
 
@@ -909,9 +978,11 @@ int mc_run_keigenvalue(mc_ctx* c, const mc_run_opts* o, mc_keig_out* out) {
   return rc != MC_OK ? rc : status;
 }
 
-int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, int32_t rng, mc_site* fission_sites, uint64_t cap,
-                      uint64_t* n_out) {
+int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_opts* o, mc_site* fission_sites,
+                      uint64_t cap, uint64_t* n_out) {
   if (!check_ctx(c)) return MC_ERR_STATE;
+  const int rng = o ? o->rng : MC_RNG_PHILOX;
+  if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (n == 0) {
     if (n_out) *n_out = 0;
     return MC_OK;
@@ -926,16 +997,17 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, int32_t rng, 
   rp.n = n;
   rp.seed = c->model.seed;
   rp.run_key = run_key(c->model.seed, 0, 0x42414e4bull);
-  rp.max_events = 1000000u;
+  rp.max_events = o && o->max_events ? o->max_events : 1000000u;
   rp.keig = 1;
   rp.score = 1;
+  rp.fast = (o && o->fast_math && rng == MC_RNG_PHILOX) ? 1 : 0;
   rp.from_bank = 1;
   rp.minstd_base = 0;  // each site's own key seeds its stream
   rp.max_yield = c->max_yield;
   rp.src = src;
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
-  int rc = run_transport(c, rp, rng, 256, nullptr);
+  int rc = run_transport(c, rp, rng, pick_block(o), nullptr, o ? o->schedule : MC_SCHEDULE_AUTO);
   if (rc != MC_OK) return rc;
   Site* bank = nullptr;
   uint64_t m = 0;

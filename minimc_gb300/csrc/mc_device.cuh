@@ -56,6 +56,7 @@ struct DevCounters {
 // Cell::NearestSurface needs three distances instead of six.
 struct BoxCell {
   double c[6];      // plane positions: x lo, x hi, y lo, y hi, z lo, z hi
+  long long key[6]; // their order-preserving integer keys
   int32_t s[6];     // surface indices
   int32_t order[6]; // position of each plane in the cell's surface list
 };
@@ -383,24 +384,68 @@ __device__ __forceinline__ int find_cell(const DevWorld& w, double x, double y, 
 // it) -- so one exact division per axis.  Ties keep the reference's order:
 // the earliest surface in the cell's list wins, and with every distance
 // infinite the cell's first surface is returned.
+// sign tests on the integer pipe (NaN never reaches them)
+__device__ __forceinline__ bool dpos(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool dneg(double x) {
+  const long long b = __double_as_longlong(x);
+  return b < 0 && b != static_cast<long long>(0x8000000000000000ull);
+}
+
+// The three candidate distances are ordered with FP32 quotients first
+// (relative error < 4e-7); when the nearest is ahead of the next by more
+// than 4e-6 relative, only its exact FP64 distance is needed.  Near ties,
+// tiny or unusable FP32 values fall back to all exact divisions, so the
+// result always equals the exact computation.
 __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, int c, const double* pos,
                                                    const double* dir, double& dist, int skip) {
   const BoxCell& B = w.boxes[box];
+  int cj[3];
+  double cv[3];
+  float tf[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double p = pos[a], d = dir[a];
+    const long long kp = dkey(p);
+    const bool hi = dpos(d) ? !(kp < __ldg(&B.key[2 * a])) : (kp > __ldg(&B.key[2 * a + 1]));
+    int j = 2 * a + (hi ? 1 : 0);
+    // the skipped surface reads as infinitely far; the axis' other plane
+    // then is the only candidate
+    if (__ldg(&B.s[j]) == skip) j ^= 1;
+    cj[a] = j;
+    // PlaneX::Distance: v = c - p, positive iff v and d have the same sign
+    const double v = dsub(__ldg(&B.c[j]), p);
+    cv[a] = v;
+    const bool ahead = __ldg(&B.s[j]) != skip && ((dpos(v) && dpos(d)) || (dneg(v) && dneg(d)));
+    tf[a] = ahead ? fabsf(__fdiv_rn(__double2float_rn(v), __double2float_rn(d))) : CUDART_INF_F;
+  }
+  int a0 = 0;
+  if (tf[1] < tf[a0]) a0 = 1;
+  if (tf[2] < tf[a0]) a0 = 2;
+  float second = CUDART_INF_F;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+    if (a != a0) second = fminf(second, tf[a]);
+  if (tf[a0] < CUDART_INF_F && tf[a0] > 1e-30f && !(second <= __fmul_rn(tf[a0], 1.000004f))) {
+    const double t = ddiv(cv[a0], dir[a0]);
+    if (t > 0 && t < CUDART_INF) {
+      dist = t;
+      return __ldg(&B.s[cj[a0]]);
+    }
+  }
+  // exact path: every candidate divided, reference tie-breaking
   int best_s = __ldg(w.cell_surf + __ldg(w.cell_begin + c));
   int best_o = 0x7fffffff;
   double bd = CUDART_INF;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const double p = pos[a], d = dir[a];
-    const double clo = __ldg(&B.c[2 * a]), chi = __ldg(&B.c[2 * a + 1]);
-    const bool hi = d > 0 ? !(p < clo) : (p > chi);
-    int j = 2 * a + (hi ? 1 : 0);
-    // the skipped surface reads as infinitely far; the axis' other plane
-    // then is the only candidate
-    if (__ldg(&B.s[j]) == skip) j ^= 1;
+    const int j = cj[a];
     const int s = __ldg(&B.s[j]);
     const int o = __ldg(&B.order[j]);
-    const double t = s == skip ? CUDART_INF : plane_distance(p, d, __ldg(&B.c[j]));
+    double t = CUDART_INF;
+    if (s != skip) {
+      const double q = ddiv(cv[a], dir[a]);
+      t = q > 0 ? q : CUDART_INF;
+    }
     if (t < bd || (t == bd && t != CUDART_INF && o < best_o)) {
       bd = t;
       best_s = s;

@@ -81,7 +81,7 @@ __device__ __forceinline__ void particle_died(const EvParams& ep, unsigned i, in
 }
 
 __device__ __forceinline__ void pend_add(const EvParams& ep, unsigned h, uint64_t bin, double s) {
-  atomicAdd(ep.rp.pend + static_cast<size_t>(h) * ep.rp.nb + bin, s);
+  atomicAdd(ep.rp.pend + bin * ep.rp.n + h, s);  // bin-major
 }
 
 }  // namespace
@@ -509,31 +509,44 @@ __global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, cons
 
 // ---------------------------------------------------------------------------
 // per-history dense scores -> sum, sum of squares
-// (ScorableProxy::CommitHistory, src/Scorable.cpp:101-106), reduced in shared
-// memory per block before one global atomic per bin
+// (ScorableProxy::CommitHistory, src/Scorable.cpp:101-106).  The array is
+// bin-major ([bin][history]); blockIdx.y is the bin, threads stride over
+// histories with coalesced reads, skip zeros with an integer test, keep the
+// two sums in registers, reduce per warp and per block, and write one atomic
+// per block.  Entries read are set back to zero, so the array is clean for
+// the next run without a memset.
 __global__ void __launch_bounds__(256) k_commit_dense(const RunParams rp) {
-  __shared__ double ssum[kDenseBins], ssq[kDenseBins];
-  const int nb = rp.nb;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    ssum[b] = 0;
-    ssq[b] = 0;
-  }
-  __syncthreads();
+  __shared__ double ws[8], wq[8];
+  const unsigned b = blockIdx.y;
+  double* row = rp.pend + static_cast<size_t>(b) * rp.n;
+  double s = 0, q = 0;
   for (unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; h < rp.n;
        h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
-    const double* p = rp.pend + h * nb;
-    for (int b = 0; b < nb; b++) {
-      const double v = p[b];
-      if (v != 0) {
-        atomicAdd(ssum + b, v);
-        atomicAdd(ssq + b, v * v);
-      }
+    const double v = row[h];
+    if (__double_as_longlong(v) != 0) {
+      s += v;
+      q += v * v;
+      row[h] = 0;
     }
   }
+  for (int off = 16; off > 0; off >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, off);
+    q += __shfl_down_sync(0xffffffffu, q, off);
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    ws[wid] = s;
+    wq[wid] = q;
+  }
   __syncthreads();
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    if (ssum[b] != 0) atomicAdd(rp.tally_sum + b, ssum[b]);
-    if (ssq[b] != 0) atomicAdd(rp.tally_sq + b, ssq[b]);
+  if (threadIdx.x == 0) {
+    double ts = 0, tq = 0;
+    for (int i = 0; i < static_cast<int>(blockDim.x >> 5); i++) {
+      ts += ws[i];
+      tq += wq[i];
+    }
+    if (ts != 0) atomicAdd(rp.tally_sum + b, ts);
+    if (tq != 0) atomicAdd(rp.tally_sq + b, tq);
   }
 }
 
@@ -545,7 +558,12 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
 }
 
 cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream) {
-  k_commit_dense<<<grid, 256, 0, stream>>>(rp);
+  if (rp.nb <= 0) return cudaSuccess;
+  // about `grid` blocks in total, spread over the bins
+  const unsigned per_bin = static_cast<unsigned>(std::max(1, grid / rp.nb));
+  const unsigned needed = static_cast<unsigned>((rp.n + 255) / 256);
+  const dim3 g(std::min(per_bin, std::max(1u, needed)), static_cast<unsigned>(rp.nb));
+  k_commit_dense<<<g, 256, 0, stream>>>(rp);
   return cudaGetLastError();
 }
 

@@ -62,11 +62,14 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
 cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream);
 
 // launches (mc_transport.cu)
+// history-schedule kernel variants differ only in their occupancy target
+// (register budget); results are identical, the autotuner times them
+int history_variants();
 cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
-                              cudaStream_t stream);
+                              cudaStream_t stream, int variant);
 cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
                               cudaStream_t stream);
-int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast);
+int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant);
 
 // bank compaction and resampling (mc_transport.cu)
 cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,

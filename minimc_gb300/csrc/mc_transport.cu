@@ -161,9 +161,10 @@ __device__ __forceinline__ double energy_value(const DevWorld& w, const Particle
 // committed by a separate kernel) or to a per-thread list (many bins).
 struct Scorer {
   Pending<kPending>* list;
-  double* dense;
+  double* dense;                // this history's column of the bin-major array
+  unsigned long long stride;    // histories per bin row
   __device__ __forceinline__ void add(uint32_t b, double s) {
-    if (dense) atomicAdd(dense + b, s);
+    if (dense) atomicAdd(dense + b * stride, s);
     else list->add(b, s);
   }
 };
@@ -252,8 +253,10 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 
 // ---------------------------------------------------------------------------
 // multigroup history kernel
-template <class Rng, bool KEIG>
-__global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunParams rp) {
+// MINB: minimum resident 256-thread blocks per SM the register allocation
+// must allow (1 = compiler's choice); the autotuner picks among variants
+template <class Rng, bool KEIG, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_history_mg(const DevWorld w, const RunParams rp) {
   extern __shared__ double smem[];
   const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
   Particle<Rng> p;
   Pending<kPending> pend;
   pend.clear();
-  Scorer sc{&pend, nullptr};
+  Scorer sc{&pend, nullptr, rp.n};
   Site stack[KEIG ? 1 : kStack];
   int sp = 0;
   bool alive = false, done = false;
@@ -314,7 +317,7 @@ __global__ void __launch_bounds__(256) k_history_mg(const DevWorld w, const RunP
           fate = kBirth;
           nbank = 0;
           alive = true;
-          sc.dense = rp.nb ? rp.pend + hist * rp.nb : nullptr;
+          sc.dense = rp.nb ? rp.pend + hist : nullptr;
           if constexpr (KEIG) rp.fis[hist].n = 0;
           if (p.cell < 0 || __ldg(w.cell_mat + p.cell) < 0) {
             // the reference throws (src/World.cpp:34-36) or dereferences a
@@ -531,28 +534,48 @@ int occupancy(K kernel, int block, size_t smem) {
 }
 }  // namespace
 
-int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast) {
-  (void)fast;
+namespace {
+template <int MINB>
+int occupancy_mg(int rng_mode, int block, bool keig) {
   const size_t smem = 2 * kSharedBins * sizeof(double);
-  if (energy_mode == 0) {
-    if (rng_mode == 1) return keig ? occupancy(k_history_mg<MinstdRng, true>, block, smem)
-                                   : occupancy(k_history_mg<MinstdRng, false>, block, smem);
-    return keig ? occupancy(k_history_mg<PhiloxRng, true>, block, smem)
-                : occupancy(k_history_mg<PhiloxRng, false>, block, smem);
+  if (rng_mode == 1) return keig ? occupancy(k_history_mg<MinstdRng, true, MINB>, block, smem)
+                                 : occupancy(k_history_mg<MinstdRng, false, MINB>, block, smem);
+  return keig ? occupancy(k_history_mg<PhiloxRng, true, MINB>, block, smem)
+              : occupancy(k_history_mg<PhiloxRng, false, MINB>, block, smem);
+}
+
+template <int MINB>
+void launch_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block, cudaStream_t stream) {
+  const size_t smem = 2 * kSharedBins * sizeof(double);
+  if (rng_mode == 1) {
+    if (rp.keig) k_history_mg<MinstdRng, true, MINB><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_mg<MinstdRng, false, MINB><<<grid, block, smem, stream>>>(w, rp);
   }
-  return 1;
+  else {
+    if (rp.keig) k_history_mg<PhiloxRng, true, MINB><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_mg<PhiloxRng, false, MINB><<<grid, block, smem, stream>>>(w, rp);
+  }
+}
+}  // namespace
+
+int history_variants() { return 3; }
+
+int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant) {
+  (void)fast;
+  if (energy_mode != 0) return 1;
+  switch (variant) {
+  case 1: return occupancy_mg<3>(rng_mode, block, keig);
+  case 2: return occupancy_mg<4>(rng_mode, block, keig);
+  default: return occupancy_mg<1>(rng_mode, block, keig);
+  }
 }
 
 cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
-                              cudaStream_t stream) {
-  const size_t smem = 2 * kSharedBins * sizeof(double);
-  if (rng_mode == 1) {
-    if (rp.keig) k_history_mg<MinstdRng, true><<<grid, block, smem, stream>>>(w, rp);
-    else k_history_mg<MinstdRng, false><<<grid, block, smem, stream>>>(w, rp);
-  }
-  else {
-    if (rp.keig) k_history_mg<PhiloxRng, true><<<grid, block, smem, stream>>>(w, rp);
-    else k_history_mg<PhiloxRng, false><<<grid, block, smem, stream>>>(w, rp);
+                              cudaStream_t stream, int variant) {
+  switch (variant) {
+  case 1: launch_mg<3>(w, rp, rng_mode, grid, block, stream); break;
+  case 2: launch_mg<4>(w, rp, rng_mode, grid, block, stream); break;
+  default: launch_mg<1>(w, rp, rng_mode, grid, block, stream); break;
   }
   return cudaGetLastError();
 }

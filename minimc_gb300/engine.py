@@ -84,7 +84,7 @@ class TallyOut(C.Structure):
                 ("histories", C.c_uint64), ("events", C.c_uint64), ("secondaries", C.c_uint64),
                 ("lost", C.c_uint64), ("capped", C.c_uint64), ("overflow", C.c_uint64),
                 ("resample_failures", C.c_uint64), ("transport_ms", C.c_double),
-                ("launches", C.c_uint64), ("reserved", C.c_double * 4)]
+                ("launches", C.c_uint64), ("kernel_ms", C.c_double), ("reserved", C.c_double * 3)]
 
 
 class KeigOut(C.Structure):
@@ -93,7 +93,7 @@ class KeigOut(C.Structure):
                 ("k_mean", C.c_double), ("k_std", C.c_double), ("k_tracklength_mean", C.c_double),
                 ("events", C.c_uint64), ("lost", C.c_uint64), ("capped", C.c_uint64),
                 ("overflow", C.c_uint64), ("transport_ms", C.c_double), ("launches", C.c_uint64),
-                ("reserved", C.c_double * 4)]
+                ("kernel_ms", C.c_double), ("reserved", C.c_double * 3)]
 
 
 _P = C.c_void_p
@@ -115,7 +115,9 @@ _SIGNATURES = {
     "mc_keig_cycle": (C.c_int, [_P, C.c_int32, _D]),
     "mc_keig_end": (C.c_int, [_P, C.POINTER(KeigOut)]),
     "mc_keig_status": (C.c_int, [_P, C.POINTER(KeigOut)]),
-    "mc_transport_bank": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "mc_schedule_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32), _D, C.c_int32]),
+    "mc_transport_bank": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(RunOpts), _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "mc_tallies_reset": (C.c_int, [_P]),
     "mc_tallies_get": (C.c_int, [_P, _D, _D]),
     "mc_find_cell": (C.c_int, [_P, _D, C.c_uint64, C.POINTER(C.c_int32)]),
@@ -283,26 +285,36 @@ class Context:
         self.check(self.lib.mc_keig_status(self.h, C.byref(out)))
         return out
 
+    def schedule_info(self) -> dict:
+        s, v, g, b = (C.c_int32() for _ in range(4))
+        t = np.zeros(8)
+        self.check(self.lib.mc_schedule_info(self.h, C.byref(s), C.byref(v), C.byref(g), C.byref(b), _dptr(t), 8))
+        names = {1: "history", 2: "event"}
+        return {"schedule": names.get(s.value, s.value), "variant": v.value, "grid": g.value, "block": b.value,
+                "tune_kernel_ms": [round(x, 4) for x in t if x > 0]}
+
     def keig_end(self) -> KeigOut:
         out = KeigOut()
         self.check(self.lib.mc_keig_end(self.h, C.byref(out)))
         return out
 
-    def transport_bank(self, sites: np.ndarray, rng: int = RNG_PHILOX, cap: int | None = None):
+    def transport_bank(self, sites: np.ndarray, cap: int | None = None, **kw):
+        """Batched Particle::Transport over a host bank; returns the fission
+        sites banked (in source order).  kw: RunOpts fields (rng, fast_math,
+        schedule, max_events)."""
         sites = np.ascontiguousarray(sites, dtype=SITE_DTYPE)
         cap = cap if cap is not None else len(sites) * max(1, self.info.max_yield)
         out = np.zeros(cap, SITE_DTYPE)
-        n_out = C.c_uint64()
-        self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), rng,
-                                              out.ctypes.data_as(_P), cap, C.byref(n_out)))
-        return out[: n_out.value]
+        n = self.transport_bank_into(sites, out, **kw)
+        return out[:n]
 
-    def transport_bank_into(self, sites: np.ndarray, out: np.ndarray, rng: int = RNG_PHILOX) -> int:
+    def transport_bank_into(self, sites: np.ndarray, out: np.ndarray, **kw) -> int:
         """Like transport_bank, with caller-owned (e.g. pinned) site arrays;
         returns the number of fission sites written to ``out``."""
         assert sites.dtype == SITE_DTYPE and out.dtype == SITE_DTYPE
+        o = self.opts(**kw)
         n_out = C.c_uint64()
-        self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), rng,
+        self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), C.byref(o),
                                               out.ctypes.data_as(_P), len(out), C.byref(n_out)))
         return int(n_out.value)
 
