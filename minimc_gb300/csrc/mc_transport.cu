@@ -558,7 +558,9 @@ void launch_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, i
 }
 }  // namespace
 
-int history_variants() { return 3; }
+// variants: minimum 256-thread blocks per SM of 1 (compiler's choice), 3, 4,
+// 5 and 6 -- register budgets of 255, 85, 64, 51 and 42 per thread
+int history_variants() { return 5; }
 
 int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant) {
   (void)fast;
@@ -566,6 +568,8 @@ int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, b
   switch (variant) {
   case 1: return occupancy_mg<3>(rng_mode, block, keig);
   case 2: return occupancy_mg<4>(rng_mode, block, keig);
+  case 3: return occupancy_mg<5>(rng_mode, block, keig);
+  case 4: return occupancy_mg<6>(rng_mode, block, keig);
   default: return occupancy_mg<1>(rng_mode, block, keig);
   }
 }
@@ -575,6 +579,8 @@ cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mo
   switch (variant) {
   case 1: launch_mg<3>(w, rp, rng_mode, grid, block, stream); break;
   case 2: launch_mg<4>(w, rp, rng_mode, grid, block, stream); break;
+  case 3: launch_mg<5>(w, rp, rng_mode, grid, block, stream); break;
+  case 4: launch_mg<6>(w, rp, rng_mode, grid, block, stream); break;
   default: launch_mg<1>(w, rp, rng_mode, grid, block, stream); break;
   }
   return cudaGetLastError();
