@@ -223,6 +223,22 @@ int mc_schedule_info(mc_ctx* ctx, int32_t* schedule, int32_t* variant, int32_t* 
  * accumulated into the context's estimators (see mc_tallies_get). */
 int mc_transport_bank(mc_ctx* ctx, const mc_site* sites, uint64_t n, const mc_run_opts* opts,
                       mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
+/* mc_transport_bank for callers that cannot allocate device memory when
+ * they transport: code recording a CUDA graph (cudaMalloc is not allowed
+ * during stream capture) and applications that fix their device-memory
+ * budget at start-up.  No counterpart in the reference.  sites and
+ * fission_sites are DEVICE pointers owned by the caller; *n_out (host) gets
+ * the number of sites banked (at most cap are written).  Allocates nothing:
+ * its scratch is a fixed 5.3 MB array that every GPU loading this library
+ * holds until exit.  Limits: n <= 16384 sites per call, multigroup problems
+ * whose fissions bank at most 4 sites; larger calls fail with MC_ERR_INPUT.
+ * The first call on a device looks the array's address up (and loads the
+ * kernels): make it before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU (other streams, other contexts on the
+ * same device) race; serialize them.  Tallies accumulate into the context's
+ * estimators as with mc_transport_bank. */
+int mc_transport_bank_noalloc(mc_ctx* ctx, const mc_site* sites, uint64_t n, const mc_run_opts* opts,
+                              mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
 int mc_tallies_reset(mc_ctx* ctx);
 int mc_tallies_get(mc_ctx* ctx, double* sum, double* sum_sq);
 

@@ -1151,3 +1151,138 @@ int mc_tsl_total(mc_ctx* c, int32_t, const double*, const double*, uint64_t, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Bank transport without allocation.
+//
+// Some callers cannot allocate device memory at the time they transport a
+// bank: code that is recording a CUDA graph (cudaMalloc is not allowed while
+// a stream is being captured), and host applications that fix their device
+// memory budget at start-up and forbid allocation afterwards (for example a
+// coupled multiphysics code that owns the GPU's memory pool).  For them,
+// mc_transport_bank_noalloc runs the same kernels as mc_transport_bank, but
+// all of its scratch memory -- run counters, fission records, per-history
+// site slots, scan sums -- lives in the fixed array below, which every GPU
+// that loads this library holds until the process exits.  The caller passes
+// its own device buffers for the input sites and the output bank.
+
+namespace {
+
+constexpr uint64_t kNoAllocMaxHistories = 16384;  // sites per call
+constexpr uint32_t kNoAllocMaxYield = 4;           // secondaries per fission
+constexpr size_t kNoAllocCounters = 256;
+constexpr size_t kNoAllocFission = kNoAllocMaxHistories * sizeof(mcd::FissionRec);
+constexpr size_t kNoAllocSlots = kNoAllocMaxHistories * kNoAllocMaxYield * sizeof(Site);
+constexpr size_t kNoAllocCount = kNoAllocMaxHistories * sizeof(uint32_t);
+constexpr size_t kNoAllocOffsets = kNoAllocMaxHistories * sizeof(unsigned long long);
+constexpr size_t kNoAllocSums = 64 * sizeof(unsigned long long);  // scan block sums + total
+constexpr size_t kNoAllocBytes =
+    kNoAllocCounters + kNoAllocFission + kNoAllocSlots + kNoAllocCount + kNoAllocOffsets + kNoAllocSums;  // 5.3 MB
+
+static_assert(sizeof(DevCounters) <= kNoAllocCounters, "counter block");
+static_assert(kNoAllocFission % 256 == 0 && kNoAllocSlots % 256 == 0 && kNoAllocCount % 256 == 0 &&
+                  kNoAllocOffsets % 256 == 0,
+              "sub-buffers keep 256-byte alignment");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// device address of g_noalloc_scratch for each device, found once
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+// compaction that never writes past the caller's capacity
+__global__ void k_compact_capped(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
+                                 unsigned long long n, uint32_t max_yield, Site* out, unsigned long long cap) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t c = count[i];
+  const unsigned long long o = offsets[i];
+  for (uint32_t k = 0; k < c; k++)
+    if (o + k < cap) out[o + k] = slots[i * max_yield + k];
+}
+
+}  // namespace
+
+extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint64_t n, const mc_run_opts* o,
+                                         mc_site* d_fission_sites, uint64_t cap, uint64_t* n_out) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n_out) *n_out = 0;
+  if (n == 0) return MC_OK;
+  if (!d_sites) return fail(c, MC_ERR_INPUT, "sites is NULL");
+  if (n > kNoAllocMaxHistories)
+    return fail(c, MC_ERR_INPUT, "mc_transport_bank_noalloc: " + std::to_string(n) + " sites exceed the limit of " +
+                                     std::to_string(kNoAllocMaxHistories) + " per call");
+  if (c->max_yield > kNoAllocMaxYield)
+    return fail(c, MC_ERR_INPUT, "mc_transport_bank_noalloc: up to " + std::to_string(kNoAllocMaxYield - 1) +
+                                     " mean secondaries per fission are supported (this problem allows " +
+                                     std::to_string(c->max_yield - 1) + ")");
+  if (c->model.energy_mode != mc::kMultigroup)
+    return fail(c, MC_ERR_INPUT, "mc_transport_bank_noalloc: multigroup problems only");
+  const int rng = o ? o->rng : MC_RNG_PHILOX;
+  if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
+  if (c->device < 0 || c->device >= kMaxDevices) return fail(c, MC_ERR_INPUT, "device index out of range");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  // set-up, once per device with that device current: the host-side symbol
+  // is not a device address, so ask the runtime for the array's address
+  if (!g_noalloc_addr[c->device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(c, MC_ERR_DEVICE, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_addr[c->device] = p;
+  }
+  char* base = static_cast<char*>(g_noalloc_addr[c->device]);
+  auto* ctr = reinterpret_cast<DevCounters*>(base);
+  auto* fis = reinterpret_cast<mcd::FissionRec*>(base + kNoAllocCounters);
+  auto* slots = reinterpret_cast<Site*>(base + kNoAllocCounters + kNoAllocFission);
+  auto* count = reinterpret_cast<uint32_t*>(base + kNoAllocCounters + kNoAllocFission + kNoAllocSlots);
+  auto* offsets =
+      reinterpret_cast<unsigned long long*>(base + kNoAllocCounters + kNoAllocFission + kNoAllocSlots + kNoAllocCount);
+  auto* sums = reinterpret_cast<unsigned long long*>(base + kNoAllocCounters + kNoAllocFission + kNoAllocSlots +
+                                                     kNoAllocCount + kNoAllocOffsets);
+  auto* total = sums + 48;  // after at most 16 block sums
+
+  // the array keeps the previous call's contents: the counters must start
+  // at zero; fission records and counts are rewritten for every history
+  CUDA_TRY(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), c->stream));
+  RunParams rp{};
+  rp.n = n;
+  rp.seed = c->model.seed;
+  rp.run_key = run_key(c->model.seed, 0, 0x42414e4bull);
+  rp.max_events = o && o->max_events ? o->max_events : 1000000u;
+  rp.keig = 1;
+  rp.score = 1;
+  rp.fast = (o && o->fast_math && rng == MC_RNG_PHILOX) ? 1 : 0;
+  rp.from_bank = 1;
+  rp.minstd_base = 0;
+  rp.max_yield = kNoAllocMaxYield;
+  rp.src = reinterpret_cast<const Site*>(d_sites);
+  rp.bank = slots;
+  rp.bank_count = count;
+  rp.ctr = ctr;
+  rp.tally_sum = c->d_sum;
+  rp.tally_sq = c->d_sq;
+  rp.total_bins = c->total_bins;
+  rp.nb = 0;  // scores go through the per-history list, no dense array
+  rp.pend = nullptr;
+  rp.fis = fis;
+  const int block = pick_block(o);
+  const int grid = grid_for(c, c->model.energy_mode, rng, block, true, rp.fast != 0);
+  CUDA_TRY(c, mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant));
+  CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
+  CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
+  if (d_fission_sites && cap) {
+    k_compact_capped<<<static_cast<unsigned>((n + 255) / 256), 256, 0, c->stream>>>(
+        slots, count, offsets, n, kNoAllocMaxYield, reinterpret_cast<Site*>(d_fission_sites), cap);
+    CUDA_TRY(c, cudaGetLastError());
+  }
+  c->launches += 6;
+  unsigned long long m = 0;
+  DevCounters h{};
+  CUDA_TRY(c, cudaMemcpyAsync(&m, total, sizeof m, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(&h, ctr, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (n_out) *n_out = m;
+  if (m > cap) return fail(c, MC_ERR_OVERFLOW, "fission bank larger than the output capacity");
+  return counters_status(c, h);
+}

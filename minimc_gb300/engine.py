@@ -118,6 +118,8 @@ _SIGNATURES = {
     "mc_schedule_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), _D, C.c_int32]),
     "mc_transport_bank": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(RunOpts), _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "mc_transport_bank_noalloc": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(RunOpts), _P, C.c_uint64,
+                                            C.POINTER(C.c_uint64)]),
     "mc_tallies_reset": (C.c_int, [_P]),
     "mc_tallies_get": (C.c_int, [_P, _D, _D]),
     "mc_find_cell": (C.c_int, [_P, _D, C.c_uint64, C.POINTER(C.c_int32)]),
@@ -316,6 +318,16 @@ class Context:
         n_out = C.c_uint64()
         self.check(self.lib.mc_transport_bank(self.h, sites.ctypes.data_as(_P), len(sites), C.byref(o),
                                               out.ctypes.data_as(_P), len(out), C.byref(n_out)))
+        return int(n_out.value)
+
+    def transport_bank_noalloc(self, d_sites: int, n: int, d_out: int, cap: int, **kw) -> int:
+        """mc_transport_bank_noalloc: device pointers in and out (for callers
+        that cannot allocate, e.g. while recording a CUDA graph); returns the
+        number of fission sites banked."""
+        o = self.opts(**kw)
+        n_out = C.c_uint64()
+        self.check(self.lib.mc_transport_bank_noalloc(self.h, _P(d_sites), n, C.byref(o), _P(d_out), cap,
+                                                      C.byref(n_out)))
         return int(n_out.value)
 
     def tallies(self):
