@@ -173,7 +173,18 @@ def run_gpu(args) -> None:
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     ctx.load_xml(xml)
-    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block, schedule=args.schedule)
+    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block, schedule=args.schedule,
+                variant=args.variant)
+    if args.mode == "kernel":
+        # profiling mode: warm-up cycles (the first runs the autotuner unless
+        # --variant is given) then `steps` active cycles; nothing else
+        ctx.keig_begin(**opts)
+        for i in range(args.warmup + args.steps):
+            k = ctx.keig_cycle(i >= args.warmup)
+        torch.cuda.synchronize()
+        print(json.dumps({"mode": "kernel", "k_last": k, "schedule": ctx.schedule_info()}), flush=True)
+        ctx.keig_end()
+        return
 
     def barrier():
         if dist is not None:
@@ -310,6 +321,9 @@ def main():
     ap.add_argument("--cpu-histories", type=int, default=1_000_000)
     ap.add_argument("--cpu-cycles", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=0, help="history-kernel variant + 1 (0: autotuned)")
+    ap.add_argument("--mode", default="full", choices=["full", "kernel"],
+                    help="kernel: only the k-eigenvalue cycles (for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -75,7 +75,8 @@ typedef struct {
   int32_t block_size;   /* 0 -> autotuned                                */
   int32_t fast_math;    /* 1: FP32 sampling arithmetic (Philox only);
                            geometry and positions stay FP64            */
-  int32_t reserved[7];
+  int32_t variant;      /* history-kernel variant + 1; 0 -> autotuned   */
+  int32_t reserved[6];
 } mc_run_opts;
 
 /* A particle in a bank: the state that Bank/Particle carry between

@@ -759,6 +759,7 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
   const int rng = o ? o->rng : 0;
   if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   const int block = pick_block(o);
+  if (o && o->variant > 0) c->variant = std::min(o->variant - 1, mcd::history_variants() - 1);
   RunParams rp{};
   rp.n = n;
   rp.seed = seed;
@@ -828,7 +829,8 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   k.launches0 = c->launches;
   // tune the history kernel on the first inactive cycle unless the caller
   // fixed the block size
-  c->tune_pending = !(o && o->block_size > 0) && k.inactive > 0;
+  c->tune_pending = !(o && (o->block_size > 0 || o->variant > 0)) && k.inactive > 0;
+  if (o && o->variant > 0) c->variant = std::min(o->variant - 1, mcd::history_variants() - 1);
   if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||

@@ -51,7 +51,7 @@ class RunOpts(C.Structure):
     _fields_ = [("histories", C.c_uint64), ("seed", C.c_uint64), ("inactive", C.c_uint32),
                 ("active", C.c_uint32), ("rng", C.c_int32), ("schedule", C.c_int32),
                 ("max_events", C.c_uint32), ("block_size", C.c_int32), ("fast_math", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("variant", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class Site(C.Structure):
