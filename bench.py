@@ -2,7 +2,11 @@
 
 Workload (the GPU-scale plain-method configuration): 8 groups, a 30 cm fuel
 cube inside a 60 cm reflector cube, vacuum outside, seeded cross sections,
-1e6 histories per cycle, FP64 tracking.  A step is one active k-eigenvalue
+1e6 histories per cycle, FP64 tracking.  ``--workload ce`` runs the
+continuous-energy plain method instead: three synthetic nuclides on 5e4-point
+log grids (1/v capture, 200 SLBW resonances, potential scattering), free-gas
+scattering at 293.6 K, a homogeneous mixture in a reflected 40 cm box,
+1e6 histories per cycle.  A step is one active k-eigenvalue
 cycle: transport of 1e6 source particles, fission-bank compaction and
 resampling of the next source.  ``value`` times the steps with CUDA events
 on the engine's stream, with the bank resident in HBM; ``e2e`` times the
@@ -35,7 +39,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "histories/s on 1 GB300, plain vs surrogate-TSL at matched k_eff sigma/spectrum chi2"
 UNIT = "histories/s"
-WORKLOAD = "8-group two-zone k-eigenvalue (fuel cube 30 cm in reflector cube 60 cm), 1e6 histories/cycle"
+WORKLOADS = {
+    "two_zone": "8-group two-zone k-eigenvalue (fuel cube 30 cm in reflector cube 60 cm), 1e6 histories/cycle",
+    "ce": "continuous-energy k-eigenvalue (3 synthetic SLBW nuclides, 5e4-point grids, free gas at 293.6 K, "
+          "reflected 40 cm box), 1e6 histories/cycle",
+}
 BYTES_PER_EVENT = 128  # minimal SoA particle state read + write per event
 
 
@@ -102,18 +110,36 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def problem(histories: int):
+def problem(workload: str, histories: int, seed: int = 1) -> dict:
+    """The workload's XML, the directory its data files live in, and the
+    fields of the JSON line that describe it."""
+    if workload == "ce":
+        import atexit
+        import shutil
+        import tempfile
+
+        from minimc_gb300 import synth_ce
+
+        base = Path(tempfile.mkdtemp(prefix="mc_ce_"))
+        atexit.register(shutil.rmtree, base, True)
+        files = synth_ce.write_nuclides(base, seed=2027, n_grid=50_000)
+        xml = synth_ce.ce_problem_xml(files, histories=histories, inactive=20, active=50)
+        xml = xml.replace("<seed>1</seed>", f"<seed>{seed}</seed>")
+        return {"xml": xml, "base": str(base), "kernel": "k_history_ce", "site_energy": 2.0,
+                "config": {"nuclides": 3, "grid_points": 50_000, "temperature_K": 293.6}}
     from minimc_gb300 import synth
 
-    return synth.two_zone_cubes(histories=histories, inactive=20, active=50)
+    p = synth.two_zone_cubes(histories=histories, inactive=20, active=50)
+    p.seed = seed
+    return {"xml": p.xml(), "base": "", "kernel": "k_history_mg", "site_energy": 1.0, "config": {"groups": 8}}
 
 
-def cpu_baseline(xml: str, histories: int, threads: int, cycles: int) -> dict:
+def cpu_baseline(xml: str, base: str, histories: int, threads: int, cycles: int) -> dict:
     """Times the CPU oracle (reference algorithm, minstd streams) on the host
     cores: `cycles` cycles of `histories` histories from the initial source."""
     from oracle.build import Oracle
 
-    o = Oracle(xml)
+    o = Oracle(xml, base)
     r = o.run_keigenvalue(histories, 1, 1, cycles - 1, threads=threads)
     hps = histories * cycles / r["seconds"]
     return {"value": hps, "unit": UNIT, "cores": threads, "kind": "port",
@@ -126,14 +152,14 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     hist = args.histories
-    xml = problem(hist).xml()
+    wl = problem(args.workload, hist)
+    xml, base = wl["xml"], wl["base"]
     threads = os.cpu_count() or 1
     # warm-up: one short cycle
     from oracle.build import Oracle
 
-    Oracle(xml).run_keigenvalue(min(hist, 100_000), 1, 1, 0, threads=threads)
-    times = []
-    o = Oracle(xml)
+    Oracle(xml, base).run_keigenvalue(min(hist, 100_000), 1, 1, 0, threads=threads)
+    o = Oracle(xml, base)
     # each step: one cycle of the workload on all host threads (the first
     # cycle starts from the point source; the bank converges in a few cycles)
     r = o.run_keigenvalue(hist, 1, args.warmup, args.steps, threads=threads)
@@ -144,7 +170,8 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / cycles,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "histories_per_cycle": hist, "rng": "minstd (reference streams)"},
+        "config": {"workload": WORKLOADS[args.workload], "histories_per_cycle": hist,
+                   "rng": "minstd (reference streams)", **wl["config"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{cycles} cycles x {hist} histories (CPU oracle restating the reference path)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -166,13 +193,12 @@ def run_gpu(args) -> None:
     from minimc_gb300 import RNG_PHILOX, SITE_DTYPE, Context
 
     hist = args.histories
-    prob = problem(hist)
-    prob.seed = 1 + rank
-    xml = prob.xml()
+    wl = problem(args.workload, hist, seed=1 + rank)
+    xml, base = wl["xml"], wl["base"]
     ctx = Context(local)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
-    ctx.load_xml(xml)
+    ctx.load_xml(xml, base)
     opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), block_size=args.block, schedule=args.schedule,
                 variant=args.variant)
     if args.mode == "kernel":
@@ -234,8 +260,8 @@ def run_gpu(args) -> None:
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         prof = json.loads(tf.read_text())
-        traffic = prof.get("k_history_mg_dram_bytes_per_launch")
-        fp64 = prof.get("k_history_mg_fp64_pipe_active")
+        traffic = prof.get(f"{wl['kernel']}_dram_bytes_per_launch")
+        fp64 = prof.get(f"{wl['kernel']}_fp64_pipe_active")
 
     # ---- end to end through the host-buffer ABI call
     n_sites = hist
@@ -252,7 +278,7 @@ def run_gpu(args) -> None:
     ph = rng.uniform(0, 2 * np.pi, n_sites)
     st = np.sqrt(1 - mu * mu)
     src["u"], src["v"], src["w"] = mu, st * np.cos(ph), st * np.sin(ph)
-    src["energy"] = 1.0
+    src["energy"] = wl["site_energy"]
     src["key"] = np.arange(n_sites, dtype=np.uint64)
     e2e_times = []
     h2d = n_sites * SITE_DTYPE.itemsize
@@ -275,14 +301,15 @@ def run_gpu(args) -> None:
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline(xml, args.cpu_histories, os.cpu_count() or 1, args.cpu_cycles)
+        cpu = cpu_baseline(xml, base, args.cpu_histories, os.cpu_count() or 1, args.cpu_cycles)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "histories_per_cycle": hist, "groups": 8, "rng": "philox",
+            "config": {"workload": WORKLOADS[args.workload], "histories_per_cycle": hist, **wl["config"],
+                       "rng": "philox",
                        "fast_math": bool(args.fast), "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas{ws}" if ws > 1 else "single GPU",
                        "schedule": sched},
@@ -290,7 +317,7 @@ def run_gpu(args) -> None:
             "events_per_history": e_h,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_history_mg", "algorithmic_bytes_per_launch": alg_bytes,
+                         "kernel": wl["kernel"], "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": launch_ms, "fp64_pipe_active_ncu": fp64,
                          "note": "state lives in registers, so DRAM traffic is far below the algorithmic "
                                  "bytes; the limiter is the FP64 pipe (2 ops/clk/SM on this part)"},
@@ -313,6 +340,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="two_zone", choices=sorted(WORKLOADS))
     ap.add_argument("--histories", type=int, default=1_000_000)
     ap.add_argument("--block", type=int, default=0, help="0: autotuned")
     ap.add_argument("--fast", type=int, default=1,

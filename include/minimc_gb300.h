@@ -259,21 +259,75 @@ int mc_surface_contains(mc_ctx* ctx, int32_t surface, const double* xyz, uint64_
  * for a neutron in `cell` at xyz with the given energy (MeV or group). */
 int mc_material_xs(mc_ctx* ctx, int32_t cell, const double* xyz, const double* energy,
                    uint64_t n, double* total, double* majorant);
-/* ContinuousMap::at bracket (src/ContinuousMap.hpp:21-56) on the energy grid
- * of a nuclide's total cross section: the std::map::upper_bound position,
- * found through the unionized grid. */
+/* ContinuousMap::at bracket (src/ContinuousMap.hpp:21-56): for each energy,
+ * the std::map::upper_bound position in each table of a continuous-energy
+ * nuclide (neutron data), found through the unionized grid.
+ * upper_index: [n][6] -- total, the reactions in input order, then the nubar
+ * tables of the fission reactions; -1 past the last table. */
 int mc_energy_index(mc_ctx* ctx, int32_t nuclide, const double* energy, uint64_t n,
                     int64_t* upper_index);
 
 /* ---- thermal scattering (ThermalScattering.cpp) --------------------------- */
-#define MC_TSL_POD 0   /* POD reconstruction, SampleBeta/SampleAlpha        */
-#define MC_TSL_MLP 1   /* MLP surrogate (POD outside the trained box)       */
+#define MC_TSL_POD 0      /* POD reconstruction, SampleBeta/SampleAlpha     */
+#define MC_TSL_MLP 1      /* MLP surrogate (POD outside the trained box)    */
+#define MC_TSL_PHILOX 0x10 /* flag: Philox streams keyed by seed, counter i;
+                              without it sample i draws from minstd seeded
+                              seed + i, as the reference would            */
+#define MC_TSL_FAST 0x20  /* flag: FP32 POD reconstruction (see DESIGN)     */
 /* ThermalScattering::Scatter (src/ThermalScattering.cpp:159-171) at the
- * sampler level: for each (E,T) draws beta then alpha.  Failures (resample
- * limit) leave NaN and are counted in *failures. */
+ * sampler level: for each (E,T) draws beta then alpha.  `method` is
+ * MC_TSL_POD or MC_TSL_MLP, or'ed with the flags.  Failures (resample
+ * limit) leave NaN and are counted in *failures.  Host arrays. */
 int mc_sample_tsl(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
                   uint64_t n, uint64_t seed, int32_t method, double* beta, double* alpha,
                   uint64_t* failures);
+/* The same on device arrays of the context's device (stream-ordered on the
+ * context's stream, synchronous on return).  No reference counterpart: the
+ * reference samples one scatter at a time inside Particle::Transport. */
+int mc_sample_tsl_device(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
+                         uint64_t n, uint64_t seed, int32_t method, double* beta, double* alpha,
+                         uint64_t* failures);
+/* ---- MLP surrogate of the thermal scattering sampler ----------------------
+ * No reference counterpart: the reference samples thermal scattering from
+ * its POD tables only.  Two networks (16 inputs, three hidden layers of 128
+ * with SiLU, one output; BF16 tensor-core products, FP32 master weights)
+ * map (E, T, u) to the quantile position of beta in [-E/kT, beta_cutoff],
+ * and (E, T, beta, u) to that of alpha between its kinematic bounds.  They
+ * are trained on the device from POD samples (`conditions` random (E, T)
+ * pairs in the box, `samples_per_condition` POD draws each, sorted into
+ * empirical quantiles) with Adam.  Sampling with MC_TSL_MLP outside the
+ * trained box falls back to the POD sampler. */
+typedef struct mc_train_desc {
+  double E_min, E_max;          /* trained incident-energy box (MeV)        */
+  double T_min, T_max;          /* and temperature box (K)                  */
+  uint64_t conditions;          /* (E, T) pairs; 0 -> 8192                  */
+  uint32_t samples_per_condition; /* power of two <= 1024; 0 -> 1024        */
+  uint32_t batch;               /* multiple of 128; 0 -> 8192               */
+  uint32_t steps;               /* Adam steps per network; 0 -> 4000        */
+  float lr;                     /* 0 -> 2e-3 (cosine-decayed to 1 %)        */
+  uint64_t seed;
+  uint64_t reserved[4];
+} mc_train_desc;
+typedef struct mc_train_out {
+  double loss_beta, loss_alpha; /* mean squared quantile error, last 5 %    */
+  double data_ms, train_ms;     /* device time: POD data, training          */
+  uint64_t samples;             /* training samples per network             */
+  uint64_t failures;            /* POD draws that hit the resample limit    */
+  uint64_t reserved[4];
+} mc_train_out;
+#define MC_MLP_PARAMS 35329     /* FP32 parameters per network              */
+int mc_train_surrogate(mc_ctx* ctx, int32_t tsl, const mc_train_desc* desc, mc_train_out* out);
+/* Trained weights and box (net 0: beta, 1: alpha; MC_MLP_PARAMS floats each). */
+int mc_surrogate_get(mc_ctx* ctx, float* beta_params, float* alpha_params, mc_train_desc* box);
+int mc_surrogate_set(mc_ctx* ctx, int32_t tsl, const mc_train_desc* box, const float* beta_params,
+                     const float* alpha_params);
+/* One forward and backward pass of a network with the given parameters on
+ * host inputs x[n][16] and targets y[n] (n a multiple of 128): the gradient
+ * of the mean squared error and the loss (for checking against a CPU
+ * reference); `out` (optional) receives the forward outputs. */
+int mc_surrogate_grad(mc_ctx* ctx, const float* params, const float* x, const float* y, uint64_t n,
+                      float* grad, float* loss, float* out);
+
 /* ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157). */
 int mc_tsl_total(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
                  uint64_t n, double* xs);

@@ -21,8 +21,9 @@ OUT_DIR = PKG / "_lib"
 OBJ_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libminimc_gb300.so"
 
-HOST_SOURCES = ["mc_xml.cpp", "mc_model.cpp"]
-CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_event.cu", "mc_probe.cu"]
+HOST_SOURCES = ["mc_xml.cpp", "mc_model.cpp", "mc_ce_tables.cpp"]
+CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_transport_ce.cu", "mc_event.cu", "mc_probe.cu", "mc_tsl.cu",
+                "mc_mlp.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -45,7 +46,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.hpp")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.hpp")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
 def _run(cmd: list[str]) -> None:

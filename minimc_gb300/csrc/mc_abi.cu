@@ -1,7 +1,10 @@
 // C ABI (include/minimc_gb300.h): context, world upload and the solvers.
 #include "../../include/minimc_gb300.h"
+#include "mc_ce_tables.hpp"
 #include "mc_event.cuh"
 #include "mc_kernels.cuh"
+#include "mc_mlp.cuh"
+#include "mc_tsl.cuh"
 #include "mc_model.hpp"
 
 #include <algorithm>
@@ -29,6 +32,7 @@ struct mc_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::string err;
+  std::string ce_fast_reason;  // why the FP32 union tables are off, if they are
   bool loaded = false;
   mc::Model model;
   std::vector<void*> world_allocs;
@@ -52,6 +56,14 @@ struct mc_ctx {
   bool tune_pending = false;
   double tune_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int last_grid = 0, last_block = 0;
+  // MLP surrogate of the thermal scattering sampler
+  mcd::MlpNet mlp[2];            // beta, alpha networks
+  mcd::MlpNet mlp_scratch;       // gradient checks
+  mcd::MlpBatch mlp_batch;       // training batch buffers
+  int mlp_batch_cap = 0;
+  mcd::MlpBox mlp_box{};
+  int32_t mlp_tsl = -1;          // library the networks were trained for
+  std::vector<void*> mlp_allocs;
   // k-eigenvalue state
   struct {
     bool active = false;
@@ -87,6 +99,7 @@ enum ScratchSlot {
   kEvCnt,
   kEvPend,
   kEvFis,
+  kTslFail,
 };
 
 int fail(mc_ctx* c, int code, const std::string& msg) {
@@ -129,6 +142,102 @@ void free_world(mc_ctx* c) {
   for (void* p : c->world_allocs) cudaFree(p);
   c->world_allocs.clear();
   c->loaded = false;
+  c->mlp_tsl = -1;  // the surrogate belongs to the problem's library
+}
+
+// POD partitions of a thermal scattering library: concatenated tables with
+// per-partition offsets, plus FP32 copies for the fast form (S * CDF modes,
+// and the grid-temperature modes)
+int build_pod(mc_ctx* c, const mc::PODPartitionSet& P, mcd::DevPOD& d) {
+  const size_t np = P.F.size();
+  d.n_parts = static_cast<int32_t>(np);
+  d.n_grid = static_cast<int32_t>(P.concat.size());
+  std::vector<uint32_t> ends, F_off, cdf_off, S_off, T_off, g_off;
+  std::vector<int32_t> nF, rank, nT;
+  std::vector<double> F, cdf, S, T, g;
+  std::vector<float> cs, gf;
+  for (size_t p = 0; p < np; p++) {
+    const size_t r = P.S[p].size();
+    if (r == 0 || r > 1024) return fail(c, MC_ERR_INPUT, "thermal scattering partition rank out of range");
+    ends.push_back(static_cast<uint32_t>(P.ends[p]));
+    nF.push_back(static_cast<int32_t>(P.F[p].size()));
+    rank.push_back(static_cast<int32_t>(r));
+    nT.push_back(static_cast<int32_t>(P.T[p].size()));
+    F_off.push_back(static_cast<uint32_t>(F.size()));
+    F.insert(F.end(), P.F[p].begin(), P.F[p].end());
+    cdf_off.push_back(static_cast<uint32_t>(cdf.size()));
+    for (size_t i = 0; i < P.F[p].size(); i++) {
+      for (size_t o = 0; o < r; o++) {
+        const double v = P.cdf_modes[p][i * r + o];
+        cdf.push_back(v);
+        cs.push_back(static_cast<float>(P.S[p][o] * v));
+      }
+    }
+    S_off.push_back(static_cast<uint32_t>(S.size()));
+    S.insert(S.end(), P.S[p].begin(), P.S[p].end());
+    T_off.push_back(static_cast<uint32_t>(T.size()));
+    T.insert(T.end(), P.T[p].begin(), P.T[p].end());
+    g_off.push_back(static_cast<uint32_t>(g.size()));
+    for (double v : P.g_t_modes[p]) {
+      g.push_back(v);
+      gf.push_back(static_cast<float>(v));
+    }
+  }
+  int rc;
+  if ((rc = upload(c, P.concat, &d.grid)) != MC_OK) return rc;
+  if ((rc = upload(c, ends, &d.ends)) != MC_OK) return rc;
+  if ((rc = upload(c, nF, &d.nF)) != MC_OK) return rc;
+  if ((rc = upload(c, rank, &d.rank)) != MC_OK) return rc;
+  if ((rc = upload(c, nT, &d.nT)) != MC_OK) return rc;
+  if ((rc = upload(c, F_off, &d.F_off)) != MC_OK) return rc;
+  if ((rc = upload(c, F, &d.F)) != MC_OK) return rc;
+  if ((rc = upload(c, cdf_off, &d.cdf_off)) != MC_OK) return rc;
+  if ((rc = upload(c, cdf, &d.cdf)) != MC_OK) return rc;
+  if ((rc = upload(c, cs, &d.cs)) != MC_OK) return rc;
+  if ((rc = upload(c, S_off, &d.S_off)) != MC_OK) return rc;
+  if ((rc = upload(c, S, &d.S)) != MC_OK) return rc;
+  if ((rc = upload(c, T_off, &d.T_off)) != MC_OK) return rc;
+  if ((rc = upload(c, T, &d.T)) != MC_OK) return rc;
+  if ((rc = upload(c, g_off, &d.g_off)) != MC_OK) return rc;
+  if ((rc = upload(c, g, &d.g)) != MC_OK) return rc;
+  if ((rc = upload(c, gf, &d.gf)) != MC_OK) return rc;
+  return MC_OK;
+}
+
+// thermal scattering libraries (src/ThermalScattering.hpp)
+int build_tsl(mc_ctx* c) {
+  const mc::Model& m = c->model;
+  std::vector<mcd::DevTSL> libs;
+  for (const mc::TSLData& t : m.tsl) {
+    mcd::DevTSL d{};
+    d.beta_cutoff = t.beta_cutoff;
+    d.alpha_cutoff = t.alpha_cutoff;
+    d.awr = t.awr;
+    d.cutoff_energy = t.cutoff_energy();
+    d.xs_nE = static_cast<int32_t>(t.xs_E.size());
+    d.xs_nT = static_cast<int32_t>(t.xs_T.size());
+    d.xs_rank = static_cast<int32_t>(t.xs_rank);
+    d.maj_n = static_cast<int32_t>(t.majorant.x.size());
+    if (d.xs_nE == 0 || d.xs_nT == 0 || d.maj_n == 0 || t.beta.F.empty() || t.alpha.F.empty())
+      return fail(c, MC_ERR_INPUT, "thermal scattering library with empty tables");
+    int rc;
+    if ((rc = upload(c, t.xs_E, &d.xs_E)) != MC_OK) return rc;
+    if ((rc = upload(c, t.xs_T, &d.xs_T)) != MC_OK) return rc;
+    if ((rc = upload(c, t.xs_E_modes, &d.xs_Em)) != MC_OK) return rc;
+    if ((rc = upload(c, t.xs_T_modes, &d.xs_Tm)) != MC_OK) return rc;
+    if ((rc = upload(c, t.xs_S, &d.xs_S)) != MC_OK) return rc;
+    if ((rc = upload(c, t.majorant.x, &d.maj_x)) != MC_OK) return rc;
+    if ((rc = upload(c, t.majorant.y, &d.maj_y)) != MC_OK) return rc;
+    if ((rc = build_pod(c, t.beta, d.beta)) != MC_OK) return rc;
+    if ((rc = build_pod(c, t.alpha, d.alpha)) != MC_OK) return rc;
+    bool fits = true;
+    for (const auto& S : t.beta.S) fits &= S.size() <= static_cast<size_t>(mcd::kFastPodRank);
+    for (const auto& S : t.alpha.S) fits &= S.size() <= static_cast<size_t>(mcd::kFastPodRank);
+    d.fast_ok = fits ? 1 : 0;
+    libs.push_back(d);
+  }
+  c->dw.n_tsl = static_cast<int32_t>(libs.size());
+  return upload(c, libs, &c->dw.tsl);
 }
 
 // Builds the flat device tables from the model (see mc_device.cuh for the
@@ -275,6 +384,55 @@ int build_world(mc_ctx* c) {
     UP(mcdf, mat_mg_nuc_cdf)
     UP(mnsf, mat_mg_nusigf)
   }
+  else {
+    for (const auto& nuc : m.nuclides) {
+      for (int t = 0; t < 2; t++) {
+        if (!nuc.present[t]) continue;
+        for (const auto& r : nuc.ce[t].reactions) {
+          // the reference dereferences the empty optional
+          // (src/ContinuousReaction.cpp:257-258)
+          if (r.kind == mc::kFission && !r.has_nubar) return fail(c, MC_ERR_INPUT, "nuclide " + nuc.name + ": fission without nubar");
+        }
+      }
+    }
+    mc::CETables ct;
+    try {
+      ct = mc::build_ce_tables(m);
+    }
+    catch (const std::exception& e) {
+      return fail(c, MC_ERR_INPUT, e.what());
+    }
+    c->max_yield = static_cast<uint32_t>(std::floor(ct.max_nubar)) + 1;
+    c->ce_fast_reason = ct.fast_reason;
+    if ((rc = build_tsl(c)) != MC_OK) return rc;
+    mcd::DevCE& ce = w.ce;
+    ce.nu = static_cast<int32_t>(ct.union_e.size());
+    ce.n_buckets = ct.n_buckets;
+    ce.shift = ct.shift;
+    ce.fast_ok = ct.fast_ok ? 1 : 0;
+    ce.kmax = ct.kmax;
+    ce.key0 = ct.key0;
+    std::vector<unsigned long long> ukey(ct.union_key.begin(), ct.union_key.end());
+    if ((rc = upload(c, ukey, &ce.ukey)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.union_e, &ce.ue)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.bucket, &ce.bucket)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.tab_off, &ce.tab_off)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.tab_grid, &ce.tab_grid)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.tab_x, &ce.tab_x)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.tab_y, &ce.tab_y)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.umap, &ce.umap)) != MC_OK) return rc;
+    if ((rc = upload(c, ct.nuc, &ce.nuc)) != MC_OK) return rc;
+    if (ct.fast_ok) {
+      if ((rc = upload(c, ct.union_inv, &ce.uinv)) != MC_OK) return rc;
+      if ((rc = upload(c, ct.mat_ncdf, &ce.mat_ncdf)) != MC_OK) return rc;
+      if ((rc = upload(c, ct.nuc_nubar, &ce.nuc_nubar)) != MC_OK) return rc;
+      const float* fp = nullptr;
+      if ((rc = upload(c, ct.mat_flight, &fp)) != MC_OK) return rc;
+      ce.mat_flight = reinterpret_cast<const float2*>(fp);
+      if ((rc = upload(c, ct.nuc_rx, &fp)) != MC_OK) return rc;
+      ce.nuc_rx = reinterpret_cast<const float4*>(fp);
+    }
+  }
 
   // estimators
   std::vector<int32_t> est_kind, est_target, est_has_cos, est_bin_kind;
@@ -404,7 +562,9 @@ int pick_block(const mc_run_opts* o) {
 }
 
 int grid_for(mc_ctx* c, int energy_mode, int rng, int block, bool keig, bool fast) {
-  int per_sm = mcd::history_blocks_per_sm(energy_mode, rng, block, keig, fast, c->variant);
+  int per_sm = energy_mode == mc::kMultigroup
+                   ? mcd::history_blocks_per_sm(energy_mode, rng, block, keig, fast, c->variant)
+                   : mcd::history_blocks_per_sm_ce(c->dw, rng, block, keig, fast, c->variant);
   if (per_sm < 1) per_sm = 1;
   return per_sm * c->num_sms;
 }
@@ -559,13 +719,15 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     cudaError_t e;
     if (c->model.energy_mode == mc::kMultigroup)
       e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
-    else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream);
+    else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream, c->variant);
     if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
     c->launches++;
   }
   CUDA_TRY(c, cudaEventRecord(c->evk1, c->stream));
-  if (keig && c->model.energy_mode == mc::kMultigroup) {
-    CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
+  if (keig) {
+    if (c->model.energy_mode == mc::kMultigroup)
+      CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
+    else CUDA_TRY(c, mcd::launch_fission_sites_ce(rp, rng, c->num_sms * 8, c->stream));
     c->launches++;
   }
   if (rp.nb) {
@@ -638,6 +800,7 @@ void mc_destroy(mc_ctx* c) {
   free_world(c);
   for (auto& b : c->scratch)
     if (b.p) cudaFree(b.p);
+  for (void* p : c->mlp_allocs) cudaFree(p);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->evk0) cudaEventDestroy(c->evk0);
@@ -673,7 +836,6 @@ int mc_load_xml(mc_ctx* c, const char* xml_text, const char* base_dir) {
   }
   if (c->model.has_perturbations)
     return fail(c, MC_ERR_INPUT, "perturbations and sensitivities are not supported by the GPU engine");
-  if (c->model.energy_mode == mc::kContinuous) return fail(c, MC_ERR_INPUT, "continuous-energy data: not yet supported");
   const int rc = build_world(c);
   if (rc != MC_OK) {
     free_world(c);
@@ -1122,13 +1284,22 @@ int mc_material_xs(mc_ctx* c, int32_t cell, const double* xyz, const double* ene
   if (cell < 0 || cell >= c->dw.n_cells) return fail(c, MC_ERR_INPUT, "cell index out of range");
   if (n == 0) return MC_OK;
   if (!energy || !total || !majorant) return fail(c, MC_ERR_INPUT, "null argument");
-  (void)xyz;  // multigroup cross sections do not depend on position
-  if (c->model.energy_mode != mc::kMultigroup) return fail(c, MC_ERR_INPUT, "continuous-energy data: not yet supported");
-  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * 8));
+  if (c->dw.cell_mat == nullptr || c->model.cells[static_cast<size_t>(cell)].material < 0)
+    return fail(c, MC_ERR_INPUT, "cell has no material");
+  // continuous-energy cross sections depend on the temperature at the point
+  const bool ce = c->model.energy_mode != mc::kMultigroup;
+  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * (ce ? 32 : 8)));
   auto* outp = static_cast<double*>(scratch(c, kProbeOut, n * 16));
   if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
   CUDA_TRY(c, cudaMemcpyAsync(in, energy, n * 8, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, mcd::launch_material_xs_mg(c->dw, cell, in, n, outp, outp + n, c->stream));
+  if (ce) {
+    if (xyz) CUDA_TRY(c, cudaMemcpyAsync(in + n, xyz, n * 24, cudaMemcpyHostToDevice, c->stream));
+    else CUDA_TRY(c, cudaMemsetAsync(in + n, 0, n * 24, c->stream));
+    CUDA_TRY(c, mcd::launch_material_xs_ce(c->dw, cell, in, in + n, n, outp, outp + n, c->stream));
+  }
+  else {
+    CUDA_TRY(c, mcd::launch_material_xs_mg(c->dw, cell, in, n, outp, outp + n, c->stream));
+  }
   c->launches++;
   CUDA_TRY(c, cudaMemcpyAsync(total, outp, n * 8, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(majorant, outp + n, n * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1136,20 +1307,464 @@ int mc_material_xs(mc_ctx* c, int32_t cell, const double* xyz, const double* ene
   return MC_OK;
 }
 
-int mc_energy_index(mc_ctx* c, int32_t, const double*, uint64_t, int64_t*) {
+int mc_energy_index(mc_ctx* c, int32_t nuclide, const double* energy, uint64_t n, int64_t* upper_index) {
   if (!check_ctx(c)) return MC_ERR_STATE;
-  return fail(c, MC_ERR_INPUT, "mc_energy_index: not yet implemented");
+  if (c->model.energy_mode != mc::kContinuous) return fail(c, MC_ERR_INPUT, "not a continuous-energy problem");
+  if (nuclide < 0 || nuclide >= c->dw.n_nuclides || !c->model.nuclides[static_cast<size_t>(nuclide)].present[0])
+    return fail(c, MC_ERR_INPUT, "nuclide index out of range or without neutron data");
+  if (n == 0) return MC_OK;
+  if (!energy || !upper_index) return fail(c, MC_ERR_INPUT, "null argument");
+  auto* in = static_cast<double*>(scratch(c, kProbeIn, n * 8));
+  auto* outp = static_cast<long long*>(scratch(c, kProbeOut, n * 48));
+  if (!in || !outp) return fail(c, MC_ERR_OOM, "probe buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(in, energy, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_energy_index(c->dw, nuclide, in, n, outp, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(upper_index, outp, n * 48, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
 }
 
-int mc_sample_tsl(mc_ctx* c, int32_t, const double*, const double*, uint64_t, uint64_t, int32_t, double*, double*,
-                  uint64_t*) {
-  if (!check_ctx(c)) return MC_ERR_STATE;
-  return fail(c, MC_ERR_INPUT, "mc_sample_tsl: not yet implemented");
+}  // extern "C"
+
+namespace {
+
+// ---- MLP surrogate: device buffers ------------------------------------------
+template <class T>
+T* mlp_alloc(mc_ctx* c, size_t n) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)) != cudaSuccess) return nullptr;
+  c->mlp_allocs.push_back(p);
+  return static_cast<T*>(p);
 }
 
-int mc_tsl_total(mc_ctx* c, int32_t, const double*, const double*, uint64_t, double*) {
+bool mlp_net_alloc(mc_ctx* c, mcd::MlpNet& n) {
+  if (n.p) return true;
+  using bf = __nv_bfloat16;
+  const size_t W = mcd::kMlpWidth;
+  n.p = mlp_alloc<float>(c, mcd::kMlpParams);
+  n.g = mlp_alloc<float>(c, mcd::kMlpParams);
+  n.m = mlp_alloc<float>(c, mcd::kMlpParams);
+  n.v = mlp_alloc<float>(c, mcd::kMlpParams);
+  n.W1 = mlp_alloc<bf>(c, W * mcd::kMlpIn);
+  n.W2 = mlp_alloc<bf>(c, W * W);
+  n.W3 = mlp_alloc<bf>(c, W * W);
+  n.W2t = mlp_alloc<bf>(c, W * W);
+  n.W3t = mlp_alloc<bf>(c, W * W);
+  return n.p && n.g && n.m && n.v && n.W1 && n.W2 && n.W3 && n.W2t && n.W3t;
+}
+
+bool mlp_batch_alloc(mc_ctx* c, int B) {
+  if (c->mlp_batch_cap >= B) {
+    c->mlp_batch.B = B;
+    return true;
+  }
+  using bf = __nv_bfloat16;
+  mcd::MlpBatch& b = c->mlp_batch;
+  const size_t n = static_cast<size_t>(B), W = mcd::kMlpWidth;
+  b.X = mlp_alloc<bf>(c, n * mcd::kMlpIn);
+  b.Xt = mlp_alloc<bf>(c, n * mcd::kMlpIn);
+  b.y = mlp_alloc<float>(c, n);
+  b.Z1 = mlp_alloc<float>(c, n * W);
+  b.Z2 = mlp_alloc<float>(c, n * W);
+  b.Z3 = mlp_alloc<float>(c, n * W);
+  b.H1 = mlp_alloc<bf>(c, n * W);
+  b.H2 = mlp_alloc<bf>(c, n * W);
+  b.H1t = mlp_alloc<bf>(c, n * W);
+  b.H2t = mlp_alloc<bf>(c, n * W);
+  b.dZ3 = mlp_alloc<bf>(c, n * W);
+  b.dZ2 = mlp_alloc<bf>(c, n * W);
+  b.dZ3t = mlp_alloc<bf>(c, n * W);
+  b.dZ2t = mlp_alloc<bf>(c, n * W);
+  b.dZ1t = mlp_alloc<bf>(c, n * W);
+  b.loss = mlp_alloc<float>(c, 1);
+  if (!(b.X && b.Xt && b.y && b.Z1 && b.Z2 && b.Z3 && b.H1 && b.H2 && b.H1t && b.H2t && b.dZ3 && b.dZ2 && b.dZ3t &&
+        b.dZ2t && b.dZ1t && b.loss))
+    return false;
+  c->mlp_batch_cap = B;
+  b.B = B;
+  return true;
+}
+
+// a tensor-core wait that gave up leaves a flag; report and clear it
+int mlp_check(mc_ctx* c) {
+  int h = 0;
+  CUDA_TRY(c, cudaMemcpy(&h, mcd::mlp_error_flag(), sizeof h, cudaMemcpyDeviceToHost));
+  if (h) {
+    const int z = 0;
+    cudaMemcpy(mcd::mlp_error_flag(), &z, sizeof z, cudaMemcpyHostToDevice);
+    return fail(c, MC_ERR_TIMEOUT, "a tensor-core product did not complete in time");
+  }
+  return MC_OK;
+}
+
+// PyTorch-style initialisation U(-1/sqrt(fan_in), 1/sqrt(fan_in))
+std::vector<float> mlp_init_params(uint64_t seed, int used_inputs) {
+  std::vector<float> p(mcd::kMlpParams, 0.0f);
+  uint64_t st = seed;
+  auto uni = [&](float a) {
+    st = mcd::splitmix64(st);
+    return a * (2.0f * static_cast<float>((st >> 11) * (1.0 / 9007199254740992.0)) - 1.0f);
+  };
+  const float a1 = 1.0f / std::sqrt(static_cast<float>(used_inputs)), a = 1.0f / std::sqrt(128.0f);
+  for (int o = 0; o < mcd::kMlpWidth; o++)
+    for (int i = 0; i < used_inputs; i++) p[mcd::kMlpW1 + o * mcd::kMlpIn + i] = uni(a1);
+  for (int i = 0; i < mcd::kMlpWidth; i++) p[mcd::kMlpB1 + i] = uni(a1);
+  for (int i = 0; i < mcd::kMlpWidth * mcd::kMlpWidth; i++) {
+    p[mcd::kMlpW2 + i] = uni(a);
+    p[mcd::kMlpW3 + i] = uni(a);
+  }
+  for (int i = 0; i < mcd::kMlpWidth; i++) {
+    p[mcd::kMlpB2 + i] = uni(a);
+    p[mcd::kMlpB3 + i] = uni(a);
+    p[mcd::kMlpW4 + i] = uni(a);
+  }
+  p[mcd::kMlpB4] = 0.5f;
+  return p;
+}
+
+// one network trained on (X, y) by Adam with a cosine-decayed rate; returns
+// the mean squared error over the last 5 % of the steps
+int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __nv_bfloat16* X, const float* y, uint64_t n, int used_inputs,
+              const mc_train_desc& d, uint64_t key, double* loss_out) {
+  const std::vector<float> p0 = mlp_init_params(key, used_inputs);
+  CUDA_TRY(c, cudaMemcpyAsync(net.p, p0.data(), p0.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(net.m, 0, mcd::kMlpParams * sizeof(float), c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(net.v, 0, mcd::kMlpParams * sizeof(float), c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_bf16(net, c->stream));
+  float* losses = mlp_alloc<float>(c, d.steps);
+  if (!losses) return fail(c, MC_ERR_OOM, "surrogate loss buffer");
+  mcd::MlpBatch b = c->mlp_batch;
+  for (uint32_t step = 1; step <= d.steps; step++) {
+    const double frac = static_cast<double>(step) / d.steps;
+    const float lr = static_cast<float>(d.lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+    b.loss = losses + (step - 1);
+    CUDA_TRY(c, mcd::launch_mlp_gather(X, y, n, key, static_cast<int>(step), b, c->stream));
+    CUDA_TRY(c, mcd::mlp_forward_backward(net, b, c->stream));
+    CUDA_TRY(c, mcd::mlp_adam(net, static_cast<int>(step), lr, c->stream));
+    c->launches += 12;
+  }
+  std::vector<float> h(d.steps);
+  CUDA_TRY(c, cudaMemcpyAsync(h.data(), losses, d.steps * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const uint32_t tail = std::max<uint32_t>(1, d.steps / 20);
+  double acc = 0;
+  for (uint32_t i = d.steps - tail; i < d.steps; i++) acc += h[i];
+  *loss_out = acc / tail / d.batch;
+  return mlp_check(c);
+}
+
+int sample_tsl_mlp(mc_ctx* c, int32_t tsl, const double* E, const double* T, uint64_t n, uint64_t seed, int32_t,
+                   double* beta, double* alpha, uint64_t* failures) {
+  if (c->mlp_tsl != tsl) return fail(c, MC_ERR_STATE, "the MLP surrogate is not trained for this library");
+  auto* d_fail = static_cast<unsigned long long*>(scratch(c, kTslFail, sizeof(unsigned long long)));
+  if (!d_fail) return fail(c, MC_ERR_OOM, "sampler counters");
+  CUDA_TRY(c, cudaMemsetAsync(d_fail, 0, sizeof(unsigned long long), c->stream));
+  CUDA_TRY(c, mcd::launch_sample_tsl_mlp(c->dw.tsl + tsl, c->mlp[0], c->mlp[1], c->mlp_box, E, T, n,
+                                         run_key(seed, 0, 0x4D4C5053ull), beta, alpha, d_fail, c->num_sms,
+                                         c->stream));
+  c->launches++;
+  unsigned long long h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, d_fail, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (failures) *failures = h;
+  return mlp_check(c);
+}
+
+// the sampler on device arrays; `method` as mc_sample_tsl
+int sample_tsl_device(mc_ctx* c, int32_t tsl, const double* E, const double* T, uint64_t n, uint64_t seed,
+                      int32_t method, double* beta, double* alpha, uint64_t* failures) {
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  const int base = method & 0xF;
+  if (base == MC_TSL_MLP) return sample_tsl_mlp(c, tsl, E, T, n, seed, method, beta, alpha, failures);
+  if (base != MC_TSL_POD) return fail(c, MC_ERR_INPUT, "unknown thermal scattering method");
+  const bool philox = (method & MC_TSL_PHILOX) != 0;
+  const bool fast = (method & MC_TSL_FAST) != 0;
+  if (fast && !c->model.tsl[static_cast<size_t>(tsl)].beta.S.empty()) {
+    const mc::TSLData& t = c->model.tsl[static_cast<size_t>(tsl)];
+    for (const auto* set : {&t.beta, &t.alpha})
+      for (const auto& S : set->S)
+        if (S.size() > static_cast<size_t>(mcd::kFastPodRank))
+          return fail(c, MC_ERR_INPUT, "the FP32 POD form supports ranks up to " + std::to_string(mcd::kFastPodRank));
+  }
+  auto* d_fail = static_cast<unsigned long long*>(scratch(c, kTslFail, sizeof(unsigned long long)));
+  if (!d_fail) return fail(c, MC_ERR_OOM, "sampler counters");
+  CUDA_TRY(c, cudaMemsetAsync(d_fail, 0, sizeof(unsigned long long), c->stream));
+  CUDA_TRY(c, mcd::launch_sample_tsl(c->dw.tsl + tsl, fast, philox ? 0 : 1, E, T, n, seed,
+                                     run_key(seed, 0, 0x54534C00ull), beta, alpha, d_fail, c->stream));
+  c->launches++;
+  unsigned long long h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, d_fail, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (failures) *failures = h;
+  return MC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mc_train_surrogate(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_train_out* out) {
   if (!check_ctx(c)) return MC_ERR_STATE;
-  return fail(c, MC_ERR_INPUT, "mc_tsl_total: not yet implemented");
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  if (!desc) return fail(c, MC_ERR_INPUT, "null argument");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  mc_train_desc d = *desc;
+  if (!d.conditions) d.conditions = 8192;
+  if (!d.samples_per_condition) d.samples_per_condition = 1024;
+  if (!d.batch) d.batch = 8192;
+  if (!d.steps) d.steps = 4000;
+  if (!(d.lr > 0)) d.lr = 2e-3f;
+  const uint32_t K = d.samples_per_condition;
+  if (K < 2 || K > 1024 || (K & (K - 1))) return fail(c, MC_ERR_INPUT, "samples_per_condition: a power of two <= 1024");
+  if (d.batch % 128 || d.batch > (1u << 20)) return fail(c, MC_ERR_INPUT, "batch: a multiple of 128 up to 2^20");
+  const mc::TSLData& t = c->model.tsl[static_cast<size_t>(tsl)];
+  if (!(d.E_min > 0 && d.E_min < d.E_max && d.E_max < t.cutoff_energy()))
+    return fail(c, MC_ERR_INPUT, "energy box must lie inside (0, cutoff energy)");
+  if (!(d.T_min > 0 && d.T_min < d.T_max)) return fail(c, MC_ERR_INPUT, "temperature box");
+  mcd::MlpBox box;
+  box.logE0 = std::log(d.E_min);
+  box.logE1 = std::log(d.E_max);
+  box.T0 = d.T_min;
+  box.T1 = d.T_max;
+  box.beta_cutoff = t.beta_cutoff;
+  box.awr = t.awr;
+  box.beta_scale = std::log1p(std::max(t.beta_cutoff, d.E_max / (mcd::kBoltzmann * d.T_min)));
+  if (!mlp_net_alloc(c, c->mlp[0]) || !mlp_net_alloc(c, c->mlp[1]) || !mlp_batch_alloc(c, static_cast<int>(d.batch)))
+    return fail(c, MC_ERR_OOM, "surrogate buffers");
+  const uint64_t Nc = d.conditions, N = Nc * K;
+  // data buffers (freed at the end)
+  std::vector<void*> tmp;
+  auto dalloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    tmp.push_back(p);
+    return p;
+  };
+  auto release = [&]() {
+    cudaStreamSynchronize(c->stream);
+    for (void* p : tmp) cudaFree(p);
+  };
+  auto* Ec = static_cast<double*>(dalloc(Nc * 8));
+  auto* Tc = static_cast<double*>(dalloc(Nc * 8));
+  auto* bc = static_cast<double*>(dalloc(Nc * 8));
+  auto* Ex = static_cast<double*>(dalloc(N * 8));
+  auto* Tx = static_cast<double*>(dalloc(N * 8));
+  auto* U = static_cast<double*>(dalloc(N * 8));
+  auto* bx = static_cast<double*>(dalloc(N * 8));
+  auto* sx = static_cast<double*>(dalloc(N * 8));
+  auto* X = static_cast<__nv_bfloat16*>(dalloc(N * mcd::kMlpIn * 2));
+  auto* y = static_cast<float*>(dalloc(N * 4));
+  auto* d_fail = static_cast<unsigned long long*>(dalloc(8));
+  if (!(Ec && Tc && bc && Ex && Tx && U && bx && sx && X && y && d_fail)) {
+    release();
+    return fail(c, MC_ERR_OOM, "surrogate training data");
+  }
+  // conditions: E log-uniform, T uniform in the box
+  std::vector<double> he(Nc), ht(Nc);
+  uint64_t st = d.seed * 0x9E3779B97F4A7C15ull + 12345;
+  for (uint64_t i = 0; i < Nc; i++) {
+    st = mcd::splitmix64(st);
+    const double a = (st >> 11) * (1.0 / 9007199254740992.0);
+    st = mcd::splitmix64(st);
+    const double b = (st >> 11) * (1.0 / 9007199254740992.0);
+    he[i] = std::exp(box.logE0 + a * (box.logE1 - box.logE0));
+    ht[i] = d.T_min + b * (d.T_max - d.T_min);
+  }
+  int rc = MC_OK;
+  mc_train_out o{};
+  double loss_b = 0, loss_a = 0;
+  do {
+    cudaError_t e;
+#define TRY_CUDA(expr)                                                                    \
+  if ((e = (expr)) != cudaSuccess) {                                                      \
+    rc = fail(c, MC_ERR_DEVICE, std::string(#expr) + ": " + cudaGetErrorString(e));       \
+    break;                                                                                \
+  }
+    TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
+    TRY_CUDA(cudaMemcpyAsync(Ec, he.data(), Nc * 8, cudaMemcpyHostToDevice, c->stream));
+    TRY_CUDA(cudaMemcpyAsync(Tc, ht.data(), Nc * 8, cudaMemcpyHostToDevice, c->stream));
+    TRY_CUDA(cudaMemsetAsync(d_fail, 0, 8, c->stream));
+    TRY_CUDA(mcd::launch_expand(Ec, N, static_cast<int>(K), Ex, c->stream));
+    TRY_CUDA(mcd::launch_expand(Tc, N, static_cast<int>(K), Tx, c->stream));
+    TRY_CUDA(mcd::launch_quantile_u(U, N, static_cast<int>(K), c->stream));
+    // beta network: sorted POD draws per condition
+    TRY_CUDA(mcd::launch_tsl_beta_draws(c->dw.tsl + tsl, Ex, Tx, N, run_key(d.seed, 1, 0x4D4C4231ull), sx, d_fail,
+                                        c->stream));
+    TRY_CUDA(mcd::launch_segment_sort(sx, Nc, static_cast<int>(K), c->stream));
+    TRY_CUDA(mcd::launch_mlp_features_beta(box, Ex, Tx, U, sx, N, X, y, c->stream));
+    TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
+    TRY_CUDA(cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.data_ms += ms;
+    TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if ((rc = mlp_train(c, c->mlp[0], X, y, N, 4, d, run_key(d.seed, 2, 0x4D4C4231ull), &loss_b)) != MC_OK) break;
+    TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
+    TRY_CUDA(cudaEventSynchronize(c->ev1));
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.train_ms += ms;
+    // alpha network: one beta per condition, sorted alpha draws given it
+    TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
+    TRY_CUDA(mcd::launch_tsl_beta_draws(c->dw.tsl + tsl, Ec, Tc, Nc, run_key(d.seed, 3, 0x4D4C4132ull), bc, d_fail,
+                                        c->stream));
+    TRY_CUDA(mcd::launch_expand(bc, N, static_cast<int>(K), bx, c->stream));
+    TRY_CUDA(mcd::launch_tsl_alpha_draws(c->dw.tsl + tsl, Ex, Tx, bx, N, run_key(d.seed, 4, 0x4D4C4132ull), sx,
+                                         d_fail, c->stream));
+    TRY_CUDA(mcd::launch_segment_sort(sx, Nc, static_cast<int>(K), c->stream));
+    TRY_CUDA(mcd::launch_mlp_features_alpha(box, Ex, Tx, bx, U, sx, N, X, y, c->stream));
+    TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
+    TRY_CUDA(cudaEventSynchronize(c->ev1));
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.data_ms += ms;
+    TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if ((rc = mlp_train(c, c->mlp[1], X, y, N, 6, d, run_key(d.seed, 5, 0x4D4C4132ull), &loss_a)) != MC_OK) break;
+    TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
+    TRY_CUDA(cudaEventSynchronize(c->ev1));
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.train_ms += ms;
+    unsigned long long f = 0;
+    TRY_CUDA(cudaMemcpy(&f, d_fail, 8, cudaMemcpyDeviceToHost));
+    o.failures = f;
+#undef TRY_CUDA
+  } while (false);
+  c->launches += 12;
+  release();
+  if (rc != MC_OK) return rc;
+  c->mlp_box = box;
+  c->mlp_tsl = tsl;
+  o.loss_beta = loss_b;
+  o.loss_alpha = loss_a;
+  o.samples = N;
+  if (out) *out = o;
+  return MC_OK;
+}
+
+int mc_surrogate_get(mc_ctx* c, float* beta_params, float* alpha_params, mc_train_desc* box) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (c->mlp_tsl < 0) return fail(c, MC_ERR_STATE, "no trained surrogate");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  if (beta_params)
+    CUDA_TRY(c, cudaMemcpy(beta_params, c->mlp[0].p, mcd::kMlpParams * sizeof(float), cudaMemcpyDeviceToHost));
+  if (alpha_params)
+    CUDA_TRY(c, cudaMemcpy(alpha_params, c->mlp[1].p, mcd::kMlpParams * sizeof(float), cudaMemcpyDeviceToHost));
+  if (box) {
+    *box = mc_train_desc{};
+    box->E_min = std::exp(c->mlp_box.logE0);
+    box->E_max = std::exp(c->mlp_box.logE1);
+    box->T_min = c->mlp_box.T0;
+    box->T_max = c->mlp_box.T1;
+  }
+  return MC_OK;
+}
+
+int mc_surrogate_set(mc_ctx* c, int32_t tsl, const mc_train_desc* box, const float* beta_params,
+                     const float* alpha_params) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  if (!box || !beta_params || !alpha_params) return fail(c, MC_ERR_INPUT, "null argument");
+  if (!(box->E_min > 0 && box->E_min < box->E_max && box->T_min > 0 && box->T_min < box->T_max))
+    return fail(c, MC_ERR_INPUT, "box");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  if (!mlp_net_alloc(c, c->mlp[0]) || !mlp_net_alloc(c, c->mlp[1])) return fail(c, MC_ERR_OOM, "surrogate buffers");
+  const mc::TSLData& t = c->model.tsl[static_cast<size_t>(tsl)];
+  mcd::MlpBox b;
+  b.logE0 = std::log(box->E_min);
+  b.logE1 = std::log(box->E_max);
+  b.T0 = box->T_min;
+  b.T1 = box->T_max;
+  b.beta_cutoff = t.beta_cutoff;
+  b.awr = t.awr;
+  b.beta_scale = std::log1p(std::max(t.beta_cutoff, box->E_max / (mcd::kBoltzmann * box->T_min)));
+  CUDA_TRY(c, cudaMemcpy(c->mlp[0].p, beta_params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->mlp[1].p, alpha_params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, mcd::mlp_refresh_bf16(c->mlp[0], c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_bf16(c->mlp[1], c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->mlp_box = b;
+  c->mlp_tsl = tsl;
+  return MC_OK;
+}
+
+int mc_surrogate_grad(mc_ctx* c, const float* params, const float* x, const float* y, uint64_t n, float* grad,
+                      float* loss, float* out) {
+  if (!c) return MC_ERR_STATE;
+  if (!params || !x || !y || !grad) return fail(c, MC_ERR_INPUT, "null argument");
+  if (n == 0 || n % 128 || n > (1u << 20)) return fail(c, MC_ERR_INPUT, "n: a multiple of 128 up to 2^20");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  if (!mlp_net_alloc(c, c->mlp_scratch) || !mlp_batch_alloc(c, static_cast<int>(n)))
+    return fail(c, MC_ERR_OOM, "surrogate buffers");
+  mcd::MlpBatch b = c->mlp_batch;
+  b.B = static_cast<int>(n);
+  std::vector<__nv_bfloat16> hx(n * mcd::kMlpIn), hxt(n * mcd::kMlpIn);
+  for (uint64_t r = 0; r < n; r++)
+    for (int f = 0; f < mcd::kMlpIn; f++) {
+      hx[r * mcd::kMlpIn + f] = __float2bfloat16_rn(x[r * mcd::kMlpIn + f]);
+      hxt[f * n + r] = hx[r * mcd::kMlpIn + f];
+    }
+  const mcd::MlpNet& net = c->mlp_scratch;
+  CUDA_TRY(c, cudaMemcpyAsync(net.p, params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(b.X, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(b.Xt, hxt.data(), hxt.size() * 2, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(b.y, y, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_bf16(net, c->stream));
+  CUDA_TRY(c, mcd::mlp_forward_backward(net, b, c->stream));
+  c->launches += 10;
+  CUDA_TRY(c, cudaMemcpyAsync(grad, net.g, mcd::kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  float hl = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&hl, b.loss, sizeof hl, cudaMemcpyDeviceToHost, c->stream));
+  if (out) {
+    float* d_out = reinterpret_cast<float*>(b.Z2);  // free after the backward pass
+    CUDA_TRY(c, mcd::mlp_forward(net, b, d_out, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(out, d_out, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (loss) *loss = hl;
+  return mlp_check(c);
+}
+
+int mc_sample_tsl_device(mc_ctx* c, int32_t tsl, const double* energy, const double* temperature, uint64_t n,
+                         uint64_t seed, int32_t method, double* beta, double* alpha, uint64_t* failures) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n == 0) return MC_OK;
+  if (!energy || !temperature || !beta || !alpha) return fail(c, MC_ERR_INPUT, "null argument");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  return sample_tsl_device(c, tsl, energy, temperature, n, seed, method, beta, alpha, failures);
+}
+
+int mc_sample_tsl(mc_ctx* c, int32_t tsl, const double* energy, const double* temperature, uint64_t n, uint64_t seed,
+                  int32_t method, double* beta, double* alpha, uint64_t* failures) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (n == 0) return MC_OK;
+  if (!energy || !temperature || !beta || !alpha) return fail(c, MC_ERR_INPUT, "null argument");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  auto* buf = static_cast<double*>(scratch(c, kProbeIn, n * 32));
+  if (!buf) return fail(c, MC_ERR_OOM, "sampler buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(buf, energy, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(buf + n, temperature, n * 8, cudaMemcpyHostToDevice, c->stream));
+  const int rc = sample_tsl_device(c, tsl, buf, buf + n, n, seed, method, buf + 2 * n, buf + 3 * n, failures);
+  if (rc != MC_OK) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(beta, buf + 2 * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(alpha, buf + 3 * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_tsl_total(mc_ctx* c, int32_t tsl, const double* energy, const double* temperature, uint64_t n, double* xs) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  if (n == 0) return MC_OK;
+  if (!energy || !temperature || !xs) return fail(c, MC_ERR_INPUT, "null argument");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  auto* buf = static_cast<double*>(scratch(c, kProbeIn, n * 24));
+  if (!buf) return fail(c, MC_ERR_OOM, "buffers");
+  CUDA_TRY(c, cudaMemcpyAsync(buf, energy, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(buf + n, temperature, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_tsl_total(c->dw.tsl + tsl, buf, buf + n, n, buf + 2 * n, c->stream));
+  c->launches++;
+  CUDA_TRY(c, cudaMemcpyAsync(xs, buf + 2 * n, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
 }
 
 }  // extern "C"

@@ -6,6 +6,8 @@
 // x86-64 without FMA, rounds every product and sum separately.
 #pragma once
 
+#include "mc_ce_layout.h"
+
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -61,6 +63,72 @@ struct BoxCell {
   int32_t order[6]; // position of each plane in the cell's surface list
 };
 
+// Continuous-energy tables (built by mc_ce_tables.cpp; lookups in mc_ce.cuh).
+struct DevCE {
+  int32_t nu;                         // union grid points
+  int32_t n_buckets;
+  int32_t shift;                      // bucket = (key(E) - key0) >> shift
+  int32_t fast_ok;                    // FP32 union tables valid
+  int32_t kmax;                       // row length of mat_ncdf
+  int32_t pad;
+  unsigned long long key0;
+  const unsigned long long* ukey;     // [nu] union energies as integer keys
+  const double* ue;                   // [nu] union energies
+  const uint32_t* bucket;             // [n_buckets + 1]
+  const uint32_t* tab_off;            // [n_tables + 1]
+  const int32_t* tab_grid;            // [n_tables]
+  const double* tab_x;
+  const double* tab_y;
+  const uint32_t* umap;               // [n_grids][nu + 1]
+  const mc::CENuclideDesc* nuc;       // [2][n_nuclides]
+  const float* uinv;                  // [nu]
+  const float2* mat_flight;           // [2][M][nu]
+  const float* mat_ncdf;              // [2][M][nu][kmax]
+  const float4* nuc_rx;               // [2][N][nu]
+  const float* nuc_nubar;             // [2][N][nu]
+};
+
+// One set of POD partitions of a thermal scattering library
+// (src/ThermalScattering.hpp:58-97): beta partitions (grid = incident
+// energies) or alpha partitions (grid = betas).  Per partition p the tables
+// are concatenated; offsets index them.
+struct DevPOD {
+  int32_t n_parts;
+  int32_t n_grid;             // concatenated grid length
+  const double* grid;         // [n_grid] Es or betas, increasing
+  const uint32_t* ends;       // [n_parts] one past each partition's last grid index
+  const int32_t* nF;          // [n_parts] CDF values
+  const int32_t* rank;        // [n_parts]
+  const int32_t* nT;          // [n_parts] temperatures
+  const uint32_t* F_off;      // [n_parts] into F
+  const double* F;
+  const uint32_t* cdf_off;    // [n_parts] into cdf ([nF][rank])
+  const double* cdf;
+  const float* cs;            // [.] S[o] * cdf[F][o] in FP32 (fast form), same offsets as cdf
+  const uint32_t* S_off;      // [n_parts] into S
+  const double* S;
+  const uint32_t* T_off;      // [n_parts] into T
+  const double* T;
+  const uint32_t* g_off;      // [n_parts] into g ([grid][nT][rank])
+  const double* g;
+  const float* gf;            // g in FP32 (fast form), same offsets
+};
+
+struct DevTSL {
+  double beta_cutoff, alpha_cutoff, awr, cutoff_energy;
+  int32_t xs_nE, xs_nT, xs_rank, maj_n;
+  int32_t fast_ok;            // every partition's rank fits the FP32 form
+  int32_t pad;
+  const double* xs_E;         // [xs_nE]
+  const double* xs_T;         // [xs_nT]
+  const double* xs_Em;        // [xs_nE][xs_rank]
+  const double* xs_Tm;        // [xs_nT][xs_rank]
+  const double* xs_S;         // [xs_rank]
+  const double* maj_x;        // majorant ContinuousMap
+  const double* maj_y;
+  DevPOD beta, alpha;
+};
+
 // Flattened world, passed to kernels by value.
 struct DevWorld {
   int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
@@ -109,6 +177,9 @@ struct DevWorld {
   const int32_t* cell_box;        // [n_cells] index into boxes, or -1
   const struct BoxCell* boxes;
   const double* mat_mg_sigma;     // [T][M][G] number_density * microscopic total
+  DevCE ce;                       // continuous energy
+  int32_t n_tsl;
+  const DevTSL* tsl;              // [n_tsl] thermal scattering libraries
   // source (src/Source.cpp)
   double src_pos[3];
   double src_dir[3];

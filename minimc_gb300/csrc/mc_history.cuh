@@ -1,0 +1,226 @@
+// Per-particle helpers shared by the history-schedule transport kernels
+// (multigroup: mc_transport.cu, continuous energy: mc_transport_ce.cu).
+#pragma once
+
+#include "mc_kernels.cuh"
+
+#include <type_traits>
+
+namespace mcd {
+namespace hist {
+
+constexpr int kStack = 32;    // fixed-source secondaries per history in flight
+constexpr int kPending = 24;  // distinct tally bins per history
+
+template <class Rng>
+struct Particle {
+  double x, y, z, u, v, w;
+  int g;          // multigroup group, 0-based
+  double E;       // continuous energy, MeV
+  int j;          // continuous energy: union-grid upper_bound index of E
+  int cell;
+  int surf;       // last surface crossed (current estimator)
+  int skip;       // robust crossing: surface just left, ignored until the next collision
+  int event;
+  int type;
+  uint32_t nev;
+  Rng rng;
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// start a particle from the problem's Source (src/Source.cpp:143-154)
+template <class Rng>
+__device__ __forceinline__ void sample_source(const DevWorld& w, const RunParams& rp, unsigned long long i,
+                                              Particle<Rng>& p) {
+  p.x = w.src_pos[0];
+  p.y = w.src_pos[1];
+  p.z = w.src_pos[2];
+  p.type = w.src_type;
+  if constexpr (std::is_same_v<Rng, MinstdRng>) {
+    // Source::Sample(seed): a fresh RNG{seed} samples position, direction,
+    // energy and type in that order, then the particle is seeded with rng()
+    MinstdRng s;
+    s.seed(rp.ref_source_seeds ? rp.seed + i : i + 1);
+    if (w.src_dir_kind == 0) {
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+    }
+    else if (w.src_dir_kind == 1) {
+      isotropic(s, p.u, p.v, p.w);
+    }
+    else {
+      // IsotropicFlux::Sample (src/Source.cpp:113-120)
+      const double mu = __dsqrt_rn(s.u01());
+      const double phi = dadd(dmul(s.u01(), 2 * kPi), 0.0);
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+      rotate(p.u, p.v, p.w, mu, phi);
+    }
+    p.rng.seed(s.next());
+  }
+  else {
+    p.rng.init(rp.run_key, i, 0);
+    if (w.src_dir_kind == 0) {
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+    }
+    else if (w.src_dir_kind == 1) {
+      if (rp.fast) isotropic_fast(p.rng, p.u, p.v, p.w);
+      else isotropic(p.rng, p.u, p.v, p.w);
+    }
+    else {
+      const double mu = sqrt(p.rng.u01());
+      const double phi = 2 * kPi * p.rng.u01();
+      p.u = w.src_dir[0];
+      p.v = w.src_dir[1];
+      p.w = w.src_dir[2];
+      rotate(p.u, p.v, p.w, mu, phi);
+    }
+  }
+  if (w.energy_mode == 0) p.g = static_cast<int>(w.src_energy) - 1;
+  else p.E = w.src_energy;
+}
+
+template <class Rng>
+__device__ __forceinline__ void start_from_site(const RunParams& rp, unsigned long long i, const Site& s,
+                                                Particle<Rng>& p, int energy_mode) {
+  p.x = s.x;
+  p.y = s.y;
+  p.z = s.z;
+  p.u = s.u;
+  p.v = s.v;
+  p.w = s.w;
+  if (energy_mode == 0) p.g = static_cast<int>(s.energy) - 1;
+  else p.E = s.energy;
+  p.type = 0;
+  if constexpr (std::is_same_v<Rng, MinstdRng>) {
+    // k-eigenvalue sources: particle i of a cycle is seeded with base + i;
+    // mc_transport_bank passes the site's own key
+    p.rng.seed(rp.minstd_base ? rp.minstd_base + i : s.key);
+  }
+  else {
+    if (rp.minstd_base) p.rng.init(rp.run_key, i, 0);
+    else p.rng.init(rp.run_key, s.key, 1);
+  }
+}
+
+template <class Rng>
+__device__ __forceinline__ double uniform(Rng& rng, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return static_cast<double>(rng.u01f());
+  }
+  return rng.u01();
+}
+
+// exponential_distribution{sigma}: -log(1 - U) / sigma
+template <class Rng>
+__device__ __forceinline__ double sample_flight(Rng& rng, double sigma, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return flight_fast(rng.u01f(), sigma);
+  }
+  return ddiv(-log(dsub(1.0, rng.u01())), sigma);
+}
+
+template <class Rng>
+__device__ __forceinline__ void sample_isotropic(Rng& rng, double& u, double& v, double& w, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) {
+      isotropic_fast(rng, u, v, w);
+      return;
+    }
+  }
+  isotropic(rng, u, v, w);
+}
+
+// first index k in [0, n) with cdf[k] > threshold, or -1
+__device__ __forceinline__ int cdf_search(const double* cdf, int n, int, double threshold) {
+  return cdf_first_above(cdf, n, threshold);
+}
+
+// score helpers -----------------------------------------------------------
+
+template <class Rng>
+__device__ __forceinline__ double energy_value(const DevWorld& w, const Particle<Rng>& p) {
+  // ParticleBins::VisitEnergy: group number or energy
+  return w.energy_mode == 0 ? static_cast<double>(p.g + 1) : p.E;
+}
+
+// Per-history scores go to the history's row of a dense array (few bins,
+// committed by a separate kernel) or to a per-thread list (many bins).
+struct Scorer {
+  Pending<kPending>* list;
+  double* dense;                // this history's column of the bin-major array
+  unsigned long long stride;    // histories per bin row
+  __device__ __forceinline__ void add(uint32_t b, double s) {
+    if (dense) atomicAdd(dense + b * stride, s);
+    else list->add(b, s);
+  }
+};
+
+// ParticleBins::GetIndex of the particle: group form (multigroup) or
+// energy form (continuous energy)
+template <bool CE, class Rng>
+__device__ __forceinline__ uint64_t bin_of(const DevWorld& w, int e, const Particle<Rng>& p) {
+  if constexpr (CE) return particle_bin(w, e, p.u, p.v, p.w, p.E);
+  else return particle_bin_mg(w, e, p.u, p.v, p.w, p.g);
+}
+
+// EstimatorSetProxy::Score (src/Estimator.cpp:247-251) for the current
+// estimator (src/Estimator.cpp:142-151): 1 on a crossing of its surface
+template <bool CE = false, class Rng>
+__device__ __forceinline__ void score_event(const DevWorld& w, const Particle<Rng>& p, Scorer& sc) {
+  if (p.event != kSurfaceCross && p.event != kLeak) return;
+  for (int e = 0; e < w.n_est; e++) {
+    if (__ldg(w.est_kind + e) != 0 || __ldg(w.est_target + e) != p.surf) continue;
+    const uint64_t b = __ldg(w.est_offset + e) + bin_of<CE>(w, e, p);
+    sc.add(static_cast<uint32_t>(b), 1.0);
+  }
+}
+
+// track-length estimator (extension): flight length inside the cell
+template <bool CE = false, class Rng>
+__device__ __forceinline__ void score_track(const DevWorld& w, const Particle<Rng>& p, double d, Scorer& sc) {
+  for (int e = 0; e < w.n_est; e++) {
+    if (__ldg(w.est_kind + e) != 1 || __ldg(w.est_target + e) != p.cell) continue;
+    const uint64_t b = __ldg(w.est_offset + e) + bin_of<CE>(w, e, p);
+    sc.add(static_cast<uint32_t>(b), d);
+  }
+}
+
+__device__ __forceinline__ void stream(double& x, double& y, double& z, double u, double v, double w, double d) {
+  // Particle::Stream (src/Particle.cpp:46-53): position += direction * d
+  x = dadd(x, dmul(u, d));
+  y = dadd(y, dmul(v, d));
+  z = dadd(z, dmul(w, d));
+}
+
+// block-shared tally cache for problems with few bins
+constexpr int kSharedBins = 512;
+
+struct TallySink {
+  double* ssum;  // shared or nullptr
+  double* ssq;
+  double* gsum;
+  double* gsq;
+  __device__ __forceinline__ void commit(const Pending<kPending>& pend) {
+    for (int i = 0; i < pend.n; i++) {
+      const double s = pend.score[i];
+      const uint32_t b = pend.bin[i];
+      if (ssum) {
+        atomicAdd(ssum + b, s);
+        atomicAdd(ssq + b, s * s);
+      }
+      else {
+        atomicAdd(gsum + b, s);
+        atomicAdd(gsq + b, s * s);
+      }
+    }
+  }
+};
+
+}  // namespace hist
+}  // namespace mcd

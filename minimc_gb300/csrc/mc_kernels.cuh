@@ -67,9 +67,22 @@ cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stre
 int history_variants();
 cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
                               cudaStream_t stream, int variant);
-cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
-                              cudaStream_t stream);
 int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant);
+
+// continuous energy (mc_transport_ce.cu)
+bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast);
+cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
+                              cudaStream_t stream, int variant);
+int history_blocks_per_sm_ce(const DevWorld& w, int rng_mode, int block, bool keig, bool fast, int variant);
+cudaError_t launch_fission_sites_ce(const RunParams& rp, int rng_mode, int grid, cudaStream_t stream);
+
+// thermal scattering sampler and totals (mc_tsl.cu); rng_mode 1 = minstd
+// seeded seed + i, else Philox keyed by `key`, counter i
+cudaError_t launch_sample_tsl(const DevTSL* tsl, bool fast, int rng_mode, const double* E, const double* T,
+                              unsigned long long n, unsigned long long seed, unsigned long long key, double* beta,
+                              double* alpha, unsigned long long* failures, cudaStream_t stream);
+cudaError_t launch_tsl_total(const DevTSL* tsl, const double* E, const double* T, unsigned long long n, double* out,
+                             cudaStream_t stream);
 
 // bank compaction and resampling (mc_transport.cu)
 cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
@@ -90,6 +103,10 @@ cudaError_t launch_surface_contains(const DevWorld& w, int32_t s, const double* 
                                     int8_t* out, cudaStream_t stream);
 cudaError_t launch_material_xs_mg(const DevWorld& w, int32_t cell, const double* energy, unsigned long long n,
                                   double* total, double* majorant, cudaStream_t stream);
+cudaError_t launch_material_xs_ce(const DevWorld& w, int32_t cell, const double* energy, const double* xyz,
+                                  unsigned long long n, double* total, double* majorant, cudaStream_t stream);
+cudaError_t launch_energy_index(const DevWorld& w, int32_t nuclide, const double* energy, unsigned long long n,
+                                long long* out, cudaStream_t stream);
 
 // Philox helper shared with the host-side resampler description
 __host__ __device__ inline unsigned long long splitmix64(unsigned long long z) {

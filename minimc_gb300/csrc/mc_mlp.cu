@@ -1,0 +1,786 @@
+// MLP surrogate kernels (layout and interfaces in mc_mlp.cuh).
+//
+// Training products, per step over a batch of B samples (B a multiple of
+// 128), all C = A * B^T with K-major BF16 operands on the tensor cores:
+//   forward   Z1 = X W1^T, Z2 = H1 W2^T, Z3 = H2 W3^T      (M = B, N = 128)
+//   backward  dH2 = dZ3 W3, dH1 = dZ2 W2                   (M = B, N = 128)
+//             dW3 = dZ3^T H2, dW2 = dZ2^T H1, dW1 = dZ1^T X (M = 128, K = B,
+//             split over K across CTAs, FP32 atomics)
+// Epilogues fuse bias, SiLU and its derivative, the transposed copies the
+// weight-gradient products read, and the bias-gradient column sums.  The
+// output layer (128 -> 1) and the loss run on the CUDA cores.
+#include "mc_mlp.cuh"
+#include "mc_tc.cuh"
+#include "mc_tsl.cuh"
+
+namespace mcd {
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+constexpr long long kWaitCycles = 2000000000LL;  // ~1 s: an MMA never takes that long
+
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = __fdividef(1.0f, 1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// generic GEMM: one CTA (128 threads) computes rows [m0, m0 + 128) x N of
+// C = A[M x K] * B[N x K]^T over the K range of its split (blockIdx.z),
+// KC columns at a time through shared memory; the accumulator lives in
+// tensor memory and is handed to the epilogue row by row.
+struct GemmArgs {
+  const bf16* A;
+  int lda;
+  const bf16* B;
+  int ldb;
+  int k_split;  // K per CTA (multiple of KC)
+  int* err;     // set when an MMA wait timed out
+};
+
+template <int N, int KC, class Epi>
+__global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 128, "N");
+  static_assert(KC % 16 == 0 && KC <= 64, "KC");
+  constexpr int kCols = N < 32 ? 32 : N;  // tensor-memory columns (power of two >= 32)
+  __shared__ __align__(1024) uint8_t sA[128 * KC * 2];
+  __shared__ __align__(1024) uint8_t sB[N * KC * 2];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * 128;
+  const int k_begin = blockIdx.z * a.k_split;
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_slot), kCols);
+  if (tid == 0) tc::mbar_init(tc::smem_addr(&mbar), 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t mb = tc::smem_addr(&mbar);
+  constexpr uint32_t idesc = tc::idesc_bf16_f32(128, N);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < a.k_split && ok; k0 += KC) {
+    // operand tiles: one 16-byte chunk (8 values of one row) per step,
+    // consecutive threads on consecutive rows
+    for (int c = tid; c < 128 * (KC / 8); c += 128) {
+      const int row = c & 127, kc = c >> 7;
+      const uint4 v = *reinterpret_cast<const uint4*>(a.A + static_cast<size_t>(m0 + row) * a.lda + k_begin + k0 + kc * 8);
+      *reinterpret_cast<uint4*>(sA + tc::tile_offset(row, kc * 8, KC)) = v;
+    }
+    for (int c = tid; c < N * (KC / 8); c += 128) {
+      const int row = c % N, kc = c / N;
+      const uint4 v = *reinterpret_cast<const uint4*>(a.B + static_cast<size_t>(row) * a.ldb + k_begin + k0 + kc * 8);
+      *reinterpret_cast<uint4*>(sB + tc::tile_offset(row, kc * 8, KC)) = v;
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t a0 = tc::smem_addr(sA), b0 = tc::smem_addr(sB);
+#pragma unroll
+      for (int s = 0; s < KC / 16; s++) {
+        const uint64_t ad = tc::smem_desc(a0 + s * 256, 128, KC * 16);
+        const uint64_t bd = tc::smem_desc(b0 + s * 256, 128, KC * 16);
+        tc::mma_bf16(tmem, ad, bd, idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+      }
+      tc::mma_commit(mb);
+    }
+    // the verdict is taken by the whole CTA so that every thread leaves the
+    // loop at the same trip
+    ok = __syncthreads_and(tc::mbar_wait(mb, phase, kWaitCycles) ? 1 : 0) != 0;
+    phase ^= 1;
+    tc::fence_after_sync();
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(a.err, 1);
+    tc::mbar_wait(mb, phase ^ 1, kWaitCycles);  // the MMAs in flight, bounded again
+  }
+  else {
+    // epilogue: warp w owns tensor-memory lanes (rows) 32 w .. 32 w + 31
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < (N + 31) / 32; c++) {
+      float v[32];
+      tc::tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
+      epi(row, c * 32, v, N - c * 32 < 32 ? N - c * 32 : 32);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, kCols);
+  }
+}
+
+// z = acc + bias; keeps Z (FP32), H = SiLU(z) in BF16 and optionally H^T
+struct EpiForward {
+  const float* bias;
+  float* Z;
+  bf16* H;
+  bf16* Ht;
+  int B;
+  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if (j < ncol) {
+        const int c = col0 + j;
+        const float z = v[j] + bias[c];
+        const float h = silu(z);
+        Z[static_cast<size_t>(row) * kMlpWidth + c] = z;
+        H[static_cast<size_t>(row) * kMlpWidth + c] = __float2bfloat16_rn(h);
+        if (Ht) Ht[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(h);
+      }
+    }
+  }
+};
+
+// dz = acc * SiLU'(Zp); stores dZ (optional) and dZ^T, adds the column sums
+// to the bias gradient
+struct EpiBackward {
+  const float* Zp;
+  bf16* dZ;
+  bf16* dZt;
+  float* db;
+  int B;
+  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if (j < ncol) {
+        const int c = col0 + j;
+        const float dz = v[j] * dsilu(Zp[static_cast<size_t>(row) * kMlpWidth + c]);
+        if (dZ) dZ[static_cast<size_t>(row) * kMlpWidth + c] = __float2bfloat16_rn(dz);
+        dZt[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(dz);
+        const float s = warp_sum(dz);
+        if ((threadIdx.x & 31) == 0) atomicAdd(db + c, s);
+      }
+    }
+  }
+};
+
+// C[row][col] += acc (split-K weight gradients)
+struct EpiAtomic {
+  float* C;
+  int ldc;
+  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (j < ncol) atomicAdd(C + static_cast<size_t>(row) * ldc + col0 + j, v[j]);
+  }
+};
+
+template <int N, int KC, class Epi>
+cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int K, int splits, int* err, const Epi& epi,
+                 cudaStream_t s) {
+  GemmArgs a{A, lda, B, ldb, K / splits, err};
+  k_gemm<N, KC, Epi><<<dim3(M / 128, 1, splits), 128, 0, s>>>(a, epi);
+  return cudaGetLastError();
+}
+
+// output layer, loss and the first backward step, one sample per thread:
+// out = b4 + w4 . SiLU(Z3); e = out - y; dZ3 = (2e / B) w4 SiLU'(Z3)
+__global__ void __launch_bounds__(128) k_head(const float* Z3, const float* p, const float* y, int B, bf16* dZ3,
+                                              bf16* dZ3t, float* g, float* loss) {
+  __shared__ float red[4][kMlpWidth];
+  const int r = blockIdx.x * 128 + threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
+  float out = p[kMlpB4];
+  for (int j = 0; j < kMlpWidth; j++) out += silu(z[j]) * p[kMlpW4 + j];
+  const float e = out - y[r];
+  const float go = 2.0f * e / static_cast<float>(B);
+  const float se = warp_sum(e * e);
+  const float sg = warp_sum(go);
+  if (lane == 0) {
+    atomicAdd(loss, se);
+    atomicAdd(g + kMlpB4, sg);
+  }
+  for (int j = 0; j < kMlpWidth; j++) {
+    const float zj = z[j];
+    const float dz = go * p[kMlpW4 + j] * dsilu(zj);
+    dZ3[static_cast<size_t>(r) * kMlpWidth + j] = __float2bfloat16_rn(dz);
+    dZ3t[static_cast<size_t>(j) * B + r] = __float2bfloat16_rn(dz);
+    const float a = warp_sum(go * silu(zj));  // dW4
+    const float b = warp_sum(dz);             // db3
+    if (lane == 0) {
+      red[warp][j] = a;
+    }
+    if (lane == 1) atomicAdd(g + kMlpB3 + j, b);
+  }
+  __syncthreads();
+  if (threadIdx.x < kMlpWidth) {
+    const int j = threadIdx.x;
+    atomicAdd(g + kMlpW4 + j, red[0][j] + red[1][j] + red[2][j] + red[3][j]);
+  }
+}
+
+// forward output only
+__global__ void k_head_forward(const float* Z3, const float* p, int B, float* out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= B) return;
+  const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
+  float o = p[kMlpB4];
+  for (int j = 0; j < kMlpWidth; j++) o += silu(z[j]) * p[kMlpW4 + j];
+  out[r] = o;
+}
+
+// Adam (Kingma and Ba), bias-corrected
+__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = 0.9f * m[i] + 0.1f * gi;
+  const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+}
+
+// BF16 weight copies (and transposes) from the FP32 master weights
+__global__ void k_refresh(const float* p, bf16* W1, bf16* W2, bf16* W3, bf16* W2t, bf16* W3t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kMlpWidth * kMlpIn) W1[i] = __float2bfloat16_rn(p[kMlpW1 + i]);
+  if (i < kMlpWidth * kMlpWidth) {
+    const int r = i / kMlpWidth, c = i % kMlpWidth;
+    W2[i] = __float2bfloat16_rn(p[kMlpW2 + i]);
+    W3[i] = __float2bfloat16_rn(p[kMlpW3 + i]);
+    W2t[c * kMlpWidth + r] = __float2bfloat16_rn(p[kMlpW2 + i]);
+    W3t[c * kMlpWidth + r] = __float2bfloat16_rn(p[kMlpW3 + i]);
+  }
+}
+
+__device__ int g_mlp_err;
+
+}  // namespace
+
+cudaError_t mlp_refresh_bf16(const MlpNet& net, cudaStream_t s) {
+  k_refresh<<<kMlpWidth * kMlpWidth / 256, 256, 0, s>>>(net.p, net.W1, net.W2, net.W3, net.W2t, net.W3t);
+  return cudaGetLastError();
+}
+
+namespace {
+int* mlp_err_ptr() {
+  static int* p = nullptr;
+  if (!p) cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_mlp_err);
+  return p;
+}
+}  // namespace
+
+cudaError_t mlp_forward(const MlpNet& net, const MlpBatch& b, float* out, cudaStream_t s) {
+  int* err = mlp_err_ptr();
+  cudaError_t e;
+  if ((e = gemm<128, 16>(b.X, kMlpIn, net.W1, kMlpIn, b.B, kMlpIn, 1, err,
+                         EpiForward{net.p + kMlpB1, b.Z1, b.H1, nullptr, b.B}, s)) != cudaSuccess)
+    return e;
+  if ((e = gemm<128, 64>(b.H1, kMlpWidth, net.W2, kMlpWidth, b.B, kMlpWidth, 1, err,
+                         EpiForward{net.p + kMlpB2, b.Z2, b.H2, nullptr, b.B}, s)) != cudaSuccess)
+    return e;
+  if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, b.B, kMlpWidth, 1, err,
+                         EpiForward{net.p + kMlpB3, b.Z3, b.H1, nullptr, b.B}, s)) != cudaSuccess)
+    return e;
+  k_head_forward<<<(b.B + 127) / 128, 128, 0, s>>>(b.Z3, net.p, b.B, out);
+  return cudaGetLastError();
+}
+
+cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s) {
+  int* err = mlp_err_ptr();
+  const int B = b.B;
+  // weight-gradient products split K = B into chunks of 128 samples
+  const int splits = B / 128;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(net.g, 0, kMlpParams * sizeof(float), s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(b.loss, 0, sizeof(float), s)) != cudaSuccess) return e;
+  if ((e = gemm<128, 16>(b.X, kMlpIn, net.W1, kMlpIn, B, kMlpIn, 1, err,
+                         EpiForward{net.p + kMlpB1, b.Z1, b.H1, b.H1t, B}, s)) != cudaSuccess)
+    return e;
+  if ((e = gemm<128, 64>(b.H1, kMlpWidth, net.W2, kMlpWidth, B, kMlpWidth, 1, err,
+                         EpiForward{net.p + kMlpB2, b.Z2, b.H2, b.H2t, B}, s)) != cudaSuccess)
+    return e;
+  // Z3 only (H3 is recomputed from Z3 by the head)
+  if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, 1, err,
+                         EpiForward{net.p + kMlpB3, b.Z3, b.dZ3, nullptr, B}, s)) != cudaSuccess)
+    return e;
+  k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // layer 3: dW3 = dZ3^T H2; dH2 = dZ3 W3 -> dZ2
+  if ((e = gemm<128, 64>(b.dZ3t, B, b.H2t, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW3, kMlpWidth}, s)) !=
+      cudaSuccess)
+    return e;
+  if ((e = gemm<128, 64>(b.dZ3, kMlpWidth, net.W3t, kMlpWidth, B, kMlpWidth, 1, err,
+                         EpiBackward{b.Z2, b.dZ2, b.dZ2t, net.g + kMlpB2, B}, s)) != cudaSuccess)
+    return e;
+  // layer 2: dW2 = dZ2^T H1; dH1 = dZ2 W2 -> dZ1 (transposed only)
+  if ((e = gemm<128, 64>(b.dZ2t, B, b.H1t, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW2, kMlpWidth}, s)) !=
+      cudaSuccess)
+    return e;
+  if ((e = gemm<128, 64>(b.dZ2, kMlpWidth, net.W2t, kMlpWidth, B, kMlpWidth, 1, err,
+                         EpiBackward{b.Z1, nullptr, b.dZ1t, net.g + kMlpB1, B}, s)) != cudaSuccess)
+    return e;
+  // layer 1: dW1 = dZ1^T X
+  return gemm<16, 64>(b.dZ1t, B, b.Xt, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW1, kMlpIn}, s);
+}
+
+cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s) {
+  const float c1 = 1.0f / (1.0f - powf(0.9f, static_cast<float>(step)));
+  const float c2 = 1.0f / (1.0f - powf(0.999f, static_cast<float>(step)));
+  k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(net.p, net.g, net.m, net.v, kMlpParams, lr, c1, c2);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return mlp_refresh_bf16(net, s);
+}
+
+// ---------------------------------------------------------------------------
+// features and targets (shared by training and inference)
+
+namespace {
+
+__device__ __forceinline__ double beta_min_of(double E, double T) { return -E / (kBoltzmann * T); }
+
+__device__ __forceinline__ void base_features(const MlpBox& box, double E, double T, double u, float* f) {
+  f[0] = static_cast<float>(2.0 * (log(E) - box.logE0) / (box.logE1 - box.logE0) - 1.0);
+  f[1] = static_cast<float>(2.0 * (T - box.T0) / (box.T1 - box.T0) - 1.0);
+  f[2] = static_cast<float>(2.0 * u - 1.0);
+  f[3] = static_cast<float>(fmin(2.0, fmax(-2.0, log(u / (1.0 - u)) / 8.0)));
+}
+
+__device__ __forceinline__ void beta_features(const MlpBox& box, double E, double T, double u, float (&f)[kMlpIn]) {
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
+  base_features(box, E, T, u, f);
+}
+
+__device__ __forceinline__ void alpha_features(const MlpBox& box, double E, double T, double beta, double u,
+                                               float (&f)[kMlpIn]) {
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
+  base_features(box, E, T, u, f);
+  const double bmin = beta_min_of(E, T);
+  f[4] = static_cast<float>(copysign(log1p(fabs(beta)), beta) / box.beta_scale);
+  f[5] = static_cast<float>(2.0 * (beta - bmin) / (box.beta_cutoff - bmin) - 1.0);
+}
+
+__device__ __forceinline__ void alpha_range(const MlpBox& box, double E, double T, double beta, double& lo,
+                                            double& hi) {
+  const double akT = box.awr * kBoltzmann * T;
+  const double s = sqrt(fmax(0.0, E + beta * kBoltzmann * T));
+  const double r = sqrt(E);
+  lo = (r - s) * (r - s) / akT;
+  hi = (r + s) * (r + s) / akT;
+}
+
+__device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* row) {
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) row[i] = __float2bfloat16_rn(f[i]);
+}
+
+// training targets: quantile positions of sorted samples within their
+// condition (u = (k + 1/2) / K)
+__global__ void k_features_beta(MlpBox box, const double* E, const double* T, const double* u, const double* beta,
+                                unsigned long long n, bf16* X, float* y) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float f[kMlpIn];
+  beta_features(box, E[i], T[i], u[i], f);
+  store_features(f, X + i * kMlpIn);
+  const double bmin = beta_min_of(E[i], T[i]);
+  const double q = (beta[i] - bmin) / (box.beta_cutoff - bmin);
+  y[i] = isfinite(q) ? static_cast<float>(q) : 0.5f;
+}
+
+__global__ void k_features_alpha(MlpBox box, const double* E, const double* T, const double* beta, const double* u,
+                                 const double* alpha, unsigned long long n, bf16* X, float* y) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float f[kMlpIn];
+  alpha_features(box, E[i], T[i], beta[i], u[i], f);
+  store_features(f, X + i * kMlpIn);
+  double lo, hi;
+  alpha_range(box, E[i], T[i], beta[i], lo, hi);
+  const double q = (alpha[i] - lo) / (hi - lo);
+  y[i] = isfinite(q) ? static_cast<float>(q) : 0.5f;
+}
+
+// bitonic sort of each K-value segment in shared memory (NaN last)
+__global__ void __launch_bounds__(1024) k_segment_sort(double* v, int K) {
+  __shared__ double s[1024];
+  double* seg = v + static_cast<size_t>(blockIdx.x) * K;
+  const int t = threadIdx.x;
+  if (t < K) {
+    const double x = seg[t];
+    s[t] = x == x ? x : CUDART_INF;
+  }
+  __syncthreads();
+  for (int size = 2; size <= K; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (t < K) {
+        const int partner = t ^ stride;
+        if (partner > t) {
+          const bool up = (t & size) == 0;
+          const double a = s[t], b = s[partner];
+          if ((a > b) == up) {
+            s[t] = b;
+            s[partner] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (t < K) seg[t] = s[t];
+}
+
+// random batch: row r of the batch is sample philox(key, step, r) mod n
+__global__ void k_gather(const bf16* X, const float* y, unsigned long long n, unsigned long long key, int step,
+                         int B, bf16* bX, bf16* bXt, float* by) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= B) return;
+  uint32_t c[4] = {static_cast<uint32_t>(r), static_cast<uint32_t>(step), 0x4D4C5000u, 0};
+  philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
+  const unsigned long long idx = ((static_cast<unsigned long long>(c[0]) << 32) | c[1]) % n;
+#pragma unroll
+  for (int f = 0; f < kMlpIn; f++) {
+    const bf16 v = X[idx * kMlpIn + f];
+    bX[static_cast<size_t>(r) * kMlpIn + f] = v;
+    bXt[static_cast<size_t>(f) * B + r] = v;
+  }
+  by[r] = y[idx];
+}
+
+// POD draws for the training sets (exact form, Philox streams)
+__global__ void k_beta_draws(const DevTSL* tsl, const double* E, const double* T, unsigned long long n,
+                             unsigned long long key, double* beta, unsigned long long* failures) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PhiloxRng rng;
+  rng.init(key, i, 4);
+  double b;
+  if (!tsl_sample_beta<false>(*tsl, rng, E[i], T[i], b)) {
+    b = CUDART_NAN;
+    atomicAdd(failures, 1ull);
+  }
+  beta[i] = b;
+}
+
+__global__ void k_alpha_draws(const DevTSL* tsl, const double* E, const double* T, const double* beta,
+                              unsigned long long n, unsigned long long key, double* alpha,
+                              unsigned long long* failures) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PhiloxRng rng;
+  rng.init(key, i, 5);
+  double a;
+  if (!(beta[i] == beta[i]) || !tsl_sample_alpha<false>(*tsl, rng, beta[i], E[i], T[i], a)) {
+    a = CUDART_NAN;
+    atomicAdd(failures, 1ull);
+  }
+  alpha[i] = a;
+}
+
+unsigned blocks256(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
+
+}  // namespace
+
+namespace {
+__global__ void k_expand(const double* src, unsigned long long n, int K, double* dst) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i / K];
+}
+__global__ void k_quantile_u(double* u, unsigned long long n, int K) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) u[i] = (static_cast<double>(i % K) + 0.5) / K;
+}
+}  // namespace
+
+cudaError_t launch_expand(const double* src, unsigned long long n, int K, double* dst, cudaStream_t s) {
+  k_expand<<<blocks256(n), 256, 0, s>>>(src, n, K, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_quantile_u(double* u, unsigned long long n, int K, cudaStream_t s) {
+  k_quantile_u<<<blocks256(n), 256, 0, s>>>(u, n, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_features_beta(const MlpBox& box, const double* E, const double* T, const double* u,
+                                     const double* beta, unsigned long long n, __nv_bfloat16* X, float* y,
+                                     cudaStream_t s) {
+  k_features_beta<<<blocks256(n), 256, 0, s>>>(box, E, T, u, beta, n, X, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_features_alpha(const MlpBox& box, const double* E, const double* T, const double* beta,
+                                      const double* u, const double* alpha, unsigned long long n, __nv_bfloat16* X,
+                                      float* y, cudaStream_t s) {
+  k_features_alpha<<<blocks256(n), 256, 0, s>>>(box, E, T, beta, u, alpha, n, X, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K, cudaStream_t s) {
+  if (K < 2 || K > 1024 || (K & (K - 1))) return cudaErrorInvalidValue;
+  k_segment_sort<<<static_cast<unsigned>(n_segments), K, 0, s>>>(v, K);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_gather(const __nv_bfloat16* X, const float* y, unsigned long long n, unsigned long long key,
+                              int step, const MlpBatch& b, cudaStream_t s) {
+  k_gather<<<(b.B + 255) / 256, 256, 0, s>>>(X, y, n, key, step, b.B, b.X, b.Xt, b.y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tsl_beta_draws(const DevTSL* tsl, const double* E, const double* T, unsigned long long n,
+                                  unsigned long long key, double* beta, unsigned long long* failures, cudaStream_t s) {
+  k_beta_draws<<<blocks256(n), 256, 0, s>>>(tsl, E, T, n, key, beta, failures);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tsl_alpha_draws(const DevTSL* tsl, const double* E, const double* T, const double* beta,
+                                   unsigned long long n, unsigned long long key, double* alpha,
+                                   unsigned long long* failures, cudaStream_t s) {
+  k_alpha_draws<<<blocks256(n), 256, 0, s>>>(tsl, E, T, beta, n, key, alpha, failures);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// fused surrogate sampler: both networks' BF16 weights resident in shared
+// memory, one 128-sample tile per loop trip, one sample per thread; each
+// layer is one tcgen05 product into tensor memory followed by a per-row
+// epilogue (bias, SiLU) that writes the next layer's operand tile
+
+namespace {
+
+struct NetView {
+  const float* p;
+  const bf16* W1;
+  const bf16* W2;
+  const bf16* W3;
+};
+
+constexpr uint32_t kTileW1 = kMlpWidth * kMlpIn * 2;      // 4 KB
+constexpr uint32_t kTileW = kMlpWidth * kMlpWidth * 2;    // 32 KB
+constexpr uint32_t kOffB1 = 0;                            // beta network W1
+constexpr uint32_t kOffB2 = kOffB1 + kTileW1;
+constexpr uint32_t kOffB3 = kOffB2 + kTileW;
+constexpr uint32_t kOffA1 = kOffB3 + kTileW;              // alpha network
+constexpr uint32_t kOffA2 = kOffA1 + kTileW1;
+constexpr uint32_t kOffA3 = kOffA2 + kTileW;
+constexpr uint32_t kOffX = kOffA3 + kTileW;               // input tile 128 x 16
+constexpr uint32_t kOffH = kOffX + kTileW1;               // hidden tile 128 x 128
+constexpr uint32_t kOffF = kOffH + kTileW;                // FP32: per net b1 b2 b3 w4 (4 x 128) + b4
+constexpr uint32_t kOffMisc = kOffF + 2 * (4 * kMlpWidth + 4) * 4;
+constexpr uint32_t kSampleSmem = kOffMisc + 64;
+
+__device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int K) {
+  for (int c = threadIdx.x; c < kMlpWidth * (K / 8); c += blockDim.x) {
+    const int row = c % kMlpWidth, kc = c / kMlpWidth;
+    *reinterpret_cast<uint4*>(dst + tc::tile_offset(row, kc * 8, K)) =
+        *reinterpret_cast<const uint4*>(src + static_cast<size_t>(row) * K + kc * 8);
+  }
+}
+
+struct SampleShared {
+  uint8_t* base;
+  uint32_t tmem, mbar;
+  uint32_t phase;
+  bool ok;
+};
+
+// one layer's product: D = act_tile * W^T (K = 16 or 128)
+__device__ __forceinline__ void layer_mma(SampleShared& sh, uint32_t act_off, uint32_t w_off, int K) {
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::fence_after_sync();
+    const uint32_t a0 = tc::smem_addr(sh.base + act_off), b0 = tc::smem_addr(sh.base + w_off);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(128, kMlpWidth);
+    for (int s = 0; s < K / 16; s++)
+      tc::mma_bf16(sh.tmem, tc::smem_desc(a0 + s * 256, 128, K * 16), tc::smem_desc(b0 + s * 256, 128, K * 16),
+                   idesc, s > 0 ? 1u : 0u);
+    tc::mma_commit(sh.mbar);
+  }
+  if (!__syncthreads_and(tc::mbar_wait(sh.mbar, sh.phase, kWaitCycles) ? 1 : 0)) sh.ok = false;
+  sh.phase ^= 1;
+  tc::fence_after_sync();
+}
+
+// hidden epilogue: h = SiLU(acc + bias) into the hidden tile (this thread's row)
+__device__ __forceinline__ void hidden_epilogue(SampleShared& sh, const float* bias) {
+  const int warp = threadIdx.x >> 5, row = threadIdx.x;
+  uint8_t* H = sh.base + kOffH;
+#pragma unroll 1
+  for (int c = 0; c < kMlpWidth / 32; c++) {
+    float v[32];
+    tc::tmem_ld32(sh.tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      __align__(16) bf16 h[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) h[j] = __float2bfloat16_rn(silu(v[q * 8 + j] + bias[c * 32 + q * 8 + j]));
+      *reinterpret_cast<uint4*>(H + tc::tile_offset(row, c * 32 + q * 8, kMlpWidth)) = *reinterpret_cast<uint4*>(h);
+    }
+  }
+}
+
+// output epilogue: b4 + w4 . SiLU(acc + b3)
+__device__ __forceinline__ float output_epilogue(SampleShared& sh, const float* f) {
+  const int warp = threadIdx.x >> 5;
+  const float* b3 = f + 2 * kMlpWidth;
+  const float* w4 = f + 3 * kMlpWidth;
+  float out = f[4 * kMlpWidth];
+#pragma unroll 1
+  for (int c = 0; c < kMlpWidth / 32; c++) {
+    float v[32];
+    tc::tmem_ld32(sh.tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
+#pragma unroll
+    for (int j = 0; j < 32; j++) out += silu(v[j] + b3[c * 32 + j]) * w4[c * 32 + j];
+  }
+  return out;
+}
+
+__device__ __forceinline__ float run_net(SampleShared& sh, uint32_t w1, uint32_t w2, uint32_t w3, const float* f) {
+  layer_mma(sh, kOffX, w1, kMlpIn);
+  hidden_epilogue(sh, f);
+  layer_mma(sh, kOffH, w2, kMlpWidth);
+  hidden_epilogue(sh, f + kMlpWidth);
+  layer_mma(sh, kOffH, w3, kMlpWidth);
+  return output_epilogue(sh, f);
+}
+
+__device__ __forceinline__ void write_x(SampleShared& sh, const float (&x)[kMlpIn]) {
+  __align__(16) bf16 h[kMlpIn];
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) h[i] = __float2bfloat16_rn(x[i]);
+  uint8_t* X = sh.base + kOffX;
+  *reinterpret_cast<uint4*>(X + tc::tile_offset(threadIdx.x, 0, kMlpIn)) = *reinterpret_cast<uint4*>(h);
+  *reinterpret_cast<uint4*>(X + tc::tile_offset(threadIdx.x, 8, kMlpIn)) = *reinterpret_cast<uint4*>(h + 8);
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_sample(const DevTSL* tsl, NetView nb, NetView na, MlpBox box,
+                                                        const double* E, const double* T, unsigned long long n,
+                                                        unsigned long long key, double* beta_out, double* alpha_out,
+                                                        unsigned long long* failures, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  SampleShared sh;
+  sh.base = smem;
+  float* fb = reinterpret_cast<float*>(smem + kOffF);
+  float* fa = fb + 4 * kMlpWidth + 4;
+  uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kOffMisc);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // weights into shared memory
+  load_tile(smem + kOffB1, nb.W1, kMlpIn);
+  load_tile(smem + kOffB2, nb.W2, kMlpWidth);
+  load_tile(smem + kOffB3, nb.W3, kMlpWidth);
+  load_tile(smem + kOffA1, na.W1, kMlpIn);
+  load_tile(smem + kOffA2, na.W2, kMlpWidth);
+  load_tile(smem + kOffA3, na.W3, kMlpWidth);
+  for (int i = tid; i < kMlpWidth; i += blockDim.x) {
+    fb[i] = nb.p[kMlpB1 + i];
+    fb[kMlpWidth + i] = nb.p[kMlpB2 + i];
+    fb[2 * kMlpWidth + i] = nb.p[kMlpB3 + i];
+    fb[3 * kMlpWidth + i] = nb.p[kMlpW4 + i];
+    fa[i] = na.p[kMlpB1 + i];
+    fa[kMlpWidth + i] = na.p[kMlpB2 + i];
+    fa[2 * kMlpWidth + i] = na.p[kMlpB3 + i];
+    fa[3 * kMlpWidth + i] = na.p[kMlpW4 + i];
+  }
+  if (tid == 0) {
+    fb[4 * kMlpWidth] = nb.p[kMlpB4];
+    fa[4 * kMlpWidth] = na.p[kMlpB4];
+    tc::mbar_init(tc::smem_addr(misc), 1);
+  }
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(misc + 2), kMlpWidth);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  sh.tmem = misc[2];
+  sh.mbar = tc::smem_addr(misc);
+  sh.phase = 0;
+  sh.ok = true;
+  const double Emin = exp(box.logE0), Emax = exp(box.logE1);
+  unsigned long long my_fail = 0;
+  const unsigned long long tiles = (n + 127) / 128;
+  for (unsigned long long tile = blockIdx.x; tile < tiles && sh.ok; tile += gridDim.x) {
+    const unsigned long long i = tile * 128 + tid;
+    const bool valid = i < n;
+    double e = valid ? E[i] : 0.5 * (Emin + Emax);
+    double t = valid ? T[i] : box.T0;
+    const bool in_box = e >= Emin && e <= Emax && t >= box.T0 && t <= box.T1;
+    if (!in_box) {  // keep the tile's arithmetic finite; the row is resampled below
+      e = Emin;
+      t = box.T0;
+    }
+    PhiloxRng rng;
+    rng.init(key, i, 3);
+    const double u1 = rng.u01();
+    float x[kMlpIn];
+    beta_features(box, e, t, fmin(fmax(u1, 1e-12), 1.0 - 1e-12), x);
+    write_x(sh, x);
+    const float qb = run_net(sh, kOffB1, kOffB2, kOffB3, fb);
+    const double bmin = beta_min_of(e, t);
+    const double b = bmin + fmin(1.0, fmax(0.0, static_cast<double>(qb))) * (box.beta_cutoff - bmin);
+    const double u2 = rng.u01();
+    alpha_features(box, e, t, b, fmin(fmax(u2, 1e-12), 1.0 - 1e-12), x);
+    write_x(sh, x);
+    const float qa = run_net(sh, kOffA1, kOffA2, kOffA3, fa);
+    double lo, hi;
+    alpha_range(box, e, t, b, lo, hi);
+    double bo = b, ao = lo + fmin(1.0, fmax(0.0, static_cast<double>(qa))) * (hi - lo);
+    if (valid && !in_box) {
+      // outside the trained box: the POD sampler (FP32 form when the ranks fit)
+      const double eo = E[i], to = T[i];
+      bool ok = tsl->fast_ok ? tsl_sample_beta<true>(*tsl, rng, eo, to, bo) : tsl_sample_beta<false>(*tsl, rng, eo, to, bo);
+      if (ok) ok = tsl->fast_ok ? tsl_sample_alpha<true>(*tsl, rng, bo, eo, to, ao)
+                                : tsl_sample_alpha<false>(*tsl, rng, bo, eo, to, ao);
+      if (!ok) {
+        bo = ao = CUDART_NAN;
+        my_fail++;
+      }
+    }
+    if (valid) {
+      beta_out[i] = bo;
+      alpha_out[i] = ao;
+    }
+  }
+  if (!sh.ok && tid == 0) atomicExch(err, 1);
+  if (my_fail) atomicAdd(failures, my_fail);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(sh.tmem, kMlpWidth);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_sample_tsl_mlp(const DevTSL* tsl, const MlpNet& beta_net, const MlpNet& alpha_net,
+                                  const MlpBox& box, const double* E, const double* T, unsigned long long n,
+                                  unsigned long long key, double* beta, double* alpha, unsigned long long* failures,
+                                  int num_sms, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(k_mlp_sample, cudaFuncAttributeMaxDynamicSharedMemorySize, kSampleSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const unsigned long long tiles = (n + 127) / 128;
+  const unsigned grid = static_cast<unsigned>(tiles < static_cast<unsigned long long>(num_sms) ? tiles : num_sms);
+  NetView nb{beta_net.p, beta_net.W1, beta_net.W2, beta_net.W3};
+  NetView na{alpha_net.p, alpha_net.W1, alpha_net.W2, alpha_net.W3};
+  k_mlp_sample<<<grid, 128, kSampleSmem, s>>>(tsl, nb, na, box, E, T, n, key, beta, alpha, failures, mlp_err_ptr());
+  return cudaGetLastError();
+}
+
+int* mlp_error_flag() { return mlp_err_ptr(); }
+
+}  // namespace mcd

@@ -1,7 +1,9 @@
 // Deterministic geometry kernels exposed through the C ABI so that parity
 // tests can compare them bit-for-bit with the CPU oracle:
 // World::FindCellContaining, Cell::NearestSurface, CSGSurface::Distance and
-// CSGSurface::Contains, one query per thread.
+// CSGSurface::Contains, one query per thread; and the continuous-energy
+// material cross sections and energy-grid search.
+#include "mc_ce.cuh"
 #include "mc_kernels.cuh"
 
 namespace mcd {
@@ -58,6 +60,38 @@ __global__ void k_material_xs_mg(const DevWorld w, int32_t cell, const double* e
   majorant[i] = t;  // Multigroup::GetMajorant returns the total
 }
 
+// Material::GetMicroscopicTotal / GetMicroscopicMajorant of a
+// continuous-energy neutron at a point of the cell (exact tables)
+__global__ void k_material_xs_ce(const DevWorld w, int32_t cell, const double* energy, const double* xyz,
+                                 unsigned long long n, double* total, double* majorant) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double E = energy[i];
+  const int j = ce_search(w.ce, E);
+  const int m = __ldg(w.cell_mat + cell);
+  const double T = cell_temperature(w, cell, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+  total[i] = ce_material_micro(w, m, 0, j, E, T, T, false);
+  majorant[i] = ce_material_micro(w, m, 0, j, E, cell_temperature_max(w, cell), T, true);
+}
+
+// std::map::upper_bound position of each energy in each table of a nuclide,
+// found through the union grid: columns total, reactions in input order,
+// nubar tables of the fission reactions, -1 past the last table
+__global__ void k_energy_index(const DevWorld w, int32_t nuc, const double* energy, unsigned long long n,
+                               long long* out) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const mc::CENuclideDesc& d = ce_desc(w, 0, nuc);
+  const int j = ce_search(w.ce, energy[i]);
+  long long* o = out + 6 * i;
+  int col = 0;
+  o[col++] = ce_table_index(w.ce, d.total, j);
+  for (int k = 0; k < d.n_rx; k++) o[col++] = ce_table_index(w.ce, d.rx_table[k], j);
+  for (int k = 0; k < d.n_rx && col < 6; k++)
+    if (d.rx_nubar[k] >= 0) o[col++] = ce_table_index(w.ce, d.rx_nubar[k], j);
+  while (col < 6) o[col++] = -1;
+}
+
 unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
 
 }  // namespace
@@ -94,6 +128,20 @@ cudaError_t launch_material_xs_mg(const DevWorld& w, int32_t cell, const double*
                                   double* total, double* majorant, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   k_material_xs_mg<<<blocks_for(n), 256, 0, stream>>>(w, cell, energy, n, total, majorant);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_material_xs_ce(const DevWorld& w, int32_t cell, const double* energy, const double* xyz,
+                                  unsigned long long n, double* total, double* majorant, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_material_xs_ce<<<blocks_for(n), 256, 0, stream>>>(w, cell, energy, xyz, n, total, majorant);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_energy_index(const DevWorld& w, int32_t nuclide, const double* energy, unsigned long long n,
+                                long long* out, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_energy_index<<<blocks_for(n), 256, 0, stream>>>(w, nuclide, energy, n, out);
   return cudaGetLastError();
 }
 

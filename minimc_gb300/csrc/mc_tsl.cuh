@@ -1,0 +1,323 @@
+// Thermal scattering (src/ThermalScattering.cpp) on the device:
+//   GetTotal / EvaluateInelastic      :111-157, :260-269
+//   BetaPartition/AlphaPartition::Evaluate  :183-256
+//   SampleBeta / SampleAlpha / Scatter      :159-171, :271-463
+//
+// Two forms of the POD reconstruction:
+//   exact: FP64 with the reference's operation order (bit-for-bit with the
+//          reference's arithmetic for the same random numbers);
+//   fast:  the temperature interpolation is applied to the mode vector
+//          once per sample (G_T = G_lo + w (G_hi - G_lo)), after which each
+//          reconstruction is one rank-r FP32 dot product with the
+//          precomputed S * CDF_modes row.  Linear interpolation commutes
+//          with the sum, so this is the same function rounded in FP32.
+// The sampling logic (grid choice, bisection, endpoints, resampling, the
+// alpha interpolation factor as the reference writes it) is shared.
+#pragma once
+
+#include "mc_device.cuh"
+
+namespace mcd {
+
+constexpr int kTslResampleLimit = 10;  // constants::beta/alpha_resample_limit
+constexpr int kFastPodRank = 32;       // fast form: mode vector in registers
+
+// std::upper_bound on a sorted array (libstdc++'s bisection)
+__device__ __forceinline__ int upper_index(const double* v, int n, double x) {
+  int first = 0, len = n;
+  while (len > 0) {
+    const int half = len >> 1, mid = first + half;
+    if (x < __ldg(v + mid)) {
+      len = half;
+    }
+    else {
+      first = mid + 1;
+      len -= half + 1;
+    }
+  }
+  return first;
+}
+
+// one partition at one temperature: the temperature bracket of
+// Evaluate (T >= T_max uses the top interval, T < T_min both ends at the
+// first point)
+struct PodAt {
+  int part, r, nT, lo, hi, nF;
+  double T, Tl, Th;
+  const double* S;
+  const double* cdf;
+  const double* g;
+  const double* F;
+  const float* cs;
+  const float* gf;
+};
+
+__device__ __forceinline__ PodAt pod_at(const DevPOD& P, int part, double T) {
+  PodAt c;
+  c.part = part;
+  c.r = __ldg(P.rank + part);
+  c.nT = __ldg(P.nT + part);
+  c.nF = __ldg(P.nF + part);
+  const double* Ts = P.T + __ldg(P.T_off + part);
+  const int cand = upper_index(Ts, c.nT, T);
+  const bool above = cand == c.nT;
+  c.hi = above ? cand - 1 : cand;
+  c.lo = c.hi == 0 ? c.hi : c.hi - 1;
+  c.T = T;
+  c.Tl = __ldg(Ts + c.lo);
+  c.Th = __ldg(Ts + c.hi);
+  c.S = P.S + __ldg(P.S_off + part);
+  c.cdf = P.cdf + __ldg(P.cdf_off + part);
+  c.cs = P.cs + __ldg(P.cdf_off + part);
+  c.g = P.g + __ldg(P.g_off + part);
+  c.gf = P.gf + __ldg(P.g_off + part);
+  c.F = P.F + __ldg(P.F_off + part);
+  return c;
+}
+
+// Evaluate(cdf_i, g_i, T), exact form
+__device__ __forceinline__ double pod_eval(const PodAt& c, int cdf_i, int g_i) {
+  const double* C = c.cdf + static_cast<size_t>(cdf_i) * c.r;
+  const double* Gh = c.g + (static_cast<size_t>(g_i) * c.nT + c.hi) * c.r;
+  const double* Gl = c.g + (static_cast<size_t>(g_i) * c.nT + c.lo) * c.r;
+  double vh = 0, vl = 0;
+  for (int o = 0; o < c.r; o++) {
+    const double sc = dmul(__ldg(c.S + o), __ldg(C + o));
+    vh = dadd(vh, dmul(sc, __ldg(Gh + o)));
+    vl = dadd(vl, dmul(sc, __ldg(Gl + o)));
+  }
+  return dadd(vl, dmul(ddiv(dsub(vh, vl), dsub(c.Th, c.Tl)), dsub(c.T, c.Tl)));
+}
+
+// fast form: the mode vector of grid point g_i interpolated to T
+struct PodVec {
+  float v[kFastPodRank];
+};
+__device__ __forceinline__ void pod_vec(const PodAt& c, int g_i, PodVec& out) {
+  const float* Gh = c.gf + (static_cast<size_t>(g_i) * c.nT + c.hi) * c.r;
+  const float* Gl = c.gf + (static_cast<size_t>(g_i) * c.nT + c.lo) * c.r;
+  const float w = static_cast<float>(ddiv(dsub(c.T, c.Tl), dsub(c.Th, c.Tl)));
+#pragma unroll
+  for (int o = 0; o < kFastPodRank; o++) {
+    if (o < c.r) {
+      const float l = __ldg(Gl + o);
+      out.v[o] = __fmaf_rn(w, __fsub_rn(__ldg(Gh + o), l), l);
+    }
+    else {
+      out.v[o] = 0.0f;
+    }
+  }
+}
+__device__ __forceinline__ double pod_eval_fast(const PodAt& c, const PodVec& gv, int cdf_i) {
+  const float* C = c.cs + static_cast<size_t>(cdf_i) * c.r;
+  float acc = 0.0f;
+#pragma unroll
+  for (int o = 0; o < kFastPodRank; o++)
+    if (o < c.r) acc = __fmaf_rn(__ldg(C + o), gv.v[o], acc);
+  return static_cast<double>(acc);
+}
+
+// partition holding global grid index i (upper_bound over the ends)
+__device__ __forceinline__ int pod_partition(const DevPOD& P, int i, int& local) {
+  int ps = 0;
+  while (ps < P.n_parts && static_cast<int>(__ldg(P.ends + ps)) <= i) ps++;
+  local = ps == 0 ? i : i - static_cast<int>(__ldg(P.ends + ps - 1));
+  return ps;
+}
+
+template <bool FAST>
+struct PodEval {
+  PodAt c;
+  PodVec gv;
+  int g_i;
+  __device__ __forceinline__ void init(const DevPOD& P, int part, int local, double T) {
+    c = pod_at(P, part, T);
+    g_i = local;
+    if constexpr (FAST) pod_vec(c, local, gv);
+  }
+  __device__ __forceinline__ double operator()(int cdf_i) const {
+    if constexpr (FAST) return pod_eval_fast(c, gv, cdf_i);
+    else return pod_eval(c, cdf_i, g_i);
+  }
+};
+
+// ThermalScattering::EvaluateInelastic
+__device__ __forceinline__ double tsl_inelastic(const DevTSL& t, int E_i, int T_i) {
+  const int r = t.xs_rank;
+  double acc = 0;
+  for (int o = 0; o < r; o++)
+    acc = dadd(acc, dmul(dmul(__ldg(t.xs_S + o), __ldg(t.xs_Em + E_i * r + o)), __ldg(t.xs_Tm + T_i * r + o)));
+  return acc;
+}
+
+// ThermalScattering::GetTotal
+__device__ __forceinline__ double tsl_total(const DevTSL& t, double E, double T) {
+  const int E_hi_i = upper_index(t.xs_E, t.xs_nE, E);
+  if (E_hi_i == t.xs_nE) return CUDART_NAN;  // E at or above the cutoff (asserted by the reference)
+  const bool below_E_min = E_hi_i == 0;
+  const int E_lo_i = below_E_min ? E_hi_i : E_hi_i - 1;
+  const int cand = upper_index(t.xs_T, t.xs_nT, T);
+  const bool above_T_max = cand == t.xs_nT;
+  const int T_hi_i = above_T_max ? cand - 1 : cand;
+  const bool below_T_min = T_hi_i == 0;
+  const int T_lo_i = below_T_min ? T_hi_i : T_hi_i - 1;
+  const double a = tsl_inelastic(t, E_lo_i, T_lo_i), b = tsl_inelastic(t, E_lo_i, T_hi_i);
+  const double c = tsl_inelastic(t, E_hi_i, T_lo_i), d = tsl_inelastic(t, E_hi_i, T_hi_i);
+  const double E_lo = __ldg(t.xs_E + E_lo_i), E_hi = __ldg(t.xs_E + E_hi_i);
+  const double r_E = below_E_min ? 1.0 : ddiv(dsub(E, E_lo), dsub(E_hi, E_lo));
+  const double xs_T_lo = dadd(a, dmul(r_E, dsub(c, a)));
+  const double xs_T_hi = dadd(b, dmul(r_E, dsub(d, b)));
+  const double T_lo = __ldg(t.xs_T + T_lo_i), T_hi = __ldg(t.xs_T + T_hi_i);
+  const double r_T = below_T_min ? 1.0 : above_T_max ? 0.0 : ddiv(dsub(T, T_lo), dsub(T_hi, T_lo));
+  return dadd(xs_T_lo, dmul(r_T, dsub(xs_T_hi, xs_T_lo)));
+}
+
+// ThermalScattering::GetMajorant: ContinuousMap::at on the majorant table
+__device__ __forceinline__ double tsl_majorant(const DevTSL& t, double E) {
+  const int hi = upper_index(t.maj_x, t.maj_n, E);
+  if (hi == t.maj_n) return __ldg(t.maj_y + t.maj_n - 1);
+  if (hi == 0) return __ldg(t.maj_y);
+  const double k_hi = __ldg(t.maj_x + hi), v_hi = __ldg(t.maj_y + hi);
+  const double k_lo = __ldg(t.maj_x + hi - 1), v_lo = __ldg(t.maj_y + hi - 1);
+  return dadd(v_lo, dmul(ddiv(dsub(v_hi, v_lo), dsub(k_hi, k_lo)), dsub(E, k_lo)));
+}
+
+// ThermalScattering::SampleBeta; false past the resample limit (the
+// reference throws)
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_sample_beta(const DevTSL& t, Rng& rng, double E, double T, double& beta) {
+  const DevPOD& P = t.beta;
+  const int n = P.n_grid;
+  const int E_hi_i = upper_index(P.grid, n, E);
+  if (E_hi_i == n) return false;  // E at or above the cutoff (asserted by the reference)
+  const double r = E_hi_i != 0 ? ddiv(dsub(E, __ldg(P.grid + E_hi_i - 1)),
+                                      dsub(__ldg(P.grid + E_hi_i), __ldg(P.grid + E_hi_i - 1)))
+                               : 1.0;
+  const int E_s_i = r <= rng.u01() ? E_hi_i - 1 : E_hi_i;
+  const double E_s = __ldg(P.grid + E_s_i);
+  int local;
+  const int ps = pod_partition(P, E_s_i, local);
+  PodEval<FAST> ev;
+  ev.init(P, ps, local, T);
+  const int nF = ev.c.nF;
+  const double kT = dmul(kBoltzmann, T);
+  for (int res = 0; res < kTslResampleLimit; res++) {
+    const double F = rng.u01();
+    const int F_hi_i = upper_index(ev.c.F, nF, F);
+    const double F_lo = F_hi_i != 0 ? __ldg(ev.c.F + F_hi_i - 1) : 0.0;
+    const double F_hi = F_hi_i != nF ? __ldg(ev.c.F + F_hi_i) : 1.0;
+    const double b_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : ddiv(-E_s, kT);
+    const double b_hi = F_hi_i != nF ? ev(F_hi_i) : t.beta_cutoff;
+    const double b_prime = dadd(b_lo, dmul(ddiv(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(b_hi, b_lo)));
+    const double b_min = ddiv(-E, kT);
+    if (b_min <= b_prime) {
+      beta = b_prime;
+      return true;
+    }
+  }
+  return false;
+}
+
+// (sqrt(E) -+ sqrt(E + b kT))^2 / (A kT): alpha bounds at beta b
+__device__ __forceinline__ void alpha_bounds(double sqrt_E, double E, double b, double T, double akT, double& a_min,
+                                             double& a_max) {
+  const double s = __dsqrt_rn(dadd(E, dmul(dmul(b, kBoltzmann), T)));
+  const double lo = dsub(sqrt_E, s), hi = dadd(sqrt_E, s);
+  a_min = ddiv(dmul(lo, lo), akT);
+  a_max = ddiv(dmul(hi, hi), akT);
+}
+
+// ThermalScattering::SampleAlpha
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, double b, double E, double T,
+                                                 double& alpha) {
+  const DevPOD& P = t.alpha;
+  const double abs_b = fabs(b);
+  const int sgn_b = (0 < b) - (b < 0);
+  const int n = P.n_grid;
+  const int b_hi_i = upper_index(P.grid, n, abs_b);
+  if (b_hi_i == n) return false;  // betas.at() throws in the reference
+  const double kT = dmul(kBoltzmann, T);
+  const double g_hi = __ldg(P.grid + b_hi_i);
+  const bool snap_to_lower = (sgn_b == 1 && t.beta_cutoff <= g_hi) || (sgn_b == -1 && -g_hi < ddiv(-E, kT));
+  const bool snap_to_min = b_hi_i == 0;
+  double r;
+  if (snap_to_lower) r = 0.0;
+  else if (snap_to_min) r = 1.0;
+  else {
+    // as written in the reference (src/ThermalScattering.cpp:363-365): the
+    // division binds before the subtraction
+    const double g_lo = __ldg(P.grid + b_hi_i - 1);
+    r = dsub(abs_b, ddiv(g_lo, dsub(g_hi, g_lo)));
+  }
+  const int b_s_i = r <= rng.u01() ? b_hi_i - 1 : b_hi_i;
+  if (b_s_i < 0) return false;  // snapped below the first beta: betas.at() throws in the reference
+  const double b_s = static_cast<double>(sgn_b) * __ldg(P.grid + b_s_i);
+  const double sqrt_E = __dsqrt_rn(E);
+  const double akT = dmul(dmul(t.awr, kBoltzmann), T);
+  double b_s_a_min, b_s_a_max;
+  alpha_bounds(sqrt_E, E, b_s, T, akT, b_s_a_min, b_s_a_max);
+  int local;
+  const int ps = pod_partition(P, b_s_i, local);
+  PodEval<FAST> ev;
+  ev.init(P, ps, local, T);
+  const int nF = ev.c.nF;
+  const double* Fs = ev.c.F;
+  // find_cdf: std::upper_bound over CDF indices with a < Evaluate(i)
+  auto find_cdf = [&](double a) {
+    int first = 0, len = nF;
+    while (len > 0) {
+      const int half = len >> 1, mid = first + half;
+      if (a < ev(mid)) {
+        len = half;
+      }
+      else {
+        first = mid + 1;
+        len -= half + 1;
+      }
+    }
+    const int F_a_hi_i = first;
+    const double F_a_lo = F_a_hi_i != 0 ? __ldg(Fs + F_a_hi_i - 1) : 0.0;
+    const double F_a_hi = F_a_hi_i != nF ? __ldg(Fs + F_a_hi_i) : 1.0;
+    const double a_lo = F_a_hi_i != 0 ? ev(F_a_hi_i - 1) : 0.0;
+    const double a_hi = F_a_hi_i != nF ? ev(F_a_hi_i) : t.alpha_cutoff;
+    return dadd(F_a_lo, ddiv(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
+  };
+  const double F_min = find_cdf(b_s_a_min);
+  const double F_max = find_cdf(b_s_a_max);
+  for (int res = 0; res < kTslResampleLimit; res++) {
+    const double F = dadd(F_min, dmul(rng.u01(), dsub(F_max, F_min)));
+    const int F_hi_i = upper_index(Fs, nF, F);
+    const double F_lo = F_hi_i != 0 ? __ldg(Fs + F_hi_i - 1) : 0.0;
+    const double F_hi = F_hi_i != nF ? __ldg(Fs + F_hi_i) : 1.0;
+    const double a_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : 0.0;
+    const double a_hi = F_hi_i != nF ? ev(F_hi_i) : t.alpha_cutoff;
+    const double a_prime = dadd(a_lo, dmul(ddiv(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(a_hi, a_lo)));
+    if (b_s_a_min < a_prime && a_prime < b_s_a_max) {
+      double b_a_min, b_a_max;
+      alpha_bounds(sqrt_E, E, b, T, akT, b_a_min, b_a_max);
+      alpha = dadd(b_a_min, ddiv(dmul(dsub(a_prime, b_s_a_min), dsub(b_a_max, b_a_min)), dsub(b_s_a_max, b_s_a_min)));
+      return true;
+    }
+  }
+  return false;
+}
+
+// ThermalScattering::Scatter: beta, alpha -> E', mu; Particle::Scatter
+// rotates the direction by mu with a fresh azimuth
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_scatter(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
+                                            double& dw) {
+  double beta, alpha;
+  if (!tsl_sample_beta<FAST>(t, rng, E, T, beta)) return false;
+  if (!tsl_sample_alpha<FAST>(t, rng, beta, E, T, alpha)) return false;
+  const double E_p = dadd(E, dmul(dmul(beta, kBoltzmann), T));
+  const double mu = ddiv(dsub(dadd(E, E_p), dmul(dmul(dmul(alpha, t.awr), kBoltzmann), T)),
+                         dmul(2.0, __dsqrt_rn(dmul(E, E_p))));
+  const double phi = dmul(2 * kPi, rng.u01());
+  rotate(du, dv, dw, mu, phi);
+  E = E_p;
+  return true;
+}
+
+}  // namespace mcd

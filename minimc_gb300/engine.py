@@ -33,6 +33,7 @@ ERRORS = {
 RNG_PHILOX, RNG_MINSTD = 0, 1
 SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT = 0, 1, 2
 TSL_POD, TSL_MLP = 0, 1
+TSL_PHILOX, TSL_FAST = 0x10, 0x20  # method flags: Philox streams, FP32 POD form
 GEOMETRY_ROBUST, GEOMETRY_REFERENCE = 0, 1
 
 # Particle::Event order (src/Particle.hpp:36-44) plus extensions
@@ -87,6 +88,22 @@ class TallyOut(C.Structure):
                 ("launches", C.c_uint64), ("kernel_ms", C.c_double), ("reserved", C.c_double * 3)]
 
 
+class TrainDesc(C.Structure):
+    """mc_train_desc: the surrogate's trained box and training settings."""
+    _fields_ = [("E_min", C.c_double), ("E_max", C.c_double), ("T_min", C.c_double), ("T_max", C.c_double),
+                ("conditions", C.c_uint64), ("samples_per_condition", C.c_uint32), ("batch", C.c_uint32),
+                ("steps", C.c_uint32), ("lr", C.c_float), ("seed", C.c_uint64), ("reserved", C.c_uint64 * 4)]
+
+
+class TrainOut(C.Structure):
+    _fields_ = [("loss_beta", C.c_double), ("loss_alpha", C.c_double), ("data_ms", C.c_double),
+                ("train_ms", C.c_double), ("samples", C.c_uint64), ("failures", C.c_uint64),
+                ("reserved", C.c_uint64 * 4)]
+
+
+MLP_PARAMS = 35329  # FP32 parameters per surrogate network
+
+
 class KeigOut(C.Structure):
     _fields_ = [("k_cycle", C.POINTER(C.c_double)), ("bank_size", C.POINTER(C.c_uint64)),
                 ("sum", C.POINTER(C.c_double)), ("sum_sq", C.POINTER(C.c_double)),
@@ -98,6 +115,7 @@ class KeigOut(C.Structure):
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _SIGNATURES = {
     "mc_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "mc_destroy": (None, [_P]),
@@ -130,7 +148,13 @@ _SIGNATURES = {
     "mc_energy_index": (C.c_int, [_P, C.c_int32, _D, C.c_uint64, C.POINTER(C.c_int64)]),
     "mc_sample_tsl": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, C.c_uint64, C.c_int32, _D, _D,
                                 C.POINTER(C.c_uint64)]),
+    "mc_sample_tsl_device": (C.c_int, [_P, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32,
+                                       C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+    "mc_train_surrogate": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), C.POINTER(TrainOut)]),
+    "mc_surrogate_get": (C.c_int, [_P, _F, _F, C.POINTER(TrainDesc)]),
+    "mc_surrogate_set": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), _F, _F]),
+    "mc_surrogate_grad": (C.c_int, [_P, _F, _F, _F, C.c_uint64, _F, _F, _F]),
 }
 
 _lib = None
@@ -162,6 +186,10 @@ def exported_symbols() -> list[str]:
 
 def _dptr(a: np.ndarray):
     return a.ctypes.data_as(_D)
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(_F)
 
 
 def _arr(a, dtype) -> np.ndarray:
@@ -365,14 +393,94 @@ class Context:
         self.check(self.lib.mc_surface_distance(self.h, surface, _dptr(xyz), _dptr(uvw), len(xyz), _dptr(out)))
         return out
 
-    def material_xs(self, cell: int, energy) -> tuple[np.ndarray, np.ndarray]:
-        """Material::GetMicroscopicTotal / Majorant for neutrons in `cell`."""
+    def material_xs(self, cell: int, energy, xyz=None) -> tuple[np.ndarray, np.ndarray]:
+        """Material::GetMicroscopicTotal / Majorant for neutrons in `cell`
+        (energy: group numbers or MeV; xyz: points, for temperature fields)."""
         e = _arr(np.atleast_1d(energy), np.float64)
         tot = np.zeros(len(e))
         maj = np.zeros(len(e))
-        xyz = np.zeros((len(e), 3))
+        xyz = np.zeros((len(e), 3)) if xyz is None else _arr(xyz, np.float64).reshape(-1, 3)
+        if len(xyz) != len(e):
+            raise ValueError("xyz must hold one point per energy")
         self.check(self.lib.mc_material_xs(self.h, cell, _dptr(xyz), _dptr(e), len(e), _dptr(tot), _dptr(maj)))
         return tot, maj
+
+    def energy_index(self, nuclide: int, energy) -> np.ndarray:
+        """std::map::upper_bound position of each energy in each table of a
+        continuous-energy nuclide, found through the unionized grid.
+        Columns: total, reactions in input order, fission nubar tables;
+        -1 past the last table."""
+        e = _arr(np.atleast_1d(energy), np.float64)
+        out = np.zeros((len(e), 6), np.int64)
+        self.check(self.lib.mc_energy_index(self.h, nuclide, _dptr(e), len(e),
+                                            out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
+
+    def sample_tsl(self, tsl: int, energy, temperature, seed: int = 1, method: int = TSL_POD):
+        """ThermalScattering::SampleBeta then SampleAlpha for each (E, T)
+        (host arrays): (beta, alpha, failures)."""
+        e = _arr(np.atleast_1d(energy), np.float64)
+        t = _arr(np.broadcast_to(temperature, e.shape), np.float64)
+        b = np.zeros(len(e))
+        a = np.zeros(len(e))
+        f = C.c_uint64()
+        self.check(self.lib.mc_sample_tsl(self.h, tsl, _dptr(e), _dptr(t), len(e), seed, method, _dptr(b), _dptr(a),
+                                          C.byref(f)))
+        return b, a, int(f.value)
+
+    def sample_tsl_device(self, tsl: int, d_energy: int, d_temperature: int, n: int, d_beta: int, d_alpha: int,
+                          seed: int = 1, method: int = TSL_POD) -> int:
+        """The sampler on device arrays (raw device addresses); returns the
+        failure count."""
+        f = C.c_uint64()
+        self.check(self.lib.mc_sample_tsl_device(self.h, tsl, C.c_void_p(d_energy), C.c_void_p(d_temperature), n,
+                                                 seed, method, C.c_void_p(d_beta), C.c_void_p(d_alpha), C.byref(f)))
+        return int(f.value)
+
+    def train_surrogate(self, tsl: int = 0, E_range=(1e-9, 3e-6), T_range=(283.6, 623.6), conditions: int = 0,
+                        samples_per_condition: int = 0, batch: int = 0, steps: int = 0, lr: float = 0.0,
+                        seed: int = 1) -> TrainOut:
+        """Trains the MLP surrogate of thermal library `tsl` on POD samples
+        (mc_train_surrogate)."""
+        d = TrainDesc(E_min=E_range[0], E_max=E_range[1], T_min=T_range[0], T_max=T_range[1],
+                      conditions=conditions, samples_per_condition=samples_per_condition, batch=batch,
+                      steps=steps, lr=lr, seed=seed)
+        out = TrainOut()
+        self.check(self.lib.mc_train_surrogate(self.h, tsl, C.byref(d), C.byref(out)))
+        return out
+
+    def surrogate_params(self):
+        """(beta params, alpha params, box) of the trained surrogate."""
+        b = np.zeros(MLP_PARAMS, np.float32)
+        a = np.zeros(MLP_PARAMS, np.float32)
+        box = TrainDesc()
+        self.check(self.lib.mc_surrogate_get(self.h, _fptr(b), _fptr(a), C.byref(box)))
+        return b, a, box
+
+    def set_surrogate(self, tsl: int, box: TrainDesc, beta_params, alpha_params):
+        b = _arr(beta_params, np.float32)
+        a = _arr(alpha_params, np.float32)
+        self.check(self.lib.mc_surrogate_set(self.h, tsl, C.byref(box), _fptr(b), _fptr(a)))
+
+    def surrogate_grad(self, params, x, y):
+        """One forward/backward pass: (gradient, loss, outputs)."""
+        p = _arr(params, np.float32)
+        x = _arr(x, np.float32).reshape(-1, 16)
+        y = _arr(y, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        out = np.zeros(len(x), np.float32)
+        loss = C.c_float()
+        self.check(self.lib.mc_surrogate_grad(self.h, _fptr(p), _fptr(x), _fptr(y), len(x), _fptr(g),
+                                              C.cast(C.byref(loss), _F), _fptr(out)))
+        return g, float(loss.value), out
+
+    def tsl_total(self, tsl: int, energy, temperature) -> np.ndarray:
+        """ThermalScattering::GetTotal at each (E, T)."""
+        e = _arr(np.atleast_1d(energy), np.float64)
+        t = _arr(np.broadcast_to(temperature, e.shape), np.float64)
+        out = np.zeros(len(e))
+        self.check(self.lib.mc_tsl_total(self.h, tsl, _dptr(e), _dptr(t), len(e), _dptr(out)))
+        return out
 
     def surface_contains(self, surface: int, xyz) -> np.ndarray:
         xyz = _arr(xyz, np.float64).reshape(-1, 3)

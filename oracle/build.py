@@ -36,7 +36,8 @@ def build(force: bool = False) -> Path:
 
 class OrcStats(C.Structure):
     _fields_ = [("events", C.c_uint64), ("lost", C.c_uint64), ("capped", C.c_uint64),
-                ("secondaries", C.c_uint64), ("seconds", C.c_double), ("k_tracklength", C.c_double)]
+                ("secondaries", C.c_uint64), ("seconds", C.c_double), ("k_tracklength", C.c_double),
+                ("resample", C.c_uint64)]
 
 
 _D = C.POINTER(C.c_double)
@@ -64,6 +65,16 @@ def load() -> C.CDLL:
         lib.orc_normalize.argtypes = [_D, _D]
         lib.orc_material_total.restype = C.c_double
         lib.orc_material_total.argtypes = [C.c_void_p, C.c_int32, C.c_uint64]
+        lib.orc_material_xs_ce.restype = C.c_int
+        lib.orc_material_xs_ce.argtypes = [C.c_void_p, C.c_int32, _D, _D, C.c_uint64, _D, _D]
+        lib.orc_energy_index.restype = C.c_int
+        lib.orc_energy_index.argtypes = [C.c_void_p, C.c_int32, _D, C.c_uint64, C.POINTER(C.c_int64)]
+        lib.orc_sample_tsl.restype = C.c_int
+        lib.orc_sample_tsl.argtypes = [C.c_void_p, C.c_int32, _D, _D, C.c_uint64, C.c_uint64, _D, _D,
+                                       C.POINTER(C.c_uint64)]
+        lib.orc_tsl_total.restype = C.c_int
+        lib.orc_tsl_total.argtypes = [C.c_void_p, C.c_int32, _D, _D, C.c_uint64, _D]
+        lib.orc_free_gas.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_uint64, _D, _D]
         lib.orc_run_fixed_source.restype = C.c_int
         lib.orc_run_fixed_source.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, _D, _D,
                                              C.POINTER(C.c_uint32), C.POINTER(C.c_int8), C.POINTER(OrcStats)]
@@ -101,6 +112,46 @@ class Oracle:
 
     def material_total(self, cell: int, group: int) -> float:
         return float(self.lib.orc_material_total(self.h, cell, group))
+
+    def material_xs_ce(self, cell, energy, xyz=None):
+        """(total, majorant) microscopic cross sections of a continuous-energy
+        material for neutrons of the given energies at the given points."""
+        energy = np.ascontiguousarray(energy, np.float64).ravel()
+        xyz = np.zeros((len(energy), 3)) if xyz is None else np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        tot = np.zeros(len(energy))
+        maj = np.zeros(len(energy))
+        if self.lib.orc_material_xs_ce(self.h, cell, _d(energy), _d(xyz), len(energy), _d(tot), _d(maj)) != 0:
+            raise ValueError("material_xs_ce: not a continuous-energy cell")
+        return tot, maj
+
+    def energy_index(self, nuclide, energy):
+        """std::map::upper_bound positions of each energy in the nuclide's
+        tables: columns total, reactions in input order, nubar (-1: absent)."""
+        energy = np.ascontiguousarray(energy, np.float64).ravel()
+        out = np.zeros((len(energy), 6), np.int64)
+        if self.lib.orc_energy_index(self.h, nuclide, _d(energy), len(energy),
+                                     out.ctypes.data_as(C.POINTER(C.c_int64))) != 0:
+            raise ValueError("energy_index: not a continuous-energy problem")
+        return out
+
+    def sample_tsl(self, tsl, energy, temperature, seed=1):
+        """ThermalScattering::SampleBeta then SampleAlpha for each (E, T),
+        sample i on minstd seeded with seed + i: (beta, alpha, failures)."""
+        E = np.ascontiguousarray(energy, np.float64).ravel()
+        T = np.ascontiguousarray(np.broadcast_to(temperature, E.shape), np.float64)
+        b, a = np.zeros(len(E)), np.zeros(len(E))
+        f = C.c_uint64()
+        if self.lib.orc_sample_tsl(self.h, tsl, _d(E), _d(T), len(E), seed, _d(b), _d(a), C.byref(f)) != 0:
+            raise ValueError("no such thermal scattering library")
+        return b, a, int(f.value)
+
+    def tsl_total(self, tsl, energy, temperature):
+        E = np.ascontiguousarray(energy, np.float64).ravel()
+        T = np.ascontiguousarray(np.broadcast_to(temperature, E.shape), np.float64)
+        out = np.zeros(len(E))
+        if self.lib.orc_tsl_total(self.h, tsl, _d(E), _d(T), len(E), _d(out)) != 0:
+            raise ValueError("no such thermal scattering library")
+        return out
 
     def find_cell(self, xyz):
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
@@ -145,6 +196,7 @@ class Oracle:
             raise RuntimeError(f"oracle fixed source failed ({rc})")
         return {"sum": s[: self.total_bins], "sum_sq": q[: self.total_bins], "events": st.events,
                 "lost": st.lost, "capped": st.capped, "secondaries": st.secondaries, "seconds": st.seconds,
+                "resample": st.resample,
                 "history_events": ev, "history_fate": fate}
 
     def run_keigenvalue(self, n, seed, inactive, active, threads=1, max_cycles=0):
@@ -159,7 +211,8 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle k-eigenvalue failed ({rc})")
         return {"k_cycle": k, "bank_size": bank, "sum": s[: self.total_bins], "sum_sq": q[: self.total_bins],
-                "events": st.events, "lost": st.lost, "seconds": st.seconds, "k_tracklength": st.k_tracklength}
+                "events": st.events, "lost": st.lost, "seconds": st.seconds, "k_tracklength": st.k_tracklength,
+                "resample": st.resample}
 
 
 def philox(counter, key):
@@ -180,6 +233,15 @@ def normalize(d) -> np.ndarray:
     out = np.zeros(3)
     load().orc_normalize(_d(d), _d(out))
     return out
+
+
+def free_gas(awr: float, T: float, E: float, n: int, seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """Free-gas elastic scattering of n neutrons of energy E (MeV) moving
+    along +x off a target of mass ratio awr at T kelvin: (E', mu_lab)."""
+    e = np.zeros(n)
+    mu = np.zeros(n)
+    load().orc_free_gas(awr, T, E, n, seed, _d(e), _d(mu))
+    return e, mu
 
 
 def minstd_canonical(seed: int, n: int) -> np.ndarray:

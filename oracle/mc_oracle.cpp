@@ -55,6 +55,8 @@ constexpr double kPi = M_PI;
 constexpr double kNudge = 10 * std::numeric_limits<double>::epsilon();
 constexpr double kOnAxis = 0.9;
 constexpr double kInf = std::numeric_limits<double>::infinity();
+constexpr double kBoltzmann = 8.617333262145e-11;     // MeV / K
+constexpr double kNeutronMass = 1.045354912280858e-18;  // MeV (s / cm)^2
 
 enum Event { kBirth = 0, kScatter, kCapture, kFission, kSurfaceCross, kLeak, kVirtual, kReflect, kLost };
 
@@ -63,6 +65,9 @@ struct Vec {
 };
 double Dot(const Vec& a, const Vec& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 Vec Cross(const Vec& a, const Vec& b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+Vec Scale(const Vec& a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+Vec Add(const Vec& a, const Vec& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+Vec Sub(const Vec& a, const Vec& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 Vec Normalized(Vec p) {
   const double n = std::sqrt(Dot(p, p));
   p.x /= n;
@@ -215,11 +220,398 @@ struct Oracle {
     int event = kBirth;
     int surf = -1;
     int skip = -1;
+    bool resample_failed = false;  // thermal scattering resample limit hit
     RNG rng;
     std::list<P> secondaries;
   };
 
-  double NuclideTotal(int n, const P& p) const { return m.nuclides[n].mg[p.type].total.at(p.g - 1); }
+  double NuclideTotal(int n, const P& p) const {
+    if (m.energy_mode == mc::kMultigroup) return m.nuclides[n].mg[p.type].total.at(p.g - 1);
+    return CETotal(m.nuclides[n].ce[p.type], p);
+  }
+
+  // Nuclide::GetMajorant; Multigroup::GetMajorant is GetTotal (src/Multigroup.cpp:40-43)
+  double NuclideMajorant(int n, const P& p) const {
+    if (m.energy_mode == mc::kMultigroup) return m.nuclides[n].mg[p.type].total.at(p.g - 1);
+    return CEMajorant(m.nuclides[n].ce[p.type], p);
+  }
+
+  // Material::GetMicroscopicMajorant (src/Material.cpp:41-50)
+  double MaterialMajorant(int mat, const P& p) const {
+    const mc::Material& M = m.materials[mat];
+    double acc = 0;
+    for (size_t k = 0; k < M.nuclides.size(); k++) acc = acc + M.afrac[k] * NuclideMajorant(M.nuclides[k], p);
+    return acc;
+  }
+
+  // ---- physics (continuous energy) --------------------------------------
+  // ContinuousMap::at (src/ContinuousMap.hpp:21-39): bracket by
+  // upper_bound, snap at both ends, linear interpolation
+  static double MapAt(const mc::Table1D& t, double k) {
+    const size_t hi = static_cast<size_t>(std::upper_bound(t.x.begin(), t.x.end(), k) - t.x.begin());
+    if (hi == t.x.size()) return t.y.back();
+    if (hi == 0) return t.y.front();
+    const double k_hi = t.x[hi], v_hi = t.y[hi], k_lo = t.x[hi - 1], v_lo = t.y[hi - 1];
+    return v_lo + (v_hi - v_lo) / (k_hi - k_lo) * (k - k_lo);
+  }
+
+  // the cell's ScalarField at the particle, and its upper bound
+  double CellT(const P& p) const { return m.fields[m.cells[p.cell].temperature].at(p.pos.x, p.pos.y, p.pos.z); }
+  double CellTmax(const P& p) const { return m.fields[m.cells[p.cell].temperature].upper; }
+
+  // ContinuousScatter::IsFreeGasScatteringValid (src/ContinuousReaction.cpp:205-223)
+  bool FreeGasValid(double awr, const P& p, double T) const {
+    if (p.type != mc::kNeutron) return false;
+    if (awr <= 1.0) return true;
+    return p.E < 500 * kBoltzmann * T / awr;
+  }
+
+  // ContinuousScatter::GetFreeGasScatterAdjustment (src/ContinuousReaction.cpp:225-237)
+  static double FreeGasAdjustment(double awr, double E, double T) {
+    if (T == 0) return 1;
+    const double x = std::sqrt(E / (kBoltzmann * T));
+    const double arg = awr * x * x;
+    return (1 + 1 / (2 * arg)) * std::erf(std::sqrt(arg)) + std::exp(-arg) / std::sqrt(kPi * arg);
+  }
+
+  // ContinuousScatter::GetCrossSection / GetMajorant at temperature T
+  // (src/ContinuousReaction.cpp:85-120)
+  double ScatterXS(const mc::CEData& d, const mc::CEReaction& r, const P& p, double T) const {
+    const double xs = MapAt(r.eval.xs, p.E);
+    if (r.eval.IsValid(T)) return xs;
+    if (FreeGasValid(d.awr, p, T))
+      return xs / FreeGasAdjustment(d.awr, p.E, r.eval.temperature) * FreeGasAdjustment(d.awr, p.E, T);
+    return xs;
+  }
+
+  // ThermalScattering::IsValid (src/ThermalScattering.cpp:100-103)
+  bool TSLValid(const mc::CEReaction& r, const P& p) const {
+    return r.tsl >= 0 && p.type == mc::kNeutron && p.E < m.tsl[r.tsl].cutoff_energy();
+  }
+
+  // ContinuousReaction::GetCrossSection (src/ContinuousReaction.cpp:51-54,
+  // :102-120): a valid thermal scattering library replaces the scatter
+  // cross section
+  double ReactionXS(const mc::CEData& d, const mc::CEReaction& r, const P& p, double T) const {
+    if (r.kind != mc::kScatter) return MapAt(r.eval.xs, p.E);
+    if (TSLValid(r, p)) return TSLTotal(m.tsl[r.tsl], p.E, CellT(p));
+    return ScatterXS(d, r, p, T);
+  }
+
+  // ContinuousReaction::GetMajorant (src/ContinuousReaction.cpp:45-49, :81-100)
+  double ReactionMajorant(const mc::CEData& d, const mc::CEReaction& r, const P& p, double T_max) const {
+    if (r.kind != mc::kScatter) return MapAt(r.eval.xs, p.E);
+    if (TSLValid(r, p)) return MapAt(m.tsl[r.tsl].majorant, p.E);
+    return ScatterXS(d, r, p, T_max);
+  }
+
+  // Continuous::ReactionsModifyTotal (src/Continuous.cpp:88-93)
+  bool ModifiesTotal(const mc::CEData& d, const P& p) const {
+    for (const auto& r : d.reactions)
+      if (r.kind == mc::kScatter && TSLValid(r, p)) return true;
+    return false;
+  }
+
+  // Continuous::GetTotal (src/Continuous.cpp:45-58)
+  double CETotal(const mc::CEData& d, const P& p) const {
+    const double T = CellT(p);
+    if (!ModifiesTotal(d, p) && d.total.IsValid(T)) return MapAt(d.total.xs, p.E);
+    double acc = 0;
+    for (const auto& r : d.reactions) acc = acc + ReactionXS(d, r, p, T);
+    return acc;
+  }
+
+  // Continuous::GetMajorant (src/Continuous.cpp:28-43): the cell's maximum
+  // temperature
+  double CEMajorant(const mc::CEData& d, const P& p) const {
+    const double T = CellTmax(p);
+    if (!ModifiesTotal(d, p) && d.total.IsValid(T)) return MapAt(d.total.xs, p.E);
+    double acc = 0;
+    for (const auto& r : d.reactions) acc = acc + ReactionMajorant(d, r, p, T);
+    return acc;
+  }
+
+  // ---- thermal scattering (src/ThermalScattering.cpp) --------------------
+  static size_t UpperIndex(const std::vector<double>& v, double x) {
+    return static_cast<size_t>(std::upper_bound(v.begin(), v.end(), x) - v.begin());
+  }
+
+  // temperature bracket shared by GetTotal and the partitions' Evaluate:
+  // T_max and above use the top interval, below T_min both ends are the
+  // first point
+  static void TBracket(const std::vector<double>& Ts, double T, size_t& lo, size_t& hi, bool& below, bool& above) {
+    const size_t cand = UpperIndex(Ts, T);
+    above = cand == Ts.size();
+    hi = above ? cand - 1 : cand;
+    below = hi == 0;
+    lo = below ? hi : hi - 1;
+  }
+
+  // BetaPartition / AlphaPartition::Evaluate (src/ThermalScattering.cpp:183-256)
+  static double PODEvaluate(const mc::PODPartitionSet& P, size_t part, size_t cdf_index, size_t g_index, double T) {
+    const std::vector<double>& Ts = P.T[part];
+    size_t lo, hi;
+    bool below, above;
+    TBracket(Ts, T, lo, hi, below, above);
+    const size_t r = P.S[part].size(), nT = Ts.size();
+    const std::vector<double>& S = P.S[part];
+    const std::vector<double>& C = P.cdf_modes[part];
+    const std::vector<double>& G = P.g_t_modes[part];
+    double v_hi = 0, v_lo = 0;
+    for (size_t o = 0; o < r; o++) {
+      v_hi += S[o] * C[cdf_index * r + o] * G[(g_index * nT + hi) * r + o];
+      v_lo += S[o] * C[cdf_index * r + o] * G[(g_index * nT + lo) * r + o];
+    }
+    const double T_hi = Ts[hi], T_lo = Ts[lo];
+    return v_lo + (v_hi - v_lo) / (T_hi - T_lo) * (T - T_lo);
+  }
+
+  // ThermalScattering::EvaluateInelastic (src/ThermalScattering.cpp:260-269)
+  static double EvaluateInelastic(const mc::TSLData& t, size_t E_index, size_t T_index) {
+    const size_t r = t.xs_rank;
+    double result = 0;
+    for (size_t o = 0; o < r; o++) result += t.xs_S[o] * t.xs_E_modes[E_index * r + o] * t.xs_T_modes[T_index * r + o];
+    return result;
+  }
+
+  // ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157)
+  static double TSLTotal(const mc::TSLData& t, double E, double T) {
+    const std::vector<double>& Es = t.xs_E;
+    const size_t E_hi_i = UpperIndex(Es, E);
+    if (E_hi_i == Es.size()) return std::numeric_limits<double>::quiet_NaN();  // asserted by the reference
+    const bool below_E_min = E_hi_i == 0;
+    const size_t E_lo_i = below_E_min ? E_hi_i : E_hi_i - 1;
+    size_t T_lo_i, T_hi_i;
+    bool below_T_min, above_T_max;
+    TBracket(t.xs_T, T, T_lo_i, T_hi_i, below_T_min, above_T_max);
+    const double xs_E_lo_T_lo = EvaluateInelastic(t, E_lo_i, T_lo_i);
+    const double xs_E_lo_T_hi = EvaluateInelastic(t, E_lo_i, T_hi_i);
+    const double xs_E_hi_T_lo = EvaluateInelastic(t, E_hi_i, T_lo_i);
+    const double xs_E_hi_T_hi = EvaluateInelastic(t, E_hi_i, T_hi_i);
+    const double E_lo = Es[E_lo_i], E_hi = Es[E_hi_i];
+    const double r_E = below_E_min ? 1 : (E - E_lo) / (E_hi - E_lo);
+    const double xs_T_lo = xs_E_lo_T_lo + r_E * (xs_E_hi_T_lo - xs_E_lo_T_lo);
+    const double xs_T_hi = xs_E_lo_T_hi + r_E * (xs_E_hi_T_hi - xs_E_lo_T_hi);
+    const double T_lo = t.xs_T[T_lo_i], T_hi = t.xs_T[T_hi_i];
+    const double r_T = below_T_min ? 1 : above_T_max ? 0 : (T - T_lo) / (T_hi - T_lo);
+    return xs_T_lo + r_T * (xs_T_hi - xs_T_lo);
+  }
+
+  // partition holding global grid index i, and i within it
+  static size_t Partition(const mc::PODPartitionSet& P, size_t i, size_t& local) {
+    const size_t ps = static_cast<size_t>(std::upper_bound(P.ends.begin(), P.ends.end(), i) - P.ends.begin());
+    local = ps == 0 ? i : i - P.ends[ps - 1];
+    return ps;
+  }
+
+  // ThermalScattering::SampleBeta (src/ThermalScattering.cpp:271-338);
+  // false when the resample limit is exceeded (the reference throws)
+  static bool SampleBeta(const mc::TSLData& t, RNG& rng, double E, double T, double& beta) {
+    const std::vector<double>& Es = t.beta.concat;
+    const size_t E_hi_i = UpperIndex(Es, E);
+    if (E_hi_i == Es.size()) return false;  // the reference asserts E < cutoff
+    const double r = E_hi_i != 0 ? (E - Es[E_hi_i - 1]) / (Es[E_hi_i] - Es[E_hi_i - 1]) : 1;
+    const size_t E_s_i = r <= std::uniform_real_distribution{}(rng) ? E_hi_i - 1 : E_hi_i;
+    const double E_s = Es[E_s_i];
+    size_t E_s_i_local;
+    const size_t ps = Partition(t.beta, E_s_i, E_s_i_local);
+    const std::vector<double>& Fs = t.beta.F[ps];
+    for (size_t resamples = 0; resamples < 10; resamples++) {
+      const double F = std::uniform_real_distribution{}(rng);
+      const size_t F_hi_i = UpperIndex(Fs, F);
+      const double F_lo = F_hi_i != 0 ? Fs[F_hi_i - 1] : 0;
+      const double F_hi = F_hi_i != Fs.size() ? Fs[F_hi_i] : 1;
+      const double b_lo = F_hi_i != 0 ? PODEvaluate(t.beta, ps, F_hi_i - 1, E_s_i_local, T) : -E_s / (kBoltzmann * T);
+      const double b_hi = F_hi_i != Fs.size() ? PODEvaluate(t.beta, ps, F_hi_i, E_s_i_local, T) : t.beta_cutoff;
+      const double b_prime = b_lo + (F - F_lo) / (F_hi - F_lo) * (b_hi - b_lo);
+      const double b_min = -E / (kBoltzmann * T);
+      if (b_min <= b_prime) {
+        beta = b_prime;
+        return true;
+      }
+    }
+    return false;
+  }
+
+  // std::upper_bound over CDF indices [0, n) with the predicate a < Evaluate(i):
+  // the standard library's bisection, so a non-monotone reconstruction
+  // probes the same points
+  static size_t UpperBoundAlpha(const mc::TSLData& t, size_t ps, size_t b_local, double T, size_t n, double a) {
+    size_t first = 0, len = n;
+    while (len > 0) {
+      const size_t half = len >> 1, middle = first + half;
+      if (a < PODEvaluate(t.alpha, ps, middle, b_local, T)) {
+        len = half;
+      }
+      else {
+        first = middle + 1;
+        len = len - half - 1;
+      }
+    }
+    return first;
+  }
+
+  // ThermalScattering::SampleAlpha (src/ThermalScattering.cpp:340-463),
+  // including its interpolation factor as written (:363-365)
+  static bool SampleAlpha(const mc::TSLData& t, RNG& rng, double b, double E, double T, double& alpha) {
+    const double abs_b = std::abs(b);
+    const int sgn_b = (0 < b) - (b < 0);
+    const std::vector<double>& betas = t.alpha.concat;
+    const size_t b_hi_i = UpperIndex(betas, abs_b);
+    if (b_hi_i == betas.size()) return false;  // betas.at() throws in the reference
+    const bool snap_to_lower = ((sgn_b == 1 && t.beta_cutoff <= betas[b_hi_i]) ||
+                                (sgn_b == -1 && -betas[b_hi_i] < -E / (kBoltzmann * T)));
+    const bool snap_to_min = b_hi_i == 0;
+    const double r = snap_to_lower ? 0
+                     : snap_to_min ? 1
+                                   : (abs_b - betas[b_hi_i - 1] / (betas[b_hi_i] - betas[b_hi_i - 1]));
+    const bool lower = r <= std::uniform_real_distribution{}(rng);
+    if (lower && b_hi_i == 0) return false;  // betas.at(-1) throws in the reference
+    const size_t b_s_i = lower ? b_hi_i - 1 : b_hi_i;
+    const double b_s = sgn_b * betas[b_s_i];
+    const double sqrt_E = std::sqrt(E);
+    const double b_s_sqrt_E_bkT = std::sqrt(E + b_s * kBoltzmann * T);
+    const double akT = t.awr * kBoltzmann * T;
+    const double b_s_a_min = std::pow(sqrt_E - b_s_sqrt_E_bkT, 2) / akT;
+    const double b_s_a_max = std::pow(sqrt_E + b_s_sqrt_E_bkT, 2) / akT;
+    size_t b_s_i_local;
+    const size_t ps = Partition(t.alpha, b_s_i, b_s_i_local);
+    const std::vector<double>& Fs = t.alpha.F[ps];
+    auto find_cdf = [&](double a) {
+      const size_t F_a_hi_i = UpperBoundAlpha(t, ps, b_s_i_local, T, Fs.size(), a);
+      const double F_a_lo = F_a_hi_i != 0 ? Fs[F_a_hi_i - 1] : 0;
+      const double F_a_hi = F_a_hi_i != Fs.size() ? Fs[F_a_hi_i] : 1;
+      const double a_lo = F_a_hi_i != 0 ? PODEvaluate(t.alpha, ps, F_a_hi_i - 1, b_s_i_local, T) : 0;
+      const double a_hi = F_a_hi_i != Fs.size() ? PODEvaluate(t.alpha, ps, F_a_hi_i, b_s_i_local, T) : t.alpha_cutoff;
+      return F_a_lo + (a - a_lo) * (F_a_hi - F_a_lo) / (a_hi - a_lo);
+    };
+    const double F_min = find_cdf(b_s_a_min);
+    const double F_max = find_cdf(b_s_a_max);
+    for (size_t resamples = 0; resamples < 10; resamples++) {
+      const double F = F_min + std::uniform_real_distribution{}(rng) * (F_max - F_min);
+      const size_t F_hi_i = UpperIndex(Fs, F);
+      const double F_lo = F_hi_i != 0 ? Fs[F_hi_i - 1] : 0;
+      const double F_hi = F_hi_i != Fs.size() ? Fs[F_hi_i] : 1;
+      const double a_lo = F_hi_i != 0 ? PODEvaluate(t.alpha, ps, F_hi_i - 1, b_s_i_local, T) : 0;
+      const double a_hi = F_hi_i != Fs.size() ? PODEvaluate(t.alpha, ps, F_hi_i, b_s_i_local, T) : t.alpha_cutoff;
+      const double a_prime = a_lo + (F - F_lo) / (F_hi - F_lo) * (a_hi - a_lo);
+      if (b_s_a_min < a_prime && a_prime < b_s_a_max) {
+        const double b_sqrt_E_bkT = std::sqrt(E + b * kBoltzmann * T);
+        const double b_a_min = std::pow(sqrt_E - b_sqrt_E_bkT, 2) / akT;
+        const double b_a_max = std::pow(sqrt_E + b_sqrt_E_bkT, 2) / akT;
+        alpha = b_a_min + (a_prime - b_s_a_min) * (b_a_max - b_a_min) / (b_s_a_max - b_s_a_min);
+        return true;
+      }
+    }
+    return false;
+  }
+
+  // ThermalScattering::Scatter (src/ThermalScattering.cpp:159-171)
+  bool TSLScatter(const mc::TSLData& t, P& p, double T) const {
+    const double E = p.E;
+    double beta, alpha;
+    if (!SampleBeta(t, p.rng, E, T, beta)) return false;
+    if (!SampleAlpha(t, p.rng, beta, E, T, alpha)) return false;
+    const double E_p = E + beta * kBoltzmann * T;
+    const double mu = (E + E_p - alpha * t.awr * kBoltzmann * T) / (2 * std::sqrt(E * E_p));
+    const double phi = 2 * kPi * std::uniform_real_distribution{}(p.rng);
+    p.dir = Rotate(p.dir, mu, phi);
+    p.E = E_p;
+    return true;
+  }
+
+  // Continuous::Interact (src/Continuous.cpp:60-72)
+  void CEInteract(int n, P& p) const {
+    const mc::CEData& d = m.nuclides[n].ce[p.type];
+    const double T = CellT(p);
+    for (;;) {
+      const double threshold = std::uniform_real_distribution{}(p.rng) * CETotal(d, p);
+      double accumulated{0};
+      for (const auto& r : d.reactions) {
+        accumulated += ReactionXS(d, r, p, T);
+        if (accumulated > threshold) {
+          if (r.kind == mc::kCapture) {
+            p.event = kCapture;
+          }
+          else if (r.kind == mc::kScatter) {
+            if (TSLValid(r, p)) {
+              p.event = kScatter;
+              // the reference throws past the resample limits
+              if (!TSLScatter(m.tsl[r.tsl], p, T)) {
+                p.event = kLost;
+                p.resample_failed = true;
+              }
+            }
+            else {
+              FreeGasScatter(d, p, T);
+            }
+          }
+          else {
+            CEFission(r, p);
+          }
+          return;
+        }
+      }
+      // no reaction found: resample (tail recursion in the reference)
+    }
+  }
+
+  // ContinuousScatter::Interact without a thermal scattering library
+  // (src/ContinuousReaction.cpp:119-189): free-gas target velocity by
+  // rejection, elastic scattering in the centre-of-mass frame
+  void FreeGasScatter(const mc::CEData& d, P& p, double T) const {
+    p.event = kScatter;
+    const double awr = d.awr;
+    constexpr double m_n = kNeutronMass;
+    const double E = p.E;
+    const double s_n = std::sqrt(2. * E / m_n);
+    const Vec v_n = Scale(p.dir, s_n);
+    const double beta = std::sqrt((awr * m_n) / (2. * kBoltzmann * T));
+    const double y = beta * s_n;
+    double x, mu;
+    do {
+      const double xi_1 = std::uniform_real_distribution{}(p.rng);
+      const double xi_2 = std::uniform_real_distribution{}(p.rng);
+      if (std::uniform_real_distribution{}(p.rng) < 2 / (std::sqrt(kPi) * y + 2)) {
+        x = std::sqrt(-std::log(xi_1 * xi_2));
+      }
+      else {
+        const double xi_3 = std::uniform_real_distribution{}(p.rng);
+        const double z = std::cos(kPi * xi_3 / 2);
+        x = std::sqrt(-std::log(xi_1) - std::log(xi_2) * z * z);
+      }
+      mu = 2 * std::uniform_real_distribution{}(p.rng) - 1;
+    } while (std::uniform_real_distribution{}(p.rng) >= std::sqrt(x * x + y * y - 2 * x * y * mu) / (x + y));
+    const double s_T = x / beta;
+    const double phi = 2 * kPi * std::uniform_real_distribution{}(p.rng);
+    const Vec v_T = Scale(Rotate(p.dir, mu, phi), s_T);
+    const Vec num = Add(v_n, Scale(v_T, awr));
+    const double den = 1 + awr;
+    const Vec v_cm{num.x / den, num.y / den, num.z / den};
+    const Vec V_n = Sub(v_n, v_cm);
+    const double mu_cm = 2 * std::uniform_real_distribution{}(p.rng) - 1;
+    const double phi_cm = 2 * kPi * std::uniform_real_distribution{}(p.rng);
+    const Vec V_dir = Rotate(Normalized(V_n), mu_cm, phi_cm);
+    const Vec V_prime = Scale(V_dir, std::sqrt(Dot(V_n, V_n)));
+    const Vec v_prime = Add(V_prime, v_cm);
+    const double E_prime = 0.5 * m_n * Dot(v_prime, v_prime);
+    // Particle::Scatter (src/Particle.cpp:55-65)
+    const double mu_lab = Dot(p.dir, Normalized(v_prime));
+    const double phi_lab = 2 * kPi * std::uniform_real_distribution{}(p.rng);
+    p.dir = Rotate(p.dir, mu_lab, phi_lab);
+    p.E = E_prime;
+  }
+
+  // ContinuousFission::Interact (src/ContinuousReaction.cpp:252-265): the
+  // secondaries keep the incident energy
+  void CEFission(const mc::CEReaction& r, P& p) const {
+    p.event = kFission;
+    const size_t yield(MapAt(r.nubar, p.E) + std::uniform_real_distribution{}(p.rng));
+    for (size_t i = 0; i < yield; i++) {
+      const Vec dir = IsotropicDirection(p.rng);
+      BankSecondaries(p, dir, p.g, p.E);
+    }
+  }
 
   double MaterialTotal(int mat, const P& p) const {
     const mc::Material& M = m.materials[mat];
@@ -239,11 +631,12 @@ struct Oracle {
     return M.nuclides.back();
   }
 
-  void BankSecondaries(P& p, const Vec& dir, uint64_t g) const {
+  void BankSecondaries(P& p, const Vec& dir, uint64_t g, double E = 0) const {
     P s;
     s.pos = p.pos;
     s.dir = dir;
     s.g = g;
+    s.E = E;
     s.type = 0;
     s.rng.seed(p.rng());
     s.cell = p.cell;
@@ -336,7 +729,7 @@ struct Oracle {
 
   // ---- transport ------------------------------------------------------------
   struct Stats {
-    uint64_t events = 0, lost = 0, capped = 0;
+    uint64_t events = 0, lost = 0, capped = 0, resample = 0;
     double ktl = 0;
   };
 
@@ -354,20 +747,30 @@ struct Oracle {
     const bool delta = m.tracking == mc::kCellDeltaTracking;
     while (p.event != kCapture && p.event != kLeak && p.event != kFission && p.event != kLost) {
       const int mat = m.cells[p.cell].material;
-      const double micro = MaterialTotal(mat, p);
+      // GetCollisionProbabilityDensity: total (surface tracking) or
+      // majorant (delta tracking), src/TransportMethod.cpp:79-82,124-127
+      const double cpd = delta ? MaterialMajorant(mat, p) : MaterialTotal(mat, p);
       const double distance_to_collision =
-          std::exponential_distribution{m.materials[mat].number_density * micro}(p.rng);
+          std::exponential_distribution{m.materials[mat].number_density * cpd}(p.rng);
       double dsurf;
       const int s = NearestSurface(p.cell, p.pos, p.dir, dsurf, p.skip);
       const bool collide = delta ? !(dsurf < distance_to_collision) : distance_to_collision < dsurf;
       if (collide) {
         if (score) ScoreTrack(p, distance_to_collision, pending);
         st.ktl += distance_to_collision * m.materials[mat].number_density * NuSigmaF(mat, p);
-        Stream(p, distance_to_collision);
-        p.skip = -1;
-        if (delta) (void)std::bernoulli_distribution{micro / micro}(p.rng);
-        const int n = SampleNuclide(p);
-        MGInteract(n, p);
+        if (delta && !std::bernoulli_distribution{MaterialTotal(mat, p) / cpd}(p.rng)) {
+          // virtual collision (src/TransportMethod.cpp:111-115)
+          Stream(p, distance_to_collision);
+          p.event = kVirtual;
+        }
+        else {
+          Stream(p, distance_to_collision);
+          p.skip = -1;
+          const int n = SampleNuclide(p);
+          if (m.energy_mode == mc::kMultigroup) MGInteract(n, p);
+          else CEInteract(n, p);
+          if (p.event == kLost) (p.resample_failed ? st.resample : st.lost)++;
+        }
       }
       else if (m.surfaces[s].reflective) {
         if (score) ScoreTrack(p, dsurf, pending);
@@ -413,12 +816,19 @@ struct Oracle {
     if (nev_out) *nev_out += nev;
   }
 
+  // sum of afrac * nubar * sigma_f (the k track-length estimator, an extension)
   double NuSigmaF(int mat, const P& p) const {
     const mc::Material& M = m.materials[mat];
     double acc = 0;
     for (size_t k = 0; k < M.nuclides.size(); k++) {
-      const mc::MGData& d = m.nuclides[M.nuclides[k]].mg[p.type];
-      if (d.has_fission) acc = acc + M.afrac[k] * (d.nubar[p.g - 1] * d.fission[p.g - 1]);
+      if (m.energy_mode == mc::kMultigroup) {
+        const mc::MGData& d = m.nuclides[M.nuclides[k]].mg[p.type];
+        if (d.has_fission) acc = acc + M.afrac[k] * (d.nubar[p.g - 1] * d.fission[p.g - 1]);
+      }
+      else {
+        for (const auto& r : m.nuclides[M.nuclides[k]].ce[p.type].reactions)
+          if (r.kind == mc::kFission && r.has_nubar) acc = acc + M.afrac[k] * (MapAt(r.nubar, p.E) * MapAt(r.eval.xs, p.E));
+      }
     }
     return acc;
   }
@@ -500,6 +910,7 @@ struct orc_stats {
   uint64_t events, lost, capped, secondaries;
   double seconds;
   double k_tracklength;
+  uint64_t resample;
 };
 
 void* orc_create(const char* xml, const char* base_dir, char* err, size_t errn) {
@@ -581,7 +992,106 @@ double orc_material_total(void* h, int32_t cell, uint64_t g) {
   Oracle::P p;
   p.g = g;
   p.type = 0;
+  p.cell = cell;
   return o->MaterialTotal(mat, p);
+}
+
+// Material::GetMicroscopicTotal and GetMicroscopicMajorant of neutrons of
+// continuous energies E[i] at points xyz[i] of cell c
+int orc_material_xs_ce(void* h, int32_t cell, const double* E, const double* xyz, uint64_t n, double* total,
+                       double* majorant) {
+  auto* o = static_cast<Oracle*>(h);
+  if (o->m.energy_mode != mc::kContinuous) return -1;
+  const int mat = o->m.cells.at(cell).material;
+  if (mat < 0) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    Oracle::P p;
+    p.type = 0;
+    p.cell = cell;
+    p.E = E[i];
+    p.pos = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    total[i] = o->MaterialTotal(mat, p);
+    majorant[i] = o->MaterialMajorant(mat, p);
+  }
+  return 0;
+}
+
+// std::map::upper_bound positions in the energy tables of nuclide `nuc`:
+// out[i * 6 + t] for t = total, then each reaction in input order, then
+// nubar (-1 where absent)
+int orc_energy_index(void* h, int32_t nuc, const double* E, uint64_t n, int64_t* out) {
+  auto* o = static_cast<Oracle*>(h);
+  if (o->m.energy_mode != mc::kContinuous) return -1;
+  const mc::CEData& d = o->m.nuclides.at(nuc).ce[0];
+  std::vector<std::map<double, double>> maps;
+  std::vector<const mc::Table1D*> tabs{&d.total.xs};
+  for (const auto& r : d.reactions) tabs.push_back(&r.eval.xs);
+  for (const auto& r : d.reactions)
+    if (r.has_nubar) tabs.push_back(&r.nubar);
+  for (const auto* t : tabs) {
+    std::map<double, double> mp;
+    for (size_t i = 0; i < t->x.size(); i++) mp[t->x[i]] = t->y[i];
+    maps.push_back(std::move(mp));
+  }
+  for (uint64_t i = 0; i < n; i++) {
+    for (size_t t = 0; t < 6; t++) {
+      if (t >= maps.size()) {
+        out[i * 6 + t] = -1;
+        continue;
+      }
+      const auto it = maps[t].upper_bound(E[i]);
+      out[i * 6 + t] = static_cast<int64_t>(std::distance(maps[t].begin(), it));
+    }
+  }
+  return 0;
+}
+
+// ContinuousScatter::Interact's free-gas kinematics for n neutrons of
+// energy E moving along +x, particle i seeded with seed + i: outgoing
+// energies and lab cosines
+void orc_free_gas(double awr, double T, double E, uint64_t n, uint64_t seed, double* E_out, double* mu_out) {
+  Oracle o;
+  mc::CEData d;
+  d.awr = awr;
+  for (uint64_t i = 0; i < n; i++) {
+    Oracle::P p;
+    p.E = E;
+    p.dir = {1, 0, 0};
+    p.rng.seed(static_cast<RNG::result_type>(seed + i));
+    o.FreeGasScatter(d, p, T);
+    E_out[i] = p.E;
+    mu_out[i] = p.dir.x;
+  }
+}
+
+// ThermalScattering::SampleBeta then SampleAlpha for (E[i], T[i]), sample i
+// drawing from minstd seeded with seed + i; NaN and a count on failure
+int orc_sample_tsl(void* h, int32_t tsl, const double* E, const double* T, uint64_t n, uint64_t seed, double* beta,
+                   double* alpha, uint64_t* failures) {
+  auto* o = static_cast<Oracle*>(h);
+  if (tsl < 0 || static_cast<size_t>(tsl) >= o->m.tsl.size()) return -1;
+  const mc::TSLData& t = o->m.tsl[static_cast<size_t>(tsl)];
+  uint64_t fails = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    RNG rng{static_cast<RNG::result_type>(seed + i)};
+    double b = std::numeric_limits<double>::quiet_NaN(), a = b;
+    if (!Oracle::SampleBeta(t, rng, E[i], T[i], b) || !Oracle::SampleAlpha(t, rng, b, E[i], T[i], a)) {
+      fails++;
+      if (!(b == b) || a != a) a = std::numeric_limits<double>::quiet_NaN();
+    }
+    beta[i] = b;
+    alpha[i] = a;
+  }
+  if (failures) *failures = fails;
+  return 0;
+}
+
+// ThermalScattering::GetTotal at (E[i], T[i])
+int orc_tsl_total(void* h, int32_t tsl, const double* E, const double* T, uint64_t n, double* out) {
+  auto* o = static_cast<Oracle*>(h);
+  if (tsl < 0 || static_cast<size_t>(tsl) >= o->m.tsl.size()) return -1;
+  for (uint64_t i = 0; i < n; i++) out[i] = Oracle::TSLTotal(o->m.tsl[static_cast<size_t>(tsl)], E[i], T[i]);
+  return 0;
 }
 
 // minstd + generate_canonical values for a seed (RNG parity checks)
@@ -594,7 +1104,6 @@ void orc_minstd_canonical(uint64_t seed, uint64_t n, double* out) {
 int orc_run_fixed_source(void* h, uint64_t n, uint64_t seed, int threads, uint32_t max_events, double* sum, double* sq,
                          uint32_t* hist_events, int8_t* hist_fate, orc_stats* stats) {
   auto* o = static_cast<Oracle*>(h);
-  if (o->m.energy_mode != mc::kMultigroup) return -1;
   const size_t nb = std::max<size_t>(1, o->m.total_bins());
   threads = std::max(1, threads);
   std::vector<std::vector<double>> ts(threads, std::vector<double>(nb, 0)), tq(threads, std::vector<double>(nb, 0));
@@ -637,6 +1146,7 @@ int orc_run_fixed_source(void* h, uint64_t n, uint64_t seed, int threads, uint32
       stats->events += st[t].events;
       stats->lost += st[t].lost;
       stats->capped += st[t].capped;
+      stats->resample += st[t].resample;
       stats->secondaries += sec[t];
     }
     stats->seconds = secs;
@@ -649,7 +1159,6 @@ int orc_run_keigenvalue(void* h, uint64_t N, uint64_t seed, uint32_t inactive, u
                         uint32_t max_cycles_timed, double* k_cycle, uint64_t* bank_size, double* sum, double* sq,
                         orc_stats* stats) {
   auto* o = static_cast<Oracle*>(h);
-  if (o->m.energy_mode != mc::kMultigroup) return -1;
   threads = std::max(1, threads);
   const size_t nb = std::max<size_t>(1, o->m.total_bins());
   std::vector<std::vector<double>> ts(threads, std::vector<double>(nb, 0)), tq(threads, std::vector<double>(nb, 0));
@@ -657,6 +1166,7 @@ int orc_run_keigenvalue(void* h, uint64_t N, uint64_t seed, uint32_t inactive, u
   struct SiteRec {
     Vec pos, dir;
     uint64_t g;
+    double E;
   };
   std::vector<SiteRec> source(N);
   std::vector<std::vector<SiteRec>> per_hist(N);
@@ -675,6 +1185,7 @@ int orc_run_keigenvalue(void* h, uint64_t N, uint64_t seed, uint32_t inactive, u
         p.pos = source[j].pos;
         p.dir = source[j].dir;
         p.g = source[j].g;
+        p.E = source[j].E;
         p.type = 0;
         p.rng.seed(static_cast<RNG::result_type>(seed + static_cast<uint64_t>(c) * N + j));
       }
@@ -684,7 +1195,7 @@ int orc_run_keigenvalue(void* h, uint64_t N, uint64_t seed, uint32_t inactive, u
       o->Transport(p, pending, s, act, 1000000u, nullptr);
       ktl[tid] += s.ktl - k0;
       per_hist[j].clear();
-      for (const auto& q : p.secondaries) per_hist[j].push_back({q.pos, q.dir, q.g});
+      for (const auto& q : p.secondaries) per_hist[j].push_back({q.pos, q.dir, q.g, q.E});
       if (act) {
         for (const auto& [b, v] : pending) {
           ts[tid][b] += v;
@@ -727,6 +1238,7 @@ int orc_run_keigenvalue(void* h, uint64_t N, uint64_t seed, uint32_t inactive, u
       stats->events += st[t].events;
       stats->lost += st[t].lost;
       stats->capped += st[t].capped;
+      stats->resample += st[t].resample;
     }
     stats->seconds = secs;
     stats->k_tracklength = active ? ktl_active / active : 0;
