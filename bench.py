@@ -334,13 +334,147 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+def tsl_problem(histories: int, seed: int = 1) -> dict:
+    """Broomstick with the synthetic POD thermal library (1 eV beam, 450 K)."""
+    import atexit
+    import shutil
+    import tempfile
+
+    from minimc_gb300 import synth_tsl
+
+    base = Path(tempfile.mkdtemp(prefix="mc_tsl_"))
+    atexit.register(shutil.rmtree, base, True)
+    tsl = synth_tsl.write_tsl(base)
+    nuc = synth_tsl.moderator_nuclide(base)
+    xml = synth_tsl.broomstick_xml(tsl, nuc, histories=histories, energy=1e-6, temperature=450.0)
+    return {"xml": xml.replace("<seed>1</seed>", f"<seed>{seed}</seed>"), "base": str(base)}
+
+
+TSL_WORKLOAD = ("thermal broomstick fixed source (POD S(alpha,beta,T) library rank 30, 4+4 partitions; "
+                "1 eV pencil beam on a 0.01 cm hydrogen-moderator cylinder at 450 K; cosine x energy leakage "
+                "tally 202 x 202 bins)")
+
+
+def run_gpu_tsl(args) -> None:
+    """Broomstick transport (histories/s, POD thermal sampling inside the
+    transport kernel) plus the sampler-level comparison of the POD forms and
+    the trained MLP surrogate on C4's incident energies with T uniform in
+    283.6-623.6 K per sample."""
+    import torch
+
+    from minimc_gb300 import RNG_PHILOX, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    hist = args.histories
+    wl = tsl_problem(hist, seed=1 + rank)
+    ctx = Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_xml(wl["xml"], wl["base"])
+    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), histories=hist)
+    for _ in range(args.warmup):
+        ctx.run_fixed_source(**opts)
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    ms, kms, walls, events, launches = [], [], [], 0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = ctx.run_fixed_source(**opts)
+        walls.append(time.perf_counter() - t0)
+        ms.append(r.raw.transport_ms)
+        kms.append(r.raw.kernel_ms)
+        events += r.raw.events
+        launches += r.raw.launches
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    value = hist * args.steps * ws / (sum(ms) / 1e3)
+    e2e_value = hist * args.steps * ws / sum(walls)
+    e_h = events / (hist * args.steps)
+    peak, peak_kind = peaks()
+    alg = e_h * BYTES_PER_EVENT * hist
+    achieved = alg / (sum(kms) / args.steps / 1e3) / 1e9
+
+    # sampler level: POD exact, POD FP32, MLP surrogate (trained here)
+    n = 4_000_000
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    E = torch.tensor([0.01e-6, 0.1e-6, 1.0e-6], dtype=torch.float64, device="cuda")[
+        torch.randint(0, 3, (n,), device="cuda", generator=g)]
+    T = 283.6 + 340.0 * torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    a = torch.empty_like(b)
+    t0 = time.perf_counter()
+    tr = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
+                             samples_per_condition=512, batch=8192, steps=3000, seed=3)
+    train_s = time.perf_counter() - t0
+    rates, samples = {}, {}
+    for name, method in (("pod_exact", TSL_POD | TSL_PHILOX), ("pod_fp32", TSL_POD | TSL_PHILOX | TSL_FAST),
+                         ("mlp", TSL_MLP)):
+        for _ in range(2):
+            ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=11, method=method)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        e0.record(stream)
+        for i in range(reps):
+            ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=11 + i,
+                                  method=method)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rates[name] = n * reps / (e0.elapsed_time(e1) / 1e3)
+        samples[name] = (b[:200_000].cpu().numpy(), a[:200_000].cpu().numpy())
+    from scipy import stats
+
+    ks = {k: {"beta": float(stats.ks_2samp(samples[k][0], samples["pod_exact"][0]).statistic),
+              "alpha": float(stats.ks_2samp(samples[k][1], samples["pod_exact"][1]).statistic)}
+          for k in ("pod_fp32", "mlp")}
+    flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two networks, multiply-adds x 2
+    bf16_peak = None
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        bf16_peak = json.loads(pk.read_text()).get("bf16_tflops")
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle.build import Oracle
+
+        o = Oracle(wl["xml"], wl["base"])
+        nc = min(hist, 2_000_000)
+        thr = os.cpu_count() or 1
+        rc = o.run_fixed_source(nc, 1, threads=thr)
+        cpu = {"value": nc / rc["seconds"], "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{nc} histories of the same broomstick (CPU oracle, {thr} threads), {rc['seconds']:.1f} s"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sum(ms) / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": TSL_WORKLOAD, "histories_per_step": hist, "rng": "philox",
+                       "fast_math": bool(args.fast), "l2": "inputs generated on device; tallies 0.65 MB"},
+            "events_per_history": e_h,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_kind": peak_kind, "kernel": "k_history_ce"},
+            "surrogate": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "train_s": train_s,
+                          "train": {"loss_beta": tr.loss_beta, "loss_alpha": tr.loss_alpha, "samples": tr.samples,
+                                    "data_ms": tr.data_ms, "train_ms": tr.train_ms},
+                          "mlp_tflops": rates["mlp"] * flops / 1e12, "bf16_peak_tflops": bf16_peak,
+                          "sample_n": n},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 2 * 8 * ctx.info.total_bins, "call": "mc_run_fixed_source"},
+            "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="two_zone", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="two_zone", choices=sorted(WORKLOADS) + ["tsl"])
     ap.add_argument("--histories", type=int, default=1_000_000)
     ap.add_argument("--block", type=int, default=0, help="0: autotuned")
     ap.add_argument("--fast", type=int, default=1,
@@ -357,6 +491,8 @@ def main():
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "tsl":
+        run_gpu_tsl(args)
     else:
         run_gpu(args)
 
