@@ -551,9 +551,12 @@ cudaError_t launch_tsl_alpha_draws(const DevTSL* tsl, const double* E, const dou
 
 // ---------------------------------------------------------------------------
 // fused surrogate sampler: both networks' BF16 weights resident in shared
-// memory, one 128-sample tile per loop trip, one sample per thread; each
-// layer is one tcgen05 product into tensor memory followed by a per-row
-// epilogue (bias, SiLU) that writes the next layer's operand tile
+// memory; each of the CTA's two warpgroups works through its own 128-sample
+// tiles (one sample per thread) with its own input and hidden tiles, its own
+// 128 tensor-memory columns and its own mbarrier, so one warpgroup's
+// epilogue overlaps the other's products.  Each layer is one tcgen05
+// product into tensor memory followed by a per-row epilogue (bias, SiLU)
+// that writes the next layer's operand tile.
 
 namespace {
 
@@ -564,6 +567,7 @@ struct NetView {
   const bf16* W3;
 };
 
+constexpr int kGroups = 2;                                // warpgroups (tiles in flight) per CTA
 constexpr uint32_t kTileW1 = kMlpWidth * kMlpIn * 2;      // 4 KB
 constexpr uint32_t kTileW = kMlpWidth * kMlpWidth * 2;    // 32 KB
 constexpr uint32_t kOffB1 = 0;                            // beta network W1
@@ -572,11 +576,39 @@ constexpr uint32_t kOffB3 = kOffB2 + kTileW;
 constexpr uint32_t kOffA1 = kOffB3 + kTileW;              // alpha network
 constexpr uint32_t kOffA2 = kOffA1 + kTileW1;
 constexpr uint32_t kOffA3 = kOffA2 + kTileW;
-constexpr uint32_t kOffX = kOffA3 + kTileW;               // input tile 128 x 16
-constexpr uint32_t kOffH = kOffX + kTileW1;               // hidden tile 128 x 128
-constexpr uint32_t kOffF = kOffH + kTileW;                // FP32: per net b1 b2 b3 w4 (4 x 128) + b4
+constexpr uint32_t kOffG = kOffA3 + kTileW;               // per warpgroup: input tile, hidden tile
+constexpr uint32_t kGroupBytes = kTileW1 + kTileW;
+constexpr uint32_t kOffF = kOffG + kGroups * kGroupBytes; // FP32: per net b1 b2 b3 w4 (4 x 128) + b4
 constexpr uint32_t kOffMisc = kOffF + 2 * (4 * kMlpWidth + 4) * 4;
 constexpr uint32_t kSampleSmem = kOffMisc + 64;
+static_assert(kSampleSmem <= 227 * 1024, "shared memory");
+
+// SiLU with the hardware tanh (max relative error about 2^-11, below the
+// BF16 rounding of the activations it feeds)
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float silu_fast(float z) {
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_fast(h), h);
+}
+
+// warpgroup barrier (named barrier 1 + g, 128 threads) and its AND vote
+__device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
+__device__ __forceinline__ bool wg_all(int g, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.and.pred p, %2, 128, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"(v ? 1u : 0u), "r"(1 + g)
+      : "memory");
+  return r != 0;
+}
 
 __device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int K) {
   for (int c = threadIdx.x; c < kMlpWidth * (K / 8); c += blockDim.x) {
@@ -586,94 +618,100 @@ __device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int K) 
   }
 }
 
-struct SampleShared {
-  uint8_t* base;
-  uint32_t tmem, mbar;
+// one warpgroup's working set
+struct Group {
+  uint8_t* base;   // shared memory base
+  uint32_t X, H;   // offsets of its input and hidden tiles
+  uint32_t tmem;   // its 128 accumulator columns
+  uint32_t mbar;
   uint32_t phase;
+  int g, lt;       // warpgroup, thread within it (the tile row)
   bool ok;
 };
 
-// one layer's product: D = act_tile * W^T (K = 16 or 128)
-__device__ __forceinline__ void layer_mma(SampleShared& sh, uint32_t act_off, uint32_t w_off, int K) {
+// D = act_tile * W^T (K = 16 or 128)
+__device__ __forceinline__ void layer_mma(Group& G, uint32_t act_off, uint32_t w_off, int K) {
   tc::fence_proxy_async();
   tc::fence_before_sync();
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  wg_sync(G.g);
+  if (G.lt == 0) {
     tc::fence_after_sync();
-    const uint32_t a0 = tc::smem_addr(sh.base + act_off), b0 = tc::smem_addr(sh.base + w_off);
+    const uint32_t a0 = tc::smem_addr(G.base + act_off), b0 = tc::smem_addr(G.base + w_off);
     constexpr uint32_t idesc = tc::idesc_bf16_f32(128, kMlpWidth);
     for (int s = 0; s < K / 16; s++)
-      tc::mma_bf16(sh.tmem, tc::smem_desc(a0 + s * 256, 128, K * 16), tc::smem_desc(b0 + s * 256, 128, K * 16),
+      tc::mma_bf16(G.tmem, tc::smem_desc(a0 + s * 256, 128, K * 16), tc::smem_desc(b0 + s * 256, 128, K * 16),
                    idesc, s > 0 ? 1u : 0u);
-    tc::mma_commit(sh.mbar);
+    tc::mma_commit(G.mbar);
   }
-  if (!__syncthreads_and(tc::mbar_wait(sh.mbar, sh.phase, kWaitCycles) ? 1 : 0)) sh.ok = false;
-  sh.phase ^= 1;
+  if (!wg_all(G.g, tc::mbar_wait(G.mbar, G.phase, kWaitCycles))) G.ok = false;
+  G.phase ^= 1;
   tc::fence_after_sync();
 }
 
-// hidden epilogue: h = SiLU(acc + bias) into the hidden tile (this thread's row)
-__device__ __forceinline__ void hidden_epilogue(SampleShared& sh, const float* bias) {
-  const int warp = threadIdx.x >> 5, row = threadIdx.x;
-  uint8_t* H = sh.base + kOffH;
+// h = SiLU(acc + bias) into the warpgroup's hidden tile (this thread's row)
+__device__ __forceinline__ void hidden_epilogue(Group& G, const float* bias) {
+  const int w = G.lt >> 5;
+  uint8_t* H = G.base + G.H;
 #pragma unroll 1
   for (int c = 0; c < kMlpWidth / 32; c++) {
     float v[32];
-    tc::tmem_ld32(sh.tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
+    tc::tmem_ld32(G.tmem + (static_cast<uint32_t>(w * 32) << 16) + c * 32, v);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      __align__(16) bf16 h[8];
+      __align__(16) __nv_bfloat162 h[4];
 #pragma unroll
-      for (int j = 0; j < 8; j++) h[j] = __float2bfloat16_rn(silu(v[q * 8 + j] + bias[c * 32 + q * 8 + j]));
-      *reinterpret_cast<uint4*>(H + tc::tile_offset(row, c * 32 + q * 8, kMlpWidth)) = *reinterpret_cast<uint4*>(h);
+      for (int j = 0; j < 4; j++) {
+        const int k = q * 8 + 2 * j;
+        h[j] = __floats2bfloat162_rn(silu_fast(v[k] + bias[c * 32 + k]), silu_fast(v[k + 1] + bias[c * 32 + k + 1]));
+      }
+      *reinterpret_cast<uint4*>(H + tc::tile_offset(G.lt, c * 32 + q * 8, kMlpWidth)) = *reinterpret_cast<uint4*>(h);
     }
   }
 }
 
-// output epilogue: b4 + w4 . SiLU(acc + b3)
-__device__ __forceinline__ float output_epilogue(SampleShared& sh, const float* f) {
-  const int warp = threadIdx.x >> 5;
+// b4 + w4 . SiLU(acc + b3)
+__device__ __forceinline__ float output_epilogue(Group& G, const float* f) {
+  const int w = G.lt >> 5;
   const float* b3 = f + 2 * kMlpWidth;
   const float* w4 = f + 3 * kMlpWidth;
   float out = f[4 * kMlpWidth];
 #pragma unroll 1
   for (int c = 0; c < kMlpWidth / 32; c++) {
     float v[32];
-    tc::tmem_ld32(sh.tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
+    tc::tmem_ld32(G.tmem + (static_cast<uint32_t>(w * 32) << 16) + c * 32, v);
 #pragma unroll
-    for (int j = 0; j < 32; j++) out += silu(v[j] + b3[c * 32 + j]) * w4[c * 32 + j];
+    for (int j = 0; j < 32; j++) out = fmaf(silu_fast(v[j] + b3[c * 32 + j]), w4[c * 32 + j], out);
   }
   return out;
 }
 
-__device__ __forceinline__ float run_net(SampleShared& sh, uint32_t w1, uint32_t w2, uint32_t w3, const float* f) {
-  layer_mma(sh, kOffX, w1, kMlpIn);
-  hidden_epilogue(sh, f);
-  layer_mma(sh, kOffH, w2, kMlpWidth);
-  hidden_epilogue(sh, f + kMlpWidth);
-  layer_mma(sh, kOffH, w3, kMlpWidth);
-  return output_epilogue(sh, f);
+__device__ __forceinline__ float run_net(Group& G, uint32_t w1, uint32_t w2, uint32_t w3, const float* f) {
+  layer_mma(G, G.X, w1, kMlpIn);
+  hidden_epilogue(G, f);
+  layer_mma(G, G.H, w2, kMlpWidth);
+  hidden_epilogue(G, f + kMlpWidth);
+  layer_mma(G, G.H, w3, kMlpWidth);
+  return output_epilogue(G, f);
 }
 
-__device__ __forceinline__ void write_x(SampleShared& sh, const float (&x)[kMlpIn]) {
-  __align__(16) bf16 h[kMlpIn];
+__device__ __forceinline__ void write_x(Group& G, const float (&x)[kMlpIn]) {
+  __align__(16) __nv_bfloat162 h[kMlpIn / 2];
 #pragma unroll
-  for (int i = 0; i < kMlpIn; i++) h[i] = __float2bfloat16_rn(x[i]);
-  uint8_t* X = sh.base + kOffX;
-  *reinterpret_cast<uint4*>(X + tc::tile_offset(threadIdx.x, 0, kMlpIn)) = *reinterpret_cast<uint4*>(h);
-  *reinterpret_cast<uint4*>(X + tc::tile_offset(threadIdx.x, 8, kMlpIn)) = *reinterpret_cast<uint4*>(h + 8);
+  for (int i = 0; i < kMlpIn / 2; i++) h[i] = __floats2bfloat162_rn(x[2 * i], x[2 * i + 1]);
+  uint8_t* X = G.base + G.X;
+  *reinterpret_cast<uint4*>(X + tc::tile_offset(G.lt, 0, kMlpIn)) = *reinterpret_cast<uint4*>(h);
+  *reinterpret_cast<uint4*>(X + tc::tile_offset(G.lt, 8, kMlpIn)) = *reinterpret_cast<uint4*>(h + 4);
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_sample(const DevTSL* tsl, NetView nb, NetView na, MlpBox box,
-                                                        const double* E, const double* T, unsigned long long n,
-                                                        unsigned long long key, double* beta_out, double* alpha_out,
-                                                        unsigned long long* failures, int* err) {
+__global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* tsl, NetView nb, NetView na,
+                                                                  MlpBox box, const double* E, const double* T,
+                                                                  unsigned long long n, unsigned long long key,
+                                                                  double* beta_out, double* alpha_out,
+                                                                  unsigned long long* failures, int* err) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  SampleShared sh;
-  sh.base = smem;
   float* fb = reinterpret_cast<float*>(smem + kOffF);
   float* fa = fb + 4 * kMlpWidth + 4;
-  uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kOffMisc);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kOffMisc);  // [0..3] two mbarriers, [4] tensor memory
   const int tid = threadIdx.x, warp = tid >> 5;
   // weights into shared memory
   load_tile(smem + kOffB1, nb.W1, kMlpIn);
@@ -695,23 +733,31 @@ __global__ void __launch_bounds__(128, 1) k_mlp_sample(const DevTSL* tsl, NetVie
   if (tid == 0) {
     fb[4 * kMlpWidth] = nb.p[kMlpB4];
     fa[4 * kMlpWidth] = na.p[kMlpB4];
-    tc::mbar_init(tc::smem_addr(misc), 1);
+    for (int g = 0; g < kGroups; g++) tc::mbar_init(tc::smem_addr(misc + 2 * g), 1);
   }
-  if (warp == 0) tc::tmem_alloc(tc::smem_addr(misc + 2), kMlpWidth);
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(misc + 4), 128 * kGroups);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  sh.tmem = misc[2];
-  sh.mbar = tc::smem_addr(misc);
-  sh.phase = 0;
-  sh.ok = true;
+  Group G;
+  G.base = smem;
+  G.g = tid >> 7;
+  G.lt = tid & 127;
+  G.X = kOffG + G.g * kGroupBytes;
+  G.H = G.X + kTileW1;
+  G.tmem = misc[4] + 128 * G.g;
+  G.mbar = tc::smem_addr(misc + 2 * G.g);
+  G.phase = 0;
+  G.ok = true;
   const double Emin = exp(box.logE0), Emax = exp(box.logE1);
   unsigned long long my_fail = 0;
   const unsigned long long tiles = (n + 127) / 128;
-  for (unsigned long long tile = blockIdx.x; tile < tiles && sh.ok; tile += gridDim.x) {
-    const unsigned long long i = tile * 128 + tid;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * kGroups;
+  for (unsigned long long tile = static_cast<unsigned long long>(blockIdx.x) * kGroups + G.g; tile < tiles && G.ok;
+       tile += stride) {
+    const unsigned long long i = tile * 128 + G.lt;
     const bool valid = i < n;
-    double e = valid ? E[i] : 0.5 * (Emin + Emax);
+    double e = valid ? E[i] : Emin;
     double t = valid ? T[i] : box.T0;
     const bool in_box = e >= Emin && e <= Emax && t >= box.T0 && t <= box.T1;
     if (!in_box) {  // keep the tile's arithmetic finite; the row is resampled below
@@ -723,14 +769,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_sample(const DevTSL* tsl, NetVie
     const double u1 = rng.u01();
     float x[kMlpIn];
     beta_features(box, e, t, fmin(fmax(u1, 1e-12), 1.0 - 1e-12), x);
-    write_x(sh, x);
-    const float qb = run_net(sh, kOffB1, kOffB2, kOffB3, fb);
+    write_x(G, x);
+    const float qb = run_net(G, kOffB1, kOffB2, kOffB3, fb);
     const double bmin = beta_min_of(e, t);
     const double b = bmin + fmin(1.0, fmax(0.0, static_cast<double>(qb))) * (box.beta_cutoff - bmin);
     const double u2 = rng.u01();
     alpha_features(box, e, t, b, fmin(fmax(u2, 1e-12), 1.0 - 1e-12), x);
-    write_x(sh, x);
-    const float qa = run_net(sh, kOffA1, kOffA2, kOffA3, fa);
+    write_x(G, x);
+    const float qa = run_net(G, kOffA1, kOffA2, kOffA3, fa);
     double lo, hi;
     alpha_range(box, e, t, b, lo, hi);
     double bo = b, ao = lo + fmin(1.0, fmax(0.0, static_cast<double>(qa))) * (hi - lo);
@@ -750,13 +796,13 @@ __global__ void __launch_bounds__(128, 1) k_mlp_sample(const DevTSL* tsl, NetVie
       alpha_out[i] = ao;
     }
   }
-  if (!sh.ok && tid == 0) atomicExch(err, 1);
+  if (!G.ok && G.lt == 0) atomicExch(err, 1);
   if (my_fail) atomicAdd(failures, my_fail);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(sh.tmem, kMlpWidth);
+    tc::tmem_dealloc(misc[4], 128 * kGroups);
   }
 }
 
@@ -774,10 +820,12 @@ cudaError_t launch_sample_tsl_mlp(const DevTSL* tsl, const MlpNet& beta_net, con
     attr = true;
   }
   const unsigned long long tiles = (n + 127) / 128;
-  const unsigned grid = static_cast<unsigned>(tiles < static_cast<unsigned long long>(num_sms) ? tiles : num_sms);
+  const unsigned long long want = (tiles + kGroups - 1) / kGroups;
+  const unsigned grid = static_cast<unsigned>(want < static_cast<unsigned long long>(num_sms) ? want : num_sms);
   NetView nb{beta_net.p, beta_net.W1, beta_net.W2, beta_net.W3};
   NetView na{alpha_net.p, alpha_net.W1, alpha_net.W2, alpha_net.W3};
-  k_mlp_sample<<<grid, 128, kSampleSmem, s>>>(tsl, nb, na, box, E, T, n, key, beta, alpha, failures, mlp_err_ptr());
+  k_mlp_sample<<<grid, 128 * kGroups, kSampleSmem, s>>>(tsl, nb, na, box, E, T, n, key, beta, alpha, failures,
+                                                         mlp_err_ptr());
   return cudaGetLastError();
 }
 
