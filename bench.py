@@ -374,6 +374,23 @@ def run_gpu_tsl(args) -> None:
     ctx.set_stream(stream.cuda_stream)
     ctx.load_xml(wl["xml"], wl["base"])
     opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), histories=hist)
+    if args.mode == "kernel":
+        # profiling mode: train the surrogate, then each sampler form on 4e6
+        # samples, `steps` times; no transport
+        n = 4_000_000
+        E = torch.full((n,), 1e-7, dtype=torch.float64, device="cuda")
+        T = torch.full((n,), 450.0, dtype=torch.float64, device="cuda")
+        b = torch.empty_like(E)
+        a = torch.empty_like(E)
+        ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
+                            samples_per_condition=512, batch=8192, steps=3000, seed=3)
+        for method in (TSL_POD | TSL_PHILOX | TSL_FAST, TSL_MLP):
+            for i in range(args.steps):
+                ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=1 + i,
+                                      method=method)
+        torch.cuda.synchronize()
+        print(json.dumps({"mode": "kernel", "beta_mean": float(b.mean())}), flush=True)
+        return
     for _ in range(args.warmup):
         ctx.run_fixed_source(**opts)
     clocks = ClockSampler(local)
@@ -468,13 +485,70 @@ def run_gpu_tsl(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+BATCH_WORKLOAD = ("64 independent 8-group two-zone k-eigenvalue problems (seeds 0..63, cube sides log-uniform "
+                  "10-80 cm, 1e4-1e6 histories/cycle log-uniform) in one batch: one transport launch per cycle, "
+                  "per-cycle CUDA graph")
+
+
+def run_gpu_batch(args) -> None:
+    """C5: the batch against the same problems run one after another
+    (single-problem k-eigenvalue path, same seeds: identical k per cycle)."""
+    import torch
+
+    from minimc_gb300 import RNG_PHILOX, Batch, Context, synth
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    probs = synth.batch_problems(count=64, seed=7 + rank)
+    b = Batch(local)
+    for p, h in probs:
+        b.add(p.xml(), histories=h, seed=p.seed)
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = b.run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
+    clk = clocks.stop()
+    cycles = args.warmup + args.steps
+    value = r["histories"] * ws / (r["transport_ms"] / 1e3)
+    # the plain form: each problem alone, the same cycles
+    seq_ms = 0.0
+    agree = True
+    for i, (p, h) in enumerate(probs):
+        ctx = Context(local)
+        ctx.load_xml(p.xml())
+        s = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=int(args.fast), histories=h, seed=p.seed,
+                                inactive=args.warmup, active=args.steps, variant=r["variant"] + 1)
+        seq_ms += s.raw.transport_ms
+        agree &= bool(np.array_equal(s.k_cycle, r["k_cycle"][i]))
+    seq_value = r["histories"] / (seq_ms / 1e3)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["transport_ms"] / cycles, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD, "problems": len(probs),
+                       "histories_per_cycle": int(sum(h for _, h in probs)), "rng": "philox",
+                       "fast_math": bool(args.fast), "timed": "all cycles of the batch run (warm-up included)"},
+            "batch": {"variant": r["variant"], "graph": bool(r["graph"]), "launches": r["launches"],
+                      "tune_ms": [round(x, 3) for x in r["tune_ms"] if x > 0],
+                      "sequential_histories_per_s": seq_value, "speedup_vs_sequential": value / seq_value,
+                      "k_identical_to_single_runs": agree,
+                      "k_mean_range": [float(r["k_mean"].min()), float(r["k_mean"].max())]},
+            "cpu_baseline": None,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "call": "mc_batch_run (results copied back once)"},
+            "gpu_launches": int(r["launches"]), "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="two_zone", choices=sorted(WORKLOADS) + ["tsl"])
+    ap.add_argument("--workload", default="two_zone", choices=sorted(WORKLOADS) + ["tsl", "batch"])
     ap.add_argument("--histories", type=int, default=1_000_000)
     ap.add_argument("--block", type=int, default=0, help="0: autotuned")
     ap.add_argument("--fast", type=int, default=1,
@@ -493,6 +567,8 @@ def main():
         run_reference(args)
     elif args.workload == "tsl":
         run_gpu_tsl(args)
+    elif args.workload == "batch":
+        run_gpu_batch(args)
     else:
         run_gpu(args)
 

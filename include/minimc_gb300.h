@@ -328,6 +328,45 @@ int mc_surrogate_set(mc_ctx* ctx, int32_t tsl, const mc_train_desc* box, const f
 int mc_surrogate_grad(mc_ctx* ctx, const float* params, const float* x, const float* y, uint64_t n,
                       float* grad, float* loss, float* out);
 
+/* ---- batched problems -------------------------------------------------------
+ * No reference counterpart: the reference runs one problem per process.
+ * Many independent multigroup k-eigenvalue problems of uneven sizes run
+ * together: one transport launch per cycle serves all of them (each CTA
+ * one problem), one prefix sum, compaction and resampling over their
+ * concatenated fission banks, and one cycle's launches are captured once
+ * as a CUDA graph and replayed every cycle.  Per problem the k per cycle
+ * equals mc_run_keigenvalue's with Philox streams and the same seed. */
+typedef struct mc_batch mc_batch;
+typedef struct mc_batch_opts {
+  uint32_t inactive, active;  /* cycles                                      */
+  int32_t fast_math;          /* FP32 sampling arithmetic                    */
+  int32_t no_graph;           /* 1: launch the cycle's kernels one by one    */
+  int32_t variant;            /* history-kernel variant + 1; 0: autotune     */
+  uint32_t max_events;        /* per-particle event cap; 0 -> 1000000        */
+  uint64_t reserved[4];
+} mc_batch_opts;
+typedef struct mc_batch_out {
+  double* k_cycle;            /* [problems][inactive + active] or NULL       */
+  double* k_mean;             /* [problems] over active cycles, or NULL      */
+  double* k_std;              /* [problems] standard error, or NULL          */
+  double transport_ms;        /* device time of all cycles                   */
+  double tune_ms[8];          /* autotuner: transport time per variant       */
+  uint64_t histories;         /* all problems, all cycles                    */
+  uint64_t events, lost, capped, overflow;
+  uint64_t launches;          /* kernel launches (graph: one per cycle)      */
+  int32_t variant;            /* chosen variant                              */
+  int32_t graph;              /* 1 if the cycles ran as a CUDA graph         */
+  uint64_t reserved[4];
+} mc_batch_out;
+int mc_batch_create(mc_batch** out, int device);
+void mc_batch_destroy(mc_batch* b);
+int mc_batch_set_stream(mc_batch* b, void* cuda_stream);
+/* adds a multigroup problem (its own XML); histories/seed 0 take the XML's.
+ * Returns the problem's index (>= 0) or an error code. */
+int mc_batch_add(mc_batch* b, const char* xml_text, const char* base_dir, uint64_t histories, uint64_t seed);
+int mc_batch_run(mc_batch* b, const mc_batch_opts* opts, mc_batch_out* out);
+int mc_batch_last_error(mc_batch* b, char* buf, size_t n);
+
 /* ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157). */
 int mc_tsl_total(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
                  uint64_t n, double* xs);

@@ -4,14 +4,14 @@ The CUDA library (``_lib/libminimc_gb300.so``) is built in-tree by
 ``minimc_gb300._build.build()``; ``minimc_gb300.engine`` binds its C ABI.
 """
 from .engine import (  # noqa: F401
-    Context, Driver, World, MCError, RunOpts, SITE_DTYPE, EVENTS,
+    Batch, Context, Driver, World, MCError, RunOpts, SITE_DTYPE, EVENTS,
     RNG_PHILOX, RNG_MINSTD, SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT, TSL_POD, TSL_MLP, TSL_PHILOX, TSL_FAST,
     GEOMETRY_ROBUST, GEOMETRY_REFERENCE, MLP_PARAMS, TrainDesc, TrainOut,
     load_library, library_path, exported_symbols,
 )
 
 __all__ = [
-    "Context", "Driver", "World", "MCError", "RunOpts", "SITE_DTYPE", "EVENTS",
+    "Batch", "Context", "Driver", "World", "MCError", "RunOpts", "SITE_DTYPE", "EVENTS",
     "RNG_PHILOX", "RNG_MINSTD", "SCHEDULE_AUTO", "SCHEDULE_HISTORY", "SCHEDULE_EVENT",
     "TSL_POD", "TSL_MLP", "TSL_PHILOX", "TSL_FAST", "GEOMETRY_ROBUST", "GEOMETRY_REFERENCE", "MLP_PARAMS", "TrainDesc", "TrainOut", "load_library", "library_path", "exported_symbols",
 ]

@@ -1903,3 +1903,346 @@ extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint
   if (m > cap) return fail(c, MC_ERR_OVERFLOW, "fission bank larger than the output capacity");
   return counters_status(c, h);
 }
+
+// ---------------------------------------------------------------------------
+// Batched problems (layout and device bookkeeping in mc_batch.cu).  Each
+// problem is loaded into its own context (world tables on the device); the
+// batch uploads their DevWorld descriptors and run parameters as arrays.
+
+struct mc_batch {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::vector<mc_ctx*> probs;
+  std::vector<uint64_t> hist, seeds;
+};
+
+namespace {
+
+int bfail(mc_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define BATCH_TRY(b, expr)                                                                            \
+  do {                                                                                                \
+    const cudaError_t e_ = (expr);                                                                    \
+    if (e_ != cudaSuccess) return bfail((b), MC_ERR_DEVICE, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// device allocations of one mc_batch_run, freed on every exit path
+struct BatchMem {
+  std::vector<void*> ptrs;
+  ~BatchMem() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  T* get(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+};
+
+// CTAs of the transport grid, proportional to each problem's histories
+// (at least one each); block_problem[b] and block_first[p]
+void batch_blocks(const std::vector<uint64_t>& hist, int grid_target, std::vector<uint32_t>& block_problem,
+                  std::vector<uint32_t>& block_first) {
+  uint64_t N = 0;
+  for (uint64_t h : hist) N += h;
+  block_problem.clear();
+  block_first.assign(1, 0);
+  for (size_t p = 0; p < hist.size(); p++) {
+    const double share = static_cast<double>(grid_target) * static_cast<double>(hist[p]) / static_cast<double>(N);
+    const uint64_t need = (hist[p] + 255) / 256;  // no more CTAs than 256-history chunks
+    const uint32_t nb = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(need, static_cast<uint64_t>(share + 0.5))));
+    for (uint32_t i = 0; i < nb; i++) block_problem.push_back(static_cast<uint32_t>(p));
+    block_first.push_back(static_cast<uint32_t>(block_problem.size()));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mc_batch_create(mc_batch** out, int device) {
+  if (!out) return MC_ERR_INPUT;
+  *out = nullptr;
+  auto* b = new (std::nothrow) mc_batch();
+  if (!b) return MC_ERR_OOM;
+  b->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return MC_ERR_DEVICE;
+  }
+  b->own_stream = true;
+  cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+  *out = b;
+  return MC_OK;
+}
+
+void mc_batch_destroy(mc_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (mc_ctx* c : b->probs) mc_destroy(c);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int mc_batch_set_stream(mc_batch* b, void* s) {
+  if (!b) return MC_ERR_INPUT;
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  b->own_stream = false;
+  b->stream = static_cast<cudaStream_t>(s);
+  return MC_OK;
+}
+
+int mc_batch_last_error(mc_batch* b, char* buf, size_t n) {
+  if (!b || !buf || n == 0) return MC_ERR_INPUT;
+  std::strncpy(buf, b->err.c_str(), n - 1);
+  buf[n - 1] = 0;
+  return MC_OK;
+}
+
+int mc_batch_add(mc_batch* b, const char* xml_text, const char* base_dir, uint64_t histories, uint64_t seed) {
+  if (!b || !xml_text) return MC_ERR_INPUT;
+  mc_ctx* c = nullptr;
+  int rc = mc_create(&c, b->device);
+  if (rc != MC_OK) return bfail(b, rc, "context creation failed");
+  rc = mc_load_xml(c, xml_text, base_dir);
+  if (rc != MC_OK) {
+    b->err = c->err;
+    mc_destroy(c);
+    return rc;
+  }
+  if (c->model.energy_mode != mc::kMultigroup) {
+    mc_destroy(c);
+    return bfail(b, MC_ERR_INPUT, "batched problems are multigroup");
+  }
+  const uint64_t h = histories ? histories : c->model.histories;
+  if (h == 0) {
+    mc_destroy(c);
+    return bfail(b, MC_ERR_INPUT, "no histories");
+  }
+  b->probs.push_back(c);
+  b->hist.push_back(h);
+  b->seeds.push_back(seed ? seed : c->model.seed);
+  return static_cast<int>(b->probs.size() - 1);
+}
+
+int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
+  if (!b || !o) return MC_ERR_INPUT;
+  if (b->probs.empty()) return bfail(b, MC_ERR_STATE, "no problems added");
+  const uint32_t cycles = o->inactive + o->active;
+  if (cycles == 0) return bfail(b, MC_ERR_INPUT, "no cycles");
+  BATCH_TRY(b, cudaSetDevice(b->device));
+  const int P = static_cast<int>(b->probs.size());
+  std::vector<unsigned long long> off(P + 1, 0);
+  for (int p = 0; p < P; p++) off[p + 1] = off[p] + b->hist[p];
+  const unsigned long long N = off[P];
+  uint32_t max_yield = 1;
+  for (mc_ctx* c : b->probs) max_yield = std::max(max_yield, c->max_yield);
+  BatchMem mem;
+  auto* d_worlds = mem.get<DevWorld>(P);
+  auto* d_rps = mem.get<RunParams>(P);
+  auto* d_ctr = mem.get<DevCounters>(P);
+  auto* d_off = mem.get<unsigned long long>(P + 1);
+  auto* d_seeds = mem.get<unsigned long long>(P);
+  auto* d_start = mem.get<unsigned long long>(P);
+  auto* d_M = mem.get<unsigned long long>(P);
+  auto* d_k = mem.get<double>(static_cast<size_t>(P) * cycles);
+  auto* d_stats = mem.get<unsigned long long>(4 * static_cast<size_t>(P));
+  auto* d_cycle = mem.get<uint32_t>(1);
+  auto* d_died = mem.get<int>(1);
+  auto* src0 = mem.get<Site>(N);
+  auto* src1 = mem.get<Site>(N);
+  auto* fis = mem.get<mcd::FissionRec>(N);
+  auto* slots = mem.get<Site>(N * max_yield);
+  auto* count = mem.get<uint32_t>(N);
+  auto* offsets = mem.get<unsigned long long>(N);
+  auto* sums = mem.get<unsigned long long>((N + 1023) / 1024 + 1);
+  auto* total = mem.get<unsigned long long>(1);
+  auto* bank = mem.get<Site>(N * max_yield);
+  if (!(d_worlds && d_rps && d_ctr && d_off && d_seeds && d_start && d_M && d_k && d_stats && d_cycle && d_died &&
+        src0 && src1 && fis && slots && count && offsets && sums && total && bank))
+    return bfail(b, MC_ERR_OOM, "batch buffers");
+  std::vector<DevWorld> worlds(P);
+  std::vector<RunParams> rps(P);
+  for (int p = 0; p < P; p++) {
+    mc_ctx* c = b->probs[p];
+    worlds[p] = c->dw;
+    RunParams& rp = rps[p];
+    rp = RunParams{};
+    rp.n = b->hist[p];
+    rp.seed = b->seeds[p];
+    rp.max_events = o->max_events ? o->max_events : 1000000u;
+    rp.keig = 1;
+    rp.score = 0;
+    rp.fast = o->fast_math ? 1 : 0;
+    rp.max_yield = max_yield;
+    rp.bank = slots + off[p] * max_yield;
+    rp.bank_count = count + off[p];
+    rp.total_bins = 0;
+    rp.ctr = d_ctr + p;
+    rp.fis = fis + off[p];
+  }
+  cudaStream_t s = b->stream;
+  BATCH_TRY(b, cudaMemcpyAsync(d_worlds, worlds.data(), P * sizeof(DevWorld), cudaMemcpyHostToDevice, s));
+  BATCH_TRY(b, cudaMemcpyAsync(d_rps, rps.data(), P * sizeof(RunParams), cudaMemcpyHostToDevice, s));
+  BATCH_TRY(b, cudaMemcpyAsync(d_off, off.data(), (P + 1) * 8, cudaMemcpyHostToDevice, s));
+  BATCH_TRY(b, cudaMemcpyAsync(d_seeds, b->seeds.data(), P * 8, cudaMemcpyHostToDevice, s));
+  BATCH_TRY(b, cudaMemsetAsync(d_stats, 0, 4 * P * 8, s));
+  BATCH_TRY(b, cudaMemsetAsync(d_cycle, 0, 4, s));
+  BATCH_TRY(b, cudaMemsetAsync(d_died, 0, 4, s));
+  mcd::BatchCycle bc{P, static_cast<int>(cycles), N, d_off, d_seeds, d_rps, d_ctr, d_start, d_M, d_k, d_stats,
+                     d_cycle, d_died};
+  mc_batch_out res{};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } evg{e0, e1};
+  // block tables per variant; autotune on cycle 0's transport
+  std::vector<uint32_t> bp, bf;
+  auto* d_bp = mem.get<uint32_t>(static_cast<size_t>(b->num_sms) * 8 + P);
+  auto* d_bf = mem.get<uint32_t>(P + 1);
+  if (!d_bp || !d_bf) return bfail(b, MC_ERR_OOM, "batch block tables");
+  auto set_blocks = [&](int v) -> int {
+    const int per_sm = std::max(1, std::min(8, mcd::history_batch_blocks_per_sm(v)));
+    batch_blocks(b->hist, per_sm * b->num_sms, bp, bf);
+    BATCH_TRY(b, cudaMemcpyAsync(d_bp, bp.data(), bp.size() * 4, cudaMemcpyHostToDevice, s));
+    BATCH_TRY(b, cudaMemcpyAsync(d_bf, bf.data(), bf.size() * 4, cudaMemcpyHostToDevice, s));
+    return MC_OK;
+  };
+  int variant = o->variant > 0 ? std::min(o->variant - 1, mcd::history_variants() - 1) : -1;
+  if (variant < 0) {
+    double best = 1e300;
+    for (int v = 0; v < mcd::history_variants() && v < 8; v++) {
+      int rc = set_blocks(v);
+      if (rc != MC_OK) return rc;
+      BATCH_TRY(b, mcd::launch_batch_begin(bc, src0, s));
+      BATCH_TRY(b, cudaEventRecord(e0, s));
+      BATCH_TRY(b, mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, static_cast<int>(bp.size()), s, v));
+      BATCH_TRY(b, cudaEventRecord(e1, s));
+      BATCH_TRY(b, cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      res.tune_ms[v] = ms;
+      res.launches += 2;
+      if (ms < best) {
+        best = ms;
+        variant = v;
+      }
+    }
+  }
+  {
+    const int rc = set_blocks(variant);
+    if (rc != MC_OK) return rc;
+  }
+  const int grid = static_cast<int>(bp.size());
+  // one cycle's launches; `from` holds this cycle's sources, `to` the next
+  auto cycle_launches = [&](const Site* from, Site* to) -> cudaError_t {
+    cudaError_t e;
+    if ((e = mcd::launch_batch_begin(bc, from, s)) != cudaSuccess) return e;
+    if ((e = mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, grid, s, variant)) != cudaSuccess) return e;
+    if ((e = mcd::launch_fission_sites_mg_batch(d_worlds, d_rps, d_bp, d_bf, grid, s)) != cudaSuccess) return e;
+    if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
+    if ((e = mcd::launch_bank_compact(slots, count, offsets, N, max_yield, bank, s)) != cudaSuccess) return e;
+    if ((e = mcd::launch_batch_tally(bc, offsets, total, s)) != cudaSuccess) return e;
+    return mcd::launch_batch_resample(bc, bank, to, s);
+  };
+  constexpr int kLaunchesPerCycle = 10;
+  BATCH_TRY(b, cudaMemsetAsync(d_cycle, 0, 4, s));
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  struct GraphGuard {
+    cudaGraphExec_t* e;
+    ~GraphGuard() {
+      for (int i = 0; i < 2; i++)
+        if (e[i]) cudaGraphExecDestroy(e[i]);
+    }
+  } gg{exec};
+  const bool graph = !o->no_graph;
+  if (graph) {
+    for (int parity = 0; parity < 2; parity++) {
+      cudaGraph_t g = nullptr;
+      BATCH_TRY(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t ce = parity == 0 ? cycle_launches(src0, src1) : cycle_launches(src1, src0);
+      const cudaError_t ee = cudaStreamEndCapture(s, &g);
+      if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bfail(b, MC_ERR_DEVICE, std::string("graph capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&exec[parity], g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return bfail(b, MC_ERR_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    }
+  }
+  BATCH_TRY(b, cudaEventRecord(e0, s));
+  for (uint32_t cyc = 0; cyc < cycles; cyc++) {
+    if (graph) {
+      BATCH_TRY(b, cudaGraphLaunch(exec[cyc & 1], s));
+      res.launches += 1;
+    }
+    else {
+      BATCH_TRY(b, (cyc & 1) ? cycle_launches(src1, src0) : cycle_launches(src0, src1));
+      res.launches += kLaunchesPerCycle;
+    }
+  }
+  BATCH_TRY(b, cudaEventRecord(e1, s));
+  BATCH_TRY(b, cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  std::vector<double> k(static_cast<size_t>(P) * cycles);
+  std::vector<unsigned long long> stats(4 * static_cast<size_t>(P));
+  int died = 0;
+  BATCH_TRY(b, cudaMemcpy(k.data(), d_k, k.size() * 8, cudaMemcpyDeviceToHost));
+  BATCH_TRY(b, cudaMemcpy(stats.data(), d_stats, stats.size() * 8, cudaMemcpyDeviceToHost));
+  BATCH_TRY(b, cudaMemcpy(&died, d_died, 4, cudaMemcpyDeviceToHost));
+  res.transport_ms = ms;
+  res.histories = N * cycles;
+  res.variant = variant;
+  res.graph = graph ? 1 : 0;
+  for (int p = 0; p < P; p++) {
+    res.events += stats[4 * p];
+    res.lost += stats[4 * p + 1];
+    res.capped += stats[4 * p + 2];
+    res.overflow += stats[4 * p + 3];
+  }
+  if (out) {
+    double* kc = out->k_cycle;
+    double* km = out->k_mean;
+    double* ks = out->k_std;
+    *out = res;
+    out->k_cycle = kc;
+    out->k_mean = km;
+    out->k_std = ks;
+    if (kc) std::copy(k.begin(), k.end(), kc);
+    for (int p = 0; p < P; p++) {
+      double sm = 0, s2 = 0;
+      for (uint32_t c = o->inactive; c < cycles; c++) {
+        const double v = k[static_cast<size_t>(p) * cycles + c];
+        sm += v;
+        s2 += v * v;
+      }
+      const double na = o->active;
+      if (km) km[p] = na ? sm / na : 0;
+      if (ks) ks[p] = na > 1 ? std::sqrt(std::max(0.0, (s2 - sm * sm / na) / (na - 1)) / na) : 0;
+    }
+  }
+  if (died) return bfail(b, MC_ERR_INPUT, "a problem's fission bank is empty: its source died out");
+  if (res.lost) return bfail(b, MC_ERR_LOST, std::to_string(res.lost) + " particles lost");
+  if (res.overflow) return bfail(b, MC_ERR_OVERFLOW, std::to_string(res.overflow) + " bank overflows");
+  if (res.capped) return bfail(b, MC_ERR_EVENT_CAP, std::to_string(res.capped) + " particles reached the event cap");
+  return MC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// Batched multigroup k-eigenvalue problems: per-cycle bookkeeping kernels.
+//
+// All problems' histories are concatenated (problem p owns histories
+// off[p] .. off[p+1]), so the fission-bank prefix sum and compaction run
+// once over all of them and problem p's bank is the contiguous range its
+// histories produced, in history order.  Keys, bank sizes, k and the
+// resampling index are computed on the device from a device-resident cycle
+// counter, so one cycle's launches form a static CUDA graph.  Per problem
+// the keys and draws are those of a single-problem run
+// (mc_keig_cycle): a problem gives the same k per cycle batched or alone.
+#include "mc_kernels.cuh"
+
+namespace mcd {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long dev_run_key(unsigned long long seed, unsigned long long cycle,
+                                                          unsigned long long salt) {
+  return splitmix64(seed * 0x9E3779B97F4A7C15ull + cycle * 0xD1B54A32D192ED03ull + salt);
+}
+
+__global__ void k_batch_begin(const BatchCycle b, const Site* src) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= b.P) return;
+  const unsigned long long c = *b.cycle;
+  RunParams& rp = b.rps[p];
+  rp.cycle = static_cast<uint32_t>(c);
+  rp.run_key = dev_run_key(b.seeds[p], c, 0x4b454947ull);
+  rp.minstd_base = b.seeds[p] + c * rp.n;
+  rp.from_bank = c > 0 ? 1 : 0;
+  rp.src = src + b.off[p];
+  b.ctr[p] = DevCounters{};
+}
+
+__global__ void k_batch_tally(const BatchCycle b, const unsigned long long* offsets, const unsigned long long* total) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= b.P) return;
+  const unsigned long long s = offsets[b.off[p]];
+  const unsigned long long e = p + 1 < b.P ? offsets[b.off[p + 1]] : *total;
+  const unsigned long long m = e - s;
+  const unsigned c = *b.cycle;
+  b.start[p] = s;
+  b.M[p] = m;
+  if (c < static_cast<unsigned>(b.max_cycles))
+    b.k[static_cast<size_t>(p) * b.max_cycles + c] = static_cast<double>(m) / static_cast<double>(b.off[p + 1] - b.off[p]);
+  if (m == 0) *b.died = 1;
+  unsigned long long* st = b.stats + 4 * p;
+  st[0] += b.ctr[p].events;
+  st[1] += b.ctr[p].lost;
+  st[2] += b.ctr[p].capped;
+  st[3] += b.ctr[p].overflow;
+}
+
+// next source j of problem p = bank[start_p + floor(U_j * M_p)], U_j from
+// Philox(run key of (seed_p, cycle), counter j) as the single-problem
+// resampler draws it
+__global__ void k_batch_resample(const BatchCycle b, const Site* bank, Site* next) {
+  const unsigned long long j = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= b.N) return;
+  int lo = 0, hi = b.P;  // last p with off[p] <= j
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b.off[mid] <= j) lo = mid;
+    else hi = mid;
+  }
+  const int p = lo;
+  const unsigned long long jj = j - b.off[p];
+  const unsigned long long m = b.M[p];
+  if (m == 0) return;
+  const unsigned long long key = dev_run_key(b.seeds[p], *b.cycle, 0x52455341ull);
+  uint32_t c[4] = {static_cast<uint32_t>(jj), static_cast<uint32_t>(jj >> 32), 0x72657361u, 0};
+  philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
+  const double u = ((c[0] >> 5) * 67108864.0 + (c[1] >> 6)) * (1.0 / 9007199254740992.0);
+  unsigned long long idx = static_cast<unsigned long long>(u * static_cast<double>(m));
+  if (idx >= m) idx = m - 1;
+  next[j] = bank[b.start[p] + idx];
+}
+
+__global__ void k_batch_next_cycle(const BatchCycle b) { *b.cycle += 1; }
+
+unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
+
+}  // namespace
+
+cudaError_t launch_batch_begin(const BatchCycle& b, const Site* src, cudaStream_t s) {
+  k_batch_begin<<<blocks_for(b.P), 256, 0, s>>>(b, src);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_tally(const BatchCycle& b, const unsigned long long* offsets,
+                               const unsigned long long* total, cudaStream_t s) {
+  k_batch_tally<<<blocks_for(b.P), 256, 0, s>>>(b, offsets, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_resample(const BatchCycle& b, const Site* bank, Site* next, cudaStream_t s) {
+  k_batch_resample<<<blocks_for(b.N), 256, 0, s>>>(b, bank, next);
+  k_batch_next_cycle<<<1, 1, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+}  // namespace mcd

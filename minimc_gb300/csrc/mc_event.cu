@@ -471,14 +471,15 @@ __global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const E
 // k-eigenvalue fission sites from the recorded stream positions
 // (Multigroup::Fission, src/Multigroup.cpp:267-286: per site a chi group,
 // an isotropic direction, then rng() seeds the secondary)
+// histories first, first + stride, ... of the problem
 template <class Rng>
-__global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, const RunParams rp) {
+__device__ __forceinline__ void fission_sites_mg(const DevWorld& w, const RunParams& rp, unsigned long long first,
+                                                 unsigned long long stride) {
   const unsigned long long n = rp.n;
   const bool fast = rp.fast != 0;
   const int G = w.G;
   unsigned long long my_overflow = 0;
-  for (unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; h < n;
-       h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+  for (unsigned long long h = first; h < n; h += stride) {
     const FissionRec f = rp.fis[h];
     uint32_t written = 0;
     if (f.n) {
@@ -505,6 +506,29 @@ __global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, cons
     rp.bank_count[h] = written;
   }
   if (my_overflow) atomicAdd(&rp.ctr->overflow, my_overflow);
+}
+
+template <class Rng>
+__global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, const RunParams rp) {
+  fission_sites_mg<Rng>(w, rp, static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x,
+                        static_cast<unsigned long long>(gridDim.x) * blockDim.x);
+}
+
+// batched problems: CTA b serves problem block_problem[b], as the rank-th of
+// its block_first[p + 1] - block_first[p] CTAs
+__global__ void __launch_bounds__(256) k_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps,
+                                                                const uint32_t* block_problem,
+                                                                const uint32_t* block_first) {
+  __shared__ DevWorld w;
+  __shared__ RunParams rp;
+  const uint32_t p = block_problem[blockIdx.x];
+  if (threadIdx.x == 0) {
+    w = worlds[p];
+    rp = rps[p];
+  }
+  __syncthreads();
+  const unsigned long long rank = blockIdx.x - block_first[p], nb = block_first[p + 1] - block_first[p];
+  fission_sites_mg<PhiloxRng>(w, rp, rank * blockDim.x + threadIdx.x, nb * blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -554,6 +578,12 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
                                     cudaStream_t stream) {
   if (rng_mode == 1) k_fission_sites_mg<MinstdRng><<<grid, 256, 0, stream>>>(w, rp);
   else k_fission_sites_mg<PhiloxRng><<<grid, 256, 0, stream>>>(w, rp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
+                                          const uint32_t* block_first, int grid, cudaStream_t stream) {
+  k_fission_sites_mg_batch<<<grid, 256, 0, stream>>>(worlds, rps, block_problem, block_first);
   return cudaGetLastError();
 }
 

@@ -69,6 +69,38 @@ cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mo
                               cudaStream_t stream, int variant);
 int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant);
 
+// batched multigroup k-eigenvalue transport (mc_transport.cu): CTA b serves
+// problem block_problem[b]
+cudaError_t launch_history_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
+                                    int grid, cudaStream_t stream, int variant);
+int history_batch_blocks_per_sm(int variant);
+cudaError_t launch_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
+                                          const uint32_t* block_first, int grid, cudaStream_t stream);
+
+// batched k-eigenvalue cycle bookkeeping (mc_batch.cu)
+struct BatchCycle {
+  int P;
+  int max_cycles;
+  unsigned long long N;                 // histories of all problems
+  const unsigned long long* off;        // [P + 1] first history of each problem
+  const unsigned long long* seeds;      // [P]
+  RunParams* rps;                       // [P]
+  DevCounters* ctr;                     // [P]
+  unsigned long long* start;            // [P] first banked site of each problem
+  unsigned long long* M;                // [P] banked sites
+  double* k;                            // [P][max_cycles]
+  unsigned long long* stats;            // [P][4] events, lost, capped, overflow (all cycles)
+  uint32_t* cycle;                      // current cycle
+  int* died;                            // a problem's bank was empty
+};
+// sets every problem's cycle fields (keys, source) for the current cycle
+cudaError_t launch_batch_begin(const BatchCycle& b, const Site* src, cudaStream_t s);
+// per-problem bank sizes and k from the global scan; counter totals
+cudaError_t launch_batch_tally(const BatchCycle& b, const unsigned long long* offsets,
+                               const unsigned long long* total, cudaStream_t s);
+// next sources of every problem from its part of the compacted bank; cycle++
+cudaError_t launch_batch_resample(const BatchCycle& b, const Site* bank, Site* next, cudaStream_t s);
+
 // continuous energy (mc_transport_ce.cu)
 bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast);
 cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,

@@ -50,12 +50,11 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// multigroup history kernel
-// MINB: minimum resident 256-thread blocks per SM the register allocation
-// must allow (1 = compiler's choice); the autotuner picks among variants
-template <class Rng, bool KEIG, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_history_mg(const DevWorld w, const RunParams rp) {
-  extern __shared__ double smem[];
+// multigroup history loop of one CTA: the body of the single-problem kernel
+// (world and run parameters in the kernel's parameter space) and of the
+// batched kernel (copied into shared memory per CTA)
+template <class Rng, bool KEIG>
+__device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& rp, double* smem) {
   const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
   if (use_smem) {
@@ -329,6 +328,33 @@ __global__ void __launch_bounds__(256, MINB) k_history_mg(const DevWorld w, cons
   }
 }
 
+// multigroup history kernel
+// MINB: minimum resident 256-thread blocks per SM the register allocation
+// must allow (1 = compiler's choice); the autotuner picks among variants
+template <class Rng, bool KEIG, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_history_mg(const DevWorld w, const RunParams rp) {
+  extern __shared__ double smem[];
+  history_mg<Rng, KEIG>(w, rp, smem);
+}
+
+// batched k-eigenvalue transport: every CTA serves one problem (its world
+// and run parameters copied to shared memory); the problems' histories
+// take their own global queues
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_history_mg_batch(const DevWorld* worlds, const RunParams* rps,
+                                                                const uint32_t* block_problem) {
+  extern __shared__ double smem[];
+  __shared__ DevWorld w;
+  __shared__ RunParams rp;
+  const uint32_t p = block_problem[blockIdx.x];
+  if (threadIdx.x == 0) {
+    w = worlds[p];
+    rp = rps[p];
+  }
+  __syncthreads();
+  history_mg<PhiloxRng, true>(w, rp, smem);
+}
+
 // ---------------------------------------------------------------------------
 // launches
 
@@ -364,6 +390,40 @@ void launch_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, i
   }
 }
 }  // namespace
+
+namespace {
+template <int MINB>
+void launch_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem, int grid,
+                     cudaStream_t stream) {
+  k_history_mg_batch<MINB><<<grid, 256, 2 * kSharedBins * sizeof(double), stream>>>(worlds, rps, block_problem);
+}
+template <int MINB>
+int occupancy_mg_batch() {
+  return occupancy(k_history_mg_batch<MINB>, 256, 2 * kSharedBins * sizeof(double));
+}
+}  // namespace
+
+cudaError_t launch_history_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
+                                    int grid, cudaStream_t stream, int variant) {
+  switch (variant) {
+  case 1: launch_mg_batch<3>(worlds, rps, block_problem, grid, stream); break;
+  case 2: launch_mg_batch<4>(worlds, rps, block_problem, grid, stream); break;
+  case 3: launch_mg_batch<5>(worlds, rps, block_problem, grid, stream); break;
+  case 4: launch_mg_batch<6>(worlds, rps, block_problem, grid, stream); break;
+  default: launch_mg_batch<1>(worlds, rps, block_problem, grid, stream); break;
+  }
+  return cudaGetLastError();
+}
+
+int history_batch_blocks_per_sm(int variant) {
+  switch (variant) {
+  case 1: return occupancy_mg_batch<3>();
+  case 2: return occupancy_mg_batch<4>();
+  case 3: return occupancy_mg_batch<5>();
+  case 4: return occupancy_mg_batch<6>();
+  default: return occupancy_mg_batch<1>();
+  }
+}
 
 // variants: minimum 256-thread blocks per SM of 1 (compiler's choice), 3, 4,
 // 5 and 6 -- register budgets of 255, 85, 64, 51 and 42 per thread

@@ -104,6 +104,19 @@ class TrainOut(C.Structure):
 MLP_PARAMS = 35329  # FP32 parameters per surrogate network
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("inactive", C.c_uint32), ("active", C.c_uint32), ("fast_math", C.c_int32), ("no_graph", C.c_int32),
+                ("variant", C.c_int32), ("max_events", C.c_uint32), ("reserved", C.c_uint64 * 4)]
+
+
+class BatchOut(C.Structure):
+    _fields_ = [("k_cycle", C.POINTER(C.c_double)), ("k_mean", C.POINTER(C.c_double)),
+                ("k_std", C.POINTER(C.c_double)), ("transport_ms", C.c_double), ("tune_ms", C.c_double * 8),
+                ("histories", C.c_uint64), ("events", C.c_uint64), ("lost", C.c_uint64), ("capped", C.c_uint64),
+                ("overflow", C.c_uint64), ("launches", C.c_uint64), ("variant", C.c_int32), ("graph", C.c_int32),
+                ("reserved", C.c_uint64 * 4)]
+
+
 class KeigOut(C.Structure):
     _fields_ = [("k_cycle", C.POINTER(C.c_double)), ("bank_size", C.POINTER(C.c_uint64)),
                 ("sum", C.POINTER(C.c_double)), ("sum_sq", C.POINTER(C.c_double)),
@@ -151,6 +164,12 @@ _SIGNATURES = {
     "mc_sample_tsl_device": (C.c_int, [_P, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32,
                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+    "mc_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "mc_batch_destroy": (None, [_P]),
+    "mc_batch_set_stream": (C.c_int, [_P, C.c_void_p]),
+    "mc_batch_add": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_uint64, C.c_uint64]),
+    "mc_batch_run": (C.c_int, [_P, C.POINTER(BatchOpts), C.POINTER(BatchOut)]),
+    "mc_batch_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
     "mc_train_surrogate": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), C.POINTER(TrainOut)]),
     "mc_surrogate_get": (C.c_int, [_P, _F, _F, C.POINTER(TrainDesc)]),
     "mc_surrogate_set": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), _F, _F]),
@@ -604,3 +623,58 @@ class Driver:
                 "energy_bins": int(e.energy_bins),
             }
         return out
+
+
+class Batch:
+    """Many independent multigroup k-eigenvalue problems run together
+    (mc_batch_*): one transport launch per cycle for all of them and one
+    CUDA graph per cycle."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.mc_batch_create(C.byref(h), device)
+        if rc != MC_OK:
+            raise MCError(rc, "mc_batch_create failed")
+        self.h = h
+        self.histories: list[int] = []
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.mc_batch_destroy(self.h)
+            self.h = None
+
+    def error(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self.lib.mc_batch_last_error(self.h, buf, 1024)
+        return buf.value.decode()
+
+    def set_stream(self, stream: int):
+        self.lib.mc_batch_set_stream(self.h, C.c_void_p(stream))
+
+    def add(self, xml_text: str, base_dir: str = "", histories: int = 0, seed: int = 0) -> int:
+        rc = self.lib.mc_batch_add(self.h, xml_text.encode(), str(base_dir).encode(), histories, seed)
+        if rc < 0:
+            raise MCError(rc, self.error())
+        self.histories.append(histories)
+        return rc
+
+    def run(self, inactive: int, active: int, fast_math: int = 1, graph: bool = True, variant: int = 0,
+            max_events: int = 0, allow=()):
+        P = len(self.histories)
+        ncyc = inactive + active
+        k = np.zeros((P, ncyc))
+        km = np.zeros(P)
+        ks = np.zeros(P)
+        o = BatchOpts(inactive=inactive, active=active, fast_math=fast_math, no_graph=0 if graph else 1,
+                      variant=variant, max_events=max_events)
+        out = BatchOut()
+        out.k_cycle = _dptr(k)
+        out.k_mean = _dptr(km)
+        out.k_std = _dptr(ks)
+        rc = self.lib.mc_batch_run(self.h, C.byref(o), C.byref(out))
+        if rc != MC_OK and rc not in allow:
+            raise MCError(rc, self.error())
+        return {"k_cycle": k, "k_mean": km, "k_std": ks, "transport_ms": out.transport_ms,
+                "histories": out.histories, "events": out.events, "launches": out.launches,
+                "variant": out.variant, "graph": out.graph, "tune_ms": list(out.tune_ms), "status": rc}

@@ -271,3 +271,21 @@ def infinite_medium(c: float = 0.25, capture: float = 0.75, fission: float = 0.0
         cells=['  <cell name="sphere" material="fissile">\n    <surface name="sphere" sense="-1"/>\n  </cell>',
                '  <void>\n    <surface name="sphere" sense="+1"/>\n  </void>'],
         histories=histories, problem=prob)
+
+
+def batch_problems(count: int = 64, seed: int = 7, h_min: int = 10_000, h_max: int = 1_000_000,
+                   side_min: float = 10.0, side_max: float = 80.0, inactive: int = 20, active: int = 50):
+    """Independent problems of the two-zone form with their own seeded cross
+    sections (seeds 0..count-1), outer cube sides log-uniform in
+    [side_min, side_max] cm (fuel cube half the side) and histories per cycle
+    log-uniform in [h_min, h_max]: a list of (Problem, histories)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        side = float(np.exp(rng.uniform(np.log(side_min), np.log(side_max))))
+        hist = int(np.exp(rng.uniform(np.log(h_min), np.log(h_max))))
+        p = two_zone_cubes(histories=hist, inactive=inactive, active=active, inner=side / 2, outer=side, seed=i)
+        p.estimators = []
+        p.seed = 1 + i
+        out.append((p, hist))
+    return out
