@@ -593,6 +593,7 @@ Model load_model(const std::string& xml_text, const std::string& base_dir) {
     for (auto& f : fr) {
       mat.nuclides.push_back(f.first);
       mat.afrac.push_back(f.second / sum);
+      mat.afrac_raw.push_back(f.second);
     }
     m.materials.push_back(std::move(mat));
     material_index[name] = static_cast<int32_t>(m.materials.size() - 1);

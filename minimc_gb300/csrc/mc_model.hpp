@@ -154,6 +154,7 @@ struct Material {
   double number_density = 0;
   std::vector<int32_t> nuclides;  // sorted by nuclide creation number
   std::vector<double> afrac;      // normalized to unit sum
+  std::vector<double> afrac_raw;  // as given in the input
 };
 
 // Bins (src/Bins.cpp): none, linspace, logspace or explicit boundaries.

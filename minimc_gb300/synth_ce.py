@@ -140,10 +140,13 @@ def ce_problem_xml(files: dict, histories: int = 1_000_000, inactive: int = 20, 
                    half: float = 20.0, afrac: tuple = (0.6, 0.3, 0.1), energy: float = 2.0,
                    temperature: float = 293.6, keig: bool = True, reflective: bool = True,
                    names: tuple = ("H1", "O16", "U235"), estimators: list[str] | None = None,
-                   tracking: str = "surface", temperature_xml: str | None = None) -> str:
+                   tracking: str = "surface", temperature_xml: str | None = None,
+                   sphere: float | None = None) -> str:
     """Homogeneous mixture of `names` in a box of side 2 * half cm; reflective
     faces make it an infinite medium.  Free-gas elastic scattering at
-    `temperature` (or the given <temperature> body)."""
+    `temperature` (or the given <temperature> body).  With `sphere` (a
+    radius) the mixture fills a vacuum-bounded sphere instead, a geometry
+    the reference's own surfaces describe (its surface is named "sphere")."""
     nucs = []
     for name in names:
         f = files[name]
@@ -156,6 +159,9 @@ def ce_problem_xml(files: dict, histories: int = 1_000_000, inactive: int = 20, 
                      f'          <nubar file="{f["nubar"]}" temperature="293.6"/>\n        </fission>')
         s += ["      </neutron>", "    </nuclide>"]
         nucs.append("\n".join(s))
+    if sphere is not None:
+        return _sphere_problem(nucs, names, afrac, sphere, histories, inactive, active, energy, temperature, keig,
+                               estimators, tracking, temperature_xml)
     r = ' reflective="true"' if reflective else ""
     planes = []
     for ax in "xyz":
@@ -186,5 +192,30 @@ def ce_problem_xml(files: dict, histories: int = 1_000_000, inactive: int = 20, 
             f'<materials>\n  <material name="mix" aden="0.1">\n{mats}\n  </material>\n</materials>\n'
             "<surfaces>\n" + "\n".join(planes) + "\n</surfaces>\n"
             "<cells>\n" + "\n".join(cell) + "\n" + "\n".join(voids) + "\n</cells>\n"
+            f"<temperature>\n{temp}\n</temperature>\n" + est +
+            f"<problemtype>\n{prob}\n</problemtype>\n</minimc>\n")
+
+
+def _sphere_problem(nucs, names, afrac, radius, histories, inactive, active, energy, temperature, keig, estimators,
+                    tracking, temperature_xml) -> str:
+    src = ('    <position>\n      <constant x="0" y="0" z="0"/>\n    </position>\n'
+           '    <direction>\n      <isotropic/>\n    </direction>\n'
+           f'    <energy>\n      <constant energy="{energy!r}"/>\n    </energy>\n'
+           '    <particletype>\n      <constant type="neutron"/>\n    </particletype>')
+    prob = (f'<keigenvalue inactive="{inactive}" active="{active}">\n  <initialsource>\n{src}\n  </initialsource>\n'
+            "</keigenvalue>") if keig else f"<fixedsource>\n{src}\n</fixedsource>"
+    mats = "\n".join(f'    <nuclide name="{n}" afrac="{float(a)!r}"/>' for n, a in zip(names, afrac))
+    est = ("<estimators>\n" + "\n".join(estimators) + "\n</estimators>\n") if estimators else ""
+    temp = temperature_xml if temperature_xml else f'  <constant c="{temperature!r}"/>'
+    trk = "" if tracking == "surface" else f"  <tracking>{tracking}</tracking>\n"
+    return ("<minimc>\n<general>\n  <particles>neutron</particles>\n"
+            f"  <histories>{histories}</histories>\n  <threads>1</threads>\n  <chunksize>1000</chunksize>\n"
+            f"  <seed>1</seed>\n{trk}</general>\n"
+            "<nuclides>\n  <continuous>\n" + "\n".join(nucs) + "\n  </continuous>\n</nuclides>\n"
+            f'<materials>\n  <material name="mix" aden="0.1">\n{mats}\n  </material>\n</materials>\n'
+            f'<surfaces>\n  <sphere name="sphere">\n    <center x="0" y="0" z="0"/>\n    <radius r="{radius!r}"/>\n'
+            "  </sphere>\n</surfaces>\n"
+            '<cells>\n  <cell name="ball" material="mix">\n    <surface name="sphere" sense="-1"/>\n  </cell>\n'
+            '  <void>\n    <surface name="sphere" sense="+1"/>\n  </void>\n</cells>\n'
             f"<temperature>\n{temp}\n</temperature>\n" + est +
             f"<problemtype>\n{prob}\n</problemtype>\n</minimc>\n")

@@ -74,6 +74,10 @@ def load() -> C.CDLL:
                                        C.POINTER(C.c_uint64)]
         lib.orc_tsl_total.restype = C.c_int
         lib.orc_tsl_total.argtypes = [C.c_void_p, C.c_int32, _D, _D, C.c_uint64, _D]
+        lib.orc_set_material_order.restype = C.c_int
+        lib.orc_set_material_order.argtypes = [C.c_void_p, C.c_int32, C.c_char_p]
+        lib.orc_cell_material.restype = C.c_int32
+        lib.orc_cell_material.argtypes = [C.c_void_p, C.c_int32]
         lib.orc_free_gas.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_uint64, _D, _D]
         lib.orc_run_fixed_source.restype = C.c_int
         lib.orc_run_fixed_source.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, _D, _D,
@@ -112,6 +116,16 @@ class Oracle:
 
     def material_total(self, cell: int, group: int) -> float:
         return float(self.lib.orc_material_total(self.h, cell, group))
+
+    def set_material_order(self, material: int, names):
+        """Iterate the material's nuclides in the given order (see
+        orc_set_material_order)."""
+        rc = self.lib.orc_set_material_order(self.h, material, " ".join(names).encode())
+        if rc != 0:
+            raise ValueError(f"set_material_order: {rc}")
+
+    def cell_material(self, cell: int) -> int:
+        return int(self.lib.orc_cell_material(self.h, cell))
 
     def material_xs_ce(self, cell, energy, xyz=None):
         """(total, majorant) microscopic cross sections of a continuous-energy

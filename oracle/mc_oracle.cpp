@@ -1094,6 +1094,53 @@ int orc_tsl_total(void* h, int32_t tsl, const double* E, const double* T, uint64
   return 0;
 }
 
+// Reorders the nuclides of material `mat` (names separated by spaces) and
+// renormalizes its atom fractions summed in that order.  The reference
+// iterates a material's nuclides in std::map order of their shared_ptr
+// addresses (src/Material.hpp:20), i.e. in the order its process happened to
+// allocate them; comparisons with the reference's own code set that order.
+int orc_set_material_order(void* h, int32_t mat, const char* names) {
+  auto* o = static_cast<Oracle*>(h);
+  if (mat < 0 || static_cast<size_t>(mat) >= o->m.materials.size()) return -1;
+  mc::Material& M = o->m.materials[static_cast<size_t>(mat)];
+  std::vector<int32_t> order;
+  std::string s(names), tok;
+  size_t pos = 0;
+  while (pos <= s.size()) {
+    const size_t e = s.find(' ', pos);
+    tok = s.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+    if (!tok.empty()) {
+      int32_t idx = -1;
+      for (size_t k = 0; k < M.nuclides.size(); k++)
+        if (o->m.nuclides[static_cast<size_t>(M.nuclides[k])].name == tok) idx = static_cast<int32_t>(k);
+      if (idx < 0) return -2;
+      order.push_back(idx);
+    }
+    if (e == std::string::npos) break;
+    pos = e + 1;
+  }
+  if (order.size() != M.nuclides.size()) return -3;
+  std::vector<int32_t> nuc;
+  std::vector<double> raw;
+  for (int32_t k : order) {
+    nuc.push_back(M.nuclides[static_cast<size_t>(k)]);
+    raw.push_back(M.afrac_raw[static_cast<size_t>(k)]);
+  }
+  double sum = 0;
+  for (double v : raw) sum += v;
+  M.nuclides = nuc;
+  M.afrac_raw = raw;
+  M.afrac.clear();
+  for (double v : raw) M.afrac.push_back(v / sum);
+  return 0;
+}
+
+int32_t orc_cell_material(void* h, int32_t cell) {
+  auto* o = static_cast<Oracle*>(h);
+  if (cell < 0 || static_cast<size_t>(cell) >= o->m.cells.size()) return -1;
+  return o->m.cells[static_cast<size_t>(cell)].material;
+}
+
 // minstd + generate_canonical values for a seed (RNG parity checks)
 void orc_minstd_canonical(uint64_t seed, uint64_t n, double* out) {
   RNG rng{static_cast<RNG::result_type>(seed)};
