@@ -328,6 +328,23 @@ int mc_surrogate_set(mc_ctx* ctx, int32_t tsl, const mc_train_desc* box, const f
 int mc_surrogate_grad(mc_ctx* ctx, const float* params, const float* x, const float* y, uint64_t n,
                       float* grad, float* loss, float* out);
 
+/* minimc's result file text (src/minimc.cpp:20-21): the batch size line, then
+ * EstimatorSet::to_string (src/Estimator.cpp:48-56, 207-213;
+ * src/Scorable.cpp:51-70; src/Bins.cpp:84-170) for the given per-bin sums
+ * and sums of squares (estimator order, as mc_tally_out / mc_keig_out
+ * return them) normalised by total_weight (the number of histories scored:
+ * the batch size for a fixed-source run, batch size x active cycles for a
+ * k-eigenvalue run).  Writes at most n bytes (NUL-terminated) into buf and
+ * the full length into *needed. */
+int mc_output_text(mc_ctx* ctx, const double* sum, const double* sum_sq, uint64_t batchsize, double total_weight,
+                   char* buf, size_t n, size_t* needed);
+
+/* The same text without a context or a device: parses the problem XML on
+ * the host (data files relative to base_dir) and formats the given sums.
+ * On an input error writes the message into buf and returns MC_ERR_INPUT. */
+int mc_output_format(const char* xml_text, const char* base_dir, const double* sum, const double* sum_sq,
+                     uint64_t batchsize, double total_weight, char* buf, size_t n, size_t* needed);
+
 /* ---- batched problems -------------------------------------------------------
  * No reference counterpart: the reference runs one problem per process.
  * Many independent multigroup k-eigenvalue problems of uneven sizes run

@@ -6,6 +6,7 @@
 #include "mc_mlp.cuh"
 #include "mc_tsl.cuh"
 #include "mc_model.hpp"
+#include "mc_output.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -1304,6 +1305,43 @@ int mc_material_xs(mc_ctx* c, int32_t cell, const double* xyz, const double* ene
   CUDA_TRY(c, cudaMemcpyAsync(total, outp, n * 8, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(majorant, outp + n, n * 8, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+namespace {
+void copy_text(const std::string& t, char* buf, size_t n, size_t* needed) {
+  if (needed) *needed = t.size();
+  if (buf && n) {
+    const size_t k = std::min(n - 1, t.size());
+    std::memcpy(buf, t.data(), k);
+    buf[k] = 0;
+  }
+}
+}  // namespace
+
+int mc_output_text(mc_ctx* c, const double* sum, const double* sum_sq, uint64_t batchsize, double total_weight,
+                   char* buf, size_t n, size_t* needed) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if ((!sum || !sum_sq) && c->total_bins) return fail(c, MC_ERR_INPUT, "null argument");
+  if (!(total_weight > 0)) return fail(c, MC_ERR_INPUT, "total weight must be positive");
+  copy_text(mc::format_output(c->model, sum, sum_sq, total_weight, batchsize), buf, n, needed);
+  return MC_OK;
+}
+
+int mc_output_format(const char* xml_text, const char* base_dir, const double* sum, const double* sum_sq,
+                     uint64_t batchsize, double total_weight, char* buf, size_t n, size_t* needed) {
+  if (!xml_text || !(total_weight > 0)) return MC_ERR_INPUT;
+  try {
+    const mc::Model m = mc::load_model(xml_text, base_dir ? base_dir : "");
+    size_t bins = 0;
+    for (const auto& e : m.estimators) bins += e.size();
+    if (bins && (!sum || !sum_sq)) return MC_ERR_INPUT;
+    copy_text(mc::format_output(m, sum, sum_sq, total_weight, batchsize), buf, n, needed);
+  }
+  catch (const std::exception& e) {
+    copy_text(e.what(), buf, n, needed);
+    return MC_ERR_INPUT;
+  }
   return MC_OK;
 }
 

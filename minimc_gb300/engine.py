@@ -164,6 +164,10 @@ _SIGNATURES = {
     "mc_sample_tsl_device": (C.c_int, [_P, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32,
                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+    "mc_output_text": (C.c_int, [_P, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
+                                 C.POINTER(C.c_size_t)]),
+    "mc_output_format": (C.c_int, [C.c_char_p, C.c_char_p, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
+                                   C.POINTER(C.c_size_t)]),
     "mc_batch_create": (C.c_int, [C.POINTER(_P), C.c_int]),
     "mc_batch_destroy": (None, [_P]),
     "mc_batch_set_stream": (C.c_int, [_P, C.c_void_p]),
@@ -201,6 +205,24 @@ def load_library() -> C.CDLL:
 
 def exported_symbols() -> list[str]:
     return list(_SIGNATURES)
+
+
+def format_output(xml_text: str, base_dir, sum, sum_sq, batchsize: int, total_weight: float | None = None) -> str:
+    """minimc's result-file text for tallies of the problem in xml_text,
+    formatted on the host (mc_output_format; no device needed)."""
+    lib = load_library()
+    s = _arr(sum, np.float64)
+    q = _arr(sum_sq, np.float64)
+    w = float(batchsize if total_weight is None else total_weight)
+    d = str(base_dir or "").encode()
+    need = C.c_size_t()
+    rc = lib.mc_output_format(xml_text.encode(), d, _dptr(s), _dptr(q), batchsize, w, None, 0, C.byref(need))
+    buf = C.create_string_buffer(need.value + 1)
+    rc = lib.mc_output_format(xml_text.encode(), d, _dptr(s), _dptr(q), batchsize, w, buf, need.value + 1,
+                              C.byref(need))
+    if rc != 0:
+        raise MCError(rc, buf.value.decode())
+    return buf.value.decode()
 
 
 def _dptr(a: np.ndarray):
@@ -435,6 +457,19 @@ class Context:
                                             out.ctypes.data_as(C.POINTER(C.c_int64))))
         return out
 
+    def output_text(self, sum, sum_sq, batchsize: int, total_weight: float | None = None) -> str:
+        """minimc's result-file text (the .out file) for these tallies,
+        normalised by total_weight (default: the batch size)."""
+        s = _arr(sum, np.float64)
+        q = _arr(sum_sq, np.float64)
+        w = float(batchsize if total_weight is None else total_weight)
+        need = C.c_size_t()
+        self.check(self.lib.mc_output_text(self.h, _dptr(s), _dptr(q), batchsize, w, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value + 1)
+        self.check(self.lib.mc_output_text(self.h, _dptr(s), _dptr(q), batchsize, w, buf, need.value + 1,
+                                           C.byref(need)))
+        return buf.value.decode()
+
     def sample_tsl(self, tsl: int, energy, temperature, seed: int = 1, method: int = TSL_POD):
         """ThermalScattering::SampleBeta then SampleAlpha for each (E, T)
         (host arrays): (beta, alpha, failures)."""
@@ -604,6 +639,24 @@ class Driver:
         if self.ctx.info.problem == 0:
             return self.ctx.run_fixed_source(**kw)
         return self.ctx.run_keigenvalue(**kw)
+
+    def output_text(self, result) -> str:
+        """The result file's text (src/minimc.cpp:20-21) for a solve's
+        result.  The reference's k-eigenvalue Solve returns its estimators
+        untouched (src/KEigenvalue.cpp:36-62); here the active cycles' tallies
+        are written, normalised by batch size x active cycles."""
+        if isinstance(result, KeigResult):
+            w = self.batchsize * result.active
+        else:
+            w = result.histories
+        return self.ctx.output_text(result.sum, result.sum_sq, self.batchsize, w)
+
+    def write_output(self, result, xml_path: str | os.PathLike) -> Path:
+        """Writes the result file beside the input, with the extension
+        replaced by .out (src/minimc.cpp:16-21); returns its path."""
+        out = Path(xml_path).with_suffix(".out")
+        out.write_text(self.output_text(result))
+        return out
 
     def estimator_results(self, result) -> dict[str, dict]:
         """Estimator means and std devs by name, normalized per history (fixed

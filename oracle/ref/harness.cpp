@@ -67,7 +67,7 @@ extern "C" {
 // batchsize), src/Scorable.cpp:32-35) in mean[nbins] and the World's
 // iteration orders of this run in orders
 int ref_solve(const char* xml_path, const char* estimator, uint64_t nbins, double* mean, char* orders,
-              size_t ordersn, char* err, size_t errn) {
+              size_t ordersn, char* text, size_t textn, char* err, size_t errn) {
   // the reference reports progress on stdout; keep the caller's output clean
   std::streambuf* saved = std::cout.rdbuf();
   std::ostringstream sink;
@@ -87,6 +87,15 @@ int ref_solve(const char* xml_path, const char* estimator, uint64_t nbins, doubl
       orders[ordersn - 1] = 0;
     }
     const EstimatorSet result = driver->Solve();
+    if (text && textn) {
+      // the result file as minimc's main writes it (src/minimc.cpp:20-21)
+      std::ostringstream os;
+      os << driver->batchsize << std::endl;
+      os << result.to_string();
+      const std::string t = os.str();
+      std::strncpy(text, t.c_str(), textn - 1);
+      text[textn - 1] = 0;
+    }
     if (estimator && estimator[0]) {
       const Estimator& e = result.FindEstimatorByName(estimator);
       for (uint64_t i = 0; i < nbins; i++) mean[i] = e.GetScore(i, static_cast<Real>(driver->batchsize));

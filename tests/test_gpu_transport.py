@@ -85,6 +85,26 @@ def test_point_source_leakage_reference_test(built_library):
             assert r.sum[0] == o["sum"][0]
 
 
+def test_result_file(built_library, tmp_path):
+    """Driver.write_output: the .out file beside the input holds the result
+    text for the GPU's tallies; with reference streams those tallies equal
+    the oracle's, so the file equals the text of the oracle's sums (which
+    the CPU suite pins on the reference's own output)."""
+    from minimc_gb300.engine import Driver, format_output
+
+    xml = (GOLDEN / "point_source_leakage.xml").read_text()
+    path = tmp_path / "leakage.xml"
+    path.write_text(xml)
+    n = KA["point_source_leakage"]["histories"]
+    drv = Driver.create(path)
+    r = drv.solve(rng=RNG_MINSTD)
+    out = drv.write_output(r, path)
+    assert out == tmp_path / "leakage.out"
+    o = Oracle(xml).run_fixed_source(n, 1)
+    assert out.read_text() == format_output(xml, GOLDEN, o["sum"], o["sum_sq"], n)
+    assert out.read_text().startswith(f"{n}\n\nleakage\n")
+
+
 def test_reference_geometry_mode_fixed_source(built_library):
     xml = (GOLDEN / "mg_spheres.xml").read_text()
     n = 50000

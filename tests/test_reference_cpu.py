@@ -33,7 +33,7 @@ def ref():
         pytest.skip("reference sources are not present")
     lib = C.CDLL(str(lib_path))
     lib.ref_solve.argtypes = [C.c_char_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_double), C.c_char_p, C.c_size_t,
-                              C.c_char_p, C.c_size_t]
+                              C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t]
     lib.ref_solve.restype = C.c_int
     return lib
 
@@ -65,12 +65,14 @@ def run_both(ref, xml: str, d: Path, tmp_path: Path, estimator: str, quirks=True
     path.write_text(absolute_paths(xml, d))
     mean = np.zeros(max(1, o.total_bins))
     orders = C.create_string_buffer(1 << 16)
+    text = C.create_string_buffer(1 << 22)
     err = C.create_string_buffer(2048)
-    rc = ref.ref_solve(str(path).encode(), estimator.encode(), len(mean), mean.ctypes.data_as(C.POINTER(C.c_double)),
-                       orders, 1 << 16, err, 2048)
+    rc = ref.ref_solve(str(path).encode(), (estimator or "").encode(), len(mean), mean.ctypes.data_as(C.POINTER(C.c_double)),
+                       orders, 1 << 16, text, 1 << 22, err, 2048)
     assert rc == 0, err.value.decode()
     align_orders(o, orders.value.decode())
     r = o.run_fixed_source(n, seed, threads=1)
+    r["ref_text"] = text.value.decode()
     return r["sum"] / n, mean[: o.total_bins], r
 
 
@@ -119,3 +121,34 @@ def test_thermal_scattering_broomstick(ref, tmp_path_factory, tmp_path):
                                    energy_bins=40)
     got, want, _ = run_both(ref, xml, d, tmp_path, "leakage")
     assert np.array_equal(got, want)
+
+
+def test_result_file_text(ref, ce_files, tmp_path, built_library):
+    """The engine's result-file text (mc_output_format, the formatter behind
+    Driver.write_output) for the oracle's tallies equals the reference's own
+    .out text character for character: batch size line, logspace and
+    linspace bin edges, 'none' bins, means and standard deviations."""
+    from minimc_gb300.engine import format_output
+
+    d, files = ce_files
+    est = [synth_ce.energy_current("leak", "sphere", bins=40),
+           '  <current name="plain" surface="sphere"/>',
+           '  <current name="angle" surface="sphere">\n    <bins>\n      <cosine u="0" v="0" w="1">'
+           '<linspace bins="7" min="-1" max="1"/></cosine>\n'
+           '      <energy><boundaries>1e-6 1e-3 0.1 1.0</boundaries></energy>\n    </bins>\n  </current>']
+    xml = synth_ce.ce_problem_xml(files, histories=3000, keig=False, sphere=6.0, afrac=(0.6, 0.3, 0.001),
+                                  estimators=est)
+    _, _, r = run_both(ref, xml, d, tmp_path, None)
+    got = format_output(xml, d, r["sum"], r["sum_sq"], 3000)
+    assert got == r["ref_text"]
+    assert got.count("mean\n----\n") == 3
+
+
+def test_result_file_text_multigroup(ref, tmp_path, built_library):
+    from minimc_gb300.engine import format_output
+
+    xml = (GOLDEN / "mg_spheres.xml").read_text()
+    est = re.search(r'<current name="([^"]+)"', xml).group(1)
+    n = int(re.search(r"<histories>(\d+)</histories>", xml).group(1))
+    _, _, r = run_both(ref, xml, GOLDEN, tmp_path, est)
+    assert format_output(xml, GOLDEN, r["sum"], r["sum_sq"], n) == r["ref_text"]
