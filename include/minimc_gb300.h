@@ -98,11 +98,16 @@ typedef struct {
   int32_t n_tsl;
   uint64_t histories, seed;
   uint32_t inactive, active;
-  uint64_t total_bins;  /* sum of estimator bin counts                  */
+  uint64_t total_bins;  /* estimator and sensitivity bins               */
   uint32_t max_yield;   /* upper bound on secondaries per fission       */
-  int32_t reserved[7];
+  int32_t n_perturbations;  /* total cross-section perturbations (<= 4) */
+  int32_t reserved[6];
 } mc_problem_info;
 
+/* An estimator's bins, then those of each of its sensitivity estimators
+ * (Estimator::sensitivities, src/Estimator.cpp:76-90; same bins,
+ * src/Scorable.cpp:22-29): sensitivity k scores into
+ * [offset + n_bins * (k + 1), offset + n_bins * (k + 2)). */
 typedef struct {
   char name[64];
   int32_t kind;         /* 0 current, 1 track length                    */
@@ -110,6 +115,9 @@ typedef struct {
   uint64_t offset;      /* first bin in the flattened tally arrays      */
   uint64_t n_bins;
   uint64_t cosine_bins, energy_bins;
+  int32_t n_sensitivities;  /* <= 4                                      */
+  int32_t sensitivity[4];   /* perturbation index of each sensitivity    */
+  int32_t reserved;
 } mc_estimator_info;
 
 /* Per-run results.  sum/sum_sq are caller-owned host arrays of
@@ -179,7 +187,7 @@ int mc_problem_info_get(mc_ctx* ctx, mc_problem_info* out);
 #define MC_GEOMETRY_REFERENCE 1
 int mc_set_geometry_mode(mc_ctx* ctx, int32_t mode);
 int mc_estimator_info_get(mc_ctx* ctx, int32_t index, mc_estimator_info* out);
-/* Name of cell/surface/material/nuclide by index (kind 0/1/2/3). */
+/* Name of cell/surface/material/nuclide/perturbation by index (kind 0-4). */
 int mc_object_name(mc_ctx* ctx, int32_t kind, int32_t index, char* buf, size_t n);
 
 /* ---- solvers ------------------------------------------------------------ */

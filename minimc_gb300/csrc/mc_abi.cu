@@ -436,15 +436,19 @@ int build_world(mc_ctx* c) {
   }
 
   // estimators
-  std::vector<int32_t> est_kind, est_target, est_has_cos, est_bin_kind;
-  std::vector<uint64_t> est_offset, est_bound_off;
+  std::vector<int32_t> est_kind, est_target, est_has_cos, est_bin_kind, est_nsens, est_sens;
+  std::vector<uint64_t> est_offset, est_bound_off, est_size;
   std::vector<double> est_cos_dir, est_bin_par, est_bounds;
   uint64_t off = 0;
   for (const auto& e : m.estimators) {
     est_kind.push_back(e.kind);
     est_target.push_back(e.kind == mc::kCurrent ? e.surface : e.cell);
     est_offset.push_back(off);
-    off += e.size();
+    off += e.span();  // the estimator's bins, then each sensitivity's
+    est_size.push_back(e.size());
+    est_nsens.push_back(static_cast<int32_t>(e.sensitivities.size()));
+    for (int k = 0; k < mcd::kMaxSens; k++)
+      est_sens.push_back(k < static_cast<int>(e.sensitivities.size()) ? e.sensitivities[static_cast<size_t>(k)] : -1);
     est_has_cos.push_back(e.has_cosine ? 1 : 0);
     for (double v : e.cosine_dir) est_cos_dir.push_back(v);
     for (const mc::Bins1D* b : {&e.cosine, &e.energy}) {
@@ -520,6 +524,20 @@ int build_world(mc_ctx* c) {
   UP(est_bin_par, est_bin_par)
   UP(est_bound_off, est_bound_off)
   UP(est_bounds, est_bounds)
+  UP(est_size, est_size)
+  UP(est_nsens, est_nsens)
+  UP(est_sens, est_sens)
+  // perturbations: per material, the perturbations whose nuclide it holds
+  // (TotalCrossSectionPerturbation::Stream, src/Perturbation.cpp:68-78)
+  bool any_sens = false;
+  for (const auto& e : m.estimators) any_sens = any_sens || !e.sensitivities.empty();
+  w.n_pert = any_sens ? static_cast<int32_t>(m.perturbations.size()) : 0;  // nothing scores them otherwise
+  std::vector<int32_t> mat_pert(std::max<size_t>(1, m.materials.size()), 0);
+  for (size_t q = 0; q < m.perturbations.size(); q++)
+    for (size_t i = 0; i < m.materials.size(); i++)
+      for (int32_t n : m.materials[i].nuclides)
+        if (n == m.perturbations[q].nuclide) mat_pert[i] |= 1 << q;
+  UP(mat_pert, mat_pert)
 #undef UP
 
   for (int i = 0; i < 3; i++) {
@@ -597,9 +615,10 @@ int counters_status(mc_ctx* c, const DevCounters& h) {
 // fused history schedule is faster than the event queues (the event kernels
 // pay a launch and a state round trip per event), so AUTO picks it; the
 // event schedule runs multigroup problems whose estimators fit the dense
-// per-history scores when asked for.
+// per-history scores, without perturbations, when asked for.
 int resolve_schedule(mc_ctx* c, int requested) {
-  const bool event_ok = c->model.energy_mode == mc::kMultigroup && c->total_bins <= mcd::kEvDenseBins;
+  const bool event_ok = c->model.energy_mode == mc::kMultigroup && c->total_bins <= mcd::kEvDenseBins &&
+                        c->model.perturbations.empty();
   if (requested == MC_SCHEDULE_EVENT) return event_ok ? MC_SCHEDULE_EVENT : -1;
   return MC_SCHEDULE_HISTORY;
 }
@@ -835,8 +854,22 @@ int mc_load_xml(mc_ctx* c, const char* xml_text, const char* base_dir) {
   catch (const std::exception& e) {
     return fail(c, MC_ERR_INPUT, e.what());
   }
-  if (c->model.has_perturbations)
-    return fail(c, MC_ERR_INPUT, "perturbations and sensitivities are not supported by the GPU engine");
+  {
+    const mc::Model& m = c->model;
+    bool sens = false;
+    for (const auto& e : m.estimators) {
+      if (e.sensitivities.size() > static_cast<size_t>(mcd::kMaxSens))
+        return fail(c, MC_ERR_INPUT, "more than 4 sensitivities on one estimator");
+      sens = sens || !e.sensitivities.empty();
+    }
+    if (m.perturbations.size() > static_cast<size_t>(mcd::kMaxPert))
+      return fail(c, MC_ERR_INPUT, "more than 4 perturbations");
+    // the reference's k-eigenvalue workers never give particles their
+    // indirect effects (only FixedSource calls Particle::SetPerturbations,
+    // src/FixedSource.cpp:63-65), so a sensitivity there has nothing to score
+    if (sens && m.problem == mc::kKEigenvalue)
+      return fail(c, MC_ERR_INPUT, "sensitivities are scored in fixed-source problems only");
+  }
   const int rc = build_world(c);
   if (rc != MC_OK) {
     free_world(c);
@@ -874,6 +907,7 @@ int mc_problem_info_get(mc_ctx* c, mc_problem_info* out) {
   out->active = static_cast<uint32_t>(m.active);
   out->total_bins = c->total_bins;
   out->max_yield = c->max_yield;
+  out->n_perturbations = static_cast<int32_t>(m.perturbations.size());
   return MC_OK;
 }
 
@@ -883,7 +917,7 @@ int mc_estimator_info_get(mc_ctx* c, int32_t index, mc_estimator_info* out) {
     return fail(c, MC_ERR_INPUT, "estimator index out of range");
   std::memset(out, 0, sizeof *out);
   uint64_t off = 0;
-  for (int32_t i = 0; i < index; i++) off += c->model.estimators[i].size();
+  for (int32_t i = 0; i < index; i++) off += c->model.estimators[i].span();
   const auto& e = c->model.estimators[index];
   std::strncpy(out->name, e.name.c_str(), sizeof(out->name) - 1);
   out->kind = e.kind;
@@ -892,6 +926,8 @@ int mc_estimator_info_get(mc_ctx* c, int32_t index, mc_estimator_info* out) {
   out->n_bins = e.size();
   out->cosine_bins = e.cosine.size();
   out->energy_bins = e.energy.size();
+  out->n_sensitivities = static_cast<int32_t>(e.sensitivities.size());
+  for (size_t k = 0; k < e.sensitivities.size() && k < 4; k++) out->sensitivity[k] = e.sensitivities[k];
   return MC_OK;
 }
 
@@ -904,6 +940,7 @@ int mc_object_name(mc_ctx* c, int32_t kind, int32_t index, char* buf, size_t n) 
     else if (kind == 1) s = m.surfaces.at(index).name;
     else if (kind == 2) s = m.materials.at(index).name;
     else if (kind == 3) s = m.nuclides.at(index).name;
+    else if (kind == 4) s = m.perturbations.at(index).name;
     else return fail(c, MC_ERR_INPUT, "unknown object kind");
   }
   catch (const std::exception&) {
@@ -1333,9 +1370,7 @@ int mc_output_format(const char* xml_text, const char* base_dir, const double* s
   if (!xml_text || !(total_weight > 0)) return MC_ERR_INPUT;
   try {
     const mc::Model m = mc::load_model(xml_text, base_dir ? base_dir : "");
-    size_t bins = 0;
-    for (const auto& e : m.estimators) bins += e.size();
-    if (bins && (!sum || !sum_sq)) return MC_ERR_INPUT;
+    if (m.total_bins() && (!sum || !sum_sq)) return MC_ERR_INPUT;
     copy_text(mc::format_output(m, sum, sum_sq, total_weight, batchsize), buf, n, needed);
   }
   catch (const std::exception& e) {

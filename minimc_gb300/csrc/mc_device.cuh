@@ -129,6 +129,9 @@ struct DevTSL {
   DevPOD beta, alpha;
 };
 
+constexpr int kMaxPert = 4;  // perturbations per problem
+constexpr int kMaxSens = 4;  // sensitivities per estimator
+
 // Flattened world, passed to kernels by value.
 struct DevWorld {
   int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
@@ -172,6 +175,12 @@ struct DevWorld {
   const double* est_bounds;
   const int32_t* est_ebin_mg;     // [n_est][G] energy bin of each group (multigroup)
   const uint64_t* est_esize;      // [n_est] number of energy bins
+  // perturbations (TotalCrossSectionPerturbation) and sensitivity estimators
+  int32_t n_pert;                 // <= kMaxPert
+  const int32_t* mat_pert;        // [n_materials] bit k: the material holds perturbation k's nuclide
+  const int32_t* est_nsens;       // [n_est] sensitivities of each estimator
+  const int32_t* est_sens;        // [n_est][kMaxSens] their perturbation indices
+  const uint64_t* est_size;       // [n_est] bins of an estimator (and of each of its sensitivities)
   // fast paths (all exact)
   const long long* surf_key;      // [n] order-preserving integer key of a plane's position
   const int32_t* cell_box;        // [n_cells] index into boxes, or -1

@@ -24,6 +24,7 @@ struct Particle {
   int event;
   int type;
   uint32_t nev;
+  double eff[kMaxPert];  // indirect effect of each perturbation (Particle::indirect_effects)
   Rng rng;
 };
 
@@ -170,14 +171,58 @@ __device__ __forceinline__ uint64_t bin_of(const DevWorld& w, int e, const Parti
 }
 
 // EstimatorSetProxy::Score (src/Estimator.cpp:247-251) for the current
-// estimator (src/Estimator.cpp:142-151): 1 on a crossing of its surface
-template <bool CE = false, class Rng>
+// estimator (src/Estimator.cpp:142-151): 1 on a crossing of its surface.
+// With PERT, each of its sensitivities scores the particle's indirect effect
+// times that 1 into the same bin of its own block
+// (CurrentTotalCrossSectionSensitivity::GetScore, src/Sensitivity.cpp:55-58);
+// zero scores are skipped as ScorableProxy::Score does.
+template <bool CE = false, bool PERT = false, class Rng>
 __device__ __forceinline__ void score_event(const DevWorld& w, const Particle<Rng>& p, Scorer& sc) {
   if (p.event != kSurfaceCross && p.event != kLeak) return;
   for (int e = 0; e < w.n_est; e++) {
     if (__ldg(w.est_kind + e) != 0 || __ldg(w.est_target + e) != p.surf) continue;
     const uint64_t b = __ldg(w.est_offset + e) + bin_of<CE>(w, e, p);
     sc.add(static_cast<uint32_t>(b), 1.0);
+    if constexpr (PERT) {
+      const int ns = __ldg(w.est_nsens + e);
+      const uint64_t size = __ldg(w.est_size + e);
+      for (int k = 0; k < ns; k++) {
+        const int q = __ldg(w.est_sens + e * kMaxSens + k);
+        double s = 0;
+#pragma unroll
+        for (int j = 0; j < kMaxPert; j++)
+          if (j == q) s = p.eff[j];
+        if (s != 0) sc.add(static_cast<uint32_t>(b + size * static_cast<uint64_t>(k + 1)), s);
+      }
+    }
+  }
+}
+
+// Perturbation::Stream of each perturbation before the particle moves d
+// (src/Particle.cpp:46-50, src/Perturbation.cpp:68-78): where the cell's
+// material holds the perturbed nuclide, the indirect effect grows by
+// 1 / cpd - d, cpd being the microscopic collision probability density the
+// flight was sampled with (total, or majorant under delta tracking)
+template <bool PERT, class Rng>
+__device__ __forceinline__ void indirect_stream(const DevWorld& w, Particle<Rng>& p, int m, double cpd, double d) {
+  if constexpr (PERT) {
+    const int mask = __ldg(w.mat_pert + m);
+    if (mask) {
+      const double r = dsub(ddiv(1.0, cpd), d);
+#pragma unroll
+      for (int k = 0; k < kMaxPert; k++)
+        if ((mask >> k) & 1) p.eff[k] = dadd(p.eff[k], r);
+    }
+  }
+}
+
+// Particle::SetPerturbations (src/Particle.cpp:71-73): every particle of a
+// history, secondaries included, starts with no indirect effect
+template <bool PERT, class Rng>
+__device__ __forceinline__ void reset_indirect(Particle<Rng>& p) {
+  if constexpr (PERT) {
+#pragma unroll
+    for (int k = 0; k < kMaxPert; k++) p.eff[k] = 0;
   }
 }
 

@@ -343,38 +343,69 @@ cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s) {
 
 namespace {
 
-__device__ __forceinline__ double beta_min_of(double E, double T) { return -E / (kBoltzmann * T); }
+// The features feed BF16 operands and the networks' outputs carry BF16-level
+// error, so everything around them runs in FP32 (the FP64 pipe is 1/64 of
+// the FP32 rate on this part).  The same functions build the training
+// inputs, so training and inference see identical features.
+struct BoxF {
+  float e_scale, e_shift;   // f0 = ln E * e_scale + e_shift  (maps [logE0, logE1] to [-1, 1])
+  float t_scale, t_shift;   // f1 = T * t_scale + t_shift
+  float beta_cutoff;
+  float inv_beta_scale;
+  float kB;                 // Boltzmann constant (MeV/K)
+  float inv_awr;
+};
 
-__device__ __forceinline__ void base_features(const MlpBox& box, double E, double T, double u, float* f) {
-  f[0] = static_cast<float>(2.0 * (log(E) - box.logE0) / (box.logE1 - box.logE0) - 1.0);
-  f[1] = static_cast<float>(2.0 * (T - box.T0) / (box.T1 - box.T0) - 1.0);
-  f[2] = static_cast<float>(2.0 * u - 1.0);
-  f[3] = static_cast<float>(fmin(2.0, fmax(-2.0, log(u / (1.0 - u)) / 8.0)));
+__device__ __forceinline__ BoxF box_f(const MlpBox& b) {
+  BoxF f;
+  const double es = 2.0 / (b.logE1 - b.logE0), ts = 2.0 / (b.T1 - b.T0);
+  f.e_scale = static_cast<float>(es);
+  f.e_shift = static_cast<float>(-b.logE0 * es - 1.0);
+  f.t_scale = static_cast<float>(ts);
+  f.t_shift = static_cast<float>(-b.T0 * ts - 1.0);
+  f.beta_cutoff = static_cast<float>(b.beta_cutoff);
+  f.inv_beta_scale = static_cast<float>(1.0 / b.beta_scale);
+  f.kB = static_cast<float>(kBoltzmann);
+  f.inv_awr = static_cast<float>(1.0 / b.awr);
+  return f;
 }
 
-__device__ __forceinline__ void beta_features(const MlpBox& box, double E, double T, double u, float (&f)[kMlpIn]) {
+__device__ __forceinline__ float beta_min_of(const BoxF& b, float E, float T) { return -E / (b.kB * T); }
+
+__device__ __forceinline__ void base_features(const BoxF& b, float E, float T, float u, float* f) {
+  f[0] = fmaf(logf(E), b.e_scale, b.e_shift);
+  f[1] = fmaf(T, b.t_scale, b.t_shift);
+  f[2] = fmaf(2.0f, u, -1.0f);
+  f[3] = fminf(2.0f, fmaxf(-2.0f, (logf(u) - log1pf(-u)) * 0.125f));
+}
+
+__device__ __forceinline__ void beta_features(const BoxF& b, float E, float T, float u, float (&f)[kMlpIn]) {
 #pragma unroll
   for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
-  base_features(box, E, T, u, f);
+  base_features(b, E, T, u, f);
 }
 
-__device__ __forceinline__ void alpha_features(const MlpBox& box, double E, double T, double beta, double u,
+__device__ __forceinline__ void alpha_features(const BoxF& b, float E, float T, float beta, float u,
                                                float (&f)[kMlpIn]) {
 #pragma unroll
   for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
-  base_features(box, E, T, u, f);
-  const double bmin = beta_min_of(E, T);
-  f[4] = static_cast<float>(copysign(log1p(fabs(beta)), beta) / box.beta_scale);
-  f[5] = static_cast<float>(2.0 * (beta - bmin) / (box.beta_cutoff - bmin) - 1.0);
+  base_features(b, E, T, u, f);
+  const float bmin = beta_min_of(b, E, T);
+  f[4] = copysignf(log1pf(fabsf(beta)), beta) * b.inv_beta_scale;
+  f[5] = 2.0f * (beta - bmin) / (b.beta_cutoff - bmin) - 1.0f;
 }
 
-__device__ __forceinline__ void alpha_range(const MlpBox& box, double E, double T, double beta, double& lo,
-                                            double& hi) {
-  const double akT = box.awr * kBoltzmann * T;
-  const double s = sqrt(fmax(0.0, E + beta * kBoltzmann * T));
-  const double r = sqrt(E);
-  lo = (r - s) * (r - s) / akT;
-  hi = (r + s) * (r + s) / akT;
+// kinematic alpha bounds (sqrt E -+ sqrt E')^2 / (A kT) with E' = E + beta kT;
+// sqrt E - sqrt E' is formed as -beta kT / (sqrt E + sqrt E') so that the
+// lower bound keeps its relative accuracy as beta -> 0
+__device__ __forceinline__ void alpha_range(const BoxF& b, float E, float T, float beta, float& lo, float& hi) {
+  const float kT = b.kB * T;
+  const float Ep = E + beta * kT;
+  const float r = sqrtf(E), s = sqrtf(fmaxf(0.0f, Ep));
+  const float d = Ep > 0.0f ? -beta * kT / (r + s) : r;
+  const float inv = b.inv_awr / kT;
+  lo = d * d * inv;
+  hi = (r + s) * (r + s) * inv;
 }
 
 __device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* row) {
@@ -388,10 +419,12 @@ __global__ void k_features_beta(MlpBox box, const double* E, const double* T, co
                                 unsigned long long n, bf16* X, float* y) {
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const BoxF b = box_f(box);
+  const float e = static_cast<float>(E[i]), t = static_cast<float>(T[i]);
   float f[kMlpIn];
-  beta_features(box, E[i], T[i], u[i], f);
+  beta_features(b, e, t, static_cast<float>(u[i]), f);
   store_features(f, X + i * kMlpIn);
-  const double bmin = beta_min_of(E[i], T[i]);
+  const double bmin = beta_min_of(b, e, t);
   const double q = (beta[i] - bmin) / (box.beta_cutoff - bmin);
   y[i] = isfinite(q) ? static_cast<float>(q) : 0.5f;
 }
@@ -400,12 +433,14 @@ __global__ void k_features_alpha(MlpBox box, const double* E, const double* T, c
                                  const double* alpha, unsigned long long n, bf16* X, float* y) {
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const BoxF b = box_f(box);
+  const float e = static_cast<float>(E[i]), t = static_cast<float>(T[i]), bt = static_cast<float>(beta[i]);
   float f[kMlpIn];
-  alpha_features(box, E[i], T[i], beta[i], u[i], f);
+  alpha_features(b, e, t, bt, static_cast<float>(u[i]), f);
   store_features(f, X + i * kMlpIn);
-  double lo, hi;
-  alpha_range(box, E[i], T[i], beta[i], lo, hi);
-  const double q = (alpha[i] - lo) / (hi - lo);
+  float lo, hi;
+  alpha_range(b, e, t, bt, lo, hi);
+  const double q = (alpha[i] - lo) / (static_cast<double>(hi) - lo);
   y[i] = isfinite(q) ? static_cast<float>(q) : 0.5f;
 }
 
@@ -583,16 +618,18 @@ constexpr uint32_t kOffMisc = kOffF + 2 * (4 * kMlpWidth + 4) * 4;
 constexpr uint32_t kSampleSmem = kOffMisc + 64;
 static_assert(kSampleSmem <= 227 * 1024, "shared memory");
 
-// SiLU with the hardware tanh (max relative error about 2^-11, below the
-// BF16 rounding of the activations it feeds)
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float silu_fast(float z) {
-  const float h = 0.5f * z;
-  return fmaf(h, tanh_fast(h), h);
+// SiLU of two pre-activations at once, in BF16 (the precision of the hidden
+// tiles it feeds): with h = z / 2, silu(z) = h + h tanh(h), using the
+// hardware's packed BF16 tanh (one MUFU operation per pair) and a packed
+// BF16 fma.  The caller passes h (the half-scaled accumulator plus the
+// half-scaled bias) in FP32.
+__device__ __forceinline__ __nv_bfloat162 silu2_bf16(float h0, float h1) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(h0, h1);
+  __nv_bfloat162 t;
+  asm("tanh.approx.bf16x2 %0, %1;"
+      : "=r"(*reinterpret_cast<uint32_t*>(&t))
+      : "r"(*reinterpret_cast<const uint32_t*>(&h)));
+  return __hfma2(h, t, h);
 }
 
 // warpgroup barrier (named barrier 1 + g, 128 threads) and its AND vote
@@ -648,8 +685,9 @@ __device__ __forceinline__ void layer_mma(Group& G, uint32_t act_off, uint32_t w
   tc::fence_after_sync();
 }
 
-// h = SiLU(acc + bias) into the warpgroup's hidden tile (this thread's row)
-__device__ __forceinline__ void hidden_epilogue(Group& G, const float* bias) {
+// h = SiLU(acc + bias) into the warpgroup's hidden tile (this thread's row);
+// `hbias` holds bias / 2
+__device__ __forceinline__ void hidden_epilogue(Group& G, const float* hbias) {
   const int w = G.lt >> 5;
   uint8_t* H = G.base + G.H;
 #pragma unroll 1
@@ -662,14 +700,14 @@ __device__ __forceinline__ void hidden_epilogue(Group& G, const float* bias) {
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const int k = q * 8 + 2 * j;
-        h[j] = __floats2bfloat162_rn(silu_fast(v[k] + bias[c * 32 + k]), silu_fast(v[k + 1] + bias[c * 32 + k + 1]));
+        h[j] = silu2_bf16(fmaf(v[k], 0.5f, hbias[c * 32 + k]), fmaf(v[k + 1], 0.5f, hbias[c * 32 + k + 1]));
       }
       *reinterpret_cast<uint4*>(H + tc::tile_offset(G.lt, c * 32 + q * 8, kMlpWidth)) = *reinterpret_cast<uint4*>(h);
     }
   }
 }
 
-// b4 + w4 . SiLU(acc + b3)
+// b4 + w4 . SiLU(acc + b3); `f` holds b1/2, b2/2, b3/2, w4, b4
 __device__ __forceinline__ float output_epilogue(Group& G, const float* f) {
   const int w = G.lt >> 5;
   const float* b3 = f + 2 * kMlpWidth;
@@ -680,7 +718,12 @@ __device__ __forceinline__ float output_epilogue(Group& G, const float* f) {
     float v[32];
     tc::tmem_ld32(G.tmem + (static_cast<uint32_t>(w * 32) << 16) + c * 32, v);
 #pragma unroll
-    for (int j = 0; j < 32; j++) out = fmaf(silu_fast(v[j] + b3[c * 32 + j]), w4[c * 32 + j], out);
+    for (int j = 0; j < 32; j += 2) {
+      const float2 a = __bfloat1622float2(
+          silu2_bf16(fmaf(v[j], 0.5f, b3[c * 32 + j]), fmaf(v[j + 1], 0.5f, b3[c * 32 + j + 1])));
+      out = fmaf(a.x, w4[c * 32 + j], out);
+      out = fmaf(a.y, w4[c * 32 + j + 1], out);
+    }
   }
   return out;
 }
@@ -720,14 +763,14 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* t
   load_tile(smem + kOffA1, na.W1, kMlpIn);
   load_tile(smem + kOffA2, na.W2, kMlpWidth);
   load_tile(smem + kOffA3, na.W3, kMlpWidth);
-  for (int i = tid; i < kMlpWidth; i += blockDim.x) {
-    fb[i] = nb.p[kMlpB1 + i];
-    fb[kMlpWidth + i] = nb.p[kMlpB2 + i];
-    fb[2 * kMlpWidth + i] = nb.p[kMlpB3 + i];
+  for (int i = tid; i < kMlpWidth; i += blockDim.x) {  // hidden biases halved for the SiLU epilogues
+    fb[i] = 0.5f * nb.p[kMlpB1 + i];
+    fb[kMlpWidth + i] = 0.5f * nb.p[kMlpB2 + i];
+    fb[2 * kMlpWidth + i] = 0.5f * nb.p[kMlpB3 + i];
     fb[3 * kMlpWidth + i] = nb.p[kMlpW4 + i];
-    fa[i] = na.p[kMlpB1 + i];
-    fa[kMlpWidth + i] = na.p[kMlpB2 + i];
-    fa[2 * kMlpWidth + i] = na.p[kMlpB3 + i];
+    fa[i] = 0.5f * na.p[kMlpB1 + i];
+    fa[kMlpWidth + i] = 0.5f * na.p[kMlpB2 + i];
+    fa[2 * kMlpWidth + i] = 0.5f * na.p[kMlpB3 + i];
     fa[3 * kMlpWidth + i] = na.p[kMlpW4 + i];
   }
   if (tid == 0) {
@@ -750,6 +793,8 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* t
   G.phase = 0;
   G.ok = true;
   const double Emin = exp(box.logE0), Emax = exp(box.logE1);
+  const BoxF bf = box_f(box);
+  const float Eminf = static_cast<float>(Emin), T0f = static_cast<float>(box.T0);
   unsigned long long my_fail = 0;
   const unsigned long long tiles = (n + 127) / 128;
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * kGroups;
@@ -757,29 +802,26 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* t
        tile += stride) {
     const unsigned long long i = tile * 128 + G.lt;
     const bool valid = i < n;
-    double e = valid ? E[i] : Emin;
-    double t = valid ? T[i] : box.T0;
-    const bool in_box = e >= Emin && e <= Emax && t >= box.T0 && t <= box.T1;
-    if (!in_box) {  // keep the tile's arithmetic finite; the row is resampled below
-      e = Emin;
-      t = box.T0;
-    }
+    const double ed = valid ? E[i] : Emin;
+    const double td = valid ? T[i] : box.T0;
+    const bool in_box = ed >= Emin && ed <= Emax && td >= box.T0 && td <= box.T1;
+    // rows outside the box keep the tile's arithmetic finite and are resampled below
+    const float e = in_box ? static_cast<float>(ed) : Eminf;
+    const float t = in_box ? static_cast<float>(td) : T0f;
     PhiloxRng rng;
     rng.init(key, i, 3);
-    const double u1 = rng.u01();
     float x[kMlpIn];
-    beta_features(box, e, t, fmin(fmax(u1, 1e-12), 1.0 - 1e-12), x);
+    beta_features(bf, e, t, rng.u01f(), x);
     write_x(G, x);
     const float qb = run_net(G, kOffB1, kOffB2, kOffB3, fb);
-    const double bmin = beta_min_of(e, t);
-    const double b = bmin + fmin(1.0, fmax(0.0, static_cast<double>(qb))) * (box.beta_cutoff - bmin);
-    const double u2 = rng.u01();
-    alpha_features(box, e, t, b, fmin(fmax(u2, 1e-12), 1.0 - 1e-12), x);
+    const float bmin = beta_min_of(bf, e, t);
+    const float b = fmaf(fminf(1.0f, fmaxf(0.0f, qb)), bf.beta_cutoff - bmin, bmin);
+    alpha_features(bf, e, t, b, rng.u01f(), x);
     write_x(G, x);
     const float qa = run_net(G, kOffA1, kOffA2, kOffA3, fa);
-    double lo, hi;
-    alpha_range(box, e, t, b, lo, hi);
-    double bo = b, ao = lo + fmin(1.0, fmax(0.0, static_cast<double>(qa))) * (hi - lo);
+    float lo, hi;
+    alpha_range(bf, e, t, b, lo, hi);
+    double bo = b, ao = fmaf(fminf(1.0f, fmaxf(0.0f, qa)), hi - lo, lo);
     if (valid && !in_box) {
       // outside the trained box: the POD sampler (FP32 form when the ranks fit)
       const double eo = E[i], to = T[i];

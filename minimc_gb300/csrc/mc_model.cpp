@@ -430,7 +430,7 @@ uint64_t Bins1D::index(double v) const {
 
 size_t Model::total_bins() const {
   size_t n = 0;
-  for (const auto& e : estimators) n += e.size();
+  for (const auto& e : estimators) n += e.span();
   return n;
 }
 
@@ -675,6 +675,25 @@ Model load_model(const std::string& xml_text, const std::string& base_dir) {
   if (m.energy_mode == kMultigroup && (m.source.group < 1 || m.source.group > m.groups))
     throw std::runtime_error("source group out of range");
 
+  // perturbations (src/Driver.cpp:38, src/Perturbation.cpp:22-50, 87-96)
+  if (const Node* ps = child(root, "perturbations")) {
+    for (const Node* pn : ps->elements()) {
+      if (pn->name != "total") throw std::runtime_error(pn->path() + ": unknown perturbation type");
+      Perturbation pert;
+      pert.name = attr(pn, "name");
+      const std::string nn = attr(pn, "nuclide");
+      auto it = nuclide_index.find(nn);
+      if (it == nuclide_index.end()) {
+        // World::FindNuclideByName (src/World.cpp:63-81)
+        std::string names;
+        for (const auto& n : m.nuclides) names += "\"" + n.name + "\", ";
+        throw std::runtime_error("Nuclide \"" + nn + "\" not found. Must be one of: [" + names + "]");
+      }
+      pert.nuclide = it->second;
+      m.perturbations.push_back(std::move(pert));
+    }
+  }
+
   // estimators (src/Estimator.cpp:21-33, :185-205)
   if (const Node* es = child(root, "estimators")) {
     for (const Node* e : es->elements()) {
@@ -713,13 +732,30 @@ Model load_model(const std::string& xml_text, const std::string& base_dir) {
       }
       est.cosine = read_bins(first_element(cosine));
       est.energy = read_bins(first_element(child(bins, "energy")));
-      if (e->child("sensitivities") && !e->child("sensitivities")->elements().empty())
-        m.has_perturbations = true;
+      if (const Node* sn = e->child("sensitivities")) {
+        for (const Node* sp : sn->elements()) {
+          // Sensitivity::Create (src/Sensitivity.cpp:13-21): the perturbation
+          // by name, then TotalCrossSectionPerturbation::CreateSensitivity
+          // (src/Perturbation.cpp:52-66), which supports current estimators
+          const std::string pname = attr(sp, "name");
+          int32_t k = -1;
+          for (size_t i = 0; i < m.perturbations.size(); i++)
+            if (m.perturbations[i].name == pname) k = static_cast<int32_t>(i);
+          if (k < 0) {
+            // PerturbationSet::FindPerturbationByName (src/Perturbation.cpp:98-118)
+            std::string names;
+            for (const auto& q : m.perturbations) names += "\"" + q.name + "\", ";
+            throw std::runtime_error("Perturbation \"" + pname + "\" not found. Must be one of: [" + names + "]");
+          }
+          if (est.kind != kCurrent)
+            throw std::runtime_error(
+                "Sensitivity to total cross section perturbation not supported for estimator: " + e->path());
+          est.sensitivities.push_back(k);
+        }
+      }
       m.estimators.push_back(std::move(est));
     }
   }
-  if (const Node* ps = child(root, "perturbations"))
-    if (!ps->elements().empty()) m.has_perturbations = true;
   return m;
 }
 

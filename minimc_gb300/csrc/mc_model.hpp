@@ -176,8 +176,21 @@ struct Estimator {
   bool has_cosine = false;
   double cosine_dir[3] = {1, 0, 0};
   Bins1D cosine, energy;
+  // Sensitivity estimators (src/Estimator.cpp:76-90): perturbation indices
+  // in the order of the `sensitivities` node; each shares the estimator's
+  // bins (src/Scorable.cpp:22-29)
+  std::vector<int32_t> sensitivities;
   uint64_t stride() const { return energy.size(); }
   uint64_t size() const { return cosine.size() * energy.size(); }
+  // flattened bins of the estimator followed by those of its sensitivities
+  uint64_t span() const { return size() * (1 + sensitivities.size()); }
+};
+
+// TotalCrossSectionPerturbation (src/Perturbation.cpp:43-83): a change in
+// one nuclide's total cross section
+struct Perturbation {
+  std::string name;
+  int32_t nuclide = -1;
 };
 
 struct Source {
@@ -211,7 +224,7 @@ struct Model {
   std::vector<Cell> cells;
   std::vector<TSLData> tsl;
   std::vector<Estimator> estimators;
-  bool has_perturbations = false;
+  std::vector<Perturbation> perturbations;
 
   bool HasConstantTemperature() const { return fields[0].IsConstant(); }
   size_t total_bins() const;

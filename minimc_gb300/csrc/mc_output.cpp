@@ -36,6 +36,17 @@ std::string bins_text(const Bins1D& b) {
   }
 }
 
+// Scorable::GetScoreAsString
+std::string score_text(const double* sum, const double* sum_sq, size_t n, double total_weight) {
+  std::string t = "mean\n----\n";
+  for (size_t i = 0; i < n; i++) sci(t, sum[i] / total_weight);
+  t += "\n\n";
+  t += "std dev\n-------\n";
+  for (size_t i = 0; i < n; i++) sci(t, std::sqrt(sum_sq[i] - sum[i] * sum[i] / total_weight) / total_weight);
+  t += "\n\n";
+  return t;
+}
+
 }  // namespace
 
 std::string format_output(const Model& m, const double* sum, const double* sum_sq, double total_weight,
@@ -47,19 +58,18 @@ std::string format_output(const Model& m, const double* sum, const double* sum_s
     // ParticleBins::to_string
     t += "cosine\n------\n" + bins_text(e.cosine) + "\n\n";
     t += "energy\n------\n" + bins_text(e.energy) + "\n\n";
-    // Scorable::GetScoreAsString
     const size_t n = e.size();
-    t += "mean\n----\n";
-    for (size_t i = 0; i < n; i++) sci(t, sum[off + i] / total_weight);
-    t += "\n\n";
-    t += "std dev\n-------\n";
-    for (size_t i = 0; i < n; i++) {
-      const double s = sum[off + i], q = sum_sq[off + i];
-      sci(t, std::sqrt(q - s * s / total_weight) / total_weight);
-    }
-    t += "\n\n";
-    out += "\n" + t + "\n";
+    t += score_text(sum + off, sum_sq + off, n, total_weight);
     off += n;
+    // Sensitivity::to_string (src/Sensitivity.cpp:25-28): name
+    // "<estimator>::<perturbation>" (src/Scorable.cpp:22-29)
+    for (int32_t k : e.sensitivities) {
+      const std::string name = e.name + "::" + m.perturbations[static_cast<size_t>(k)].name;
+      t += name + "\n" + std::string(name.size(), '=') + "\n\n" + score_text(sum + off, sum_sq + off, n, total_weight) +
+           "\n";
+      off += n;
+    }
+    out += "\n" + t + "\n";
   }
   return out;
 }

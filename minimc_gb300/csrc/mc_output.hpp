@@ -1,6 +1,7 @@
 // minimc's result file (.out): the batch size line followed by
 // EstimatorSet::to_string (src/minimc.cpp:20-21, src/Estimator.cpp:48-56,
-// 207-213, src/Scorable.cpp:51-70, src/Bins.cpp:84-170).
+// 207-213, src/Scorable.cpp:51-70, src/Bins.cpp:84-170,
+// src/Sensitivity.cpp:25-28).
 #pragma once
 
 #include "mc_model.hpp"

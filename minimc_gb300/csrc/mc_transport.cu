@@ -53,7 +53,7 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 // multigroup history loop of one CTA: the body of the single-problem kernel
 // (world and run parameters in the kernel's parameter space) and of the
 // batched kernel (copied into shared memory per CTA)
-template <class Rng, bool KEIG>
+template <class Rng, bool KEIG, bool PERT = false>
 __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& rp, double* smem) {
   const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
@@ -113,6 +113,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           p.surf = -1;
           p.skip = -1;
           p.nev = 0;
+          reset_indirect<PERT>(p);
           hist_nev = 0;
           fate = kBirth;
           dropped = false;
@@ -153,6 +154,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       if (collide) {
         if (rp.score) score_track(w, p, dcol, sc);
         if (KEIG) my_ktl += dcol * __ldg(w.mat_mg_nusigf + mg);
+        indirect_stream<PERT>(w, p, m, micro, dcol);
         stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
         p.skip = -1;
         // multigroup majorant == total, so CellDeltaTracking's rejection
@@ -226,6 +228,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           // normal component, stay in the cell
           if (rp.score) score_track(w, p, dsurf, sc);
           if (KEIG) my_ktl += dsurf * __ldg(w.mat_mg_nusigf + mg);
+          indirect_stream<PERT>(w, p, m, micro, dsurf);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
           const int kind = __ldg(w.surf_kind + s);
           if (kind == kPlaneX) p.u = -p.u;
@@ -239,6 +242,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           const double d = dadd(dsurf, kNudge);
           if (rp.score) score_track(w, p, d, sc);
           if (KEIG) my_ktl += d * __ldg(w.mat_mg_nusigf + mg);
+          indirect_stream<PERT>(w, p, m, micro, d);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, d);
           if (w.quirks) {
             p.cell = find_cell(w, p.x, p.y, p.z);
@@ -260,7 +264,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           }
         }
       }
-      if (rp.score) score_event(w, p, sc);
+      if (rp.score) score_event<false, PERT>(w, p, sc);
       p.nev++;
       hist_nev++;
       my_events++;
@@ -291,6 +295,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           p.surf = -1;
           p.skip = -1;
           p.nev = 0;
+          reset_indirect<PERT>(p);
           alive = p.cell >= 0 && __ldg(w.cell_mat + p.cell) >= 0;
           if (!alive) my_lost++;
         }
@@ -335,6 +340,14 @@ template <class Rng, bool KEIG, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_history_mg(const DevWorld w, const RunParams rp) {
   extern __shared__ double smem[];
   history_mg<Rng, KEIG>(w, rp, smem);
+}
+
+// fixed-source kernel carrying the indirect effects of perturbations and
+// scoring sensitivity estimators
+template <class Rng>
+__global__ void __launch_bounds__(256, 1) k_history_mg_pert(const DevWorld w, const RunParams rp) {
+  extern __shared__ double smem[];
+  history_mg<Rng, false, true>(w, rp, smem);
 }
 
 // batched k-eigenvalue transport: every CTA serves one problem (its world
@@ -443,6 +456,12 @@ int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, b
 
 cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
                               cudaStream_t stream, int variant) {
+  if (w.n_pert > 0 && !rp.keig) {
+    const size_t smem = 2 * kSharedBins * sizeof(double);
+    if (rng_mode == 1) k_history_mg_pert<MinstdRng><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_mg_pert<PhiloxRng><<<grid, block, smem, stream>>>(w, rp);
+    return cudaGetLastError();
+  }
   switch (variant) {
   case 1: launch_mg<3>(w, rp, rng_mode, grid, block, stream); break;
   case 2: launch_mg<4>(w, rp, rng_mode, grid, block, stream); break;

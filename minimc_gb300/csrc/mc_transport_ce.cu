@@ -116,8 +116,9 @@ __device__ __forceinline__ double ce_nubar(const DevWorld& w, const Particle<Rng
 // FX: FP32 union tables (launched only for Philox streams in fast mode when
 // the tables are valid); otherwise the exact tables, with FP32 free-gas
 // kinematics when the stream is Philox in fast mode
-template <class Rng, bool KEIG, int MINB, bool FX>
+template <class Rng, bool KEIG, int MINB, bool FX, bool PERT = false>
 __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, const RunParams rp) {
+  static_assert(!(PERT && (FX || KEIG)), "indirect effects need the exact tables of a fixed-source run");
   extern __shared__ double smem[];
   const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           p.surf = -1;
           p.skip = -1;
           p.nev = 0;
+          reset_indirect<PERT>(p);
           hist_nev = 0;
           fate = kBirth;
           dropped = false;
@@ -244,6 +246,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
             real = u < ddiv(ce_material_micro(w, m, t, p.j, p.E, T_pos, T_pos, false), cpd);
           }
         }
+        indirect_stream<PERT>(w, p, m, cpd, dcol);
         stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
         if (!real) {
           p.event = kVirtualCollision;
@@ -339,6 +342,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
         if (refl) {
           if (rp.score) score_track<true>(w, p, dsurf, sc);
           if (KEIG) my_ktl += dsurf * nsf;
+          indirect_stream<PERT>(w, p, m, cpd, dsurf);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
           const int kind = __ldg(w.surf_kind + s);
           if (kind == kPlaneX) p.u = -p.u;
@@ -352,6 +356,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           const double dd = dadd(dsurf, kNudge);
           if (rp.score) score_track<true>(w, p, dd, sc);
           if (KEIG) my_ktl += dd * nsf;
+          indirect_stream<PERT>(w, p, m, cpd, dd);
           stream(p.x, p.y, p.z, p.u, p.v, p.w, dd);
           if (w.quirks) {
             p.cell = find_cell(w, p.x, p.y, p.z);
@@ -371,7 +376,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           }
         }
       }
-      if (rp.score) score_event<true>(w, p, sc);
+      if (rp.score) score_event<true, PERT>(w, p, sc);
       p.nev++;
       hist_nev++;
       my_events++;
@@ -402,6 +407,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           p.surf = -1;
           p.skip = -1;
           p.nev = 0;
+          reset_indirect<PERT>(p);
           alive = p.cell >= 0 && __ldg(w.cell_mat + p.cell) >= 0;
           if (!alive) my_lost++;
         }
@@ -519,7 +525,9 @@ void launch_exact(const DevWorld& w, const RunParams& rp, int rng_mode, int grid
 }
 }  // namespace
 
-bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast) { return rng_mode != 1 && fast && w.ce.fast_ok; }
+bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast) {
+  return rng_mode != 1 && fast && w.ce.fast_ok && w.n_pert == 0;
+}
 
 int history_blocks_per_sm_ce(const DevWorld& w, int rng_mode, int block, bool keig, bool fast, int variant) {
   if (!ce_uses_fp32_tables(w, rng_mode, fast)) return occupancy_exact(rng_mode, block, keig);
@@ -534,6 +542,13 @@ int history_blocks_per_sm_ce(const DevWorld& w, int rng_mode, int block, bool ke
 
 cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
                               cudaStream_t stream, int variant) {
+  if (w.n_pert > 0 && !rp.keig) {
+    // perturbations: the exact tables, with indirect effects
+    const size_t smem = 2 * kSharedBins * sizeof(double);
+    if (rng_mode == 1) k_history_ce<MinstdRng, false, 1, false, true><<<grid, block, smem, stream>>>(w, rp);
+    else k_history_ce<PhiloxRng, false, 1, false, true><<<grid, block, smem, stream>>>(w, rp);
+    return cudaGetLastError();
+  }
   if (!ce_uses_fp32_tables(w, rng_mode, rp.fast != 0)) {
     launch_exact(w, rp, rng_mode, grid, block, stream);
     return cudaGetLastError();

@@ -70,13 +70,14 @@ class ProblemInfo(C.Structure):
                 ("n_nuclides", C.c_int32), ("groups", C.c_int32), ("n_estimators", C.c_int32),
                 ("n_tsl", C.c_int32), ("histories", C.c_uint64), ("seed", C.c_uint64),
                 ("inactive", C.c_uint32), ("active", C.c_uint32), ("total_bins", C.c_uint64),
-                ("max_yield", C.c_uint32), ("reserved", C.c_int32 * 7)]
+                ("max_yield", C.c_uint32), ("n_perturbations", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class EstimatorInfo(C.Structure):
     _fields_ = [("name", C.c_char * 64), ("kind", C.c_int32), ("target", C.c_int32),
                 ("offset", C.c_uint64), ("n_bins", C.c_uint64), ("cosine_bins", C.c_uint64),
-                ("energy_bins", C.c_uint64)]
+                ("energy_bins", C.c_uint64), ("n_sensitivities", C.c_int32), ("sensitivity", C.c_int32 * 4),
+                ("reserved", C.c_int32)]
 
 
 class TallyOut(C.Structure):
@@ -667,14 +668,18 @@ class Driver:
             n = result.histories
         out = {}
         for e in self.ctx.estimators():
-            sl = slice(e.offset, e.offset + e.n_bins)
-            s, s2 = result.sum[sl], result.sum_sq[sl]
-            out[e.name.decode()] = {
-                "mean": s / n,
-                "std": np.sqrt(np.maximum(s2 - s * s / n, 0.0)) / n,
-                "cosine_bins": int(e.cosine_bins),
-                "energy_bins": int(e.energy_bins),
-            }
+            # the estimator, then its sensitivities "<estimator>::<perturbation>"
+            names = [e.name.decode()] + [e.name.decode() + "::" + self.ctx.object_name(4, e.sensitivity[k])
+                                         for k in range(e.n_sensitivities)]
+            for k, name in enumerate(names):
+                sl = slice(e.offset + k * e.n_bins, e.offset + (k + 1) * e.n_bins)
+                s, s2 = result.sum[sl], result.sum_sq[sl]
+                out[name] = {
+                    "mean": s / n,
+                    "std": np.sqrt(np.maximum(s2 - s * s / n, 0.0)) / n,
+                    "cosine_bins": int(e.cosine_bins),
+                    "energy_bins": int(e.energy_bins),
+                }
         return out
 
 

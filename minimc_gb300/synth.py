@@ -14,6 +14,8 @@ Conventions of the reference input (test/minimc.xsd):
 """
 from __future__ import annotations
 
+import re
+
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -289,3 +291,14 @@ def batch_problems(count: int = 64, seed: int = 7, h_min: int = 10_000, h_max: i
         p.seed = 1 + i
         out.append((p, hist))
     return out
+
+
+def with_sensitivities(xml: str, perts: list[tuple[str, str]]) -> str:
+    """Adds total cross-section perturbations (name, nuclide) to a problem
+    and, to every current estimator, a sensitivity to each of them."""
+    pxml = "<perturbations>\n" + "".join(f'  <total name="{n}" nuclide="{nuc}"/>\n' for n, nuc in perts) + \
+        "</perturbations>\n"
+    sens = "<sensitivities>" + "".join(f'<perturbation name="{n}"/>' for n, _ in perts) + "</sensitivities>"
+    xml = re.sub(r"(<current [^>]*?[^/]>)", rf"\1{sens}", xml)
+    xml = re.sub(r"(<current [^>]*?)/>", rf"\1>{sens}</current>", xml)
+    return xml.replace("</minimc>", pxml + "</minimc>")

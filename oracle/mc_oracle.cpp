@@ -19,6 +19,8 @@
 //   Multigroup::Interact/Scatter/Fission   src/Multigroup.cpp:49-73,245-286
 //   Source::Sample                src/Source.cpp:143-154
 //   ScorableProxy::Score/CommitHistory     src/Scorable.cpp:81-106
+//   TotalCrossSectionPerturbation::Stream  src/Perturbation.cpp:68-78
+//   CurrentTotalCrossSectionSensitivity::GetScore  src/Sensitivity.cpp:55-58
 // Random numbers come from std::minstd_rand and the standard library's
 // distributions, exactly as in the reference (src/BasicTypes.hpp:27).
 //
@@ -221,6 +223,7 @@ struct Oracle {
     int surf = -1;
     int skip = -1;
     bool resample_failed = false;  // thermal scattering resample limit hit
+    double eff[4] = {0, 0, 0, 0};  // indirect effect of each perturbation (Particle::indirect_effects)
     RNG rng;
     std::list<P> secondaries;
   };
@@ -704,12 +707,32 @@ struct Oracle {
 
   std::vector<size_t> offsets;
 
+  // EstimatorProxy::Score (src/Estimator.cpp:104-110): the estimator, then
+  // each sensitivity, whose score is the indirect effect times the
+  // estimator's (src/Sensitivity.cpp:55-58); ScorableProxy::Score skips
+  // zero scores (src/Scorable.cpp:80-99)
   void Score(const P& p, std::map<size_t, double>& pending) const {
     if (p.event != kSurfaceCross && p.event != kLeak) return;
     for (size_t e = 0; e < m.estimators.size(); e++) {
       const auto& est = m.estimators[e];
       if (est.kind != mc::kCurrent || est.surface != p.surf) continue;
-      pending[offsets[e] + BinIndex(e, p)] += 1;
+      const double score = 1;
+      const size_t b = BinIndex(e, p);
+      pending[offsets[e] + b] += score;
+      for (size_t k = 0; k < est.sensitivities.size(); k++) {
+        const double s = p.eff[est.sensitivities[k]] * score;
+        if (s != 0) pending[offsets[e] + est.size() * (k + 1) + b] += s;
+      }
+    }
+  }
+
+  // TotalCrossSectionPerturbation::Stream (src/Perturbation.cpp:68-78),
+  // accumulated by Particle::Stream before the move (src/Particle.cpp:46-50)
+  void Indirect(P& p, int mat, double cpd, double d) const {
+    for (size_t k = 0; k < m.perturbations.size(); k++) {
+      const auto& nucs = m.materials[mat].nuclides;
+      if (std::find(nucs.begin(), nucs.end(), m.perturbations[k].nuclide) == nucs.end()) continue;
+      p.eff[k] += 1 / cpd - d;
     }
   }
 
@@ -745,6 +768,9 @@ struct Oracle {
       return;
     }
     const bool delta = m.tracking == mc::kCellDeltaTracking;
+    // Particle::SetPerturbations before each particle's transport
+    // (src/FixedSource.cpp:63-65)
+    for (double& e : p.eff) e = 0;
     while (p.event != kCapture && p.event != kLeak && p.event != kFission && p.event != kLost) {
       const int mat = m.cells[p.cell].material;
       // GetCollisionProbabilityDensity: total (surface tracking) or
@@ -760,10 +786,12 @@ struct Oracle {
         st.ktl += distance_to_collision * m.materials[mat].number_density * NuSigmaF(mat, p);
         if (delta && !std::bernoulli_distribution{MaterialTotal(mat, p) / cpd}(p.rng)) {
           // virtual collision (src/TransportMethod.cpp:111-115)
+          Indirect(p, mat, cpd, distance_to_collision);
           Stream(p, distance_to_collision);
           p.event = kVirtual;
         }
         else {
+          Indirect(p, mat, cpd, distance_to_collision);
           Stream(p, distance_to_collision);
           p.skip = -1;
           const int n = SampleNuclide(p);
@@ -775,6 +803,7 @@ struct Oracle {
       else if (m.surfaces[s].reflective) {
         if (score) ScoreTrack(p, dsurf, pending);
         st.ktl += dsurf * m.materials[mat].number_density * NuSigmaF(mat, p);
+        Indirect(p, mat, cpd, dsurf);
         Stream(p, dsurf);
         const int kind = m.surfaces[s].kind;
         if (kind == mc::kPlaneX) p.dir.x = -p.dir.x;
@@ -788,6 +817,7 @@ struct Oracle {
         const double d = dsurf + kNudge;
         if (score) ScoreTrack(p, d, pending);
         st.ktl += d * m.materials[mat].number_density * NuSigmaF(mat, p);
+        Indirect(p, mat, cpd, d);
         Stream(p, d);
         if (quirks) {
           p.cell = FindCellContaining(p.pos);
@@ -929,7 +959,7 @@ void* orc_create(const char* xml, const char* base_dir, char* err, size_t errn) 
   size_t off = 0;
   for (const auto& e : o->m.estimators) {
     o->offsets.push_back(off);
-    off += e.size();
+    off += e.span();
   }
   return o;
 }

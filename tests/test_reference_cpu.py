@@ -17,6 +17,7 @@ import numpy as np
 import pytest
 
 from minimc_gb300 import synth_ce, synth_tsl
+from minimc_gb300.synth import with_sensitivities
 from oracle.build import Oracle
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
@@ -152,3 +153,60 @@ def test_result_file_text_multigroup(ref, tmp_path, built_library):
     n = int(re.search(r"<histories>(\d+)</histories>", xml).group(1))
     _, _, r = run_both(ref, xml, GOLDEN, tmp_path, est)
     assert format_output(xml, GOLDEN, r["sum"], r["sum_sq"], n) == r["ref_text"]
+
+
+def check_sensitivity_text(ref, xml, d, tmp_path):
+    from minimc_gb300.engine import format_output
+
+    n = int(re.search(r"<histories>(\d+)</histories>", xml).group(1))
+    _, _, r = run_both(ref, xml, d, tmp_path, None)
+    text = r["ref_text"]
+    assert "::" in text
+    assert format_output(xml, d, r["sum"], r["sum_sq"], n) == text
+    return r
+
+
+def test_sensitivities_multigroup(ref, tmp_path, built_library):
+    """Sensitivity estimators of a current estimator to total cross-section
+    perturbations of two nuclides (src/Perturbation.cpp:68-78,
+    src/Sensitivity.cpp:55-58): the oracle's scores give the reference's
+    own result text."""
+    xml = with_sensitivities((GOLDEN / "mg_spheres.xml").read_text(), [("dH", "hydrogen"), ("dO", "oxygen")])
+    r = check_sensitivity_text(ref, xml, GOLDEN, tmp_path)
+    # estimator bins, then one block per sensitivity
+    assert len(r["sum"]) == 3 and r["sum"][1] != 0 and r["sum"][2] != 0
+
+
+@pytest.mark.parametrize("tracking", ["surface", "cell delta"])
+def test_sensitivities_continuous_energy(ref, ce_files, tmp_path, built_library, tracking):
+    d, files = ce_files
+    temp = None
+    if tracking == "cell delta":
+        temp = ("  <linear>\n    <gradient x=\"10.0\" y=\"0\" z=\"0\"/>\n    <intercept b=\"393.6\"/>\n"
+                "    <bounds upper=\"493.6\" lower=\"293.6\"/>\n  </linear>")
+    xml = synth_ce.ce_problem_xml(files, histories=2000, keig=False, sphere=6.0, afrac=(0.6, 0.3, 0.001),
+                                  tracking=tracking, temperature_xml=temp,
+                                  estimators=[synth_ce.energy_current("leak", "sphere", bins=20),
+                                              '  <current name="plain" surface="sphere"/>'])
+    xml = with_sensitivities(xml, [("dH1", "H1"), ("dU", "U235")])
+    check_sensitivity_text(ref, xml, d, tmp_path)
+
+
+@pytest.mark.parametrize("case", ["perturbation", "nuclide"])
+def test_sensitivity_input_errors(tmp_path, built_library, case):
+    """Unknown perturbation or nuclide names.  The reference forms these
+    messages (src/Perturbation.cpp:98-118, src/World.cpp:63-81) inside
+    noexcept constructors (src/Estimator.cpp:76-90, src/Perturbation.cpp:87-96),
+    so its process terminates; here the load fails with the message."""
+    from minimc_gb300.engine import MCError, format_output
+
+    xml = with_sensitivities((GOLDEN / "mg_spheres.xml").read_text(), [("dH", "hydrogen")])
+    if case == "perturbation":
+        xml = xml.replace('<perturbation name="dH"/>', '<perturbation name="dX"/>')
+        want = 'Perturbation "dX" not found. Must be one of: ["dH", ]'
+    else:
+        xml = xml.replace('nuclide="hydrogen"/>\n</perturbations>', 'nuclide="helium"/>\n</perturbations>')
+        want = 'Nuclide "helium" not found. Must be one of: ['
+    with pytest.raises(MCError) as e:
+        format_output(xml, GOLDEN, [0.0] * 3, [0.0] * 3, 1)
+    assert e.value.message.startswith(want), e.value.message
