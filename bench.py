@@ -362,7 +362,7 @@ def run_gpu_tsl(args) -> None:
     283.6-623.6 K per sample."""
     import torch
 
-    from minimc_gb300 import RNG_PHILOX, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context
+    from minimc_gb300 import RNG_PHILOX, THERMAL_SURROGATE, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context
 
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -447,6 +447,43 @@ def run_gpu_tsl(args) -> None:
     ks = {k: {"beta": float(stats.ks_2samp(samples[k][0], samples["pod_exact"][0]).statistic),
               "alpha": float(stats.ks_2samp(samples[k][1], samples["pod_exact"][1]).statistic)}
           for k in ("pod_fp32", "mlp")}
+    # transport with the surrogate: thermal scatters through the queue
+    # (one tensor-core sampler launch per round), same histories per step
+    sur_opts = dict(opts, thermal=THERMAL_SURROGATE)
+    pod_ref = ctx.run_fixed_source(**dict(opts, seed=101))
+    for _ in range(args.warmup):
+        ctx.run_fixed_source(**sur_opts)
+    sms, skms, slaunch = [], [], 0
+    for _ in range(args.steps):
+        r = ctx.run_fixed_source(**sur_opts)
+        sms.append(r.raw.transport_ms)
+        skms.append(r.raw.kernel_ms)
+        slaunch += r.raw.launches
+    sur_ref = ctx.run_fixed_source(**dict(sur_opts, seed=202))
+    sur_value = hist * args.steps * ws / (sum(sms) / 1e3)
+    spectra = {}
+    e0 = ctx.estimators()[0]
+    for name, rr in (("pod", pod_ref), ("surrogate", sur_ref)):
+        t = rr.sum[e0.offset:e0.offset + e0.n_bins].reshape(int(e0.cosine_bins), int(e0.energy_bins))
+        spectra[name] = (t.sum(0), t.sum(1))
+    from scipy import stats as sst
+
+    def chi2_two_sample(a, b):
+        keep = (a + b) >= 10
+        a, b = a[keep], b[keep]
+        ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+        chi2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
+        dof = int(keep.sum()) - 1
+        return {"chi2": chi2, "dof": dof, "p": float(sst.chi2.sf(chi2, dof))}
+
+    surrogate_transport = {
+        "value": sur_value, "unit": UNIT, "vs_pod_transport": sur_value / value,
+        "ms_per_step": sum(sms) / args.steps, "kernel_ms_per_step": sum(skms) / args.steps,
+        "launches_per_step": slaunch / args.steps,
+        "energy_spectrum_chi2_vs_pod": chi2_two_sample(spectra["surrogate"][0], spectra["pod"][0]),
+        "cosine_spectrum_chi2_vs_pod": chi2_two_sample(spectra["surrogate"][1], spectra["pod"][1]),
+        "spectrum_histories": hist,
+    }
     flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two networks, multiply-adds x 2
     bf16_peak = None
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -472,6 +509,7 @@ def run_gpu_tsl(args) -> None:
             "events_per_history": e_h,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_kind": peak_kind, "kernel": "k_history_ce"},
+            "surrogate_transport": surrogate_transport,
             "surrogate": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "train_s": train_s,
                           "train": {"loss_beta": tr.loss_beta, "loss_alpha": tr.loss_alpha, "samples": tr.samples,
                                     "data_ms": tr.data_ms, "train_ms": tr.train_ms},

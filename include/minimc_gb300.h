@@ -55,6 +55,13 @@ extern "C" {
  *   follows the same random walk as the reference's. */
 #define MC_RNG_PHILOX 0
 #define MC_RNG_MINSTD 1
+/* Thermal scattering in fixed-source transport: the POD sampler inside the
+ * history kernel, or the trained MLP surrogate (mc_train_surrogate) run as a
+ * batched tensor-core launch over a queue of the particles that reach a
+ * thermal scatter of its library inside its trained (E, T) box (Philox
+ * streams, continuous energy); outside the box the POD sampler serves. */
+#define MC_THERMAL_POD 0
+#define MC_THERMAL_SURROGATE 1
 
 /* How the event loop is scheduled on the device. */
 #define MC_SCHEDULE_AUTO 0     /* autotuner's choice                      */
@@ -76,7 +83,8 @@ typedef struct {
   int32_t fast_math;    /* 1: FP32 sampling arithmetic (Philox only);
                            geometry and positions stay FP64            */
   int32_t variant;      /* history-kernel variant + 1; 0 -> autotuned   */
-  int32_t reserved[6];
+  int32_t thermal;      /* MC_THERMAL_*: thermal scattering sampler      */
+  int32_t reserved[5];
 } mc_run_opts;
 
 /* A particle in a bank: the state that Bank/Particle carry between
@@ -213,6 +221,18 @@ int mc_keig_end(mc_ctx* ctx, mc_keig_out* out);
 /* Running totals of the cycles run so far (events, transport_ms, launches,
  * counters); k_cycle/bank_size/sum/sum_sq are filled when non-NULL. */
 int mc_keig_status(mc_ctx* ctx, mc_keig_out* out);
+
+/* Checkpoint / resume between cycles (no reference counterpart: the
+ * reference's k-eigenvalue Solve is a stub, src/KEigenvalue.cpp:36-62).
+ * The checkpoint holds the run options, the cycle number, per-cycle k and
+ * bank sizes, counters, tallies and the next cycle's source bank; every
+ * later random stream is keyed by (seed, cycle), so a run resumed from it
+ * (in this or another context holding the same problem) gives results
+ * identical to one that did not stop.  mc_keig_checkpoint writes *size
+ * bytes into buf (pass buf = NULL to query the size); mc_keig_resume
+ * replaces mc_keig_begin and continues with mc_keig_cycle / mc_keig_end. */
+int mc_keig_checkpoint(mc_ctx* ctx, void* buf, uint64_t cap, uint64_t* size);
+int mc_keig_resume(mc_ctx* ctx, const void* buf, uint64_t size);
 
 /* What the last transport ran: schedule (MC_SCHEDULE_*), the autotuned
  * history-kernel variant, grid and block, and the kernel times the tuner

@@ -22,7 +22,8 @@ OBJ_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libminimc_gb300.so"
 
 HOST_SOURCES = ["mc_xml.cpp", "mc_model.cpp", "mc_ce_tables.cpp", "mc_output.cpp"]
-CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_transport_ce.cu", "mc_event.cu", "mc_probe.cu", "mc_tsl.cu",
+CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_transport_ce.cu", "mc_transport_ce_fx1.cu", "mc_transport_ce_fx2.cu",
+                "mc_transport_ce_exact.cu", "mc_transport_ce_ext.cu", "mc_event.cu", "mc_probe.cu", "mc_tsl.cu",
                 "mc_mlp.cu", "mc_batch.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -81,7 +82,7 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc: list[str] | No
         if force or _stale(obj, [src, *headers]):
             todo.append(cmd)
     if todo:
-        with ThreadPoolExecutor(max_workers=min(8, len(todo))) as ex:
+        with ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 8, len(todo)))) as ex:
             for cmd in todo:
                 if verbose:
                     print(" ".join(cmd), flush=True)

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -50,7 +51,7 @@ struct mc_ctx {
   size_t pend_clean_bytes = 0;
   uint64_t launches = 0;
   // scratch, grown on demand
-  DevBuffer scratch[20];
+  DevBuffer scratch[24];
   int last_schedule = MC_SCHEDULE_HISTORY;
   // autotuner: history-kernel variant (occupancy target) chosen by timing
   int variant = 0;
@@ -101,6 +102,11 @@ enum ScratchSlot {
   kEvPend,
   kEvFis,
   kTslFail,
+  kParkA,
+  kParkB,
+  kTqIn,
+  kTqOut,
+  kTqCnt,
 };
 
 int fail(mc_ctx* c, int code, const std::string& msg) {
@@ -227,6 +233,15 @@ int build_tsl(mc_ctx* c) {
     if ((rc = upload(c, t.xs_E_modes, &d.xs_Em)) != MC_OK) return rc;
     if ((rc = upload(c, t.xs_T_modes, &d.xs_Tm)) != MC_OK) return rc;
     if ((rc = upload(c, t.xs_S, &d.xs_S)) != MC_OK) return rc;
+    {
+      // FP32 forms of the total's modes for fast-mode transport
+      std::vector<float> ems(t.xs_E_modes.size()), tm(t.xs_T_modes.size());
+      const size_t r = t.xs_rank;
+      for (size_t i = 0; i < ems.size(); i++) ems[i] = static_cast<float>(t.xs_S[i % r] * t.xs_E_modes[i]);
+      for (size_t i = 0; i < tm.size(); i++) tm[i] = static_cast<float>(t.xs_T_modes[i]);
+      if ((rc = upload(c, ems, &d.xs_EmS_f)) != MC_OK) return rc;
+      if ((rc = upload(c, tm, &d.xs_Tm_f)) != MC_OK) return rc;
+    }
     if ((rc = upload(c, t.majorant.x, &d.maj_x)) != MC_OK) return rc;
     if ((rc = upload(c, t.majorant.y, &d.maj_y)) != MC_OK) return rc;
     if ((rc = build_pod(c, t.beta, d.beta)) != MC_OK) return rc;
@@ -631,6 +646,7 @@ void count_launches(void* ctx, int n) { static_cast<mc_ctx*>(ctx)->launches += n
 // particle's stream is keyed by its own identity, not its slot, so the
 // repeat draws the same numbers).
 int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap);
+int run_tq(mc_ctx* c, RunParams rp, int grid, int block);
 
 int run_event(mc_ctx* c, RunParams& rp, int rng) {
   uint64_t cap = rp.keig ? rp.n : rp.n * 4 + 65536;
@@ -736,12 +752,18 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     const int grid = grid_for(c, c->model.energy_mode, rng, block, keig, rp.fast != 0);
     c->last_grid = grid;
     c->last_block = block;
-    cudaError_t e;
-    if (c->model.energy_mode == mc::kMultigroup)
-      e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
-    else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream, c->variant);
-    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
-    c->launches++;
+    if (rp.tq) {
+      const int rc = run_tq(c, rp, grid, block);
+      if (rc != MC_OK) return rc;
+    }
+    else {
+      cudaError_t e;
+      if (c->model.energy_mode == mc::kMultigroup)
+        e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
+      else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream, c->variant);
+      if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
+      c->launches++;
+    }
   }
   CUDA_TRY(c, cudaEventRecord(c->evk1, c->stream));
   if (keig) {
@@ -763,6 +785,57 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     *ms = f;
     CUDA_TRY(c, cudaEventElapsedTime(&f, c->evk0, c->evk1));
     c->last_kernel_ms = f;
+  }
+  return MC_OK;
+}
+
+// Fixed source with the thermal-scatter queue: the source launch parks
+// particles at thermal scatters; each round samples the parked rows with
+// the surrogate (one tensor-core launch) and resumes them (one history
+// launch), which may park them again.  Counts stay on the device, so the
+// rounds need no host synchronisation; the last resume samples inline.
+int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
+  const uint64_t n = rp.n;
+  auto* A = static_cast<mcd::ParkRec*>(scratch(c, kParkA, n * sizeof(mcd::ParkRec)));
+  auto* B = static_cast<mcd::ParkRec*>(scratch(c, kParkB, n * sizeof(mcd::ParkRec)));
+  auto* qin = static_cast<float4*>(scratch(c, kTqIn, n * sizeof(float4)));
+  auto* qout = static_cast<float2*>(scratch(c, kTqOut, n * sizeof(float2)));
+  auto* cnt = static_cast<unsigned long long*>(scratch(c, kTqCnt, 2 * (mcd::kTqRounds + 1) * 8));
+  if (!A || !B || !qin || !qout || !cnt) return fail(c, MC_ERR_OOM, "thermal queue buffers");
+  unsigned long long* heads = cnt + mcd::kTqRounds + 1;
+  CUDA_TRY(c, cudaMemsetAsync(cnt, 0, 2 * (mcd::kTqRounds + 1) * 8, c->stream));
+  rp.tq = 1;
+  rp.tq_tsl = c->mlp_tsl;
+  rp.tq_box[0] = std::exp(c->mlp_box.logE0);
+  rp.tq_box[1] = std::exp(c->mlp_box.logE1);
+  rp.tq_box[2] = c->mlp_box.T0;
+  rp.tq_box[3] = c->mlp_box.T1;
+  rp.park_cap = n;
+  rp.tq_in = qin;
+  rp.tq_out = qout;
+  rp.head = nullptr;
+  rp.n_resume = nullptr;
+  rp.park_in = nullptr;
+  rp.park_out = A;
+  rp.park_count = cnt;
+  cudaError_t e = mcd::launch_history_ce_tq(c->dw, rp, grid, block, c->stream);
+  if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
+  c->launches++;
+  for (int r = 0; r < mcd::kTqRounds; r++) {
+    mcd::ParkRec* in = r % 2 == 0 ? A : B;
+    mcd::ParkRec* out = r % 2 == 0 ? B : A;
+    e = mcd::launch_sample_tsl_mlp_queue(c->mlp[0], c->mlp[1], c->mlp_box, qin, cnt + r, n, qout, c->num_sms,
+                                         c->stream);
+    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("surrogate launch: ") + cudaGetErrorString(e));
+    rp.tq = r + 1 < mcd::kTqRounds ? 1 : 0;
+    rp.head = heads + r;
+    rp.n_resume = cnt + r;
+    rp.park_in = in;
+    rp.park_out = out;
+    rp.park_count = cnt + r + 1;
+    e = mcd::launch_history_ce_tq(c->dw, rp, grid, block, c->stream);
+    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("transport launch: ") + cudaGetErrorString(e));
+    c->launches += 2;
   }
   return MC_OK;
 }
@@ -971,6 +1044,17 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
   rp.from_bank = 0;
   rp.ref_source_seeds = 1;
   rp.max_yield = c->max_yield;
+  if (o && o->thermal == MC_THERMAL_SURROGATE) {
+    if (c->model.energy_mode != mc::kContinuous || rng != MC_RNG_PHILOX)
+      return fail(c, MC_ERR_INPUT, "the surrogate thermal sampler needs a continuous-energy problem and Philox streams");
+    if (c->mlp_tsl < 0) return fail(c, MC_ERR_STATE, "no trained surrogate (mc_train_surrogate)");
+    if (!c->model.perturbations.empty())
+      return fail(c, MC_ERR_INPUT, "the surrogate thermal sampler does not carry indirect effects");
+    rp.tq = 1;  // run_transport takes the queue form
+  }
+  else if (o && o->thermal != MC_THERMAL_POD) {
+    return fail(c, MC_ERR_INPUT, "unknown thermal sampler");
+  }
   if (out && out->history_events) {
     rp.hist_events = static_cast<uint32_t*>(scratch(c, kHistEvents, n * 4));
     if (!rp.hist_events) return fail(c, MC_ERR_OOM, "history buffer");
@@ -1160,6 +1244,158 @@ int mc_keig_end(mc_ctx* c, mc_keig_out* out) {
   const int rc = mc_keig_status(c, out);
   if (rc != MC_OK) return rc;
   c->keig.active = false;
+  return MC_OK;
+}
+
+// ---- checkpoint / resume of a k-eigenvalue run -----------------------------
+// Between cycles a run is fully described by its options, the cycle number,
+// the per-cycle k / bank-size history, the counters, the tallies and the
+// next cycle's source bank: every random stream of a later cycle is keyed by
+// (seed, cycle) (Philox) or seeded from seed + cycle * n (minstd), so nothing
+// else carries over.
+
+namespace {
+
+constexpr char kCkptMagic[8] = {'M', 'C', 'K', 'E', 'I', 'G', '1', 0};
+
+struct CkptHeader {
+  char magic[8];
+  uint64_t n, seed, total_bins, max_yield, fingerprint;
+  uint32_t inactive, act, cycle, max_events;
+  int32_t rng, fast, block, schedule;
+  uint64_t events, lost, capped, overflow;
+  double transport_ms, kernel_ms;
+  uint64_t ncycles;
+};
+static_assert(offsetof(CkptHeader, cycle) == 56, "the Python reader expects the cycle number at byte 56");
+
+// FNV-1a over the problem's shape and names: a checkpoint resumes only into
+// the problem it was taken from
+uint64_t model_fingerprint(const mc::Model& m) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p, size_t n) {
+    const auto* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+  };
+  const int64_t dims[] = {m.energy_mode, static_cast<int64_t>(m.groups), static_cast<int64_t>(m.cells.size()),
+                          static_cast<int64_t>(m.surfaces.size()), static_cast<int64_t>(m.materials.size()),
+                          static_cast<int64_t>(m.nuclides.size()), static_cast<int64_t>(m.estimators.size()),
+                          static_cast<int64_t>(m.total_bins()), m.problem, m.tracking};
+  mix(dims, sizeof dims);
+  for (const auto& x : m.cells) mix(x.name.data(), x.name.size() + 1);
+  for (const auto& x : m.materials) {
+    mix(x.name.data(), x.name.size() + 1);
+    mix(&x.number_density, sizeof x.number_density);
+  }
+  for (const auto& x : m.nuclides) mix(x.name.data(), x.name.size() + 1);
+  for (const auto& x : m.estimators) mix(x.name.data(), x.name.size() + 1);
+  return h;
+}
+
+}  // namespace
+
+int mc_keig_checkpoint(mc_ctx* c, void* buf, uint64_t cap, uint64_t* size) {
+  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "no k-eigenvalue run in progress");
+  auto& k = c->keig;
+  const uint64_t nc = k.k.size();
+  const uint64_t tb = c->total_bins;
+  const uint64_t bytes = sizeof(CkptHeader) + nc * (8 + 8 + 8) + 2 * tb * 8 + k.n * sizeof(Site);
+  if (size) *size = bytes;
+  if (!buf) return MC_OK;
+  if (cap < bytes) return fail(c, MC_ERR_OVERFLOW, "checkpoint buffer too small");
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.n = k.n;
+  h.seed = k.seed;
+  h.total_bins = tb;
+  h.max_yield = c->max_yield;
+  h.fingerprint = model_fingerprint(c->model);
+  h.inactive = k.inactive;
+  h.act = k.act;
+  h.cycle = k.cycle;
+  h.max_events = k.max_events;
+  h.rng = k.rng;
+  h.fast = k.fast;
+  h.block = k.block;
+  h.schedule = k.schedule;
+  h.events = k.events;
+  h.lost = k.lost;
+  h.capped = k.capped;
+  h.overflow = k.overflow;
+  h.transport_ms = k.transport_ms;
+  h.kernel_ms = k.kernel_ms;
+  h.ncycles = nc;
+  auto* out = static_cast<char*>(buf);
+  std::memcpy(out, &h, sizeof h);
+  out += sizeof h;
+  std::memcpy(out, k.k.data(), nc * 8);
+  out += nc * 8;
+  std::memcpy(out, k.ktl.data(), nc * 8);
+  out += nc * 8;
+  std::memcpy(out, k.bank.data(), nc * 8);
+  out += nc * 8;
+  CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sum, tb * 8, cudaMemcpyDeviceToHost, c->stream));
+  out += tb * 8;
+  CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sq, tb * 8, cudaMemcpyDeviceToHost, c->stream));
+  out += tb * 8;
+  CUDA_TRY(c, cudaMemcpyAsync(out, c->scratch[kSrc].p, k.n * sizeof(Site), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return MC_OK;
+}
+
+int mc_keig_resume(mc_ctx* c, const void* buf, uint64_t size) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (!buf || size < sizeof(CkptHeader)) return fail(c, MC_ERR_INPUT, "checkpoint too short");
+  CkptHeader h;
+  std::memcpy(&h, buf, sizeof h);
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0) return fail(c, MC_ERR_INPUT, "not a k-eigenvalue checkpoint");
+  const uint64_t bytes = sizeof(CkptHeader) + h.ncycles * 24 + 2 * h.total_bins * 8 + h.n * sizeof(Site);
+  if (h.n == 0 || h.ncycles != h.cycle || size != bytes) return fail(c, MC_ERR_INPUT, "corrupt checkpoint");
+  if (h.fingerprint != model_fingerprint(c->model) || h.total_bins != c->total_bins || h.max_yield != c->max_yield)
+    return fail(c, MC_ERR_INPUT, "checkpoint belongs to another problem");
+  cudaSetDevice(c->device);
+  auto& k = c->keig;
+  k = decltype(c->keig){};
+  k.n = h.n;
+  k.seed = h.seed;
+  k.inactive = h.inactive;
+  k.act = h.act;
+  k.cycle = h.cycle;
+  k.max_events = h.max_events;
+  k.rng = h.rng;
+  k.fast = h.fast;
+  k.block = h.block;
+  k.schedule = h.schedule;
+  k.events = h.events;
+  k.lost = h.lost;
+  k.capped = h.capped;
+  k.overflow = h.overflow;
+  k.transport_ms = h.transport_ms;
+  k.kernel_ms = h.kernel_ms;
+  k.launches0 = c->launches;
+  const char* in = static_cast<const char*>(buf) + sizeof h;
+  k.k.assign(reinterpret_cast<const double*>(in), reinterpret_cast<const double*>(in) + h.ncycles);
+  in += h.ncycles * 8;
+  k.ktl.assign(reinterpret_cast<const double*>(in), reinterpret_cast<const double*>(in) + h.ncycles);
+  in += h.ncycles * 8;
+  k.bank.assign(reinterpret_cast<const uint64_t*>(in), reinterpret_cast<const uint64_t*>(in) + h.ncycles);
+  in += h.ncycles * 8;
+  // the variants give identical results, so the resumed run keeps the
+  // current one rather than tuning again
+  c->tune_pending = false;
+  if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
+      !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
+    return fail(c, MC_ERR_OOM, "k-eigenvalue bank allocation failed");
+  const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_sum, in, h.total_bins * 8, cudaMemcpyHostToDevice, c->stream));
+  in += h.total_bins * 8;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_sq, in, h.total_bins * 8, cudaMemcpyHostToDevice, c->stream));
+  in += h.total_bins * 8;
+  CUDA_TRY(c, cudaMemcpyAsync(c->scratch[kSrc].p, in, k.n * sizeof(Site), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  k.active = true;
   return MC_OK;
 }
 

@@ -97,15 +97,40 @@ __device__ __forceinline__ bool ce_tsl_valid(const DevWorld& w, const mc::CENucl
   return t >= 0 && type == 0 && E < w.tsl[t].cutoff_energy;
 }
 
+// ThermalScattering::GetTotal is a pure function of (library, E, T) and the
+// history loop asks for it several times per event (flight, nuclide choice,
+// reaction choice) at the same arguments: one value per particle is kept.
+// The reference recomputes it; the memo returns the identical double.
+// In fast mode (Philox streams, FP32 sampling arithmetic) the memo also
+// selects the FP32 rank sums.
+struct TslMemo {
+  int t = -1;
+  bool fast32 = false;
+  double E = 0, T = 0, v = 0;
+};
+
+__device__ __forceinline__ double tsl_total_memo(const DevWorld& w, int ti, double E, double T, TslMemo* memo) {
+  if (memo && memo->t == ti && memo->E == E && memo->T == T) return memo->v;
+  const double v = memo && memo->fast32 ? tsl_total_fast(w.tsl[ti], E, T) : tsl_total(w.tsl[ti], E, T);
+  if (memo) {
+    memo->t = ti;
+    memo->E = E;
+    memo->T = T;
+    memo->v = v;
+  }
+  return v;
+}
+
 // ContinuousReaction::GetCrossSection (majorant = false) or GetMajorant
 // (majorant = true).  T is the temperature the free-gas rules use (the
 // particle's, or the cell's maximum for majorants); T_pos is the particle's
 // (thermal scattering totals).
 __device__ __forceinline__ double ce_reaction_xs(const DevWorld& w, const mc::CENuclideDesc& d, int k, int type,
-                                                 int j, double E, double T, double T_pos, bool majorant) {
+                                                 int j, double E, double T, double T_pos, bool majorant,
+                                                 TslMemo* memo = nullptr) {
   if (d.rx_kind[k] == 1 && ce_tsl_valid(w, d, k, type, E)) {
-    const DevTSL& t = w.tsl[d.rx_tsl[k]];
-    return majorant ? tsl_majorant(t, E) : tsl_total(t, E, T_pos);
+    if (majorant) return tsl_majorant(w.tsl[d.rx_tsl[k]], E);
+    return tsl_total_memo(w, d.rx_tsl[k], E, T_pos, memo);
   }
   const double xs = ce_table_at(w.ce, d.rx_table[k], j, E);
   if (d.rx_kind[k] != 1) return xs;
@@ -117,24 +142,25 @@ __device__ __forceinline__ double ce_reaction_xs(const DevWorld& w, const mc::CE
 
 // Continuous::GetTotal / GetMajorant (src/Continuous.cpp:26-58)
 __device__ __forceinline__ double ce_nuclide_total(const DevWorld& w, const mc::CENuclideDesc& d, int type, int j,
-                                                   double E, double T, double T_pos, bool majorant) {
+                                                   double E, double T, double T_pos, bool majorant,
+                                                   TslMemo* memo = nullptr) {
   bool modifies = false;  // Continuous::ReactionsModifyTotal
   for (int k = 0; k < d.n_rx; k++) modifies |= d.rx_kind[k] == 1 && ce_tsl_valid(w, d, k, type, E);
   if (!modifies && ce_valid(d.total_T, T)) return ce_table_at(w.ce, d.total, j, E);
   double acc = 0;
-  for (int k = 0; k < d.n_rx; k++) acc = dadd(acc, ce_reaction_xs(w, d, k, type, j, E, T, T_pos, majorant));
+  for (int k = 0; k < d.n_rx; k++) acc = dadd(acc, ce_reaction_xs(w, d, k, type, j, E, T, T_pos, majorant, memo));
   return acc;
 }
 
 // Material::GetMicroscopicTotal (or Majorant) in the reference's summation
 // order
 __device__ __forceinline__ double ce_material_micro(const DevWorld& w, int mat, int type, int j, double E, double T,
-                                                    double T_pos, bool majorant) {
+                                                    double T_pos, bool majorant, TslMemo* memo = nullptr) {
   const int nb = __ldg(w.mat_begin + mat), ne = __ldg(w.mat_begin + mat + 1);
   double acc = 0;
   for (int i = nb; i < ne; i++)
-    acc = dadd(acc, dmul(__ldg(w.mat_afrac + i),
-                         ce_nuclide_total(w, ce_desc(w, type, __ldg(w.mat_nuc + i)), type, j, E, T, T_pos, majorant)));
+    acc = dadd(acc, dmul(__ldg(w.mat_afrac + i), ce_nuclide_total(w, ce_desc(w, type, __ldg(w.mat_nuc + i)), type, j,
+                                                                  E, T, T_pos, majorant, memo)));
   return acc;
 }
 

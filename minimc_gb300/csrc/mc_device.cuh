@@ -124,6 +124,8 @@ struct DevTSL {
   const double* xs_Em;        // [xs_nE][xs_rank]
   const double* xs_Tm;        // [xs_nT][xs_rank]
   const double* xs_S;         // [xs_rank]
+  const float* xs_EmS_f;      // [xs_nE][xs_rank] S[o] * Em[E][o] in FP32 (fast-mode totals)
+  const float* xs_Tm_f;       // [xs_nT][xs_rank]
   const double* maj_x;        // majorant ContinuousMap
   const double* maj_y;
   DevPOD beta, alpha;

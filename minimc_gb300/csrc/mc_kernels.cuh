@@ -28,6 +28,32 @@ struct FissionRec {
 // most tally bins kept densely per history; more bins use a per-thread list
 constexpr int kDenseBins = 64;
 
+// Thermal-scatter queue (surrogate sampler).  A fixed-source particle whose
+// collision is a thermal scatter of the surrogate's library, inside its
+// trained (E, T) box, is parked: its state goes to a ParkRec and its
+// sampler inputs (E, T and two uniforms from its own stream) to a float4
+// row; the history kernel moves on.  One batched tensor-core launch samples
+// (beta, alpha) for all parked rows, and a resume launch of the history
+// kernel applies each outcome and continues the particle.
+constexpr int kParkPending = 4;  // pending tally bins a parked history may carry
+constexpr int kTqRounds = 6;     // park/sample/resume rounds; the last resume samples inline
+
+struct ParkRec {
+  double x, y, z, u, v, w, E, T;
+  unsigned long long hist;
+  unsigned long long rng_id;   // Philox counter words h0 | h1 << 32
+  int32_t cell, surf, skip, type;
+  uint32_t nev, hist_nev;
+  uint32_t rng_pos;            // PhiloxRng::save()
+  uint32_t rng_tag;
+  int32_t fate;                // history fate so far
+  int32_t flags;               // bit 0: dropped secondaries
+  int32_t pend_n;              // pending tally entries (<= kParkPending); bit 8: overflow
+  int32_t tsl;
+  uint32_t pend_bin[kParkPending];
+  double pend_score[kParkPending];
+};
+
 struct RunParams {
   unsigned long long n;        // source particles (histories)
   unsigned long long seed;     // run seed
@@ -53,6 +79,18 @@ struct RunParams {
   double* pend;        // dense per-history scores [n][nb] when nb <= kDenseBins
   int32_t nb;
   FissionRec* fis;     // k-eigenvalue fission records [n]
+  // thermal-scatter queue (continuous-energy fixed source, Philox streams)
+  int32_t tq;                          // 1: park thermal scatters of library tq_tsl inside tq_box
+  int32_t tq_tsl;
+  double tq_box[4];                    // E min, E max (MeV), T min, T max (K)
+  unsigned long long* head;            // queue head of this launch (null: &ctr->next)
+  const unsigned long long* n_resume;  // resume launch: parked records to continue (device count)
+  const ParkRec* park_in;
+  const float2* tq_out;                // (beta, alpha) per parked record; NaN: sample inline
+  ParkRec* park_out;
+  float4* tq_in;                       // (E, T, u1, u2) per parked record
+  unsigned long long* park_count;      // records parked by this launch
+  unsigned long long park_cap;
 };
 
 // k-eigenvalue sites from fission records and the per-history commit of
@@ -106,6 +144,9 @@ bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast);
 cudaError_t launch_history_ce(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, int block,
                               cudaStream_t stream, int variant);
 int history_blocks_per_sm_ce(const DevWorld& w, int rng_mode, int block, bool keig, bool fast, int variant);
+// fixed source with the thermal-scatter queue (Philox streams, exact tables):
+// a source launch (rp.n_resume null) or a resume launch
+cudaError_t launch_history_ce_tq(const DevWorld& w, const RunParams& rp, int grid, int block, cudaStream_t stream);
 cudaError_t launch_fission_sites_ce(const RunParams& rp, int rng_mode, int grid, cudaStream_t stream);
 
 // thermal scattering sampler and totals (mc_tsl.cu); rng_mode 1 = minstd

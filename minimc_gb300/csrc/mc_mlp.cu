@@ -746,16 +746,35 @@ __device__ __forceinline__ void write_x(Group& G, const float (&x)[kMlpIn]) {
   *reinterpret_cast<uint4*>(X + tc::tile_offset(G.lt, 8, kMlpIn)) = *reinterpret_cast<uint4*>(h + 4);
 }
 
-__global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* tsl, NetView nb, NetView na,
-                                                                  MlpBox box, const double* E, const double* T,
-                                                                  unsigned long long n, unsigned long long key,
-                                                                  double* beta_out, double* alpha_out,
-                                                                  unsigned long long* failures, int* err) {
+// inputs and outputs of one sampler launch: the array API (E, T per row,
+// Philox uniforms keyed by the row, POD fallback outside the box) or the
+// thermal-scatter queue (E, T and the particle's own two uniforms per row;
+// rows are inside the box by construction, outputs in FP32)
+struct SampleIO {
+  const DevTSL* tsl;
+  const double* E;
+  const double* T;
+  unsigned long long n;
+  unsigned long long key;
+  double* beta_out;
+  double* alpha_out;
+  unsigned long long* failures;
+  const float4* qin;                 // queue form
+  const unsigned long long* qcount;
+  unsigned long long qcap;
+  float2* qout;
+};
+
+template <bool QUEUE>
+__global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(NetView nb, NetView na, MlpBox box, SampleIO io,
+                                                                  int* err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   float* fb = reinterpret_cast<float*>(smem + kOffF);
   float* fa = fb + 4 * kMlpWidth + 4;
   uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kOffMisc);  // [0..3] two mbarriers, [4] tensor memory
   const int tid = threadIdx.x, warp = tid >> 5;
+  const unsigned long long n = QUEUE ? (*io.qcount < io.qcap ? *io.qcount : io.qcap) : io.n;
+  if (n == 0) return;  // uniform across the grid: nothing allocated yet
   // weights into shared memory
   load_tile(smem + kOffB1, nb.W1, kMlpIn);
   load_tile(smem + kOffB2, nb.W2, kMlpWidth);
@@ -802,50 +821,85 @@ __global__ void __launch_bounds__(128 * kGroups, 1) k_mlp_sample(const DevTSL* t
        tile += stride) {
     const unsigned long long i = tile * 128 + G.lt;
     const bool valid = i < n;
-    const double ed = valid ? E[i] : Emin;
-    const double td = valid ? T[i] : box.T0;
-    const bool in_box = ed >= Emin && ed <= Emax && td >= box.T0 && td <= box.T1;
-    // rows outside the box keep the tile's arithmetic finite and are resampled below
-    const float e = in_box ? static_cast<float>(ed) : Eminf;
-    const float t = in_box ? static_cast<float>(td) : T0f;
+    float e, t, u1, u2;
+    bool in_box = true;
     PhiloxRng rng;
-    rng.init(key, i, 3);
+    if constexpr (QUEUE) {
+      const float4 q = valid ? io.qin[i] : make_float4(Eminf, T0f, 0.5f, 0.5f);
+      e = q.x;
+      t = q.y;
+      u1 = q.z;
+      u2 = q.w;
+    }
+    else {
+      const double ed = valid ? io.E[i] : Emin;
+      const double td = valid ? io.T[i] : box.T0;
+      in_box = ed >= Emin && ed <= Emax && td >= box.T0 && td <= box.T1;
+      // rows outside the box keep the tile's arithmetic finite and are resampled below
+      e = in_box ? static_cast<float>(ed) : Eminf;
+      t = in_box ? static_cast<float>(td) : T0f;
+      rng.init(io.key, i, 3);
+      u1 = rng.u01f();
+      u2 = rng.u01f();
+    }
     float x[kMlpIn];
-    beta_features(bf, e, t, rng.u01f(), x);
+    beta_features(bf, e, t, u1, x);
     write_x(G, x);
     const float qb = run_net(G, kOffB1, kOffB2, kOffB3, fb);
     const float bmin = beta_min_of(bf, e, t);
     const float b = fmaf(fminf(1.0f, fmaxf(0.0f, qb)), bf.beta_cutoff - bmin, bmin);
-    alpha_features(bf, e, t, b, rng.u01f(), x);
+    alpha_features(bf, e, t, b, u2, x);
     write_x(G, x);
     const float qa = run_net(G, kOffA1, kOffA2, kOffA3, fa);
     float lo, hi;
     alpha_range(bf, e, t, b, lo, hi);
-    double bo = b, ao = fmaf(fminf(1.0f, fmaxf(0.0f, qa)), hi - lo, lo);
-    if (valid && !in_box) {
-      // outside the trained box: the POD sampler (FP32 form when the ranks fit)
-      const double eo = E[i], to = T[i];
-      bool ok = tsl->fast_ok ? tsl_sample_beta<true>(*tsl, rng, eo, to, bo) : tsl_sample_beta<false>(*tsl, rng, eo, to, bo);
-      if (ok) ok = tsl->fast_ok ? tsl_sample_alpha<true>(*tsl, rng, bo, eo, to, ao)
-                                : tsl_sample_alpha<false>(*tsl, rng, bo, eo, to, ao);
-      if (!ok) {
-        bo = ao = CUDART_NAN;
-        my_fail++;
-      }
+    const float a = fmaf(fminf(1.0f, fmaxf(0.0f, qa)), hi - lo, lo);
+    if constexpr (QUEUE) {
+      if (valid) io.qout[i] = make_float2(b, a);
     }
-    if (valid) {
-      beta_out[i] = bo;
-      alpha_out[i] = ao;
+    else {
+      double bo = b, ao = a;
+      if (valid && !in_box) {
+        // outside the trained box: the POD sampler (FP32 form when the ranks fit)
+        const double eo = io.E[i], to = io.T[i];
+        const DevTSL* tsl = io.tsl;
+        bool ok = tsl->fast_ok ? tsl_sample_beta<true>(*tsl, rng, eo, to, bo)
+                               : tsl_sample_beta<false>(*tsl, rng, eo, to, bo);
+        if (ok) ok = tsl->fast_ok ? tsl_sample_alpha<true>(*tsl, rng, bo, eo, to, ao)
+                                  : tsl_sample_alpha<false>(*tsl, rng, bo, eo, to, ao);
+        if (!ok) {
+          bo = ao = CUDART_NAN;
+          my_fail++;
+        }
+      }
+      if (valid) {
+        io.beta_out[i] = bo;
+        io.alpha_out[i] = ao;
+      }
     }
   }
   if (!G.ok && G.lt == 0) atomicExch(err, 1);
-  if (my_fail) atomicAdd(failures, my_fail);
+  if constexpr (!QUEUE) {
+    if (my_fail) atomicAdd(io.failures, my_fail);
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_dealloc(misc[4], 128 * kGroups);
   }
+}
+
+template <bool QUEUE>
+cudaError_t sample_attr() {
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_mlp_sample<QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSampleSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -855,19 +909,41 @@ cudaError_t launch_sample_tsl_mlp(const DevTSL* tsl, const MlpNet& beta_net, con
                                   unsigned long long key, double* beta, double* alpha, unsigned long long* failures,
                                   int num_sms, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(k_mlp_sample, cudaFuncAttributeMaxDynamicSharedMemorySize, kSampleSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = sample_attr<false>();
+  if (e != cudaSuccess) return e;
   const unsigned long long tiles = (n + 127) / 128;
   const unsigned long long want = (tiles + kGroups - 1) / kGroups;
   const unsigned grid = static_cast<unsigned>(want < static_cast<unsigned long long>(num_sms) ? want : num_sms);
   NetView nb{beta_net.p, beta_net.W1, beta_net.W2, beta_net.W3};
   NetView na{alpha_net.p, alpha_net.W1, alpha_net.W2, alpha_net.W3};
-  k_mlp_sample<<<grid, 128 * kGroups, kSampleSmem, s>>>(tsl, nb, na, box, E, T, n, key, beta, alpha, failures,
-                                                         mlp_err_ptr());
+  SampleIO io{};
+  io.tsl = tsl;
+  io.E = E;
+  io.T = T;
+  io.n = n;
+  io.key = key;
+  io.beta_out = beta;
+  io.alpha_out = alpha;
+  io.failures = failures;
+  k_mlp_sample<false><<<grid, 128 * kGroups, kSampleSmem, s>>>(nb, na, box, io, mlp_err_ptr());
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_tsl_mlp_queue(const MlpNet& beta_net, const MlpNet& alpha_net, const MlpBox& box,
+                                        const float4* qin, const unsigned long long* count, unsigned long long cap,
+                                        float2* qout, int num_sms, cudaStream_t s) {
+  if (cap == 0) return cudaSuccess;
+  cudaError_t e = sample_attr<true>();
+  if (e != cudaSuccess) return e;
+  NetView nb{beta_net.p, beta_net.W1, beta_net.W2, beta_net.W3};
+  NetView na{alpha_net.p, alpha_net.W1, alpha_net.W2, alpha_net.W3};
+  SampleIO io{};
+  io.qin = qin;
+  io.qcount = count;
+  io.qcap = cap;
+  io.qout = qout;
+  // the row count is known on the device only: one persistent CTA per SM
+  k_mlp_sample<true><<<num_sms, 128 * kGroups, kSampleSmem, s>>>(nb, na, box, io, mlp_err_ptr());
   return cudaGetLastError();
 }
 

@@ -89,6 +89,13 @@ cudaError_t launch_sample_tsl_mlp(const DevTSL* tsl, const MlpNet& beta_net, con
                                   unsigned long long key, double* beta, double* alpha, unsigned long long* failures,
                                   int num_sms, cudaStream_t s);
 
+// the same networks on the thermal-scatter queue: rows (E, T, u1, u2) of
+// parked particles, *count of them (at most cap, read on the device), to
+// (beta, alpha) in FP32
+cudaError_t launch_sample_tsl_mlp_queue(const MlpNet& beta_net, const MlpNet& alpha_net, const MlpBox& box,
+                                        const float4* qin, const unsigned long long* count, unsigned long long cap,
+                                        float2* qout, int num_sms, cudaStream_t s);
+
 // training data: inputs and quantile targets from POD samples
 cudaError_t launch_mlp_features_beta(const MlpBox& box, const double* E, const double* T, const double* u,
                                      const double* beta, unsigned long long n, __nv_bfloat16* X, float* y,

@@ -172,6 +172,37 @@ __device__ __forceinline__ double tsl_total(const DevTSL& t, double E, double T)
   return dadd(xs_T_lo, dmul(r_T, dsub(xs_T_hi, xs_T_lo)));
 }
 
+// GetTotal's form for fast-mode transport: the same brackets and weights,
+// the rank sums in FP32
+__device__ __forceinline__ float tsl_inelastic_f(const DevTSL& t, int E_i, int T_i) {
+  const int r = t.xs_rank;
+  const float* a = t.xs_EmS_f + static_cast<size_t>(E_i) * r;
+  const float* b = t.xs_Tm_f + static_cast<size_t>(T_i) * r;
+  float acc = 0.0f;
+  for (int o = 0; o < r; o++) acc = fmaf(__ldg(a + o), __ldg(b + o), acc);
+  return acc;
+}
+
+__device__ __forceinline__ double tsl_total_fast(const DevTSL& t, double E, double T) {
+  const int E_hi_i = upper_index(t.xs_E, t.xs_nE, E);
+  if (E_hi_i == t.xs_nE) return CUDART_NAN;
+  const bool below_E_min = E_hi_i == 0;
+  const int E_lo_i = below_E_min ? E_hi_i : E_hi_i - 1;
+  const int cand = upper_index(t.xs_T, t.xs_nT, T);
+  const bool above_T_max = cand == t.xs_nT;
+  const int T_hi_i = above_T_max ? cand - 1 : cand;
+  const bool below_T_min = T_hi_i == 0;
+  const int T_lo_i = below_T_min ? T_hi_i : T_hi_i - 1;
+  const float a = tsl_inelastic_f(t, E_lo_i, T_lo_i), b = tsl_inelastic_f(t, E_lo_i, T_hi_i);
+  const float c = tsl_inelastic_f(t, E_hi_i, T_lo_i), d = tsl_inelastic_f(t, E_hi_i, T_hi_i);
+  const double E_lo = __ldg(t.xs_E + E_lo_i), E_hi = __ldg(t.xs_E + E_hi_i);
+  const float r_E = below_E_min ? 1.0f : static_cast<float>((E - E_lo) / (E_hi - E_lo));
+  const float lo = fmaf(r_E, c - a, a), hi = fmaf(r_E, d - b, b);
+  const double T_lo = __ldg(t.xs_T + T_lo_i), T_hi = __ldg(t.xs_T + T_hi_i);
+  const float r_T = below_T_min ? 1.0f : above_T_max ? 0.0f : static_cast<float>((T - T_lo) / (T_hi - T_lo));
+  return static_cast<double>(fmaf(r_T, hi - lo, lo));
+}
+
 // ThermalScattering::GetMajorant: ContinuousMap::at on the majorant table
 __device__ __forceinline__ double tsl_majorant(const DevTSL& t, double E) {
   const int hi = upper_index(t.maj_x, t.maj_n, E);

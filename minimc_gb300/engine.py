@@ -33,6 +33,7 @@ ERRORS = {
 RNG_PHILOX, RNG_MINSTD = 0, 1
 SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT = 0, 1, 2
 TSL_POD, TSL_MLP = 0, 1
+THERMAL_POD, THERMAL_SURROGATE = 0, 1  # run option `thermal` (MC_THERMAL_*)
 TSL_PHILOX, TSL_FAST = 0x10, 0x20  # method flags: Philox streams, FP32 POD form
 GEOMETRY_ROBUST, GEOMETRY_REFERENCE = 0, 1
 
@@ -52,7 +53,7 @@ class RunOpts(C.Structure):
     _fields_ = [("histories", C.c_uint64), ("seed", C.c_uint64), ("inactive", C.c_uint32),
                 ("active", C.c_uint32), ("rng", C.c_int32), ("schedule", C.c_int32),
                 ("max_events", C.c_uint32), ("block_size", C.c_int32), ("fast_math", C.c_int32),
-                ("variant", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("variant", C.c_int32), ("thermal", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Site(C.Structure):
@@ -147,6 +148,8 @@ _SIGNATURES = {
     "mc_keig_cycle": (C.c_int, [_P, C.c_int32, _D]),
     "mc_keig_end": (C.c_int, [_P, C.POINTER(KeigOut)]),
     "mc_keig_status": (C.c_int, [_P, C.POINTER(KeigOut)]),
+    "mc_keig_checkpoint": (C.c_int, [_P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "mc_keig_resume": (C.c_int, [_P, C.c_void_p, C.c_uint64]),
     "mc_schedule_info": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_int32), _D, C.c_int32]),
     "mc_transport_bank": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(RunOpts), _P, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -224,6 +227,11 @@ def format_output(xml_text: str, base_dir, sum, sum_sq, batchsize: int, total_we
     if rc != 0:
         raise MCError(rc, buf.value.decode())
     return buf.value.decode()
+
+
+# byte offset of the cycle number in a k-eigenvalue checkpoint (after the
+# 8-byte magic, five uint64 fields and two uint32 fields)
+_CKPT_CYCLE_OFFSET = 8 + 5 * 8 + 2 * 4
 
 
 def _dptr(a: np.ndarray):
@@ -356,6 +364,53 @@ class Context:
         out = KeigOut()
         self.check(self.lib.mc_keig_status(self.h, C.byref(out)))
         return out
+
+    def keig_checkpoint(self) -> bytes:
+        """The state of the k-eigenvalue run between cycles (mc_keig_checkpoint)."""
+        n = C.c_uint64()
+        self.check(self.lib.mc_keig_checkpoint(self.h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self.check(self.lib.mc_keig_checkpoint(self.h, buf, n.value, C.byref(n)))
+        return buf.raw[: n.value]
+
+    def keig_resume(self, state: bytes):
+        """Continues a run from keig_checkpoint's bytes (replaces keig_begin)."""
+        self.check(self.lib.mc_keig_resume(self.h, state, len(state)))
+
+    def run_keigenvalue_checkpointed(self, path, every: int = 1, **kw) -> KeigResult:
+        """run_keigenvalue that writes a checkpoint file after every `every`
+        cycles and, when `path` already holds one for this problem, resumes
+        from it instead of starting over."""
+        p = Path(path)
+        o = self.opts(**kw)
+        inactive = o.inactive if (o.inactive or o.active) else self.info.inactive
+        active = o.active if (o.inactive or o.active) else self.info.active
+        done = 0
+        if p.exists():
+            state = p.read_bytes()
+            self.keig_resume(state)
+            done = int(np.frombuffer(state, np.uint32, count=1, offset=_CKPT_CYCLE_OFFSET)[0])
+        else:
+            self.keig_begin(**kw)
+        ncyc = inactive + active
+        for c in range(done, ncyc):
+            self.keig_cycle(c >= inactive)
+            if (c + 1) % every == 0 and c + 1 < ncyc:
+                tmp = p.with_suffix(p.suffix + ".tmp")
+                tmp.write_bytes(self.keig_checkpoint())
+                os.replace(tmp, p)
+        k = np.zeros(ncyc)
+        bank = np.zeros(ncyc, np.uint64)
+        nb = max(1, self.info.total_bins)
+        s, s2 = np.zeros(nb), np.zeros(nb)
+        out = KeigOut()
+        out.k_cycle = _dptr(k)
+        out.bank_size = bank.ctypes.data_as(C.POINTER(C.c_uint64))
+        out.sum = _dptr(s)
+        out.sum_sq = _dptr(s2)
+        self.check(self.lib.mc_keig_end(self.h, C.byref(out)))
+        return KeigResult(MC_OK, k, bank, s[: self.info.total_bins], s2[: self.info.total_bins], out,
+                          inactive, active)
 
     def schedule_info(self) -> dict:
         s, v, g, b = (C.c_int32() for _ in range(4))

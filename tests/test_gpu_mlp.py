@@ -16,7 +16,8 @@ import numpy as np
 import pytest
 from scipy import stats
 
-from minimc_gb300 import MLP_PARAMS, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context, synth_tsl
+from minimc_gb300 import (MLP_PARAMS, RNG_PHILOX, THERMAL_SURROGATE, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context,
+                          synth_tsl)
 
 pytestmark = pytest.mark.gpu
 EV = 1e-6
@@ -162,3 +163,38 @@ def test_fallback_outside_box(trained):
     pb, pa, _ = ctx.sample_tsl(0, E, 450.0, seed=5, method=TSL_POD | TSL_PHILOX)
     assert stats.ks_2samp(mb, pb).pvalue > 1e-3
     assert stats.ks_2samp(ma, pa).pvalue > 1e-3
+
+
+def spectra(ctx, r):
+    """Leakage energy and cosine marginals (counts) of the broomstick tally."""
+    e = ctx.estimators()[0]
+    t = r.sum[e.offset:e.offset + e.n_bins].reshape(int(e.cosine_bins), int(e.energy_bins))
+    return t.sum(0), t.sum(1)
+
+
+def test_surrogate_in_transport(trained):
+    """Thermal-scatter queue: the broomstick transported with the surrogate
+    sampler (parked particles, one tensor-core launch per round) against the
+    POD sampler inside the history kernel: the same events per history, no
+    lost particles, and leakage energy / cosine spectra within 0.02 in CDF."""
+    ctx, _, _ = trained
+    n = 400_000
+    pod = ctx.run_fixed_source(rng=RNG_PHILOX, histories=n, seed=5)
+    sur = ctx.run_fixed_source(rng=RNG_PHILOX, histories=n, seed=6, thermal=THERMAL_SURROGATE)
+    assert sur.raw.lost == 0 and sur.raw.resample_failures == 0 and sur.raw.capped == 0
+    assert abs(sur.raw.events / n - pod.raw.events / n) < 0.02
+    # leakage probability (most histories leak once after one scatter)
+    ls, lp = sur.sum.sum() / n, pod.sum.sum() / n
+    assert abs(ls - lp) < 5 * math.sqrt(2 * lp * (1 - lp) / n) + 1e-6, (ls, lp)
+    for a, b in zip(spectra(ctx, sur), spectra(ctx, pod)):
+        d = np.abs(np.cumsum(a) / a.sum() - np.cumsum(b) / b.sum()).max()
+        assert d < 0.02, d
+    # the queue really served the scatters: more launches than the POD form
+    assert sur.raw.launches > pod.raw.launches
+
+
+def test_surrogate_transport_reproducible(trained):
+    ctx, _, _ = trained
+    a = ctx.run_fixed_source(rng=RNG_PHILOX, histories=50_000, seed=9, thermal=THERMAL_SURROGATE)
+    b = ctx.run_fixed_source(rng=RNG_PHILOX, histories=50_000, seed=9, thermal=THERMAL_SURROGATE)
+    assert np.array_equal(a.sum, b.sum) and a.raw.events == b.raw.events
