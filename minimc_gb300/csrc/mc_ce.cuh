@@ -202,43 +202,6 @@ __device__ __forceinline__ UnionPos ce_union_pos(const DevCE& ce, int j, double 
 __device__ __forceinline__ float lerpf(float lo, float hi, float f) { return __fmaf_rn(f, __fsub_rn(hi, lo), lo); }
 
 // ---------------------------------------------------------------------------
-// directions in FP32 (fast form): Direction(d, mu, phi) with phi drawn as
-// (U - 1/2) 2 pi, normalized in FP32
-__device__ __forceinline__ void rotate_f(float& dx, float& dy, float& dz, float mu, float uphi) {
-  const bool off_x = dx <= 0.9f && dx > -0.9f;
-  float ux, uy, uz;
-  if (off_x) {  // d x (1, 0, 0)
-    ux = 0.0f;
-    uy = dz;
-    uz = -dy;
-  }
-  else {  // d x (0, 1, 0)
-    ux = -dz;
-    uy = 0.0f;
-    uz = dx;
-  }
-  const float ru = __frsqrt_rn(__fmaf_rn(ux, ux, __fmaf_rn(uy, uy, __fmul_rn(uz, uz))));
-  ux = __fmul_rn(ux, ru);
-  uy = __fmul_rn(uy, ru);
-  uz = __fmul_rn(uz, ru);
-  // v = d x u
-  const float vx = __fsub_rn(__fmul_rn(dy, uz), __fmul_rn(dz, uy));
-  const float vy = __fsub_rn(__fmul_rn(dz, ux), __fmul_rn(dx, uz));
-  const float vz = __fsub_rn(__fmul_rn(dx, uy), __fmul_rn(dy, ux));
-  float s, c;
-  __sincosf(__fmul_rn(__fsub_rn(uphi, 0.5f), 6.28318530717958647692f), &s, &c);
-  const float st = __fsqrt_rn(fmaxf(0.0f, __fmaf_rn(-mu, mu, 1.0f)));
-  const float a = __fmul_rn(st, c), b = __fmul_rn(st, s);
-  const float rx = __fmaf_rn(a, ux, __fmaf_rn(b, vx, __fmul_rn(mu, dx)));
-  const float ry = __fmaf_rn(a, uy, __fmaf_rn(b, vy, __fmul_rn(mu, dy)));
-  const float rz = __fmaf_rn(a, uz, __fmaf_rn(b, vz, __fmul_rn(mu, dz)));
-  const float rn = __frsqrt_rn(__fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz))));
-  dx = __fmul_rn(rx, rn);
-  dy = __fmul_rn(ry, rn);
-  dz = __fmul_rn(rz, rn);
-}
-
-// ---------------------------------------------------------------------------
 // free-gas elastic scattering (ContinuousScatter::Interact without a thermal
 // scattering library).  The target speed x (in units of 1/beta) and the
 // cosine mu between neutron and target velocities are sampled by rejection

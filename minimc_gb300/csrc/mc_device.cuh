@@ -655,6 +655,43 @@ __device__ __forceinline__ int cdf_first_above(const double* cdf, int n, double 
   return -1;
 }
 
+// directions in FP32 (fast form): Direction(d, mu, phi) with phi drawn as
+// (U - 1/2) 2 pi, normalized in FP32
+__device__ __forceinline__ void rotate_f(float& dx, float& dy, float& dz, float mu, float uphi) {
+  const bool off_x = dx <= 0.9f && dx > -0.9f;
+  float ux, uy, uz;
+  if (off_x) {  // d x (1, 0, 0)
+    ux = 0.0f;
+    uy = dz;
+    uz = -dy;
+  }
+  else {  // d x (0, 1, 0)
+    ux = -dz;
+    uy = 0.0f;
+    uz = dx;
+  }
+  const float ru = __frsqrt_rn(__fmaf_rn(ux, ux, __fmaf_rn(uy, uy, __fmul_rn(uz, uz))));
+  ux = __fmul_rn(ux, ru);
+  uy = __fmul_rn(uy, ru);
+  uz = __fmul_rn(uz, ru);
+  // v = d x u
+  const float vx = __fsub_rn(__fmul_rn(dy, uz), __fmul_rn(dz, uy));
+  const float vy = __fsub_rn(__fmul_rn(dz, ux), __fmul_rn(dx, uz));
+  const float vz = __fsub_rn(__fmul_rn(dx, uy), __fmul_rn(dy, ux));
+  float s, c;
+  __sincosf(__fmul_rn(__fsub_rn(uphi, 0.5f), 6.28318530717958647692f), &s, &c);
+  const float st = __fsqrt_rn(fmaxf(0.0f, __fmaf_rn(-mu, mu, 1.0f)));
+  const float a = __fmul_rn(st, c), b = __fmul_rn(st, s);
+  const float rx = __fmaf_rn(a, ux, __fmaf_rn(b, vx, __fmul_rn(mu, dx)));
+  const float ry = __fmaf_rn(a, uy, __fmaf_rn(b, vy, __fmul_rn(mu, dy)));
+  const float rz = __fmaf_rn(a, uz, __fmaf_rn(b, vz, __fmul_rn(mu, dz)));
+  const float rn = __frsqrt_rn(__fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz))));
+  dx = __fmul_rn(rx, rn);
+  dy = __fmul_rn(ry, rn);
+  dz = __fmul_rn(rz, rn);
+}
+
+
 // Direction(d, mu, phi) (src/Point.cpp:98-121), normalized on assignment
 __device__ __forceinline__ void rotate(double& dx, double& dy, double& dz, double mu, double phi) {
   const bool off_x = dx <= kOnAxisTolerance && dx > -kOnAxisTolerance;

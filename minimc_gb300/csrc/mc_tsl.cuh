@@ -17,6 +17,8 @@
 
 #include "mc_device.cuh"
 
+#include <type_traits>
+
 namespace mcd {
 
 constexpr int kTslResampleLimit = 10;  // constants::beta/alpha_resample_limit
@@ -115,6 +117,25 @@ __device__ __forceinline__ double pod_eval_fast(const PodAt& c, const PodVec& gv
   for (int o = 0; o < kFastPodRank; o++)
     if (o < c.r) acc = __fmaf_rn(__ldg(C + o), gv.v[o], acc);
   return static_cast<double>(acc);
+}
+
+// Arithmetic around the reconstructions: the reference's FP64 operations in
+// the exact form; FP32 in the fast form (the reconstructions there are FP32
+// already), with FP32 uniforms from Philox streams.
+template <bool FAST>
+__device__ __forceinline__ double sdiv(double a, double b) {
+  if constexpr (FAST) return static_cast<double>(__fdiv_rn(__double2float_rn(a), __double2float_rn(b)));
+  else return ddiv(a, b);
+}
+template <bool FAST>
+__device__ __forceinline__ double ssqrt(double a) {
+  if constexpr (FAST) return static_cast<double>(__fsqrt_rn(__double2float_rn(a)));
+  else return __dsqrt_rn(a);
+}
+template <bool FAST, class Rng>
+__device__ __forceinline__ double su01(Rng& rng) {
+  if constexpr (FAST && std::is_same_v<Rng, PhiloxRng>) return static_cast<double>(rng.u01f());
+  else return rng.u01();
 }
 
 // partition holding global grid index i (upper_bound over the ends)
@@ -221,10 +242,10 @@ __device__ __forceinline__ bool tsl_sample_beta(const DevTSL& t, Rng& rng, doubl
   const int n = P.n_grid;
   const int E_hi_i = upper_index(P.grid, n, E);
   if (E_hi_i == n) return false;  // E at or above the cutoff (asserted by the reference)
-  const double r = E_hi_i != 0 ? ddiv(dsub(E, __ldg(P.grid + E_hi_i - 1)),
-                                      dsub(__ldg(P.grid + E_hi_i), __ldg(P.grid + E_hi_i - 1)))
+  const double r = E_hi_i != 0 ? sdiv<FAST>(dsub(E, __ldg(P.grid + E_hi_i - 1)),
+                                            dsub(__ldg(P.grid + E_hi_i), __ldg(P.grid + E_hi_i - 1)))
                                : 1.0;
-  const int E_s_i = r <= rng.u01() ? E_hi_i - 1 : E_hi_i;
+  const int E_s_i = r <= su01<FAST>(rng) ? E_hi_i - 1 : E_hi_i;
   const double E_s = __ldg(P.grid + E_s_i);
   int local;
   const int ps = pod_partition(P, E_s_i, local);
@@ -233,14 +254,14 @@ __device__ __forceinline__ bool tsl_sample_beta(const DevTSL& t, Rng& rng, doubl
   const int nF = ev.c.nF;
   const double kT = dmul(kBoltzmann, T);
   for (int res = 0; res < kTslResampleLimit; res++) {
-    const double F = rng.u01();
+    const double F = su01<FAST>(rng);
     const int F_hi_i = upper_index(ev.c.F, nF, F);
     const double F_lo = F_hi_i != 0 ? __ldg(ev.c.F + F_hi_i - 1) : 0.0;
     const double F_hi = F_hi_i != nF ? __ldg(ev.c.F + F_hi_i) : 1.0;
-    const double b_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : ddiv(-E_s, kT);
+    const double b_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : sdiv<FAST>(-E_s, kT);
     const double b_hi = F_hi_i != nF ? ev(F_hi_i) : t.beta_cutoff;
-    const double b_prime = dadd(b_lo, dmul(ddiv(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(b_hi, b_lo)));
-    const double b_min = ddiv(-E, kT);
+    const double b_prime = dadd(b_lo, dmul(sdiv<FAST>(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(b_hi, b_lo)));
+    const double b_min = sdiv<FAST>(-E, kT);
     if (b_min <= b_prime) {
       beta = b_prime;
       return true;
@@ -250,12 +271,13 @@ __device__ __forceinline__ bool tsl_sample_beta(const DevTSL& t, Rng& rng, doubl
 }
 
 // (sqrt(E) -+ sqrt(E + b kT))^2 / (A kT): alpha bounds at beta b
+template <bool FAST>
 __device__ __forceinline__ void alpha_bounds(double sqrt_E, double E, double b, double T, double akT, double& a_min,
                                              double& a_max) {
-  const double s = __dsqrt_rn(dadd(E, dmul(dmul(b, kBoltzmann), T)));
+  const double s = ssqrt<FAST>(dadd(E, dmul(dmul(b, kBoltzmann), T)));
   const double lo = dsub(sqrt_E, s), hi = dadd(sqrt_E, s);
-  a_min = ddiv(dmul(lo, lo), akT);
-  a_max = ddiv(dmul(hi, hi), akT);
+  a_min = sdiv<FAST>(dmul(lo, lo), akT);
+  a_max = sdiv<FAST>(dmul(hi, hi), akT);
 }
 
 // ThermalScattering::SampleAlpha
@@ -270,7 +292,7 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
   if (b_hi_i == n) return false;  // betas.at() throws in the reference
   const double kT = dmul(kBoltzmann, T);
   const double g_hi = __ldg(P.grid + b_hi_i);
-  const bool snap_to_lower = (sgn_b == 1 && t.beta_cutoff <= g_hi) || (sgn_b == -1 && -g_hi < ddiv(-E, kT));
+  const bool snap_to_lower = (sgn_b == 1 && t.beta_cutoff <= g_hi) || (sgn_b == -1 && -g_hi < sdiv<FAST>(-E, kT));
   const bool snap_to_min = b_hi_i == 0;
   double r;
   if (snap_to_lower) r = 0.0;
@@ -279,15 +301,15 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
     // as written in the reference (src/ThermalScattering.cpp:363-365): the
     // division binds before the subtraction
     const double g_lo = __ldg(P.grid + b_hi_i - 1);
-    r = dsub(abs_b, ddiv(g_lo, dsub(g_hi, g_lo)));
+    r = dsub(abs_b, sdiv<FAST>(g_lo, dsub(g_hi, g_lo)));
   }
-  const int b_s_i = r <= rng.u01() ? b_hi_i - 1 : b_hi_i;
+  const int b_s_i = r <= su01<FAST>(rng) ? b_hi_i - 1 : b_hi_i;
   if (b_s_i < 0) return false;  // snapped below the first beta: betas.at() throws in the reference
   const double b_s = static_cast<double>(sgn_b) * __ldg(P.grid + b_s_i);
-  const double sqrt_E = __dsqrt_rn(E);
+  const double sqrt_E = ssqrt<FAST>(E);
   const double akT = dmul(dmul(t.awr, kBoltzmann), T);
   double b_s_a_min, b_s_a_max;
-  alpha_bounds(sqrt_E, E, b_s, T, akT, b_s_a_min, b_s_a_max);
+  alpha_bounds<FAST>(sqrt_E, E, b_s, T, akT, b_s_a_min, b_s_a_max);
   int local;
   const int ps = pod_partition(P, b_s_i, local);
   PodEval<FAST> ev;
@@ -312,22 +334,23 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
     const double F_a_hi = F_a_hi_i != nF ? __ldg(Fs + F_a_hi_i) : 1.0;
     const double a_lo = F_a_hi_i != 0 ? ev(F_a_hi_i - 1) : 0.0;
     const double a_hi = F_a_hi_i != nF ? ev(F_a_hi_i) : t.alpha_cutoff;
-    return dadd(F_a_lo, ddiv(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
+    return dadd(F_a_lo, sdiv<FAST>(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
   };
   const double F_min = find_cdf(b_s_a_min);
   const double F_max = find_cdf(b_s_a_max);
   for (int res = 0; res < kTslResampleLimit; res++) {
-    const double F = dadd(F_min, dmul(rng.u01(), dsub(F_max, F_min)));
+    const double F = dadd(F_min, dmul(su01<FAST>(rng), dsub(F_max, F_min)));
     const int F_hi_i = upper_index(Fs, nF, F);
     const double F_lo = F_hi_i != 0 ? __ldg(Fs + F_hi_i - 1) : 0.0;
     const double F_hi = F_hi_i != nF ? __ldg(Fs + F_hi_i) : 1.0;
     const double a_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : 0.0;
     const double a_hi = F_hi_i != nF ? ev(F_hi_i) : t.alpha_cutoff;
-    const double a_prime = dadd(a_lo, dmul(ddiv(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(a_hi, a_lo)));
+    const double a_prime = dadd(a_lo, dmul(sdiv<FAST>(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(a_hi, a_lo)));
     if (b_s_a_min < a_prime && a_prime < b_s_a_max) {
       double b_a_min, b_a_max;
-      alpha_bounds(sqrt_E, E, b, T, akT, b_a_min, b_a_max);
-      alpha = dadd(b_a_min, ddiv(dmul(dsub(a_prime, b_s_a_min), dsub(b_a_max, b_a_min)), dsub(b_s_a_max, b_s_a_min)));
+      alpha_bounds<FAST>(sqrt_E, E, b, T, akT, b_a_min, b_a_max);
+      alpha = dadd(b_a_min,
+                   sdiv<FAST>(dmul(dsub(a_prime, b_s_a_min), dsub(b_a_max, b_a_min)), dsub(b_s_a_max, b_s_a_min)));
       return true;
     }
   }
@@ -343,10 +366,24 @@ __device__ __forceinline__ bool tsl_scatter(const DevTSL& t, Rng& rng, double T,
   if (!tsl_sample_beta<FAST>(t, rng, E, T, beta)) return false;
   if (!tsl_sample_alpha<FAST>(t, rng, beta, E, T, alpha)) return false;
   const double E_p = dadd(E, dmul(dmul(beta, kBoltzmann), T));
-  const double mu = ddiv(dsub(dadd(E, E_p), dmul(dmul(dmul(alpha, t.awr), kBoltzmann), T)),
-                         dmul(2.0, __dsqrt_rn(dmul(E, E_p))));
-  const double phi = dmul(2 * kPi, rng.u01());
-  rotate(du, dv, dw, mu, phi);
+  if constexpr (FAST && std::is_same_v<Rng, PhiloxRng>) {
+    // E' and mu from the sampled pair, the direction in FP32
+    const float mu = fminf(1.0f, fmaxf(-1.0f, __fdiv_rn(__double2float_rn(dsub(dadd(E, E_p),
+                                                                                  dmul(dmul(dmul(alpha, t.awr),
+                                                                                            kBoltzmann), T))),
+                                                         __fmul_rn(2.0f, __fsqrt_rn(__double2float_rn(dmul(E, E_p)))))));
+    float dx = static_cast<float>(du), dy = static_cast<float>(dv), dz = static_cast<float>(dw);
+    rotate_f(dx, dy, dz, mu, rng.u01f());
+    du = dx;
+    dv = dy;
+    dw = dz;
+  }
+  else {
+    const double mu = ddiv(dsub(dadd(E, E_p), dmul(dmul(dmul(alpha, t.awr), kBoltzmann), T)),
+                           dmul(2.0, __dsqrt_rn(dmul(E, E_p))));
+    const double phi = dmul(2 * kPi, rng.u01());
+    rotate(du, dv, dw, mu, phi);
+  }
   E = E_p;
   return true;
 }
