@@ -1717,7 +1717,12 @@ std::vector<float> mlp_init_params(uint64_t seed, int used_inputs) {
   };
   const float a1 = 1.0f / std::sqrt(static_cast<float>(used_inputs)), a = 1.0f / std::sqrt(128.0f);
   for (int o = 0; o < mcd::kMlpWidth; o++)
-    for (int i = 0; i < used_inputs; i++) p[mcd::kMlpW1 + o * mcd::kMlpIn + i] = uni(a1);
+    for (int i = 0; i < used_inputs; i++) {
+      // input i and its residual (slot 8 + i, scaled by 256) start as one input
+      const float wi = uni(a1);
+      p[mcd::kMlpW1 + o * mcd::kMlpIn + i] = wi;
+      p[mcd::kMlpW1 + o * mcd::kMlpIn + 8 + i] = wi / 256.0f;
+    }
   for (int i = 0; i < mcd::kMlpWidth; i++) p[mcd::kMlpB1 + i] = uni(a1);
   for (int i = 0; i < mcd::kMlpWidth * mcd::kMlpWidth; i++) {
     p[mcd::kMlpW2 + i] = uni(a);

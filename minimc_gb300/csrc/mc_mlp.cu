@@ -20,7 +20,28 @@ namespace {
 using bf16 = __nv_bfloat16;
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s: an MMA never takes that long
 
-__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+// The activation is evaluated the same way in training and in the sampler,
+// so that the trained function is the one the sampler runs:
+//   hidden layers: packed BF16, silu(z) = h + h tanh(h) with h = z / 2, from
+//     the hardware's packed tanh (one MUFU operation per pair) and a packed
+//     fma -- the result is a BF16 activation either way;
+//   output layer: FP32, h + h tanh(h) with the FP32 hardware tanh.
+// Gradients use the derivative of the exact SiLU.
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float silu_h(float h) { return fmaf(h, tanh_approx(h), h); }
+__device__ __forceinline__ float silu_t(float z) { return silu_h(0.5f * z); }
+__device__ __forceinline__ __nv_bfloat162 silu2_bf16(float h0, float h1) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(h0, h1);
+  __nv_bfloat162 t;
+  asm("tanh.approx.bf16x2 %0, %1;"
+      : "=r"(*reinterpret_cast<uint32_t*>(&t))
+      : "r"(*reinterpret_cast<const uint32_t*>(&h)));
+  return __hfma2(h, t, h);
+}
 __device__ __forceinline__ float dsilu(float z) {
   const float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
@@ -131,14 +152,18 @@ struct EpiForward {
   int B;
   __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
-      if (j < ncol) {
+    for (int j = 0; j < 32; j += 2) {
+      if (j < ncol) {  // ncol is even (N = 128)
         const int c = col0 + j;
-        const float z = v[j] + bias[c];
-        const float h = silu(z);
-        Z[static_cast<size_t>(row) * kMlpWidth + c] = z;
-        H[static_cast<size_t>(row) * kMlpWidth + c] = __float2bfloat16_rn(h);
-        if (Ht) Ht[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(h);
+        const float z0 = v[j] + bias[c], z1 = v[j + 1] + bias[c + 1];
+        const __nv_bfloat162 h = silu2_bf16(0.5f * z0, 0.5f * z1);
+        Z[static_cast<size_t>(row) * kMlpWidth + c] = z0;
+        Z[static_cast<size_t>(row) * kMlpWidth + c + 1] = z1;
+        *reinterpret_cast<__nv_bfloat162*>(H + static_cast<size_t>(row) * kMlpWidth + c) = h;
+        if (Ht) {
+          Ht[static_cast<size_t>(c) * B + row] = h.x;
+          Ht[static_cast<size_t>(c + 1) * B + row] = h.y;
+        }
       }
     }
   }
@@ -195,7 +220,7 @@ __global__ void __launch_bounds__(128) k_head(const float* Z3, const float* p, c
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
   float out = p[kMlpB4];
-  for (int j = 0; j < kMlpWidth; j++) out += silu(z[j]) * p[kMlpW4 + j];
+  for (int j = 0; j < kMlpWidth; j++) out = fmaf(silu_t(z[j]), p[kMlpW4 + j], out);
   const float e = out - y[r];
   const float go = 2.0f * e / static_cast<float>(B);
   const float se = warp_sum(e * e);
@@ -209,7 +234,7 @@ __global__ void __launch_bounds__(128) k_head(const float* Z3, const float* p, c
     const float dz = go * p[kMlpW4 + j] * dsilu(zj);
     dZ3[static_cast<size_t>(r) * kMlpWidth + j] = __float2bfloat16_rn(dz);
     dZ3t[static_cast<size_t>(j) * B + r] = __float2bfloat16_rn(dz);
-    const float a = warp_sum(go * silu(zj));  // dW4
+    const float a = warp_sum(go * silu_t(zj));  // dW4
     const float b = warp_sum(dz);             // db3
     if (lane == 0) {
       red[warp][j] = a;
@@ -229,7 +254,7 @@ __global__ void k_head_forward(const float* Z3, const float* p, int B, float* ou
   if (r >= B) return;
   const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
   float o = p[kMlpB4];
-  for (int j = 0; j < kMlpWidth; j++) o += silu(z[j]) * p[kMlpW4 + j];
+  for (int j = 0; j < kMlpWidth; j++) o = fmaf(silu_t(z[j]), p[kMlpW4 + j], o);
   out[r] = o;
 }
 
@@ -408,9 +433,27 @@ __device__ __forceinline__ void alpha_range(const BoxF& b, float E, float T, flo
   hi = (r + s) * (r + s) * inv;
 }
 
-__device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* row) {
+// The features enter the first product as BF16; each used feature k is
+// split into its BF16 value (slot k) and the residual scaled by 256 (slot
+// 8 + k), so the product sees about 16 significant bits of it (a BF16 input
+// alone would quantise E, T and the uniform to 2^-8 relative).
+constexpr int kMlpFeatures = 6;
+__device__ __forceinline__ void split_features(const float (&f)[kMlpIn], bf16 (&x)[kMlpIn]) {
 #pragma unroll
-  for (int i = 0; i < kMlpIn; i++) row[i] = __float2bfloat16_rn(f[i]);
+  for (int i = 0; i < kMlpIn; i++) x[i] = __float2bfloat16_rn(0.0f);
+#pragma unroll
+  for (int k = 0; k < kMlpFeatures; k++) {
+    const bf16 hi = __float2bfloat16_rn(f[k]);
+    x[k] = hi;
+    x[8 + k] = __float2bfloat16_rn((f[k] - __bfloat162float(hi)) * 256.0f);
+  }
+}
+
+__device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* row) {
+  bf16 x[kMlpIn];
+  split_features(f, x);
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) row[i] = x[i];
 }
 
 // training targets: quantile positions of sorted samples within their
@@ -618,20 +661,6 @@ constexpr uint32_t kOffMisc = kOffF + 2 * (4 * kMlpWidth + 4) * 4;
 constexpr uint32_t kSampleSmem = kOffMisc + 64;
 static_assert(kSampleSmem <= 227 * 1024, "shared memory");
 
-// SiLU of two pre-activations at once, in BF16 (the precision of the hidden
-// tiles it feeds): with h = z / 2, silu(z) = h + h tanh(h), using the
-// hardware's packed BF16 tanh (one MUFU operation per pair) and a packed
-// BF16 fma.  The caller passes h (the half-scaled accumulator plus the
-// half-scaled bias) in FP32.
-__device__ __forceinline__ __nv_bfloat162 silu2_bf16(float h0, float h1) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(h0, h1);
-  __nv_bfloat162 t;
-  asm("tanh.approx.bf16x2 %0, %1;"
-      : "=r"(*reinterpret_cast<uint32_t*>(&t))
-      : "r"(*reinterpret_cast<const uint32_t*>(&h)));
-  return __hfma2(h, t, h);
-}
-
 // warpgroup barrier (named barrier 1 + g, 128 threads) and its AND vote
 __device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
 __device__ __forceinline__ bool wg_all(int g, bool v) {
@@ -718,12 +747,7 @@ __device__ __forceinline__ float output_epilogue(Group& G, const float* f) {
     float v[32];
     tc::tmem_ld32(G.tmem + (static_cast<uint32_t>(w * 32) << 16) + c * 32, v);
 #pragma unroll
-    for (int j = 0; j < 32; j += 2) {
-      const float2 a = __bfloat1622float2(
-          silu2_bf16(fmaf(v[j], 0.5f, b3[c * 32 + j]), fmaf(v[j + 1], 0.5f, b3[c * 32 + j + 1])));
-      out = fmaf(a.x, w4[c * 32 + j], out);
-      out = fmaf(a.y, w4[c * 32 + j + 1], out);
-    }
+    for (int j = 0; j < 32; j++) out = fmaf(silu_h(fmaf(v[j], 0.5f, b3[c * 32 + j])), w4[c * 32 + j], out);
   }
   return out;
 }
@@ -737,10 +761,15 @@ __device__ __forceinline__ float run_net(Group& G, uint32_t w1, uint32_t w2, uin
   return output_epilogue(G, f);
 }
 
-__device__ __forceinline__ void write_x(Group& G, const float (&x)[kMlpIn]) {
+__device__ __forceinline__ void write_x(Group& G, const float (&f)[kMlpIn]) {
+  bf16 x[kMlpIn];
+  split_features(f, x);
   __align__(16) __nv_bfloat162 h[kMlpIn / 2];
 #pragma unroll
-  for (int i = 0; i < kMlpIn / 2; i++) h[i] = __floats2bfloat162_rn(x[2 * i], x[2 * i + 1]);
+  for (int i = 0; i < kMlpIn / 2; i++) {
+    h[i].x = x[2 * i];
+    h[i].y = x[2 * i + 1];
+  }
   uint8_t* X = G.base + G.X;
   *reinterpret_cast<uint4*>(X + tc::tile_offset(G.lt, 0, kMlpIn)) = *reinterpret_cast<uint4*>(h);
   *reinterpret_cast<uint4*>(X + tc::tile_offset(G.lt, 8, kMlpIn)) = *reinterpret_cast<uint4*>(h + 4);

@@ -217,10 +217,12 @@ __device__ __forceinline__ double tsl_total_fast(const DevTSL& t, double E, doub
   const float a = tsl_inelastic_f(t, E_lo_i, T_lo_i), b = tsl_inelastic_f(t, E_lo_i, T_hi_i);
   const float c = tsl_inelastic_f(t, E_hi_i, T_lo_i), d = tsl_inelastic_f(t, E_hi_i, T_hi_i);
   const double E_lo = __ldg(t.xs_E + E_lo_i), E_hi = __ldg(t.xs_E + E_hi_i);
-  const float r_E = below_E_min ? 1.0f : static_cast<float>((E - E_lo) / (E_hi - E_lo));
+  const float r_E = below_E_min ? 1.0f : __fdiv_rn(__double2float_rn(E - E_lo), __double2float_rn(E_hi - E_lo));
   const float lo = fmaf(r_E, c - a, a), hi = fmaf(r_E, d - b, b);
   const double T_lo = __ldg(t.xs_T + T_lo_i), T_hi = __ldg(t.xs_T + T_hi_i);
-  const float r_T = below_T_min ? 1.0f : above_T_max ? 0.0f : static_cast<float>((T - T_lo) / (T_hi - T_lo));
+  const float r_T = below_T_min  ? 1.0f
+                    : above_T_max ? 0.0f
+                                  : __fdiv_rn(__double2float_rn(T - T_lo), __double2float_rn(T_hi - T_lo));
   return static_cast<double>(fmaf(r_T, hi - lo, lo));
 }
 

@@ -1,9 +1,9 @@
 """GPU MLP surrogate of the thermal scattering sampler, through the C ABI.
 
 * Forward outputs and the full parameter gradient of one training step
-  (tcgen05 BF16 products, FP32 accumulation) against a CPU reference that
-  applies the same BF16 roundings in FP64 arithmetic, and against plain
-  FP64 (loose tolerance).
+  (tcgen05 BF16 products, FP32 accumulation, packed-BF16 hidden SiLU)
+  against a CPU reference that applies the same BF16 roundings in FP64
+  arithmetic, and against plain FP64 (loose tolerance).
 * Training on POD samples of the synthetic library, then sampling: beta and
   alpha distributions against the POD sampler (KS distance, 200-bin
   chi-square at C4's energies with T uniform per sample), the fallback
@@ -46,6 +46,14 @@ def silu(z):
     return z / (1 + np.exp(-z))
 
 
+def silu_bf16(z):
+    """Hidden activations as the kernels form them: h = bf16(z / 2), then the
+    packed BF16 tanh and fma h + h tanh(h), rounded to BF16."""
+    h = bf16(np.asarray(z) / 2)
+    t = bf16(np.tanh(h))
+    return bf16(h + h * t)
+
+
 def dsilu(z):
     s = 1 / (1 + np.exp(-z))
     return s * (1 + z * (1 - s))
@@ -58,10 +66,11 @@ def reference(p, x, y, emulate=True):
     W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p)
     n = len(x)
     X = q(x)
+    act = silu_bf16 if emulate else silu
     Z1 = X @ q(W1).T + b1
-    H1 = q(silu(Z1))
+    H1 = act(Z1)
     Z2 = H1 @ q(W2).T + b2
-    H2 = q(silu(Z2))
+    H2 = act(Z2)
     Z3 = H2 @ q(W3).T + b3
     out = silu(Z3) @ w4 + b4
     e = out - y
