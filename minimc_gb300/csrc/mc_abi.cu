@@ -1655,9 +1655,9 @@ bool mlp_net_alloc(mc_ctx* c, mcd::MlpNet& n) {
   n.g = mlp_alloc<float>(c, mcd::kMlpParams);
   n.m = mlp_alloc<float>(c, mcd::kMlpParams);
   n.v = mlp_alloc<float>(c, mcd::kMlpParams);
-  n.W1 = mlp_alloc<bf>(c, W * mcd::kMlpIn);
-  n.W2 = mlp_alloc<bf>(c, W * W);
-  n.W3 = mlp_alloc<bf>(c, W * W);
+  n.W1 = mlp_alloc<__half>(c, W * mcd::kMlpIn);
+  n.W2 = mlp_alloc<__half>(c, W * W);
+  n.W3 = mlp_alloc<__half>(c, W * W);
   n.W2t = mlp_alloc<bf>(c, W * W);
   n.W3t = mlp_alloc<bf>(c, W * W);
   return n.p && n.g && n.m && n.v && n.W1 && n.W2 && n.W3 && n.W2t && n.W3t;
@@ -1671,14 +1671,14 @@ bool mlp_batch_alloc(mc_ctx* c, int B) {
   using bf = __nv_bfloat16;
   mcd::MlpBatch& b = c->mlp_batch;
   const size_t n = static_cast<size_t>(B), W = mcd::kMlpWidth;
-  b.X = mlp_alloc<bf>(c, n * mcd::kMlpIn);
+  b.X = mlp_alloc<__half>(c, n * mcd::kMlpIn);
   b.Xt = mlp_alloc<bf>(c, n * mcd::kMlpIn);
   b.y = mlp_alloc<float>(c, n);
   b.Z1 = mlp_alloc<float>(c, n * W);
   b.Z2 = mlp_alloc<float>(c, n * W);
   b.Z3 = mlp_alloc<float>(c, n * W);
-  b.H1 = mlp_alloc<bf>(c, n * W);
-  b.H2 = mlp_alloc<bf>(c, n * W);
+  b.H1 = mlp_alloc<__half>(c, n * W);
+  b.H2 = mlp_alloc<__half>(c, n * W);
   b.H1t = mlp_alloc<bf>(c, n * W);
   b.H2t = mlp_alloc<bf>(c, n * W);
   b.dZ3 = mlp_alloc<bf>(c, n * W);
@@ -1718,10 +1718,10 @@ std::vector<float> mlp_init_params(uint64_t seed, int used_inputs) {
   const float a1 = 1.0f / std::sqrt(static_cast<float>(used_inputs)), a = 1.0f / std::sqrt(128.0f);
   for (int o = 0; o < mcd::kMlpWidth; o++)
     for (int i = 0; i < used_inputs; i++) {
-      // input i and its residual (slot 8 + i, scaled by 256) start as one input
+      // input i and its residual (slot 8 + i, scaled by 2048) start as one input
       const float wi = uni(a1);
       p[mcd::kMlpW1 + o * mcd::kMlpIn + i] = wi;
-      p[mcd::kMlpW1 + o * mcd::kMlpIn + 8 + i] = wi / 256.0f;
+      p[mcd::kMlpW1 + o * mcd::kMlpIn + 8 + i] = wi / 2048.0f;
     }
   for (int i = 0; i < mcd::kMlpWidth; i++) p[mcd::kMlpB1 + i] = uni(a1);
   for (int i = 0; i < mcd::kMlpWidth * mcd::kMlpWidth; i++) {
@@ -1739,7 +1739,7 @@ std::vector<float> mlp_init_params(uint64_t seed, int used_inputs) {
 
 // one network trained on (X, y) by Adam with a cosine-decayed rate; returns
 // the mean squared error over the last 5 % of the steps
-int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __nv_bfloat16* X, const float* y, uint64_t n, int used_inputs,
+int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __half* X, const float* y, uint64_t n, int used_inputs,
               const mc_train_desc& d, uint64_t key, double* loss_out) {
   const std::vector<float> p0 = mlp_init_params(key, used_inputs);
   CUDA_TRY(c, cudaMemcpyAsync(net.p, p0.data(), p0.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -1867,7 +1867,7 @@ int mc_train_surrogate(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_tra
   auto* U = static_cast<double*>(dalloc(N * 8));
   auto* bx = static_cast<double*>(dalloc(N * 8));
   auto* sx = static_cast<double*>(dalloc(N * 8));
-  auto* X = static_cast<__nv_bfloat16*>(dalloc(N * mcd::kMlpIn * 2));
+  auto* X = static_cast<__half*>(dalloc(N * mcd::kMlpIn * 2));
   auto* y = static_cast<float*>(dalloc(N * 4));
   auto* d_fail = static_cast<unsigned long long*>(dalloc(8));
   if (!(Ec && Tc && bc && Ex && Tx && U && bx && sx && X && y && d_fail)) {
@@ -2010,11 +2010,13 @@ int mc_surrogate_grad(mc_ctx* c, const float* params, const float* x, const floa
     return fail(c, MC_ERR_OOM, "surrogate buffers");
   mcd::MlpBatch b = c->mlp_batch;
   b.B = static_cast<int>(n);
-  std::vector<__nv_bfloat16> hx(n * mcd::kMlpIn), hxt(n * mcd::kMlpIn);
+  // forward input in FP16, its transpose (weight gradients) in BF16
+  std::vector<__half> hx(n * mcd::kMlpIn);
+  std::vector<__nv_bfloat16> hxt(n * mcd::kMlpIn);
   for (uint64_t r = 0; r < n; r++)
     for (int f = 0; f < mcd::kMlpIn; f++) {
-      hx[r * mcd::kMlpIn + f] = __float2bfloat16_rn(x[r * mcd::kMlpIn + f]);
-      hxt[f * n + r] = hx[r * mcd::kMlpIn + f];
+      hx[r * mcd::kMlpIn + f] = __float2half_rn(x[r * mcd::kMlpIn + f]);
+      hxt[f * n + r] = __float2bfloat16_rn(__half2float(hx[r * mcd::kMlpIn + f]));
     }
   const mcd::MlpNet& net = c->mlp_scratch;
   CUDA_TRY(c, cudaMemcpyAsync(net.p, params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream));

@@ -13,18 +13,21 @@
 #include "mc_tc.cuh"
 #include "mc_tsl.cuh"
 
+#include <type_traits>
+
 namespace mcd {
 
 namespace {
 
 using bf16 = __nv_bfloat16;
+using f16 = __half;
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s: an MMA never takes that long
 
 // The activation is evaluated the same way in training and in the sampler,
 // so that the trained function is the one the sampler runs:
-//   hidden layers: packed BF16, silu(z) = h + h tanh(h) with h = z / 2, from
+//   hidden layers: packed FP16, silu(z) = h + h tanh(h) with h = z / 2, from
 //     the hardware's packed tanh (one MUFU operation per pair) and a packed
-//     fma -- the result is a BF16 activation either way;
+//     fma -- the result is an FP16 activation either way;
 //   output layer: FP32, h + h tanh(h) with the FP32 hardware tanh.
 // Gradients use the derivative of the exact SiLU.
 __device__ __forceinline__ float tanh_approx(float x) {
@@ -34,10 +37,10 @@ __device__ __forceinline__ float tanh_approx(float x) {
 }
 __device__ __forceinline__ float silu_h(float h) { return fmaf(h, tanh_approx(h), h); }
 __device__ __forceinline__ float silu_t(float z) { return silu_h(0.5f * z); }
-__device__ __forceinline__ __nv_bfloat162 silu2_bf16(float h0, float h1) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(h0, h1);
-  __nv_bfloat162 t;
-  asm("tanh.approx.bf16x2 %0, %1;"
+__device__ __forceinline__ __half2 silu2_f16(float h0, float h1) {
+  const __half2 h = __floats2half2_rn(h0, h1);
+  __half2 t;
+  asm("tanh.approx.f16x2 %0, %1;"
       : "=r"(*reinterpret_cast<uint32_t*>(&t))
       : "r"(*reinterpret_cast<const uint32_t*>(&h)));
   return __hfma2(h, t, h);
@@ -59,15 +62,15 @@ __device__ __forceinline__ float warp_sum(float v) {
 // KC columns at a time through shared memory; the accumulator lives in
 // tensor memory and is handed to the epilogue row by row.
 struct GemmArgs {
-  const bf16* A;
+  const uint16_t* A;  // 16-bit operands: FP16 (forward) or BF16 (backward)
   int lda;
-  const bf16* B;
+  const uint16_t* B;
   int ldb;
   int k_split;  // K per CTA (multiple of KC)
   int* err;     // set when an MMA wait timed out
 };
 
-template <int N, int KC, class Epi>
+template <int N, int KC, class Epi, bool F16>
 __global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
   static_assert(N % 16 == 0 && N >= 16 && N <= 128, "N");
   static_assert(KC % 16 == 0 && KC <= 64, "KC");
@@ -86,7 +89,7 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   const uint32_t mb = tc::smem_addr(&mbar);
-  constexpr uint32_t idesc = tc::idesc_bf16_f32(128, N);
+  constexpr uint32_t idesc = F16 ? tc::idesc_f16_f32(128, N) : tc::idesc_bf16_f32(128, N);
   uint32_t phase = 0;
   bool ok = true;
   for (int k0 = 0; k0 < a.k_split && ok; k0 += KC) {
@@ -143,11 +146,12 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
   }
 }
 
-// z = acc + bias; keeps Z (FP32), H = SiLU(z) in BF16 and optionally H^T
+// z = acc + bias; keeps Z (FP32) and optionally H = SiLU(z) (FP16, the next
+// forward operand) and H^T (BF16, for the weight gradients)
 struct EpiForward {
   const float* bias;
   float* Z;
-  bf16* H;
+  f16* H;
   bf16* Ht;
   int B;
   __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
@@ -156,13 +160,15 @@ struct EpiForward {
       if (j < ncol) {  // ncol is even (N = 128)
         const int c = col0 + j;
         const float z0 = v[j] + bias[c], z1 = v[j + 1] + bias[c + 1];
-        const __nv_bfloat162 h = silu2_bf16(0.5f * z0, 0.5f * z1);
         Z[static_cast<size_t>(row) * kMlpWidth + c] = z0;
         Z[static_cast<size_t>(row) * kMlpWidth + c + 1] = z1;
-        *reinterpret_cast<__nv_bfloat162*>(H + static_cast<size_t>(row) * kMlpWidth + c) = h;
-        if (Ht) {
-          Ht[static_cast<size_t>(c) * B + row] = h.x;
-          Ht[static_cast<size_t>(c + 1) * B + row] = h.y;
+        if (H) {
+          const __half2 h = silu2_f16(0.5f * z0, 0.5f * z1);
+          *reinterpret_cast<__half2*>(H + static_cast<size_t>(row) * kMlpWidth + c) = h;
+          if (Ht) {
+            Ht[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(__low2float(h));
+            Ht[static_cast<size_t>(c + 1) * B + row] = __float2bfloat16_rn(__high2float(h));
+          }
         }
       }
     }
@@ -203,11 +209,13 @@ struct EpiAtomic {
   }
 };
 
-template <int N, int KC, class Epi>
-cudaError_t gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int K, int splits, int* err, const Epi& epi,
+template <int N, int KC, class Epi, class T>
+cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int K, int splits, int* err, const Epi& epi,
                  cudaStream_t s) {
-  GemmArgs a{A, lda, B, ldb, K / splits, err};
-  k_gemm<N, KC, Epi><<<dim3(M / 128, 1, splits), 128, 0, s>>>(a, epi);
+  static_assert(sizeof(T) == 2, "16-bit operands");
+  constexpr bool kF16 = std::is_same_v<T, f16>;
+  GemmArgs a{reinterpret_cast<const uint16_t*>(A), lda, reinterpret_cast<const uint16_t*>(B), ldb, K / splits, err};
+  k_gemm<N, KC, Epi, kF16><<<dim3(M / 128, 1, splits), 128, 0, s>>>(a, epi);
   return cudaGetLastError();
 }
 
@@ -270,14 +278,14 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int n, floa
   p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
 }
 
-// BF16 weight copies (and transposes) from the FP32 master weights
-__global__ void k_refresh(const float* p, bf16* W1, bf16* W2, bf16* W3, bf16* W2t, bf16* W3t) {
+// FP16 forward weight copies and BF16 transposes from the FP32 master weights
+__global__ void k_refresh(const float* p, f16* W1, f16* W2, f16* W3, bf16* W2t, bf16* W3t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < kMlpWidth * kMlpIn) W1[i] = __float2bfloat16_rn(p[kMlpW1 + i]);
+  if (i < kMlpWidth * kMlpIn) W1[i] = __float2half_rn(p[kMlpW1 + i]);
   if (i < kMlpWidth * kMlpWidth) {
     const int r = i / kMlpWidth, c = i % kMlpWidth;
-    W2[i] = __float2bfloat16_rn(p[kMlpW2 + i]);
-    W3[i] = __float2bfloat16_rn(p[kMlpW3 + i]);
+    W2[i] = __float2half_rn(p[kMlpW2 + i]);
+    W3[i] = __float2half_rn(p[kMlpW3 + i]);
     W2t[c * kMlpWidth + r] = __float2bfloat16_rn(p[kMlpW2 + i]);
     W3t[c * kMlpWidth + r] = __float2bfloat16_rn(p[kMlpW3 + i]);
   }
@@ -310,7 +318,7 @@ cudaError_t mlp_forward(const MlpNet& net, const MlpBatch& b, float* out, cudaSt
                          EpiForward{net.p + kMlpB2, b.Z2, b.H2, nullptr, b.B}, s)) != cudaSuccess)
     return e;
   if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, b.B, kMlpWidth, 1, err,
-                         EpiForward{net.p + kMlpB3, b.Z3, b.H1, nullptr, b.B}, s)) != cudaSuccess)
+                         EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, b.B}, s)) != cudaSuccess)
     return e;
   k_head_forward<<<(b.B + 127) / 128, 128, 0, s>>>(b.Z3, net.p, b.B, out);
   return cudaGetLastError();
@@ -332,7 +340,7 @@ cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStrea
     return e;
   // Z3 only (H3 is recomputed from Z3 by the head)
   if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, 1, err,
-                         EpiForward{net.p + kMlpB3, b.Z3, b.dZ3, nullptr, B}, s)) != cudaSuccess)
+                         EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, B}, s)) != cudaSuccess)
     return e;
   k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -433,24 +441,25 @@ __device__ __forceinline__ void alpha_range(const BoxF& b, float E, float T, flo
   hi = (r + s) * (r + s) * inv;
 }
 
-// The features enter the first product as BF16; each used feature k is
-// split into its BF16 value (slot k) and the residual scaled by 256 (slot
-// 8 + k), so the product sees about 16 significant bits of it (a BF16 input
-// alone would quantise E, T and the uniform to 2^-8 relative).
+// The features enter the first product as FP16; each used feature k is
+// split into its FP16 value (slot k) and the residual scaled by 2048 (slot
+// 8 + k), so the product sees the FP32 feature to about 22 significant
+// bits (one FP16 input would quantise E, T and the uniform to 2^-11).
 constexpr int kMlpFeatures = 6;
-__device__ __forceinline__ void split_features(const float (&f)[kMlpIn], bf16 (&x)[kMlpIn]) {
+constexpr float kResidualScale = 2048.0f;
+__device__ __forceinline__ void split_features(const float (&f)[kMlpIn], f16 (&x)[kMlpIn]) {
 #pragma unroll
-  for (int i = 0; i < kMlpIn; i++) x[i] = __float2bfloat16_rn(0.0f);
+  for (int i = 0; i < kMlpIn; i++) x[i] = __float2half_rn(0.0f);
 #pragma unroll
   for (int k = 0; k < kMlpFeatures; k++) {
-    const bf16 hi = __float2bfloat16_rn(f[k]);
+    const f16 hi = __float2half_rn(f[k]);
     x[k] = hi;
-    x[8 + k] = __float2bfloat16_rn((f[k] - __bfloat162float(hi)) * 256.0f);
+    x[8 + k] = __float2half_rn((f[k] - __half2float(hi)) * kResidualScale);
   }
 }
 
-__device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* row) {
-  bf16 x[kMlpIn];
+__device__ __forceinline__ void store_features(const float (&f)[kMlpIn], f16* row) {
+  f16 x[kMlpIn];
   split_features(f, x);
 #pragma unroll
   for (int i = 0; i < kMlpIn; i++) row[i] = x[i];
@@ -459,7 +468,7 @@ __device__ __forceinline__ void store_features(const float (&f)[kMlpIn], bf16* r
 // training targets: quantile positions of sorted samples within their
 // condition (u = (k + 1/2) / K)
 __global__ void k_features_beta(MlpBox box, const double* E, const double* T, const double* u, const double* beta,
-                                unsigned long long n, bf16* X, float* y) {
+                                unsigned long long n, f16* X, float* y) {
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const BoxF b = box_f(box);
@@ -473,7 +482,7 @@ __global__ void k_features_beta(MlpBox box, const double* E, const double* T, co
 }
 
 __global__ void k_features_alpha(MlpBox box, const double* E, const double* T, const double* beta, const double* u,
-                                 const double* alpha, unsigned long long n, bf16* X, float* y) {
+                                 const double* alpha, unsigned long long n, f16* X, float* y) {
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const BoxF b = box_f(box);
@@ -517,8 +526,8 @@ __global__ void __launch_bounds__(1024) k_segment_sort(double* v, int K) {
 }
 
 // random batch: row r of the batch is sample philox(key, step, r) mod n
-__global__ void k_gather(const bf16* X, const float* y, unsigned long long n, unsigned long long key, int step,
-                         int B, bf16* bX, bf16* bXt, float* by) {
+__global__ void k_gather(const f16* X, const float* y, unsigned long long n, unsigned long long key, int step,
+                         int B, f16* bX, bf16* bXt, float* by) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= B) return;
   uint32_t c[4] = {static_cast<uint32_t>(r), static_cast<uint32_t>(step), 0x4D4C5000u, 0};
@@ -526,9 +535,9 @@ __global__ void k_gather(const bf16* X, const float* y, unsigned long long n, un
   const unsigned long long idx = ((static_cast<unsigned long long>(c[0]) << 32) | c[1]) % n;
 #pragma unroll
   for (int f = 0; f < kMlpIn; f++) {
-    const bf16 v = X[idx * kMlpIn + f];
+    const f16 v = X[idx * kMlpIn + f];
     bX[static_cast<size_t>(r) * kMlpIn + f] = v;
-    bXt[static_cast<size_t>(f) * B + r] = v;
+    bXt[static_cast<size_t>(f) * B + r] = __float2bfloat16_rn(__half2float(v));
   }
   by[r] = y[idx];
 }
@@ -589,14 +598,14 @@ cudaError_t launch_quantile_u(double* u, unsigned long long n, int K, cudaStream
 }
 
 cudaError_t launch_mlp_features_beta(const MlpBox& box, const double* E, const double* T, const double* u,
-                                     const double* beta, unsigned long long n, __nv_bfloat16* X, float* y,
+                                     const double* beta, unsigned long long n, __half* X, float* y,
                                      cudaStream_t s) {
   k_features_beta<<<blocks256(n), 256, 0, s>>>(box, E, T, u, beta, n, X, y);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mlp_features_alpha(const MlpBox& box, const double* E, const double* T, const double* beta,
-                                      const double* u, const double* alpha, unsigned long long n, __nv_bfloat16* X,
+                                      const double* u, const double* alpha, unsigned long long n, __half* X,
                                       float* y, cudaStream_t s) {
   k_features_alpha<<<blocks256(n), 256, 0, s>>>(box, E, T, beta, u, alpha, n, X, y);
   return cudaGetLastError();
@@ -608,7 +617,7 @@ cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K,
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_gather(const __nv_bfloat16* X, const float* y, unsigned long long n, unsigned long long key,
+cudaError_t launch_mlp_gather(const __half* X, const float* y, unsigned long long n, unsigned long long key,
                               int step, const MlpBatch& b, cudaStream_t s) {
   k_gather<<<(b.B + 255) / 256, 256, 0, s>>>(X, y, n, key, step, b.B, b.X, b.Xt, b.y);
   return cudaGetLastError();
@@ -640,9 +649,9 @@ namespace {
 
 struct NetView {
   const float* p;
-  const bf16* W1;
-  const bf16* W2;
-  const bf16* W3;
+  const f16* W1;  // FP16 forward copies
+  const f16* W2;
+  const f16* W3;
 };
 
 constexpr int kGroups = 2;                                // warpgroups (tiles in flight) per CTA
@@ -676,7 +685,7 @@ __device__ __forceinline__ bool wg_all(int g, bool v) {
   return r != 0;
 }
 
-__device__ __forceinline__ void load_tile(uint8_t* dst, const bf16* src, int K) {
+__device__ __forceinline__ void load_tile(uint8_t* dst, const f16* src, int K) {
   for (int c = threadIdx.x; c < kMlpWidth * (K / 8); c += blockDim.x) {
     const int row = c % kMlpWidth, kc = c / kMlpWidth;
     *reinterpret_cast<uint4*>(dst + tc::tile_offset(row, kc * 8, K)) =
@@ -703,7 +712,7 @@ __device__ __forceinline__ void layer_mma(Group& G, uint32_t act_off, uint32_t w
   if (G.lt == 0) {
     tc::fence_after_sync();
     const uint32_t a0 = tc::smem_addr(G.base + act_off), b0 = tc::smem_addr(G.base + w_off);
-    constexpr uint32_t idesc = tc::idesc_bf16_f32(128, kMlpWidth);
+    constexpr uint32_t idesc = tc::idesc_f16_f32(128, kMlpWidth);
     for (int s = 0; s < K / 16; s++)
       tc::mma_bf16(G.tmem, tc::smem_desc(a0 + s * 256, 128, K * 16), tc::smem_desc(b0 + s * 256, 128, K * 16),
                    idesc, s > 0 ? 1u : 0u);
@@ -725,11 +734,11 @@ __device__ __forceinline__ void hidden_epilogue(Group& G, const float* hbias) {
     tc::tmem_ld32(G.tmem + (static_cast<uint32_t>(w * 32) << 16) + c * 32, v);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      __align__(16) __nv_bfloat162 h[4];
+      __align__(16) __half2 h[4];
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const int k = q * 8 + 2 * j;
-        h[j] = silu2_bf16(fmaf(v[k], 0.5f, hbias[c * 32 + k]), fmaf(v[k + 1], 0.5f, hbias[c * 32 + k + 1]));
+        h[j] = silu2_f16(fmaf(v[k], 0.5f, hbias[c * 32 + k]), fmaf(v[k + 1], 0.5f, hbias[c * 32 + k + 1]));
       }
       *reinterpret_cast<uint4*>(H + tc::tile_offset(G.lt, c * 32 + q * 8, kMlpWidth)) = *reinterpret_cast<uint4*>(h);
     }
@@ -762,9 +771,9 @@ __device__ __forceinline__ float run_net(Group& G, uint32_t w1, uint32_t w2, uin
 }
 
 __device__ __forceinline__ void write_x(Group& G, const float (&f)[kMlpIn]) {
-  bf16 x[kMlpIn];
+  f16 x[kMlpIn];
   split_features(f, x);
-  __align__(16) __nv_bfloat162 h[kMlpIn / 2];
+  __align__(16) __half2 h[kMlpIn / 2];
 #pragma unroll
   for (int i = 0; i < kMlpIn / 2; i++) {
     h[i].x = x[2 * i];

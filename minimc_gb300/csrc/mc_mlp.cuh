@@ -4,9 +4,11 @@
 // Each network maps 16 input features (a few used, the rest zero) through
 // three hidden layers of width 128 (SiLU) to one output:
 //     x[16] -> 128 -> 128 -> 128 -> 1
-// Hidden-layer products run on the tensor cores (tcgen05, BF16 operands,
-// FP32 accumulation in tensor memory); master weights and Adam moments are
-// FP32.  The beta network predicts the quantile position of beta in
+// Hidden-layer products run on the tensor cores (tcgen05, FP32 accumulation
+// in tensor memory): the forward products (training and sampling) take FP16
+// operands -- 11 significant bits, which the surrogate's output precision
+// needs -- and the backward products BF16 ones (range for the gradients);
+// master weights and Adam moments are FP32.  The beta network predicts the quantile position of beta in
 // [-E/kT, beta_cutoff]; the alpha network, given beta, the position of alpha
 // between the kinematic bounds alpha_min(beta) and alpha_max(beta).
 #pragma once
@@ -14,6 +16,7 @@
 #include "mc_device.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 
 namespace mcd {
@@ -47,25 +50,25 @@ struct MlpNet {
   float* g = nullptr;       // gradients
   float* m = nullptr;       // Adam moments
   float* v = nullptr;
-  __nv_bfloat16* W1 = nullptr;   // [128][16]
-  __nv_bfloat16* W2 = nullptr;   // [128][128]
-  __nv_bfloat16* W3 = nullptr;
-  __nv_bfloat16* W2t = nullptr;  // transposes for the backward products
+  __half* W1 = nullptr;          // [128][16] forward copies (FP16)
+  __half* W2 = nullptr;          // [128][128]
+  __half* W3 = nullptr;
+  __nv_bfloat16* W2t = nullptr;  // BF16 transposes for the backward products
   __nv_bfloat16* W3t = nullptr;
 };
 
 // scratch of one training step over a batch of B samples
 struct MlpBatch {
   int B = 0;
-  __nv_bfloat16* X = nullptr;    // [B][16]
+  __half* X = nullptr;           // [B][16] forward input
   __nv_bfloat16* Xt = nullptr;   // [16][B]
   float* y = nullptr;            // [B] targets
   float* Z1 = nullptr;           // [B][128] pre-activations
   float* Z2 = nullptr;
   float* Z3 = nullptr;
-  __nv_bfloat16* H1 = nullptr;   // [B][128]
-  __nv_bfloat16* H2 = nullptr;
-  __nv_bfloat16* H1t = nullptr;  // [128][B]
+  __half* H1 = nullptr;          // [B][128] forward activations
+  __half* H2 = nullptr;
+  __nv_bfloat16* H1t = nullptr;  // [128][B] BF16 copies for the weight gradients
   __nv_bfloat16* H2t = nullptr;
   __nv_bfloat16* dZ3 = nullptr;  // [B][128]
   __nv_bfloat16* dZ2 = nullptr;
@@ -98,10 +101,10 @@ cudaError_t launch_sample_tsl_mlp_queue(const MlpNet& beta_net, const MlpNet& al
 
 // training data: inputs and quantile targets from POD samples
 cudaError_t launch_mlp_features_beta(const MlpBox& box, const double* E, const double* T, const double* u,
-                                     const double* beta, unsigned long long n, __nv_bfloat16* X, float* y,
+                                     const double* beta, unsigned long long n, __half* X, float* y,
                                      cudaStream_t s);
 cudaError_t launch_mlp_features_alpha(const MlpBox& box, const double* E, const double* T, const double* beta,
-                                      const double* u, const double* alpha, unsigned long long n, __nv_bfloat16* X,
+                                      const double* u, const double* alpha, unsigned long long n, __half* X,
                                       float* y, cudaStream_t s);
 // dst[i] = src[i / K] for i < n; u[i] = ((i mod K) + 1/2) / K
 cudaError_t launch_expand(const double* src, unsigned long long n, int K, double* dst, cudaStream_t s);
@@ -112,7 +115,7 @@ int* mlp_error_flag();
 cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K, cudaStream_t s);
 // gathers a random batch (Philox key, step) of B rows of X / y into the
 // batch buffers (and X transposed)
-cudaError_t launch_mlp_gather(const __nv_bfloat16* X, const float* y, unsigned long long n, unsigned long long key,
+cudaError_t launch_mlp_gather(const __half* X, const float* y, unsigned long long n, unsigned long long key,
                               int step, const MlpBatch& b, cudaStream_t s);
 // sampler-side POD draws used to build the training sets
 cudaError_t launch_tsl_beta_draws(const DevTSL* tsl, const double* E, const double* T, unsigned long long n,

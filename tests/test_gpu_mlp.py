@@ -1,9 +1,10 @@
 """GPU MLP surrogate of the thermal scattering sampler, through the C ABI.
 
 * Forward outputs and the full parameter gradient of one training step
-  (tcgen05 BF16 products, FP32 accumulation, packed-BF16 hidden SiLU)
-  against a CPU reference that applies the same BF16 roundings in FP64
-  arithmetic, and against plain FP64 (loose tolerance).
+  (tcgen05 products with FP32 accumulation: FP16 forward operands and
+  packed-FP16 hidden SiLU, BF16 backward operands) against a CPU reference
+  that applies the same roundings in FP64 arithmetic, and against plain
+  FP64 (loose tolerance).
 * Training on POD samples of the synthetic library, then sampling: beta and
   alpha distributions against the POD sampler (KS distance, 200-bin
   chi-square at C4's energies with T uniform per sample), the fallback
@@ -46,12 +47,17 @@ def silu(z):
     return z / (1 + np.exp(-z))
 
 
-def silu_bf16(z):
-    """Hidden activations as the kernels form them: h = bf16(z / 2), then the
-    packed BF16 tanh and fma h + h tanh(h), rounded to BF16."""
-    h = bf16(np.asarray(z) / 2)
-    t = bf16(np.tanh(h))
-    return bf16(h + h * t)
+def f16(a):
+    """Round to FP16 (nearest even), returned as float64."""
+    return np.asarray(a, np.float64).astype(np.float16).astype(np.float64)
+
+
+def silu_f16(z):
+    """Hidden activations as the kernels form them: h = f16(z / 2), then the
+    packed FP16 tanh and fma h + h tanh(h), rounded to FP16."""
+    h = f16(np.asarray(z) / 2)
+    t = f16(np.tanh(h))
+    return f16(h + h * t)
 
 
 def dsilu(z):
@@ -61,17 +67,20 @@ def dsilu(z):
 
 def reference(p, x, y, emulate=True):
     """Forward and backward of the network; `emulate` applies the kernel's
-    BF16 roundings (operands of every tensor-core product)."""
-    q = bf16 if emulate else (lambda a: np.asarray(a, np.float64))
+    roundings: FP16 operands of the forward products, BF16 operands of the
+    backward products."""
+    ident = lambda a: np.asarray(a, np.float64)  # noqa: E731
+    q = bf16 if emulate else ident
+    h16 = f16 if emulate else ident
     W1, b1, W2, b2, W3, b3, w4, b4 = unpack(p)
     n = len(x)
-    X = q(x)
-    act = silu_bf16 if emulate else silu
-    Z1 = X @ q(W1).T + b1
+    X = h16(x)
+    act = silu_f16 if emulate else silu
+    Z1 = X @ h16(W1).T + b1
     H1 = act(Z1)
-    Z2 = H1 @ q(W2).T + b2
+    Z2 = H1 @ h16(W2).T + b2
     H2 = act(Z2)
-    Z3 = H2 @ q(W3).T + b3
+    Z3 = H2 @ h16(W3).T + b3
     out = silu(Z3) @ w4 + b4
     e = out - y
     go = 2 * e / n
@@ -80,13 +89,13 @@ def reference(p, x, y, emulate=True):
     g[OFF["b4"]] = go.sum()
     dZ3 = go[:, None] * w4[None, :] * dsilu(Z3)
     g[OFF["b3"]:OFF["w4"]] = dZ3.sum(0)
-    g[OFF["W3"]:OFF["b3"]] = (q(dZ3).T @ H2).ravel()
+    g[OFF["W3"]:OFF["b3"]] = (q(dZ3).T @ q(H2)).ravel()
     dZ2 = (q(dZ3) @ q(W3)) * dsilu(Z2)
     g[OFF["b2"]:OFF["W3"]] = dZ2.sum(0)
-    g[OFF["W2"]:OFF["b2"]] = (q(dZ2).T @ H1).ravel()
+    g[OFF["W2"]:OFF["b2"]] = (q(dZ2).T @ q(H1)).ravel()
     dZ1 = (q(dZ2) @ q(W2)) * dsilu(Z1)
     g[OFF["b1"]:OFF["W2"]] = dZ1.sum(0)
-    g[OFF["W1"]:OFF["b1"]] = (q(dZ1).T @ X).ravel()
+    g[OFF["W1"]:OFF["b1"]] = (q(dZ1).T @ q(X)).ravel()
     return g, float((e * e).sum()), out
 
 
