@@ -424,8 +424,8 @@ def run_gpu_tsl(args) -> None:
     b = torch.empty(n, dtype=torch.float64, device="cuda")
     a = torch.empty_like(b)
     t0 = time.perf_counter()
-    tr = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
-                             samples_per_condition=512, batch=8192, steps=3000, seed=3)
+    tr = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=16384,
+                             samples_per_condition=1024, batch=16384, steps=12000, lr=1e-3, seed=3)
     train_s = time.perf_counter() - t0
     rates, samples = {}, {}
     for name, method in (("pod_exact", TSL_POD | TSL_PHILOX), ("pod_fp32", TSL_POD | TSL_PHILOX | TSL_FAST),

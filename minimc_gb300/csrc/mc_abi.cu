@@ -1913,7 +1913,7 @@ int mc_train_surrogate(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_tra
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     o.data_ms += ms;
     TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
-    if ((rc = mlp_train(c, c->mlp[0], X, y, N, 4, d, run_key(d.seed, 2, 0x4D4C4231ull), &loss_b)) != MC_OK) break;
+    if ((rc = mlp_train(c, c->mlp[0], X, y, N, 7, d, run_key(d.seed, 2, 0x4D4C4231ull), &loss_b)) != MC_OK) break;
     TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
     TRY_CUDA(cudaEventSynchronize(c->ev1));
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -1932,7 +1932,7 @@ int mc_train_surrogate(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_tra
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     o.data_ms += ms;
     TRY_CUDA(cudaEventRecord(c->ev0, c->stream));
-    if ((rc = mlp_train(c, c->mlp[1], X, y, N, 6, d, run_key(d.seed, 5, 0x4D4C4132ull), &loss_a)) != MC_OK) break;
+    if ((rc = mlp_train(c, c->mlp[1], X, y, N, 7, d, run_key(d.seed, 5, 0x4D4C4132ull), &loss_a)) != MC_OK) break;
     TRY_CUDA(cudaEventRecord(c->ev1, c->stream));
     TRY_CUDA(cudaEventSynchronize(c->ev1));
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);

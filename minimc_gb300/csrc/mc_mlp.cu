@@ -387,6 +387,7 @@ struct BoxF {
   float inv_beta_scale;
   float kB;                 // Boltzmann constant (MeV/K)
   float inv_awr;
+  float r_scale, r_shift;   // f6 = ln(E / kT) * r_scale + r_shift (the box's range to [-1, 1])
 };
 
 __device__ __forceinline__ BoxF box_f(const MlpBox& b) {
@@ -400,16 +401,25 @@ __device__ __forceinline__ BoxF box_f(const MlpBox& b) {
   f.inv_beta_scale = static_cast<float>(1.0 / b.beta_scale);
   f.kB = static_cast<float>(kBoltzmann);
   f.inv_awr = static_cast<float>(1.0 / b.awr);
+  const double r0 = b.logE0 - log(kBoltzmann * b.T1), r1 = b.logE1 - log(kBoltzmann * b.T0);
+  const double rs = 2.0 / (r1 - r0);
+  f.r_scale = static_cast<float>(rs);
+  f.r_shift = static_cast<float>(-r0 * rs - 1.0);
   return f;
 }
 
 __device__ __forceinline__ float beta_min_of(const BoxF& b, float E, float T) { return -E / (b.kB * T); }
 
+// features: ln E, T, u, logit(u) / 8, [alpha only: beta, beta's position],
+// ln(E / kT) -- the free-gas scaling variable, on which the distributions
+// mostly depend
 __device__ __forceinline__ void base_features(const BoxF& b, float E, float T, float u, float* f) {
-  f[0] = fmaf(logf(E), b.e_scale, b.e_shift);
+  const float lE = logf(E);
+  f[0] = fmaf(lE, b.e_scale, b.e_shift);
   f[1] = fmaf(T, b.t_scale, b.t_shift);
   f[2] = fmaf(2.0f, u, -1.0f);
   f[3] = fminf(2.0f, fmaxf(-2.0f, (logf(u) - log1pf(-u)) * 0.125f));
+  f[6] = fmaf(lE - logf(b.kB * T), b.r_scale, b.r_shift);
 }
 
 __device__ __forceinline__ void beta_features(const BoxF& b, float E, float T, float u, float (&f)[kMlpIn]) {
@@ -445,7 +455,7 @@ __device__ __forceinline__ void alpha_range(const BoxF& b, float E, float T, flo
 // split into its FP16 value (slot k) and the residual scaled by 2048 (slot
 // 8 + k), so the product sees the FP32 feature to about 22 significant
 // bits (one FP16 input would quantise E, T and the uniform to 2^-11).
-constexpr int kMlpFeatures = 6;
+constexpr int kMlpFeatures = 7;
 constexpr float kResidualScale = 2048.0f;
 __device__ __forceinline__ void split_features(const float (&f)[kMlpIn], f16 (&x)[kMlpIn]) {
 #pragma unroll
