@@ -143,19 +143,19 @@ def trained(tmp_path_factory):
     ctx = Context(0)
     ctx.load_xml(xml, d)
     t0 = time.perf_counter()
-    out = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
-                              samples_per_condition=512, batch=8192, steps=3000, seed=3)
+    out = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=8192,
+                              samples_per_condition=1024, batch=16384, steps=8000, lr=1e-3, seed=3)
     return ctx, out, time.perf_counter() - t0
 
 
 def test_training_converges(trained):
     """The mean squared quantile error reaches the noise of the targets
     themselves: an empirical quantile of K samples scatters by about
-    sqrt(u (1 - u) / K) in CDF units (~5e-4 squared for K = 512)."""
+    sqrt(u (1 - u) / K) in CDF units (~2.4e-4 squared for K = 1024)."""
     ctx, out, wall = trained
     assert out.failures == 0
     assert out.loss_beta < 1e-3 and out.loss_alpha < 1e-3, (out.loss_beta, out.loss_alpha)
-    assert out.samples == 4096 * 512
+    assert out.samples == 8192 * 1024
 
 
 @pytest.mark.parametrize("E", [0.01 * EV, 0.1 * EV, 1.0 * EV])
