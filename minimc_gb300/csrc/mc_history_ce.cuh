@@ -591,6 +591,10 @@ int occupancy_of(K kernel, int block, size_t smem) {
 }
 
 constexpr size_t kCeSmem = 2 * kSharedBins * sizeof(double);
+// register budget of the exact-table fixed-source kernels with Philox
+// streams (thermal problems): two resident blocks per SM (128 registers,
+// a few hundred bytes of spills) hide more latency than one (~185)
+constexpr int kExactFixedMinb = 2;
 
 }  // namespace
 

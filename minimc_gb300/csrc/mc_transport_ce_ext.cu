@@ -12,7 +12,7 @@ void launch_pert(const DevWorld& w, const RunParams& rp, int rng_mode, int grid,
 }
 
 void launch_tq(const DevWorld& w, const RunParams& rp, int grid, int block, cudaStream_t stream) {
-  k_history_ce<PhiloxRng, false, 1, false, false, true><<<grid, block, kCeSmem, stream>>>(w, rp);
+  k_history_ce<PhiloxRng, false, kExactFixedMinb, false, false, true><<<grid, block, kCeSmem, stream>>>(w, rp);
 }
 
 }  // namespace cevar

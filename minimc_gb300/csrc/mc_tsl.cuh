@@ -24,12 +24,17 @@ namespace mcd {
 constexpr int kTslResampleLimit = 10;  // constants::beta/alpha_resample_limit
 constexpr int kFastPodRank = 32;       // fast form: mode vector in registers
 
-// std::upper_bound on a sorted array (libstdc++'s bisection)
+// std::upper_bound on a sorted array (libstdc++'s bisection); the
+// comparisons run on order-preserving integer keys (the same outcome as the
+// FP64 comparison for every value, on the integer pipe)
 __device__ __forceinline__ int upper_index(const double* v, int n, double x) {
+  // a NaN compares false with every element
+  if ((__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) return n;
+  const long long kx = dkey(x);
   int first = 0, len = n;
   while (len > 0) {
     const int half = len >> 1, mid = first + half;
-    if (x < __ldg(v + mid)) {
+    if (kx < dkey(__ldg(v + mid))) {
       len = half;
     }
     else {
@@ -362,7 +367,7 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
 // ThermalScattering::Scatter: beta, alpha -> E', mu; Particle::Scatter
 // rotates the direction by mu with a fresh azimuth
 template <bool FAST, class Rng>
-__device__ __forceinline__ bool tsl_scatter(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
+__device__ __forceinline__ bool tsl_scatter_body(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
                                             double& dw) {
   double beta, alpha;
   if (!tsl_sample_beta<FAST>(t, rng, E, T, beta)) return false;
@@ -388,6 +393,12 @@ __device__ __forceinline__ bool tsl_scatter(const DevTSL& t, Rng& rng, double T,
   }
   E = E_p;
   return true;
+}
+
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_scatter(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
+                                            double& dw) {
+  return tsl_scatter_body<FAST>(t, rng, T, E, du, dv, dw);
 }
 
 }  // namespace mcd
