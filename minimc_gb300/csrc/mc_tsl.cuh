@@ -165,6 +165,15 @@ struct PodEval {
     if constexpr (FAST) return pod_eval_fast(c, gv, cdf_i);
     else return pod_eval(c, cdf_i, g_i);
   }
+  // fast form: the reconstruction in FP32, without the conversion
+  __device__ __forceinline__ float f32(int cdf_i) const {
+    const float* C = c.cs + static_cast<size_t>(cdf_i) * c.r;
+    float acc = 0.0f;
+#pragma unroll
+    for (int o = 0; o < kFastPodRank; o++)
+      if (o < c.r) acc = __fmaf_rn(__ldg(C + o), gv.v[o], acc);
+    return acc;
+  }
 };
 
 // ThermalScattering::EvaluateInelastic
@@ -326,9 +335,14 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
   // find_cdf: std::upper_bound over CDF indices with a < Evaluate(i)
   auto find_cdf = [&](double a) {
     int first = 0, len = nF;
+    // the fast form compares in FP32 (its reconstructions are FP32 values)
+    const float af = __double2float_rn(a);
     while (len > 0) {
       const int half = len >> 1, mid = first + half;
-      if (a < ev(mid)) {
+      bool below;
+      if constexpr (FAST) below = af < ev.f32(mid);
+      else below = a < ev(mid);
+      if (below) {
         len = half;
       }
       else {
