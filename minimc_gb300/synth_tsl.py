@@ -38,6 +38,7 @@ from pathlib import Path
 
 import numpy as np
 
+from . import pod
 from .synth_ce import write_table
 
 KB = 8.617333262145e-11  # MeV / K
@@ -101,10 +102,6 @@ def _inverse(x, cdf, F):
     return np.interp(F, cdf[keep], x[keep])
 
 
-def _pod(M, rank):
-    U, S, Vt = np.linalg.svd(M, full_matrices=False)
-    r = min(rank, len(S))
-    return U[:, :r], S[:r], Vt[:r].T
 
 
 def cdf_grid(n):
@@ -113,11 +110,40 @@ def cdf_grid(n):
     return 0.5 * (1 - np.cos(np.pi * t))
 
 
+def beta_table(Es, Ts, awr: float, beta_cutoff: float, n_F: int, sigma_b: float):
+    """The full beta inverse-CDF table [F][E][T] and the total inelastic
+    cross section [E][T] of the analytic law."""
+    Fb = cdf_grid(n_F)
+    beta_inv = np.zeros((n_F, len(Es), len(Ts)))
+    xs = np.zeros((len(Es), len(Ts)))
+    for i, E in enumerate(Es):
+        for j, T in enumerate(Ts):
+            b, cdf, tot = beta_marginal_cdf(E, T, awr, beta_cutoff)
+            beta_inv[:, i, j] = _inverse(b, cdf / tot, Fb)
+            xs[i, j] = sigma_b * awr * KB * T / (4 * E) * tot
+    return pod.Table(Fb, np.asarray(Es, np.float64), np.asarray(Ts, np.float64), beta_inv), xs
+
+
+def alpha_table(betas, Ts, alpha_cutoff: float, n_F: int):
+    """The full alpha inverse-CDF table [F][|beta|][T] of the analytic law."""
+    Fa = cdf_grid(n_F)
+    alpha_inv = np.zeros((n_F, len(betas), len(Ts)))
+    for k, b in enumerate(betas):
+        for j, T in enumerate(Ts):
+            a, cdf = alpha_conditional_cdf(b, T, alpha_cutoff)
+            alpha_inv[:, k, j] = _inverse(a, cdf, Fa)
+    return pod.Table(Fa, np.asarray(betas, np.float64), np.asarray(Ts, np.float64), alpha_inv)
+
+
 def write_tsl(directory: Path, prefix: str = "tsl", awr: float = 0.999167339, sigma_b: float = 80.0,
               temperatures=None, n_E: int = 80, E_min: float = 1e-5 * EV, E_cutoff: float = 4.0 * EV,
               n_beta_grid: int = 300, beta_cutoff: float = 20.0, n_F_beta: int = 120, n_F_alpha: int = 160,
-              rank: int = 30, partitions: int = 4, xs_rank: int = 10) -> dict:
-    """Writes the tables; returns the <tsl> attributes and partition files."""
+              rank: int = 30, partitions: int = 4, xs_rank: int = 10, rel_tol: float | None = None,
+              device: str | None = "numpy") -> dict:
+    """Writes the tables; returns the <tsl> attributes and partition files.
+    Partitions are equal splits of the outer grids, truncated to `rank`, or,
+    with `rel_tol`, the POD pipeline's adaptive ranks (minimc_gb300.pod)
+    with non-monotone CDFs removed."""
     directory = Path(directory)
     directory.mkdir(parents=True, exist_ok=True)
     Ts = np.asarray(temperatures if temperatures is not None else np.linspace(283.6, 623.6, 18), dtype=np.float64)
@@ -125,52 +151,27 @@ def write_tsl(directory: Path, prefix: str = "tsl", awr: float = 0.999167339, si
     # alpha range needed at the highest energy and beta, lowest temperature
     a_max = (np.sqrt(E_cutoff) + np.sqrt(E_cutoff + beta_cutoff * KB * Ts.max())) ** 2 / (awr * KB * Ts.min())
     alpha_cutoff = float(1.25 * a_max)
-
-    # ---- beta marginals: inverse CDFs and total cross sections
-    Fb = cdf_grid(n_F_beta)
-    beta_inv = np.zeros((n_F_beta, n_E, len(Ts)))
-    xs = np.zeros((n_E, len(Ts)))
-    for i, E in enumerate(Es):
-        for j, T in enumerate(Ts):
-            b, cdf, tot = beta_marginal_cdf(E, T, awr, beta_cutoff)
-            beta_inv[:, i, j] = _inverse(b, cdf / tot, Fb)
-            xs[i, j] = sigma_b * awr * KB * T / (4 * E) * tot
-    files = {"beta": [], "alpha": []}
-    for p, idx in enumerate(np.array_split(np.arange(n_E), partitions)):
-        M = beta_inv[:, idx, :].reshape(n_F_beta, -1)
-        U, S, V = _pod(M, rank)
-        r = len(S)
-        names = {k: f"{prefix}-beta{p}-{k}.mctab" for k in ("CDF", "S", "E_T")}
-        write_table(directory / names["CDF"], [Fb, np.arange(r, dtype=np.float64)], U)
-        write_table(directory / names["S"], [np.arange(r, dtype=np.float64)], S)
-        write_table(directory / names["E_T"], [Es[idx], Ts, np.arange(r, dtype=np.float64)],
-                    V.reshape(len(idx), len(Ts), r))
-        files["beta"].append(names)
-
-    # ---- alpha conditionals on a |beta| grid reaching the largest downscatter
+    # alpha conditionals on a |beta| grid reaching the largest downscatter
     # (-beta up to E_cutoff / kT_min) and the upscatter cutoff
     beta_top = 1.02 * max(beta_cutoff, E_cutoff / (KB * Ts.min()))
     betas = np.concatenate([[1e-3], np.geomspace(1e-2, beta_top, n_beta_grid - 1)])
-    Fa = cdf_grid(n_F_alpha)
-    alpha_inv = np.zeros((n_F_alpha, n_beta_grid, len(Ts)))
-    for k, b in enumerate(betas):
-        for j, T in enumerate(Ts):
-            a, cdf = alpha_conditional_cdf(b, T, alpha_cutoff)
-            alpha_inv[:, k, j] = _inverse(a, cdf, Fa)
-    for p, idx in enumerate(np.array_split(np.arange(n_beta_grid), partitions)):
-        M = alpha_inv[:, idx, :].reshape(n_F_alpha, -1)
-        U, S, V = _pod(M, rank)
-        r = len(S)
-        names = {k: f"{prefix}-alpha{p}-{k}.mctab" for k in ("CDF", "S", "beta_T")}
-        write_table(directory / names["CDF"], [Fa, np.arange(r, dtype=np.float64)], U)
-        write_table(directory / names["S"], [np.arange(r, dtype=np.float64)], S)
-        write_table(directory / names["beta_T"], [betas[idx], Ts, np.arange(r, dtype=np.float64)],
-                    V.reshape(len(idx), len(Ts), r))
-        files["alpha"].append(names)
+
+    def decompose(table):
+        cuts = [len(a) for a in np.array_split(np.arange(len(table.outer)), partitions)]
+        parts = pod.split(table, np.cumsum(cuts)[:-1])
+        if rel_tol is not None:
+            return pod.adaptive_coarsen(parts, rel_frobenius_norm_tol=rel_tol, device=device)
+        return [pod.truncate(p, rank, device) for p in parts]
+
+    bt, xs = beta_table(Es, Ts, awr, beta_cutoff, n_F_beta, sigma_b)
+    at = alpha_table(betas, Ts, alpha_cutoff, n_F_alpha)
+    files = {"beta": pod.write_partitions(decompose(bt), directory, prefix, "beta"),
+             "alpha": pod.write_partitions(decompose(at), directory, prefix, "alpha")}
 
     # ---- total inelastic cross section and majorant
-    U, S, V = _pod(xs, xs_rank)
-    r = len(S)
+    U, S, Vt = np.linalg.svd(xs, full_matrices=False)
+    r = min(xs_rank, len(S))
+    U, S, V = U[:, :r], S[:r], Vt[:r].T
     tot = {"E": f"{prefix}-total-E.mctab", "S": f"{prefix}-total-S.mctab", "T": f"{prefix}-total-T.mctab",
            "majorant": f"{prefix}-majorant.mctab"}
     write_table(directory / tot["E"], [Es, np.arange(r, dtype=np.float64)], U)
