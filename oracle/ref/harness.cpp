@@ -18,6 +18,7 @@
 #include <exception>
 #include <iostream>
 #include <sstream>
+#include <streambuf>
 #include <string>
 
 namespace {
@@ -27,13 +28,14 @@ void copy_message(const std::exception& e, char* err, size_t errn) {
     err[errn - 1] = 0;
   }
 }
-}  // namespace
-
-extern "C" {
-
-}  // extern "C"
-
-namespace {
+// Discards everything written to it.  It keeps no buffer or other state,
+// so the reference's worker threads may report progress through it at the
+// same time (a string stream in its place is a data race).
+class NullBuf : public std::streambuf {
+ protected:
+  int overflow(int c) override { return traits_type::not_eof(c); }
+  std::streamsize xsputn(const char*, std::streamsize n) override { return n; }
+};
 
 // FixedSource with its World visible, constructed exactly as
 // Driver::Create does (document first, then the driver)
@@ -70,8 +72,8 @@ int ref_solve(const char* xml_path, const char* estimator, uint64_t nbins, doubl
               size_t ordersn, char* text, size_t textn, char* err, size_t errn) {
   // the reference reports progress on stdout; keep the caller's output clean
   std::streambuf* saved = std::cout.rdbuf();
-  std::ostringstream sink;
-  std::cout.rdbuf(sink.rdbuf());
+  NullBuf sink;
+  std::cout.rdbuf(&sink);
   int rc = 0;
   try {
     std::unique_ptr<ProbedFixedSource> driver;
