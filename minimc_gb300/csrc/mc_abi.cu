@@ -603,6 +603,10 @@ int grid_for(mc_ctx* c, int energy_mode, int rng, int block, bool keig, bool fas
   return per_sm * c->num_sms;
 }
 
+// one thread per history record for the fission-site kernels (most
+// records hold no fission, so the latency of the others needs many threads)
+int sites_grid(uint64_t n) { return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 1u << 20))); }
+
 unsigned long long run_key(uint64_t seed, uint64_t cycle, uint64_t salt) {
   return mcd::splitmix64(seed * 0x9E3779B97F4A7C15ull + cycle * 0xD1B54A32D192ED03ull + salt);
 }
@@ -768,8 +772,8 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   CUDA_TRY(c, cudaEventRecord(c->evk1, c->stream));
   if (keig) {
     if (c->model.energy_mode == mc::kMultigroup)
-      CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
-    else CUDA_TRY(c, mcd::launch_fission_sites_ce(rp, rng, c->num_sms * 8, c->stream));
+      CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, sites_grid(rp.n), c->stream));
+    else CUDA_TRY(c, mcd::launch_fission_sites_ce(rp, rng, sites_grid(rp.n), c->stream));
     c->launches++;
   }
   if (rp.nb) {
@@ -2202,7 +2206,7 @@ extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint
   const int block = pick_block(o);
   const int grid = grid_for(c, c->model.energy_mode, rng, block, true, rp.fast != 0);
   CUDA_TRY(c, mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant));
-  CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, c->num_sms * 8, c->stream));
+  CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, sites_grid(rp.n), c->stream));
   CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
   if (d_fission_sites && cap) {
     k_compact_capped<<<static_cast<unsigned>((n + 255) / 256), 256, 0, c->stream>>>(

@@ -544,8 +544,23 @@ __global__ void __launch_bounds__(256) k_commit_dense(const RunParams rp) {
   const unsigned b = blockIdx.y;
   double* row = rp.pend + static_cast<size_t>(b) * rp.n;
   double s = 0, q = 0;
-  for (unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; h < rp.n;
-       h += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+  const unsigned long long S = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  // four independent loads in flight per thread (the array is read once)
+  for (; h + 3 * S < rp.n; h += 4 * S) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) v[j] = __ldcs(row + h + j * S);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (__double_as_longlong(v[j]) != 0) {
+        s += v[j];
+        q += v[j] * v[j];
+        row[h + j * S] = 0;
+      }
+    }
+  }
+  for (; h < rp.n; h += S) {
     const double v = row[h];
     if (__double_as_longlong(v) != 0) {
       s += v;
