@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
       const bool delta = w.tracking == 1;
       const double density = __ldg(w.mat_density + m);
       UnionPos up{0, 0, 0.0f};
-      double sigma, nsf = 0, cpd = 0;
+      double sigma, nsf = 0, cpd = 0, T_pos = 0;
       if (fx) {
         up = ce_union_pos(w.ce, p.j, p.E);
         const size_t row = static_cast<size_t>(t * w.n_materials + m) * w.ce.nu;
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
       else {
         // GetCollisionProbabilityDensity: total, or the majorant at the
         // cell's maximum temperature (src/TransportMethod.cpp:79-82,124-127)
-        const double T_pos = cell_temperature(w, p.cell, p.x, p.y, p.z);
+        T_pos = cell_temperature(w, p.cell, p.x, p.y, p.z);
         cpd = delta ? ce_material_micro(w, m, t, p.j, p.E, cell_temperature_max(w, p.cell), T_pos, true, &memo)
                     : ce_material_micro(w, m, t, p.j, p.E, T_pos, T_pos, false, &memo);
         sigma = dmul(density, cpd);
@@ -313,22 +313,25 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
       double dsurf;
       const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
+      const bool refl = !collide && __ldg(w.surf_refl + s) != 0;
+      bool real = true;
+      if (collide && delta) {
+        // bernoulli(total / majorant) before the particle moves
+        // (src/TransportMethod.cpp:106-110); the FP32 tables hold no
+        // temperature dependence, so there the ratio is one
+        const double u = uniform(p.rng, fast);
+        if (!fx) real = u < ddiv(ce_material_micro(w, m, t, p.j, p.E, T_pos, T_pos, false, &memo), cpd);
+      }
+      // the move -- to the collision, onto a reflecting plane, or across a
+      // surface plus the nudge -- once for the whole warp (FP64 issue does
+      // not shrink with the active lanes)
+      const double dcross = dadd(dsurf, kNudge);
+      const double dmove = collide ? dcol : (refl ? dsurf : dcross);
+      if (rp.score) score_track<true>(w, p, dmove, sc);
+      if (KEIG) my_ktl += dmove * nsf;
+      indirect_stream<PERT>(w, p, m, cpd, dmove);
+      stream(p.x, p.y, p.z, p.u, p.v, p.w, dmove);
       if (collide) {
-        if (rp.score) score_track<true>(w, p, dcol, sc);
-        if (KEIG) my_ktl += dcol * nsf;
-        bool real = true;
-        if (delta) {
-          // bernoulli(total / majorant) before the particle moves
-          // (src/TransportMethod.cpp:106-110); the FP32 tables hold no
-          // temperature dependence, so there the ratio is one
-          const double u = uniform(p.rng, fast);
-          if (!fx) {
-            const double T_pos = cell_temperature(w, p.cell, p.x, p.y, p.z);
-            real = u < ddiv(ce_material_micro(w, m, t, p.j, p.E, T_pos, T_pos, false, &memo), cpd);
-          }
-        }
-        indirect_stream<PERT>(w, p, m, cpd, dcol);
-        stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
         if (!real) {
           p.event = kVirtualCollision;
         }
@@ -467,12 +470,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
         }
       }
       else {
-        const bool refl = __ldg(w.surf_refl + s) != 0;
         if (refl) {
-          if (rp.score) score_track<true>(w, p, dsurf, sc);
-          if (KEIG) my_ktl += dsurf * nsf;
-          indirect_stream<PERT>(w, p, m, cpd, dsurf);
-          stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
           const int kind = __ldg(w.surf_kind + s);
           if (kind == kPlaneX) p.u = -p.u;
           else if (kind == kPlaneY) p.v = -p.v;
@@ -482,11 +480,6 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           p.skip = s;
         }
         else {
-          const double dd = dadd(dsurf, kNudge);
-          if (rp.score) score_track<true>(w, p, dd, sc);
-          if (KEIG) my_ktl += dd * nsf;
-          indirect_stream<PERT>(w, p, m, cpd, dd);
-          stream(p.x, p.y, p.z, p.u, p.v, p.w, dd);
           if (w.quirks) {
             p.cell = find_cell(w, p.x, p.y, p.z);
           }

@@ -151,11 +151,18 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
       const bool delta = w.tracking == 1;
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
+      const bool refl = !collide && __ldg(w.surf_refl + s) != 0;
+      // The move is the same arithmetic in every branch -- to the collision,
+      // onto a reflecting plane, or across a surface plus the nudge -- so it
+      // runs once for the whole warp (FP64 issue does not shrink with the
+      // active lanes), before the branch-specific work.
+      const double dcross = dadd(dsurf, kNudge);
+      const double dmove = collide ? dcol : (refl ? dsurf : dcross);
+      if (rp.score) score_track(w, p, dmove, sc);
+      if (KEIG) my_ktl += dmove * __ldg(w.mat_mg_nusigf + mg);
+      indirect_stream<PERT>(w, p, m, micro, dmove);
+      stream(p.x, p.y, p.z, p.u, p.v, p.w, dmove);
       if (collide) {
-        if (rp.score) score_track(w, p, dcol, sc);
-        if (KEIG) my_ktl += dcol * __ldg(w.mat_mg_nusigf + mg);
-        indirect_stream<PERT>(w, p, m, micro, dcol);
-        stream(p.x, p.y, p.z, p.u, p.v, p.w, dcol);
         p.skip = -1;
         // multigroup majorant == total, so CellDeltaTracking's rejection
         // (src/TransportMethod.cpp:106-108) always accepts; it still draws
@@ -222,14 +229,9 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
         }
       }
       else {
-        const bool refl = __ldg(w.surf_refl + s) != 0;
         if (refl) {
           // reflective boundary (extension): stop on the plane, mirror the
           // normal component, stay in the cell
-          if (rp.score) score_track(w, p, dsurf, sc);
-          if (KEIG) my_ktl += dsurf * __ldg(w.mat_mg_nusigf + mg);
-          indirect_stream<PERT>(w, p, m, micro, dsurf);
-          stream(p.x, p.y, p.z, p.u, p.v, p.w, dsurf);
           const int kind = __ldg(w.surf_kind + s);
           if (kind == kPlaneX) p.u = -p.u;
           else if (kind == kPlaneY) p.v = -p.v;
@@ -239,11 +241,6 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           p.skip = s;
         }
         else {
-          const double d = dadd(dsurf, kNudge);
-          if (rp.score) score_track(w, p, d, sc);
-          if (KEIG) my_ktl += d * __ldg(w.mat_mg_nusigf + mg);
-          indirect_stream<PERT>(w, p, m, micro, d);
-          stream(p.x, p.y, p.z, p.u, p.v, p.w, d);
           if (w.quirks) {
             p.cell = find_cell(w, p.x, p.y, p.z);
           }
