@@ -83,6 +83,18 @@ struct mc_ctx {
 
 namespace {
 
+// compaction that never writes past the caller's capacity
+__global__ void k_compact_capped(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
+                                 unsigned long long n, uint32_t max_yield, Site* out, unsigned long long cap) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t c = count[i];
+  const unsigned long long o = offsets[i];
+  for (uint32_t k = 0; k < c; k++)
+    if (o + k < cap) out[o + k] = slots[i * max_yield + k];
+}
+
+
 enum ScratchSlot {
   kSrc = 0,
   kSlots,
@@ -1431,10 +1443,24 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   }
   if (!sites) return fail(c, MC_ERR_INPUT, "sites is NULL");
   cudaSetDevice(c->device);
-  auto* src = static_cast<Site*>(scratch(c, kSrc, n * sizeof(Site)));
-  if (!src || !scratch(c, kSlots, n * c->max_yield * sizeof(Site)) || !scratch(c, kCount, n * 4))
+  if (!scratch(c, kSlots, n * c->max_yield * sizeof(Site)) || !scratch(c, kCount, n * 4))
     return fail(c, MC_ERR_OOM, "bank allocation failed");
-  CUDA_TRY(c, cudaMemcpyAsync(src, sites, n * sizeof(Site), cudaMemcpyHostToDevice, c->stream));
+  // Sites in page-locked host memory are read in place by the transport
+  // kernel (each site once, coalesced, when its history starts), so the
+  // host-to-device transfer overlaps the transport instead of preceding it;
+  // pageable memory is copied first.
+  const Site* src = nullptr;
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, sites) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+    src = static_cast<const Site*>(pa.devicePointer);
+  }
+  else {
+    (void)cudaGetLastError();
+    auto* dst = static_cast<Site*>(scratch(c, kSrc, n * sizeof(Site)));
+    if (!dst) return fail(c, MC_ERR_OOM, "bank allocation failed");
+    CUDA_TRY(c, cudaMemcpyAsync(dst, sites, n * sizeof(Site), cudaMemcpyHostToDevice, c->stream));
+    src = dst;
+  }
   RunParams rp{};
   rp.n = n;
   rp.seed = c->model.seed;
@@ -1451,6 +1477,9 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
   int rc = run_transport(c, rp, rng, pick_block(o), nullptr, o ? o->schedule : MC_SCHEDULE_AUTO);
   if (rc != MC_OK) return rc;
+  // the bank is compacted on the device and copied out (a compaction kernel
+  // writing it into page-locked host memory in place measured slower: its
+  // scattered 64-byte writes cross the chip-to-chip link one site at a time)
   Site* bank = nullptr;
   uint64_t m = 0;
   rc = compact_bank(c, n, &bank, &m);
@@ -2126,17 +2155,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 // device address of g_noalloc_scratch for each device, found once
 constexpr int kMaxDevices = 64;
 void* g_noalloc_addr[kMaxDevices] = {};
-
-// compaction that never writes past the caller's capacity
-__global__ void k_compact_capped(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
-                                 unsigned long long n, uint32_t max_yield, Site* out, unsigned long long cap) {
-  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t c = count[i];
-  const unsigned long long o = offsets[i];
-  for (uint32_t k = 0; k < c; k++)
-    if (o + k < cap) out[o + k] = slots[i * max_yield + k];
-}
 
 }  // namespace
 

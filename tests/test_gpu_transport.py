@@ -180,3 +180,53 @@ def test_lost_particle_reported(built_library):
     with pytest.raises(MCError) as e:
         ctx.run_fixed_source(rng=RNG_PHILOX, histories=100)
     assert e.value.code == -5 and "Point does not belong to any Cell" in e.value.message
+
+
+def test_transport_bank_pinned_sites_read_in_place(built_library):
+    """mc_transport_bank reads sites in page-locked host memory in place
+    (copies pageable ones first): with page-locked or pageable inputs and
+    outputs it gives the same fission bank, and a too-small output is not
+    overrun."""
+    import ctypes as C
+
+    import torch
+
+    from minimc_gb300 import SITE_DTYPE
+
+    p = synth.two_zone_cubes(histories=20000, groups=4)
+    ctx = gpu_ctx(p.xml())
+    n = 20000
+    rng = np.random.default_rng(3)
+    sites = np.zeros(n, SITE_DTYPE)
+    mu = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    sites["u"], sites["v"], sites["w"] = mu, np.sqrt(1 - mu * mu) * np.cos(ph), np.sqrt(1 - mu * mu) * np.sin(ph)
+    sites["x"] = rng.uniform(-10, 10, n)
+    sites["energy"] = 1.0
+    sites["key"] = np.arange(n, dtype=np.uint64) + 1
+    pinned = torch.empty(n * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(SITE_DTYPE)
+    pinned[:] = sites
+    cap = n * max(1, ctx.info.max_yield)
+
+    def pinned_out(k):
+        return torch.empty(k * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(SITE_DTYPE)
+
+    out1 = np.zeros(cap, SITE_DTYPE)
+    m1 = ctx.transport_bank_into(sites, out1, rng=RNG_MINSTD)
+    assert m1 > 0
+    for src, out in ((pinned, np.zeros(cap, SITE_DTYPE)), (sites, pinned_out(cap)), (pinned, pinned_out(cap))):
+        m = ctx.transport_bank_into(src, out, rng=RNG_MINSTD)
+        assert m == m1
+        assert np.array_equal(out[:m], out1[:m1])
+    # a page-locked output of half the bank: the call reports the overflow,
+    # writes the first half and nothing past it
+    half = m1 // 2
+    guard = pinned_out(half + 64)
+    guard[:] = np.zeros(1, SITE_DTYPE)
+    guard["key"][half:] = 0xABCDEF
+    with pytest.raises(MCError):
+        ctx.check(ctx.lib.mc_transport_bank(ctx.h, pinned.ctypes.data_as(C.c_void_p), n,
+                                            C.byref(ctx.opts(rng=RNG_MINSTD)), guard.ctypes.data_as(C.c_void_p),
+                                            half, C.byref(C.c_uint64())))
+    assert np.array_equal(guard[:half], out1[:half])
+    assert (guard["key"][half:] == 0xABCDEF).all()
