@@ -1778,7 +1778,7 @@ int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __half* X, const float* y, uint
   CUDA_TRY(c, cudaMemcpyAsync(net.p, p0.data(), p0.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(net.m, 0, mcd::kMlpParams * sizeof(float), c->stream));
   CUDA_TRY(c, cudaMemsetAsync(net.v, 0, mcd::kMlpParams * sizeof(float), c->stream));
-  CUDA_TRY(c, mcd::mlp_refresh_bf16(net, c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_weights(net, c->stream));
   float* losses = mlp_alloc<float>(c, d.steps);
   if (!losses) return fail(c, MC_ERR_OOM, "surrogate loss buffer");
   mcd::MlpBatch b = c->mlp_batch;
@@ -2025,8 +2025,8 @@ int mc_surrogate_set(mc_ctx* c, int32_t tsl, const mc_train_desc* box, const flo
   b.beta_scale = std::log1p(std::max(t.beta_cutoff, box->E_max / (mcd::kBoltzmann * box->T_min)));
   CUDA_TRY(c, cudaMemcpy(c->mlp[0].p, beta_params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->mlp[1].p, alpha_params, mcd::kMlpParams * sizeof(float), cudaMemcpyHostToDevice));
-  CUDA_TRY(c, mcd::mlp_refresh_bf16(c->mlp[0], c->stream));
-  CUDA_TRY(c, mcd::mlp_refresh_bf16(c->mlp[1], c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_weights(c->mlp[0], c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_weights(c->mlp[1], c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->mlp_box = b;
   c->mlp_tsl = tsl;
@@ -2056,7 +2056,7 @@ int mc_surrogate_grad(mc_ctx* c, const float* params, const float* x, const floa
   CUDA_TRY(c, cudaMemcpyAsync(b.X, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(b.Xt, hxt.data(), hxt.size() * 2, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(b.y, y, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, mcd::mlp_refresh_bf16(net, c->stream));
+  CUDA_TRY(c, mcd::mlp_refresh_weights(net, c->stream));
   CUDA_TRY(c, mcd::mlp_forward_backward(net, b, c->stream));
   c->launches += 10;
   CUDA_TRY(c, cudaMemcpyAsync(grad, net.g, mcd::kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream));

@@ -295,7 +295,7 @@ __device__ int g_mlp_err;
 
 }  // namespace
 
-cudaError_t mlp_refresh_bf16(const MlpNet& net, cudaStream_t s) {
+cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s) {
   k_refresh<<<kMlpWidth * kMlpWidth / 256, 256, 0, s>>>(net.p, net.W1, net.W2, net.W3, net.W2t, net.W3t);
   return cudaGetLastError();
 }
@@ -368,7 +368,7 @@ cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s) {
   k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(net.p, net.g, net.m, net.v, kMlpParams, lr, c1, c2);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return mlp_refresh_bf16(net, s);
+  return mlp_refresh_weights(net, s);
 }
 
 // ---------------------------------------------------------------------------

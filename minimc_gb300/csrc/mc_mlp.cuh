@@ -79,7 +79,7 @@ struct MlpBatch {
 };
 
 // launches (mc_mlp.cu); all stream-ordered
-cudaError_t mlp_refresh_bf16(const MlpNet& net, cudaStream_t s);
+cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s);
 cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s);
 cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s);
 // inference on a batch of inputs (debug/grad-check path): out[B]
