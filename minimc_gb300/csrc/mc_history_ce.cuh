@@ -220,13 +220,26 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
             const float2 ba = rp.tq_out[qi];
             bool ok = false;
             if (isfinite(ba.x) && isfinite(ba.y)) {
-              // ThermalScattering::Scatter's kinematics (src/ThermalScattering.cpp:159-171)
+              // ThermalScattering::Scatter's kinematics (src/ThermalScattering.cpp:159-171);
+              // the outgoing energy in FP64, the cosine and the rotation in
+              // FP32 in fast mode (the surrogate's (beta, alpha) are FP32)
               const double kT = kBoltzmann * R.T;
               const double Ep = p.E + static_cast<double>(ba.x) * kT;
               if (Ep > 0) {
-                const double mu = fmin(1.0, fmax(-1.0, (p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT) /
-                                                           (2.0 * sqrt(p.E * Ep))));
-                rotate(p.u, p.v, p.w, mu, 2 * kPi * p.rng.u01());
+                if (ffg) {
+                  const float num = __double2float_rn(p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT);
+                  const float mu = fminf(1.0f, fmaxf(-1.0f, __fdiv_rn(num, 2.0f * __fsqrt_rn(__double2float_rn(p.E * Ep)))));
+                  float dx = static_cast<float>(p.u), dy = static_cast<float>(p.v), dz = static_cast<float>(p.w);
+                  rotate_f(dx, dy, dz, mu, p.rng.u01f());
+                  p.u = dx;
+                  p.v = dy;
+                  p.w = dz;
+                }
+                else {
+                  const double mu = fmin(1.0, fmax(-1.0, (p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT) /
+                                                             (2.0 * sqrt(p.E * Ep))));
+                  rotate(p.u, p.v, p.w, mu, 2 * kPi * p.rng.u01());
+                }
                 p.E = Ep;
                 ok = true;
               }
