@@ -325,7 +325,9 @@ def run_gpu(args) -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": int(d2h_total / max(1, args.steps)),
                     "call": "mc_transport_bank (pinned host banks: the transport kernel reads the sites in host "
-                            "memory over the chip-to-chip link; the fission bank is copied out)"},
+                            "memory over the chip-to-chip link; multigroup Philox fission sites are sampled "
+                            "straight into the host bank, coalesced, while the score commit runs on a second "
+                            "stream)"},
             "gpu_launches": int(launches),
             "clocks": clk,
             "wall_s": wall,

@@ -69,6 +69,16 @@ extern "C" {
                                   dead lanes refilled from the queue      */
 #define MC_SCHEDULE_EVENT 2    /* event kernels over compacted queues     */
 
+/* How k-eigenvalue fission sites reach the compacted bank.  Both paths give
+ * the same bank, site for site. */
+#define MC_BANK_AUTO 0    /* direct where it applies, else slots          */
+#define MC_BANK_SLOTS 1   /* per-history slots, a scan, then a compaction */
+#define MC_BANK_DIRECT 2  /* counts known before sampling (multigroup,
+                             Philox streams, every chi cdf ending above the
+                             largest uniform drawn): a scan, then the sites
+                             sampled straight into their bank positions;
+                             MC_ERR_INPUT where that does not hold        */
+
 typedef struct mc_ctx mc_ctx;
 
 typedef struct {
@@ -84,7 +94,8 @@ typedef struct {
                            geometry and positions stay FP64            */
   int32_t variant;      /* history-kernel variant + 1; 0 -> autotuned   */
   int32_t thermal;      /* MC_THERMAL_*: thermal scattering sampler      */
-  int32_t reserved[5];
+  int32_t bank_path;    /* MC_BANK_*: k-eigenvalue fission-site path     */
+  int32_t reserved[4];
 } mc_run_opts;
 
 /* A particle in a bank: the state that Bank/Particle carry between

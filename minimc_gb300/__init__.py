@@ -7,6 +7,7 @@ from .engine import (  # noqa: F401
     Batch, Context, Driver, World, MCError, RunOpts, SITE_DTYPE, EVENTS,
     RNG_PHILOX, RNG_MINSTD, SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT, TSL_POD, TSL_MLP, TSL_PHILOX, TSL_FAST,
     GEOMETRY_ROBUST, GEOMETRY_REFERENCE, MLP_PARAMS, TrainDesc, TrainOut, THERMAL_POD, THERMAL_SURROGATE,
+    BANK_AUTO, BANK_SLOTS, BANK_DIRECT,
     load_library, library_path, exported_symbols,
 )
 
@@ -14,5 +15,5 @@ __all__ = [
     "Batch", "Context", "Driver", "World", "MCError", "RunOpts", "SITE_DTYPE", "EVENTS",
     "RNG_PHILOX", "RNG_MINSTD", "SCHEDULE_AUTO", "SCHEDULE_HISTORY", "SCHEDULE_EVENT",
     "TSL_POD", "TSL_MLP", "TSL_PHILOX", "TSL_FAST", "GEOMETRY_ROBUST", "GEOMETRY_REFERENCE", "MLP_PARAMS", "TrainDesc", "TrainOut",
-    "THERMAL_POD", "THERMAL_SURROGATE", "load_library", "library_path", "exported_symbols",
+    "THERMAL_POD", "THERMAL_SURROGATE", "BANK_AUTO", "BANK_SLOTS", "BANK_DIRECT", "load_library", "library_path", "exported_symbols",
 ]

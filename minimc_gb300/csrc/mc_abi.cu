@@ -41,11 +41,21 @@ struct mc_ctx {
   DevWorld dw{};
   int32_t geometry_mode = MC_GEOMETRY_ROBUST;
   uint32_t max_yield = 1;
+  // smallest last entry of a chi cdf that a fission can draw from (+inf
+  // without fission): the direct bank path needs it above every threshold
+  double chi_last_min = HUGE_VAL;
+  // page-locked staging for the values a call reads back at its one
+  // synchronisation: bank size, then the counters
+  void* h_small = nullptr;
   uint64_t total_bins = 0;
   DevCounters* d_ctr = nullptr;
   double* d_sum = nullptr;
   double* d_sq = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  // second stream: the dense-score commit overlaps the bank kernels there
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool side_pending = false;  // the main stream has not yet waited for ev_join
   double last_kernel_ms = 0;  // main transport kernel(s) of the last run_transport
   const double* pend_clean = nullptr;  // dense score array known to be all zero
   size_t pend_clean_bytes = 0;
@@ -71,7 +81,7 @@ struct mc_ctx {
     bool active = false;
     uint64_t n = 0, seed = 1;
     uint32_t inactive = 0, act = 0, cycle = 0;
-    int rng = 0, fast = 0, block = 256, schedule = 0;
+    int rng = 0, fast = 0, block = 256, schedule = 0, bank_path = 0;
     uint32_t max_events = 1000000;
     std::vector<double> k, ktl;
     std::vector<uint64_t> bank;
@@ -92,6 +102,19 @@ __global__ void k_compact_capped(const Site* slots, const uint32_t* count, const
   const unsigned long long o = offsets[i];
   for (uint32_t k = 0; k < c; k++)
     if (o + k < cap) out[o + k] = slots[i * max_yield + k];
+}
+
+// the compacted bank, min(*total, cap) sites, into page-locked host memory:
+// coalesced 16-byte stores (the bank size stays on the device, so the copy
+// needs no host round trip first)
+static_assert(sizeof(Site) % sizeof(uint4) == 0, "sites are copied as 16-byte words");
+__global__ void k_copy_bank_out(const uint4* bank, const unsigned long long* total, unsigned long long cap,
+                                uint4* out) {
+  const unsigned long long m = *total < cap ? *total : cap;
+  const unsigned long long words = m * (sizeof(Site) / sizeof(uint4));
+  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < words;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    out[i] = __ldcs(bank + i);
 }
 
 
@@ -340,6 +363,7 @@ int build_world(mc_ctx* c) {
   UP(mat_afrac, mat_afrac)
 
   c->max_yield = 1;
+  c->chi_last_min = HUGE_VAL;
   if (m.energy_mode == mc::kMultigroup) {
     const size_t G = m.groups, N = m.nuclides.size(), M = m.materials.size(), T = 2;
     std::vector<double> total(T * N * G, 0), rx(T * N * G * 3, 0), scat(T * N * G * G, 0), nubar(T * N * G, 0),
@@ -376,6 +400,7 @@ int build_world(mc_ctx* c) {
               a = a + d.chi[g * G + go];
               chi[i * G + go] = a;
             }
+            if (d.nubar[g] > 0) c->chi_last_min = std::min(c->chi_last_min, a);
           }
         }
       }
@@ -728,7 +753,21 @@ int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap) {
 }
 
 // one transport launch over rp.n particles; returns elapsed device ms
-int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int schedule = MC_SCHEDULE_AUTO) {
+// the main stream waits for the work on the side stream
+int join_side(mc_ctx* c) {
+  if (c->side_pending) {
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    c->side_pending = false;
+  }
+  return MC_OK;
+}
+
+// side_commit: the dense-score commit runs on the side stream, overlapping
+// what the caller queues next on the main stream; join_side (or read_back)
+// orders it before anything that reads the tallies or the score array.
+int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int schedule = MC_SCHEDULE_AUTO,
+                  bool side_commit = false) {
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
   CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
   rp.ctr = c->d_ctr;
   rp.tally_sum = c->d_sum;
@@ -782,15 +821,25 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     }
   }
   CUDA_TRY(c, cudaEventRecord(c->evk1, c->stream));
-  if (keig) {
+  if (keig && !rp.direct_sites) {  // direct: the sites are sampled into the bank later
     if (c->model.energy_mode == mc::kMultigroup)
       CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, sites_grid(rp.n), c->stream));
     else CUDA_TRY(c, mcd::launch_fission_sites_ce(rp, rng, sites_grid(rp.n), c->stream));
     c->launches++;
   }
   if (rp.nb) {
-    CUDA_TRY(c, mcd::launch_commit_dense(rp, c->num_sms * 8, c->stream));
+    cudaStream_t cs = c->stream;
+    if (side_commit) {
+      CUDA_TRY(c, cudaEventRecord(c->ev_fork, c->stream));
+      CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+      cs = c->side;
+    }
+    CUDA_TRY(c, mcd::launch_commit_dense(rp, c->num_sms * 8, cs));
     c->launches++;
+    if (side_commit) {
+      CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
+      c->side_pending = true;
+    }
   }
   c->pend_clean = pend_before;
   CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
@@ -856,23 +905,73 @@ int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
   return MC_OK;
 }
 
-// scan + compact the per-history fission slots; returns the bank size
-int compact_bank(mc_ctx* c, uint64_t n, Site** bank_out, uint64_t* m_out) {
-  auto* slots = static_cast<Site*>(c->scratch[kSlots].p);
+// Fission sites go straight into the compacted bank (no per-history slots)
+// when each record's site count is known before sampling: multigroup,
+// Philox streams, every chi cdf a fission draws from ending above the
+// largest uniform the stream draws (1 - 2^-24 in the FP32 form, 1 - 2^-52 in
+// the FP64 form), and a CTA's sites fitting its shared-memory stage.
+// 1: direct, 0: slots, -1: MC_BANK_DIRECT asked for where it does not apply.
+int bank_direct(const mc_ctx* c, int rng, bool fast, int path) {
+  if (path == MC_BANK_SLOTS) return 0;
+  const bool ok = c->model.energy_mode == mc::kMultigroup && rng == MC_RNG_PHILOX &&
+                  c->chi_last_min > (fast ? 1.0 - 0x1p-24 : 1.0 - 0x1p-52) && mcd::sites_out_fits(c->max_yield);
+  if (path == MC_BANK_DIRECT) return ok ? 1 : -1;
+  return ok ? 1 : 0;
+}
+
+// The cycle's fission sites as a compacted bank in history order.  Slot
+// path: the slot kernel has run; a scan of its counts places each history's
+// sites and a compaction copies them into the device bank.  Direct path:
+// counts from the fission records, their scan, then the sites sampled
+// straight into `dest` (16-byte aligned page-locked host memory, `cap`
+// sites) or else into the device bank.  *bank_out is the device bank (null
+// when the sites went to `dest`); the size stays on the device (scratch
+// kTotal) unless read_size, which reads it into *m_out.
+int emit_bank(mc_ctx* c, const RunParams& rp, Site* dest, uint64_t cap, Site** bank_out, uint64_t* m_out,
+              bool read_size = true) {
+  const uint64_t n = rp.n;
   auto* count = static_cast<uint32_t*>(c->scratch[kCount].p);
   auto* offsets = static_cast<unsigned long long*>(scratch(c, kOffsets, n * 8));
   auto* sums = static_cast<unsigned long long*>(scratch(c, kScanSums, ((n + 1023) / 1024 + 1) * 8));
   auto* total = static_cast<unsigned long long*>(scratch(c, kTotal, 8));
-  auto* bank = static_cast<Site*>(scratch(c, kBank, n * c->max_yield * sizeof(Site)));
-  if (!offsets || !sums || !total || !bank) return fail(c, MC_ERR_OOM, "bank scratch allocation failed");
-  CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
-  CUDA_TRY(c, mcd::launch_bank_compact(slots, count, offsets, n, c->max_yield, bank, c->stream));
-  c->launches += 4;
+  Site* bank = dest ? nullptr : static_cast<Site*>(scratch(c, kBank, n * c->max_yield * sizeof(Site)));
+  if (!offsets || !sums || !total || (!dest && !bank)) return fail(c, MC_ERR_OOM, "bank scratch allocation failed");
+  if (rp.direct_sites) {
+    RunParams q = rp;
+    q.ctr = c->d_ctr;
+    q.bank_count = count;
+    CUDA_TRY(c, mcd::launch_fission_counts_mg(q, c->stream));
+    CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
+    CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, dest ? cap : n * c->max_yield,
+                                                 dest ? dest : bank, c->stream));
+    c->launches += 5;
+  }
+  else {
+    auto* slots = static_cast<Site*>(c->scratch[kSlots].p);
+    CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
+    CUDA_TRY(c, mcd::launch_bank_compact(slots, count, offsets, n, c->max_yield, bank, c->stream));
+    c->launches += 4;
+  }
   unsigned long long m = 0;
-  CUDA_TRY(c, cudaMemcpyAsync(&m, total, 8, cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (read_size) {
+    CUDA_TRY(c, cudaMemcpyAsync(&m, total, 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
   *bank_out = bank;
   *m_out = m;
+  return MC_OK;
+}
+
+// bank size (when m) and counters, read back with one synchronisation
+int read_back(mc_ctx* c, uint64_t* m, DevCounters* h) {
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
+  auto* hm = static_cast<unsigned long long*>(c->h_small);
+  auto* hc = reinterpret_cast<DevCounters*>(static_cast<char*>(c->h_small) + 64);
+  if (m) CUDA_TRY(c, cudaMemcpyAsync(hm, c->scratch[kTotal].p, 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(hc, c->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (m) *m = *hm;
+  *h = *hc;
   return MC_OK;
 }
 
@@ -893,6 +992,15 @@ int mc_create(mc_ctx** out, int device) {
     return MC_ERR_DEVICE;
   }
   c->own_stream = true;
+  if (cudaMallocHost(&c->h_small, 512) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+    if (c->h_small) cudaFreeHost(c->h_small);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MC_ERR_OOM;
+  }
+  cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
@@ -914,6 +1022,13 @@ void mc_destroy(mc_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->evk0) cudaEventDestroy(c->evk0);
   if (c->evk1) cudaEventDestroy(c->evk1);
+  if (c->h_small) cudaFreeHost(c->h_small);
+  if (c->side) {
+    cudaStreamSynchronize(c->side);
+    cudaStreamDestroy(c->side);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1126,6 +1241,7 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   k.block = pick_block(o);
   k.schedule = o ? o->schedule : 0;
   k.max_events = o && o->max_events ? o->max_events : 1000000u;
+  k.bank_path = o ? o->bank_path : MC_BANK_AUTO;
   k.launches0 = c->launches;
   // tune the history kernel on the first inactive cycle unless the caller
   // fixed the block size
@@ -1133,6 +1249,10 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   if (o && o->variant > 0) c->variant = std::min(o->variant - 1, mcd::history_variants() - 1);
   if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
+  if (k.bank_path < MC_BANK_AUTO || k.bank_path > MC_BANK_DIRECT) return fail(c, MC_ERR_INPUT, "unknown bank path");
+  if (bank_direct(c, k.rng, k.fast != 0, k.bank_path) < 0)
+    return fail(c, MC_ERR_INPUT, "the direct bank path needs multigroup data, Philox streams and chi cdfs that end "
+                                 "above every threshold the stream draws");
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
       !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
     return fail(c, MC_ERR_OOM, "k-eigenvalue bank allocation failed");
@@ -1162,7 +1282,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.src = static_cast<const Site*>(c->scratch[kSrc].p);
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
-  double ms = 0;
+  rp.direct_sites = bank_direct(c, k.rng, k.fast != 0, k.bank_path) > 0 ? 1 : 0;
   if (!active && c->tune_pending && resolve_schedule(c, k.schedule) == MC_SCHEDULE_HISTORY) {
     // Autotuner: every variant transports this (inactive, unscored) cycle;
     // the variants draw the same numbers and give identical results, so
@@ -1183,16 +1303,23 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
     }
     c->variant = best;
   }
-  int rc = run_transport(c, rp, k.rng, k.block, &ms, k.schedule);
+  // transport, bank and read-back with one synchronisation; the cycle's
+  // timing events have completed by then
+  int rc = run_transport(c, rp, k.rng, k.block, nullptr, k.schedule, /*side_commit=*/true);
   if (rc != MC_OK) return rc;
-  k.transport_ms += ms;
-  k.kernel_ms += c->last_kernel_ms;
   Site* bank = nullptr;
   uint64_t m = 0;
-  rc = compact_bank(c, k.n, &bank, &m);
+  rc = emit_bank(c, rp, nullptr, 0, &bank, &m, /*read_size=*/false);
   if (rc != MC_OK) return rc;
   DevCounters h{};
-  CUDA_TRY(c, cudaMemcpy(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost));
+  rc = read_back(c, &m, &h);
+  if (rc != MC_OK) return rc;
+  float f = 0;
+  CUDA_TRY(c, cudaEventElapsedTime(&f, c->ev0, c->ev1));
+  k.transport_ms += f;
+  CUDA_TRY(c, cudaEventElapsedTime(&f, c->evk0, c->evk1));
+  c->last_kernel_ms = f;
+  k.kernel_ms += f;
   k.events += h.events;
   k.lost += h.lost;
   k.capped += h.capped;
@@ -1215,6 +1342,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
 int mc_keig_status(mc_ctx* c, mc_keig_out* out) {
   if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
   auto& k = c->keig;
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   if (out) {
     const size_t nc = k.k.size();
@@ -1319,6 +1447,7 @@ int mc_keig_checkpoint(mc_ctx* c, void* buf, uint64_t cap, uint64_t* size) {
   if (size) *size = bytes;
   if (!buf) return MC_OK;
   if (cap < bytes) return fail(c, MC_ERR_OVERFLOW, "checkpoint buffer too small");
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
   CkptHeader h{};
   std::memcpy(h.magic, kCkptMagic, 8);
   h.n = k.n;
@@ -1442,8 +1571,15 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
     return MC_OK;
   }
   if (!sites) return fail(c, MC_ERR_INPUT, "sites is NULL");
+  const int path = o ? o->bank_path : MC_BANK_AUTO;
+  if (path < MC_BANK_AUTO || path > MC_BANK_DIRECT) return fail(c, MC_ERR_INPUT, "unknown bank path");
+  const bool fast = o && o->fast_math && rng == MC_RNG_PHILOX;
+  const int direct = bank_direct(c, rng, fast, path);
+  if (direct < 0)
+    return fail(c, MC_ERR_INPUT, "the direct bank path needs multigroup data, Philox streams and chi cdfs that end "
+                                 "above every threshold the stream draws");
   cudaSetDevice(c->device);
-  if (!scratch(c, kSlots, n * c->max_yield * sizeof(Site)) || !scratch(c, kCount, n * 4))
+  if ((!direct && !scratch(c, kSlots, n * c->max_yield * sizeof(Site))) || !scratch(c, kCount, n * 4))
     return fail(c, MC_ERR_OOM, "bank allocation failed");
   // Sites in page-locked host memory are read in place by the transport
   // kernel (each site once, coalesced, when its history starts), so the
@@ -1475,20 +1611,43 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   rp.src = src;
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
-  int rc = run_transport(c, rp, rng, pick_block(o), nullptr, o ? o->schedule : MC_SCHEDULE_AUTO);
+  rp.direct_sites = direct;
+  int rc = run_transport(c, rp, rng, pick_block(o), nullptr, o ? o->schedule : MC_SCHEDULE_AUTO,
+                         /*side_commit=*/true);
   if (rc != MC_OK) return rc;
-  // the bank is compacted on the device and copied out (a compaction kernel
-  // writing it into page-locked host memory in place measured slower: its
-  // scattered 64-byte writes cross the chip-to-chip link one site at a time)
+  // Page-locked output (16-byte aligned) is written in place over the
+  // chip-to-chip link with coalesced 16-byte stores, by the direct site
+  // kernel or by a copy kernel after the compaction, and the bank size stays
+  // on the device until the one read-back; pageable output gets a copy after
+  // the size is read.  (A compaction kernel writing into host memory one site
+  // per thread measured slower: its scattered 64-byte writes cross the link
+  // one site at a time.)
+  Site* out_mapped = nullptr;
+  if (fission_sites && cap) {
+    cudaPointerAttributes oa{};
+    if (cudaPointerGetAttributes(&oa, fission_sites) == cudaSuccess && oa.type == cudaMemoryTypeHost &&
+        oa.devicePointer && reinterpret_cast<uintptr_t>(oa.devicePointer) % 16 == 0)
+      out_mapped = static_cast<Site*>(oa.devicePointer);
+    else
+      (void)cudaGetLastError();
+  }
   Site* bank = nullptr;
   uint64_t m = 0;
-  rc = compact_bank(c, n, &bank, &m);
+  rc = emit_bank(c, rp, direct ? out_mapped : nullptr, cap, &bank, &m, /*read_size=*/out_mapped == nullptr);
   if (rc != MC_OK) return rc;
-  if (fission_sites && cap)
+  if (out_mapped && bank) {
+    k_copy_bank_out<<<c->num_sms * 8, 256, 0, c->stream>>>(
+        reinterpret_cast<const uint4*>(bank), static_cast<const unsigned long long*>(c->scratch[kTotal].p), cap,
+        reinterpret_cast<uint4*>(out_mapped));
+    CUDA_TRY(c, cudaGetLastError());
+    c->launches++;
+  }
+  else if (!out_mapped && fission_sites && cap) {
     CUDA_TRY(c, cudaMemcpyAsync(fission_sites, bank, std::min(m, cap) * sizeof(Site), cudaMemcpyDeviceToHost, c->stream));
+  }
   DevCounters h{};
-  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  rc = read_back(c, out_mapped ? &m : nullptr, &h);
+  if (rc != MC_OK) return rc;
   if (n_out) *n_out = m;
   if (m > cap) return fail(c, MC_ERR_OVERFLOW, "fission bank larger than the output capacity");
   return counters_status(c, h);
@@ -1496,6 +1655,7 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
 
 int mc_tallies_reset(mc_ctx* c) {
   if (!check_ctx(c)) return MC_ERR_STATE;
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
   const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
   CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
@@ -1505,6 +1665,7 @@ int mc_tallies_reset(mc_ctx* c) {
 
 int mc_tallies_get(mc_ctx* c, double* sum, double* sum_sq) {
   if (!check_ctx(c)) return MC_ERR_STATE;
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
   if (sum) CUDA_TRY(c, cudaMemcpyAsync(sum, c->d_sum, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
   if (sum_sq) CUDA_TRY(c, cudaMemcpyAsync(sum_sq, c->d_sq, c->total_bins * 8, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

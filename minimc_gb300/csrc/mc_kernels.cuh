@@ -91,6 +91,7 @@ struct RunParams {
   float4* tq_in;                       // (E, T, u1, u2) per parked record
   unsigned long long* park_count;      // records parked by this launch
   unsigned long long park_cap;
+  int32_t direct_sites;  // k-eigenvalue: sites go straight into the bank (no slot kernel)
 };
 
 // k-eigenvalue sites from fission records and the per-history commit of
@@ -98,6 +99,21 @@ struct RunParams {
 cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid,
                                     cudaStream_t stream);
 cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream);
+
+// k-eigenvalue sites straight into a compacted bank (multigroup, Philox
+// streams), for chi cdfs that all end above the largest uniform the stream
+// draws: per-history counts min(n, max_yield) into bank_count, then (after a
+// scan of the counts) the sites, staged per CTA of kSitesOutHist histories in
+// shared memory and stored to `out` (device or page-locked host memory,
+// 16-byte aligned) with coalesced 16-byte writes; sites at or past `cap` are
+// not written
+constexpr int kSitesOutHist = 128;
+constexpr size_t kSitesOutMaxSmem = 192 * 1024;
+cudaError_t launch_fission_counts_mg(const RunParams& rp, cudaStream_t stream);
+bool sites_out_fits(uint32_t max_yield);
+cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
+                                        const unsigned long long* total, unsigned long long cap, Site* out,
+                                        cudaStream_t stream);
 
 // launches (mc_transport.cu)
 // history-schedule kernel variants differ only in their occupancy target

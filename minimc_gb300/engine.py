@@ -34,6 +34,7 @@ RNG_PHILOX, RNG_MINSTD = 0, 1
 SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT = 0, 1, 2
 TSL_POD, TSL_MLP = 0, 1
 THERMAL_POD, THERMAL_SURROGATE = 0, 1  # run option `thermal` (MC_THERMAL_*)
+BANK_AUTO, BANK_SLOTS, BANK_DIRECT = 0, 1, 2  # run option `bank_path` (MC_BANK_*)
 TSL_PHILOX, TSL_FAST = 0x10, 0x20  # method flags: Philox streams, FP32 POD form
 GEOMETRY_ROBUST, GEOMETRY_REFERENCE = 0, 1
 
@@ -53,7 +54,8 @@ class RunOpts(C.Structure):
     _fields_ = [("histories", C.c_uint64), ("seed", C.c_uint64), ("inactive", C.c_uint32),
                 ("active", C.c_uint32), ("rng", C.c_int32), ("schedule", C.c_int32),
                 ("max_events", C.c_uint32), ("block_size", C.c_int32), ("fast_math", C.c_int32),
-                ("variant", C.c_int32), ("thermal", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("variant", C.c_int32), ("thermal", C.c_int32), ("bank_path", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Site(C.Structure):

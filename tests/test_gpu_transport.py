@@ -14,8 +14,8 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from minimc_gb300 import (GEOMETRY_REFERENCE, RNG_MINSTD, RNG_PHILOX, SCHEDULE_EVENT, SCHEDULE_HISTORY, Context,
-                          MCError, synth)
+from minimc_gb300 import (BANK_DIRECT, BANK_SLOTS, GEOMETRY_REFERENCE, RNG_MINSTD, RNG_PHILOX, SCHEDULE_EVENT,
+                          SCHEDULE_HISTORY, Context, MCError, synth)
 from oracle.build import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -230,3 +230,93 @@ def test_transport_bank_pinned_sites_read_in_place(built_library):
                                             half, C.byref(C.c_uint64())))
     assert np.array_equal(guard[:half], out1[:half])
     assert (guard["key"][half:] == 0xABCDEF).all()
+
+
+def _bank_sites(n, seed):
+    rng = np.random.default_rng(seed)
+    from minimc_gb300 import SITE_DTYPE
+
+    sites = np.zeros(n, SITE_DTYPE)
+    mu = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    sites["u"], sites["v"], sites["w"] = mu, np.sqrt(1 - mu * mu) * np.cos(ph), np.sqrt(1 - mu * mu) * np.sin(ph)
+    sites["x"] = rng.uniform(-10, 10, n)
+    sites["energy"] = 1.0
+    sites["key"] = np.arange(n, dtype=np.uint64) + 7
+    return sites
+
+
+@pytest.mark.parametrize("fast", [0, 1])
+def test_bank_direct_path_equals_slot_path(fast, built_library):
+    """Philox fission sites sampled straight into their bank positions (into
+    page-locked host memory in place, or into the device bank) equal the
+    per-history slots + compaction path site for site; a too-small
+    page-locked output is filled to its end and not overrun."""
+    import ctypes as C
+
+    import torch
+
+    from minimc_gb300 import SITE_DTYPE
+
+    p = synth.two_zone_cubes(histories=20000, groups=4)
+    ctx = gpu_ctx(p.xml())
+    n = 20000
+    sites = _bank_sites(n, 5)
+    cap = n * max(1, ctx.info.max_yield)
+
+    def pinned(k):
+        return torch.empty(k * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(SITE_DTYPE)
+
+    opts = dict(rng=RNG_PHILOX, fast_math=fast)
+    ref = np.zeros(cap, SITE_DTYPE)
+    m0 = ctx.transport_bank_into(sites, ref, bank_path=BANK_SLOTS, **opts)
+    assert m0 > 0
+    for path, out in ((BANK_SLOTS, pinned(cap)), (BANK_DIRECT, np.zeros(cap, SITE_DTYPE)), (BANK_DIRECT, pinned(cap))):
+        m = ctx.transport_bank_into(sites, out, bank_path=path, **opts)
+        assert m == m0
+        assert np.array_equal(out[:m].view(np.uint8), ref[:m0].view(np.uint8))
+    half = m0 // 2
+    guard = pinned(half + 64)
+    guard[:] = np.zeros(1, SITE_DTYPE)
+    guard["key"][half:] = 0xABCDEF
+    with pytest.raises(MCError):
+        ctx.check(ctx.lib.mc_transport_bank(ctx.h, sites.ctypes.data_as(C.c_void_p), n,
+                                            C.byref(ctx.opts(bank_path=BANK_DIRECT, **opts)),
+                                            guard.ctypes.data_as(C.c_void_p), half, C.byref(C.c_uint64())))
+    assert np.array_equal(guard[:half].view(np.uint8), ref[:half].view(np.uint8))
+    assert (guard["key"][half:] == 0xABCDEF).all()
+
+
+def test_bank_direct_path_keig_cycles(built_library):
+    """k-eigenvalue cycles give the same bank sizes (k per cycle) and tallies
+    on both bank paths, in both Philox forms."""
+    p = synth.two_zone_cubes(histories=50000, inactive=2, active=3)
+    xml = p.xml()
+    for fast in (0, 1):
+        a = gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=fast, bank_path=BANK_SLOTS)
+        b = gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=fast, bank_path=BANK_DIRECT)
+        assert np.array_equal(a.bank_size, b.bank_size)
+        assert np.array_equal(a.k_cycle, b.k_cycle)
+        np.testing.assert_allclose(b.sum, a.sum, rtol=FP_RTOL)
+
+
+def test_bank_direct_path_rejected_where_counts_are_unknown(built_library):
+    """The direct path needs Philox streams and chi cdfs that end above every
+    threshold drawn: reference streams are refused, and so is the FP64 form
+    for a chi whose normalised cdf ends one ulp short of the largest uniform
+    it draws (the automatic choice takes the slot path there)."""
+    p = synth.two_zone_cubes(histories=2000, groups=4, inactive=1, active=1)
+    ctx = gpu_ctx(p.xml())
+    with pytest.raises(MCError, match="direct bank path"):
+        ctx.run_keigenvalue(rng=RNG_MINSTD, bank_path=BANK_DIRECT)
+    # chi (1, 4, 1, 1) / 7: the cdf ends at 1 - 2^-52, the FP64 form's
+    # largest uniform (the FP32 form draws at most 1 - 2^-24)
+    p.nuclides[0].chi = np.tile(np.array([1.0, 4.0, 1.0, 1.0])[:, None], (1, 4))
+    ctx = gpu_ctx(p.xml())
+    with pytest.raises(MCError, match="direct bank path"):
+        ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=0, bank_path=BANK_DIRECT)
+    a = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=1, bank_path=BANK_DIRECT)
+    b = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=1, bank_path=BANK_SLOTS)
+    assert np.array_equal(a.bank_size, b.bank_size)
+    r = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=0)
+    assert (np.asarray(r.bank_size) > 0).all()
