@@ -906,15 +906,18 @@ int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
 }
 
 // Fission sites go straight into the compacted bank (no per-history slots)
-// when each record's site count is known before sampling: multigroup,
-// Philox streams, every chi cdf a fission draws from ending above the
-// largest uniform the stream draws (1 - 2^-24 in the FP32 form, 1 - 2^-52 in
-// the FP64 form), and a CTA's sites fitting its shared-memory stage.
+// when each record's site count is known before sampling and a CTA's sites
+// fit its shared-memory stage.  Continuous energy: always (the sites take
+// the incident energy).  Multigroup: Philox streams and every chi cdf a
+// fission draws from ending above the largest uniform the stream draws
+// (1 - 2^-24 in the FP32 form, 1 - 2^-52 in the FP64 form; a minstd uniform
+// can round to 1).
 // 1: direct, 0: slots, -1: MC_BANK_DIRECT asked for where it does not apply.
 int bank_direct(const mc_ctx* c, int rng, bool fast, int path) {
   if (path == MC_BANK_SLOTS) return 0;
-  const bool ok = c->model.energy_mode == mc::kMultigroup && rng == MC_RNG_PHILOX &&
-                  c->chi_last_min > (fast ? 1.0 - 0x1p-24 : 1.0 - 0x1p-52) && mcd::sites_out_fits(c->max_yield);
+  const bool counts_known = c->model.energy_mode != mc::kMultigroup ||
+                            (rng == MC_RNG_PHILOX && c->chi_last_min > (fast ? 1.0 - 0x1p-24 : 1.0 - 0x1p-52));
+  const bool ok = counts_known && mcd::sites_out_fits(c->max_yield);
   if (path == MC_BANK_DIRECT) return ok ? 1 : -1;
   return ok ? 1 : 0;
 }
@@ -927,7 +930,7 @@ int bank_direct(const mc_ctx* c, int rng, bool fast, int path) {
 // sites) or else into the device bank.  *bank_out is the device bank (null
 // when the sites went to `dest`); the size stays on the device (scratch
 // kTotal) unless read_size, which reads it into *m_out.
-int emit_bank(mc_ctx* c, const RunParams& rp, Site* dest, uint64_t cap, Site** bank_out, uint64_t* m_out,
+int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap, Site** bank_out, uint64_t* m_out,
               bool read_size = true) {
   const uint64_t n = rp.n;
   auto* count = static_cast<uint32_t*>(c->scratch[kCount].p);
@@ -940,10 +943,12 @@ int emit_bank(mc_ctx* c, const RunParams& rp, Site* dest, uint64_t cap, Site** b
     RunParams q = rp;
     q.ctr = c->d_ctr;
     q.bank_count = count;
-    CUDA_TRY(c, mcd::launch_fission_counts_mg(q, c->stream));
+    CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
     CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
-    CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, dest ? cap : n * c->max_yield,
-                                                 dest ? dest : bank, c->stream));
+    const uint64_t qcap = dest ? cap : n * c->max_yield;
+    if (c->model.energy_mode == mc::kMultigroup)
+      CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, qcap, dest ? dest : bank, c->stream));
+    else CUDA_TRY(c, mcd::launch_fission_sites_out_ce(q, rng, offsets, total, qcap, dest ? dest : bank, c->stream));
     c->launches += 5;
   }
   else {
@@ -1251,7 +1256,7 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
   if (k.bank_path < MC_BANK_AUTO || k.bank_path > MC_BANK_DIRECT) return fail(c, MC_ERR_INPUT, "unknown bank path");
   if (bank_direct(c, k.rng, k.fast != 0, k.bank_path) < 0)
-    return fail(c, MC_ERR_INPUT, "the direct bank path needs multigroup data, Philox streams and chi cdfs that end "
+    return fail(c, MC_ERR_INPUT, "the direct bank path needs (multigroup) Philox streams and chi cdfs that end "
                                  "above every threshold the stream draws");
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
       !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
@@ -1309,7 +1314,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   if (rc != MC_OK) return rc;
   Site* bank = nullptr;
   uint64_t m = 0;
-  rc = emit_bank(c, rp, nullptr, 0, &bank, &m, /*read_size=*/false);
+  rc = emit_bank(c, rp, k.rng, nullptr, 0, &bank, &m, /*read_size=*/false);
   if (rc != MC_OK) return rc;
   DevCounters h{};
   rc = read_back(c, &m, &h);
@@ -1576,7 +1581,7 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   const bool fast = o && o->fast_math && rng == MC_RNG_PHILOX;
   const int direct = bank_direct(c, rng, fast, path);
   if (direct < 0)
-    return fail(c, MC_ERR_INPUT, "the direct bank path needs multigroup data, Philox streams and chi cdfs that end "
+    return fail(c, MC_ERR_INPUT, "the direct bank path needs (multigroup) Philox streams and chi cdfs that end "
                                  "above every threshold the stream draws");
   cudaSetDevice(c->device);
   if ((!direct && !scratch(c, kSlots, n * c->max_yield * sizeof(Site))) || !scratch(c, kCount, n * 4))
@@ -1633,7 +1638,7 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   }
   Site* bank = nullptr;
   uint64_t m = 0;
-  rc = emit_bank(c, rp, direct ? out_mapped : nullptr, cap, &bank, &m, /*read_size=*/out_mapped == nullptr);
+  rc = emit_bank(c, rp, rng, direct ? out_mapped : nullptr, cap, &bank, &m, /*read_size=*/out_mapped == nullptr);
   if (rc != MC_OK) return rc;
   if (out_mapped && bank) {
     k_copy_bank_out<<<c->num_sms * 8, 256, 0, c->stream>>>(

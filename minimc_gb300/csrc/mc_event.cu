@@ -514,12 +514,12 @@ __global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, cons
                         static_cast<unsigned long long>(gridDim.x) * blockDim.x);
 }
 
-// Sites straight into the compacted bank.  When no chi draw can fall past
-// the end of its cdf (the caller checks every cdf's last entry against the
-// largest uniform the stream draws), each record yields exactly
-// min(n, max_yield) sites, so the counts are known before sampling and a
-// scan of them gives every history its place in the bank.
-__global__ void __launch_bounds__(256) k_fission_counts_mg(const RunParams rp) {
+// Sites straight into the compacted bank.  Where every record yields exactly
+// min(n, max_yield) sites (multigroup: no chi draw can fall past the end of
+// its cdf, which the caller checks against the largest uniform the stream
+// draws; continuous energy: always), the counts are known before sampling
+// and a scan of them gives every history its place in the bank.
+__global__ void __launch_bounds__(256) k_fission_counts(const RunParams rp) {
   const unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (h >= rp.n) return;
   const uint32_t f = rp.fis[h].n;
@@ -528,52 +528,34 @@ __global__ void __launch_bounds__(256) k_fission_counts_mg(const RunParams rp) {
   if (f > rp.max_yield) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(f - rp.max_yield));
 }
 
-// A CTA samples the sites of its kSitesOutHist histories into shared memory
-// at their bank positions (offsets[h] - offsets[first]), then stores its
-// contiguous share of the bank with coalesced 16-byte writes, to device
-// memory or to page-locked host memory over the chip-to-chip link.  Sites at
-// or past `cap` are not written (the host reports the overflow).  The draws
-// are those of fission_sites_mg, site for site.
+// The multigroup direct-bank CTA: the draws are those of fission_sites_mg,
+// site for site.
 template <bool FAST>
 __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_mg(const DevWorld w, const RunParams rp,
                                                                         const unsigned long long* offsets,
                                                                         const unsigned long long* total,
                                                                         unsigned long long cap, uint4* out) {
   extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
-  const unsigned long long n = rp.n;
-  const unsigned long long first = static_cast<unsigned long long>(blockIdx.x) * kSitesOutHist;
-  const unsigned long long last = first + kSitesOutHist < n ? first + kSitesOutHist : n;
-  const unsigned long long base = offsets[first];
-  const unsigned long long end = last < n ? offsets[last] : *total;
-  const unsigned long long h = first + threadIdx.x;
-  if (h < n) {
-    const uint32_t c = rp.bank_count[h];
-    if (c) {
-      const FissionRec f = rp.fis[h];
-      PhiloxRng rng;
-      rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
-      const int G = w.G;
-      const double* chi = w.mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
-      Site* dst = reinterpret_cast<Site*>(stage) + (offsets[h] - base);
-      for (uint32_t y = 0; y < c; y++) {
-        // go >= 0: the cdf ends above every threshold this stream draws
-        const int go = first_above(chi, G, uni(rng, FAST));
-        Site s;
-        iso(rng, s.u, s.v, s.w, FAST);
-        s.x = f.x;
-        s.y = f.y;
-        s.z = f.z;
-        s.energy = static_cast<double>(go + 1);
-        s.key = rng.child_key();
-        dst[y] = s;
-      }
-    }
-  }
-  __syncthreads();
-  const unsigned long long m = end - base;
-  const unsigned long long keep = base >= cap ? 0 : (m < cap - base ? m : cap - base);
-  constexpr unsigned kWords = sizeof(Site) / sizeof(uint4);
-  for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[base * kWords + i] = stage[i];
+  sites_out_cta(rp.n, rp.bank_count, offsets, total, cap, out, stage,
+                [&](unsigned long long h, uint32_t c, Site* dst) {
+                  const FissionRec f = rp.fis[h];
+                  PhiloxRng rng;
+                  rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
+                  const int G = w.G;
+                  const double* chi = w.mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
+                  for (uint32_t y = 0; y < c; y++) {
+                    // go >= 0: the cdf ends above every threshold this stream draws
+                    const int go = first_above(chi, G, uni(rng, FAST));
+                    Site s;
+                    iso(rng, s.u, s.v, s.w, FAST);
+                    s.x = f.x;
+                    s.y = f.y;
+                    s.z = f.z;
+                    s.energy = static_cast<double>(go + 1);
+                    s.key = rng.child_key();
+                    dst[y] = s;
+                  }
+                });
 }
 
 // batched problems: CTA b serves problem block_problem[b], as the rank-th of
@@ -658,8 +640,8 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fission_counts_mg(const RunParams& rp, cudaStream_t stream) {
-  k_fission_counts_mg<<<static_cast<unsigned>((rp.n + 255) / 256), 256, 0, stream>>>(rp);
+cudaError_t launch_fission_counts(const RunParams& rp, cudaStream_t stream) {
+  k_fission_counts<<<static_cast<unsigned>((rp.n + 255) / 256), 256, 0, stream>>>(rp);
   return cudaGetLastError();
 }
 
@@ -670,7 +652,6 @@ bool sites_out_fits(uint32_t max_yield) { return sites_out_smem(max_yield) <= kS
 cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream) {
-  static_assert(sizeof(Site) % sizeof(uint4) == 0, "sites are stored as 16-byte words");
   const size_t smem = sites_out_smem(rp.max_yield);
   if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
   const unsigned grid = static_cast<unsigned>((rp.n + kSitesOutHist - 1) / kSitesOutHist);

@@ -100,20 +100,52 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
                                     cudaStream_t stream);
 cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stream);
 
-// k-eigenvalue sites straight into a compacted bank (multigroup, Philox
-// streams), for chi cdfs that all end above the largest uniform the stream
-// draws: per-history counts min(n, max_yield) into bank_count, then (after a
-// scan of the counts) the sites, staged per CTA of kSitesOutHist histories in
-// shared memory and stored to `out` (device or page-locked host memory,
-// 16-byte aligned) with coalesced 16-byte writes; sites at or past `cap` are
-// not written
+// k-eigenvalue sites straight into a compacted bank, where every fission
+// record's site count is known before sampling (multigroup: Philox streams
+// and chi cdfs that all end above the largest uniform the stream draws;
+// continuous energy: always): per-history counts min(n, max_yield) into
+// bank_count, then (after a scan of the counts) the sites, staged per CTA of
+// kSitesOutHist histories in shared memory and stored to `out` (device or
+// page-locked host memory, 16-byte aligned) with coalesced 16-byte writes;
+// sites at or past `cap` are not written
 constexpr int kSitesOutHist = 128;
 constexpr size_t kSitesOutMaxSmem = 192 * 1024;
-cudaError_t launch_fission_counts_mg(const RunParams& rp, cudaStream_t stream);
+cudaError_t launch_fission_counts(const RunParams& rp, cudaStream_t stream);
+size_t sites_out_smem(uint32_t max_yield);
 bool sites_out_fits(uint32_t max_yield);
 cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream);
+cudaError_t launch_fission_sites_out_ce(const RunParams& rp, int rng_mode, const unsigned long long* offsets,
+                                        const unsigned long long* total, unsigned long long cap, Site* out,
+                                        cudaStream_t stream);
+
+// One CTA of the direct bank path.  The CTA owns histories
+// [blockIdx.x * kSitesOutHist, ...) of n; sample(h, c, dst) writes history
+// h's c = count[h] sites to dst (shared memory, at the history's bank
+// position relative to the CTA's first site); then the CTA stores its
+// contiguous share of the bank with coalesced 16-byte writes, skipping sites
+// at or past cap.
+template <class Sample>
+__device__ __forceinline__ void sites_out_cta(unsigned long long n, const uint32_t* count,
+                                              const unsigned long long* offsets, const unsigned long long* total,
+                                              unsigned long long cap, uint4* out, uint4* stage, Sample&& sample) {
+  static_assert(sizeof(Site) % sizeof(uint4) == 0, "sites are stored as 16-byte words");
+  const unsigned long long first = static_cast<unsigned long long>(blockIdx.x) * kSitesOutHist;
+  const unsigned long long last = first + kSitesOutHist < n ? first + kSitesOutHist : n;
+  const unsigned long long base = offsets[first];
+  const unsigned long long end = last < n ? offsets[last] : *total;
+  const unsigned long long h = first + threadIdx.x;
+  if (h < n) {
+    const uint32_t c = count[h];
+    if (c) sample(h, c, reinterpret_cast<Site*>(stage) + (offsets[h] - base));
+  }
+  __syncthreads();
+  const unsigned long long m = end - base;
+  const unsigned long long keep = base >= cap ? 0 : (m < cap - base ? m : cap - base);
+  constexpr unsigned kWords = sizeof(Site) / sizeof(uint4);
+  for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[base * kWords + i] = stage[i];
+}
 
 // launches (mc_transport.cu)
 // history-schedule kernel variants differ only in their occupancy target

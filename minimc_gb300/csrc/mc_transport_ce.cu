@@ -40,8 +40,60 @@ __global__ void __launch_bounds__(256) k_fission_sites_ce(const RunParams rp) {
   if (my_overflow) atomicAdd(&rp.ctr->overflow, my_overflow);
 }
 
+// direct bank path: the same draws as k_fission_sites_ce, each history's
+// min(n, max_yield) sites staged at their bank positions
+template <class Rng>
+__global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_ce(const RunParams rp,
+                                                                        const unsigned long long* offsets,
+                                                                        const unsigned long long* total,
+                                                                        unsigned long long cap, uint4* out) {
+  extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
+  const bool fast = rp.fast != 0;
+  sites_out_cta(rp.n, rp.bank_count, offsets, total, cap, out, stage,
+                [&](unsigned long long h, uint32_t c, Site* dst) {
+                  const FissionRec f = rp.fis[h];
+                  Rng rng;
+                  rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
+                  const double E = record_energy(f);
+                  for (uint32_t y = 0; y < c; y++) {
+                    Site s;
+                    sample_isotropic(rng, s.u, s.v, s.w, fast);
+                    s.x = f.x;
+                    s.y = f.y;
+                    s.z = f.z;
+                    s.energy = E;
+                    s.key = rng.child_key();
+                    dst[y] = s;
+                  }
+                });
+}
+
 constexpr int kMinb[5] = {1, 3, 4, 5, 6};  // occupancy variants (autotuner index)
 }  // namespace
+
+cudaError_t launch_fission_sites_out_ce(const RunParams& rp, int rng_mode, const unsigned long long* offsets,
+                                        const unsigned long long* total, unsigned long long cap, Site* out,
+                                        cudaStream_t stream) {
+  const size_t smem = sites_out_smem(rp.max_yield);
+  if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((rp.n + kSitesOutHist - 1) / kSitesOutHist);
+  auto* o = reinterpret_cast<uint4*>(out);
+  // the attribute is per device, so it is set at every launch (a host-side call)
+  cudaError_t e;
+  if (rng_mode == 1) {
+    e = cudaFuncSetAttribute(k_fission_sites_out_ce<MinstdRng>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k_fission_sites_out_ce<MinstdRng><<<grid, kSitesOutHist, smem, stream>>>(rp, offsets, total, cap, o);
+  }
+  else {
+    e = cudaFuncSetAttribute(k_fission_sites_out_ce<PhiloxRng>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k_fission_sites_out_ce<PhiloxRng><<<grid, kSitesOutHist, smem, stream>>>(rp, offsets, total, cap, o);
+  }
+  return cudaGetLastError();
+}
 
 bool ce_uses_fp32_tables(const DevWorld& w, int rng_mode, bool fast) {
   return rng_mode != 1 && fast && w.ce.fast_ok && w.n_pert == 0;

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 from scipy import stats
 
-from minimc_gb300 import RNG_MINSTD, RNG_PHILOX, Context, synth_ce
+from minimc_gb300 import BANK_DIRECT, BANK_SLOTS, RNG_MINSTD, RNG_PHILOX, Context, synth_ce
 from oracle.build import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -93,10 +93,13 @@ def test_keig_reference_streams_identical(ce_data, built_library):
     d, files = ce_data
     n = 20_000
     xml = synth_ce.ce_problem_xml(files, histories=n, inactive=2, active=3)
-    g = gpu_ctx(xml, d).run_keigenvalue(rng=RNG_MINSTD)
     o = Oracle(xml, d).run_keigenvalue(n, 1, 2, 3, threads=8)
-    assert np.array_equal(g.bank_size, o["bank_size"])
-    assert np.array_equal(g.k_cycle, o["k_cycle"])
+    # both bank paths: sites sampled straight into the bank, or per-history
+    # slots and a compaction
+    for path in (BANK_DIRECT, BANK_SLOTS):
+        g = gpu_ctx(xml, d).run_keigenvalue(rng=RNG_MINSTD, bank_path=path)
+        assert np.array_equal(g.bank_size, o["bank_size"])
+        assert np.array_equal(g.k_cycle, o["k_cycle"])
 
 
 def test_fixed_source_reference_streams_identical(ce_data, built_library):
@@ -181,3 +184,32 @@ def test_flat_infinite_medium_k(tmp_path, built_library):
         r = gpu_ctx(xml, tmp_path).run_keigenvalue(rng=RNG_PHILOX, fast_math=fast)
         k = r.k_cycle[2:]
         assert abs(k.mean() - 1.0) < 4 * k.std(ddof=1) / math.sqrt(len(k)) + 1e-4, (fast, k.mean())
+
+
+def test_transport_bank_direct_path_equals_slot_path(ce_data, built_library):
+    """mc_transport_bank on a continuous-energy problem: the sites sampled
+    straight into page-locked host output equal the slot path's, site for
+    site, for both stream kinds."""
+    import torch
+
+    from minimc_gb300 import SITE_DTYPE
+
+    d, files = ce_data
+    n = 20_000
+    ctx = gpu_ctx(synth_ce.ce_problem_xml(files, histories=n, inactive=1, active=1), d)
+    rng = np.random.default_rng(9)
+    sites = np.zeros(n, SITE_DTYPE)
+    mu = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    sites["u"], sites["v"], sites["w"] = mu, np.sqrt(1 - mu * mu) * np.cos(ph), np.sqrt(1 - mu * mu) * np.sin(ph)
+    sites["energy"] = 2.0
+    sites["key"] = np.arange(n, dtype=np.uint64) + 11
+    cap = n * max(1, ctx.info.max_yield)
+    for opts in (dict(rng=RNG_MINSTD), dict(rng=RNG_PHILOX, fast_math=1)):
+        ref = np.zeros(cap, SITE_DTYPE)
+        m0 = ctx.transport_bank_into(sites, ref, bank_path=BANK_SLOTS, **opts)
+        assert m0 > 0
+        out = torch.empty(cap * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(SITE_DTYPE)
+        m = ctx.transport_bank_into(sites, out, bank_path=BANK_DIRECT, **opts)
+        assert m == m0
+        assert np.array_equal(out[:m].view(np.uint8), ref[:m0].view(np.uint8))
