@@ -1063,14 +1063,23 @@ int orc_energy_index(void* h, int32_t nuc, const double* E, uint64_t n, int64_t*
     for (size_t i = 0; i < t->x.size(); i++) mp[t->x[i]] = t->y[i];
     maps.push_back(std::move(mp));
   }
+  // the position of map::upper_bound is that of std::upper_bound over the
+  // map's (sorted, unique) keys; walking the map iterator would be linear
+  std::vector<std::vector<double>> keys;
+  for (const auto& mp : maps) {
+    std::vector<double> k;
+    k.reserve(mp.size());
+    for (const auto& kv : mp) k.push_back(kv.first);
+    keys.push_back(std::move(k));
+  }
   for (uint64_t i = 0; i < n; i++) {
     for (size_t t = 0; t < 6; t++) {
-      if (t >= maps.size()) {
+      if (t >= keys.size()) {
         out[i * 6 + t] = -1;
         continue;
       }
-      const auto it = maps[t].upper_bound(E[i]);
-      out[i * 6 + t] = static_cast<int64_t>(std::distance(maps[t].begin(), it));
+      const auto it = std::upper_bound(keys[t].begin(), keys[t].end(), E[i]);
+      out[i * 6 + t] = static_cast<int64_t>(it - keys[t].begin());
     }
   }
   return 0;
