@@ -399,7 +399,9 @@ typedef struct mc_batch_opts {
   int32_t no_graph;           /* 1: launch the cycle's kernels one by one    */
   int32_t variant;            /* history-kernel variant + 1; 0: autotune     */
   uint32_t max_events;        /* per-particle event cap; 0 -> 1000000        */
-  uint64_t reserved[4];
+  int32_t bank_path;          /* MC_BANK_*: fission-site path                */
+  int32_t pad;
+  uint64_t reserved[3];
 } mc_batch_opts;
 typedef struct mc_batch_out {
   double* k_cycle;            /* [problems][inactive + active] or NULL       */

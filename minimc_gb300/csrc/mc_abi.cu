@@ -2550,6 +2550,15 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
   const unsigned long long N = off[P];
   uint32_t max_yield = 1;
   for (mc_ctx* c : b->probs) max_yield = std::max(max_yield, c->max_yield);
+  // fission sites straight into the bank when every problem's counts are
+  // known before sampling (bank_direct) and a CTA's sites fit its stage
+  if (o->bank_path < MC_BANK_AUTO || o->bank_path > MC_BANK_DIRECT)
+    return bfail(b, MC_ERR_INPUT, "unknown bank path");
+  bool direct = o->bank_path != MC_BANK_SLOTS && mcd::sites_out_fits(max_yield);
+  for (mc_ctx* c : b->probs) direct = direct && bank_direct(c, MC_RNG_PHILOX, o->fast_math != 0, MC_BANK_AUTO) > 0;
+  if (o->bank_path == MC_BANK_DIRECT && !direct)
+    return bfail(b, MC_ERR_INPUT, "the direct bank path needs chi cdfs that end above every threshold the stream draws");
+  if (direct) BATCH_TRY(b, mcd::sites_out_batch_prepare(max_yield));
   BatchMem mem;
   auto* d_worlds = mem.get<DevWorld>(P);
   auto* d_rps = mem.get<RunParams>(P);
@@ -2565,14 +2574,14 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
   auto* src0 = mem.get<Site>(N);
   auto* src1 = mem.get<Site>(N);
   auto* fis = mem.get<mcd::FissionRec>(N);
-  auto* slots = mem.get<Site>(N * max_yield);
+  auto* slots = direct ? nullptr : mem.get<Site>(N * max_yield);
   auto* count = mem.get<uint32_t>(N);
   auto* offsets = mem.get<unsigned long long>(N);
   auto* sums = mem.get<unsigned long long>((N + 1023) / 1024 + 1);
   auto* total = mem.get<unsigned long long>(1);
   auto* bank = mem.get<Site>(N * max_yield);
   if (!(d_worlds && d_rps && d_ctr && d_off && d_seeds && d_start && d_M && d_k && d_stats && d_cycle && d_died &&
-        src0 && src1 && fis && slots && count && offsets && sums && total && bank))
+        src0 && src1 && fis && (direct || slots) && count && offsets && sums && total && bank))
     return bfail(b, MC_ERR_OOM, "batch buffers");
   std::vector<DevWorld> worlds(P);
   std::vector<RunParams> rps(P);
@@ -2588,7 +2597,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
     rp.score = 0;
     rp.fast = o->fast_math ? 1 : 0;
     rp.max_yield = max_yield;
-    rp.bank = slots + off[p] * max_yield;
+    rp.bank = direct ? nullptr : slots + off[p] * max_yield;
     rp.bank_count = count + off[p];
     rp.total_bins = 0;
     rp.ctr = d_ctr + p;
@@ -2653,14 +2662,31 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
     if (rc != MC_OK) return rc;
   }
   const int grid = static_cast<int>(bp.size());
+  // the direct path's count kernel sees the concatenated records as one run
+  // (max_yield bounds every problem's yield, so no count is cut)
+  RunParams all{};
+  all.n = N;
+  all.fis = fis;
+  all.bank_count = count;
+  all.max_yield = max_yield;
+  all.ctr = d_ctr;
   // one cycle's launches; `from` holds this cycle's sources, `to` the next
   auto cycle_launches = [&](const Site* from, Site* to) -> cudaError_t {
     cudaError_t e;
     if ((e = mcd::launch_batch_begin(bc, from, s)) != cudaSuccess) return e;
     if ((e = mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, grid, s, variant)) != cudaSuccess) return e;
-    if ((e = mcd::launch_fission_sites_mg_batch(d_worlds, d_rps, d_bp, d_bf, grid, s)) != cudaSuccess) return e;
-    if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
-    if ((e = mcd::launch_bank_compact(slots, count, offsets, N, max_yield, bank, s)) != cudaSuccess) return e;
+    if (direct) {
+      if ((e = mcd::launch_fission_counts(all, s)) != cudaSuccess) return e;
+      if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
+      if ((e = mcd::launch_fission_sites_out_mg_batch(d_worlds, d_rps, d_off, P, N, max_yield, o->fast_math != 0,
+                                                      fis, count, offsets, total, bank, s)) != cudaSuccess)
+        return e;
+    }
+    else {
+      if ((e = mcd::launch_fission_sites_mg_batch(d_worlds, d_rps, d_bp, d_bf, grid, s)) != cudaSuccess) return e;
+      if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
+      if ((e = mcd::launch_bank_compact(slots, count, offsets, N, max_yield, bank, s)) != cudaSuccess) return e;
+    }
     if ((e = mcd::launch_batch_tally(bc, offsets, total, s)) != cudaSuccess) return e;
     return mcd::launch_batch_resample(bc, bank, to, s);
   };

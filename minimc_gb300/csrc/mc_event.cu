@@ -558,6 +558,41 @@ __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_mg(const De
                 });
 }
 
+// Batched problems on the direct bank path: CTAs run over the concatenated
+// histories (a CTA may span problems); history h belongs to the problem p
+// with off[p] <= h < off[p + 1], whose world and run key it samples with.
+template <bool FAST>
+__global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_mg_batch(
+    const DevWorld* worlds, const RunParams* rps, const unsigned long long* off, int P, unsigned long long N,
+    const FissionRec* fis, const uint32_t* count, const unsigned long long* offsets, const unsigned long long* total,
+    unsigned long long cap, uint4* out) {
+  extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
+  sites_out_cta(N, count, offsets, total, cap, out, stage, [&](unsigned long long h, uint32_t c, Site* dst) {
+    int lo = 0, hi = P;  // off[lo] <= h < off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (off[mid] <= h) lo = mid;
+      else hi = mid;
+    }
+    const FissionRec f = fis[h];
+    PhiloxRng rng;
+    rng.restore(rps[lo].run_key, f.id, f.tag & 1u, f.rng);
+    const int G = worlds[lo].G;
+    const double* chi = worlds[lo].mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
+    for (uint32_t y = 0; y < c; y++) {
+      const int go = first_above(chi, G, uni(rng, FAST));
+      Site s;
+      iso(rng, s.u, s.v, s.w, FAST);
+      s.x = f.x;
+      s.y = f.y;
+      s.z = f.z;
+      s.energy = static_cast<double>(go + 1);
+      s.key = rng.child_key();
+      dst[y] = s;
+    }
+  });
+}
+
 // batched problems: CTA b serves problem block_problem[b], as the rank-th of
 // its block_first[p + 1] - block_first[p] CTAs
 __global__ void __launch_bounds__(256) k_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps,
@@ -671,6 +706,33 @@ cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, 
     k_fission_sites_out_mg<false><<<grid, kSitesOutHist, smem, stream>>>(w, rp, offsets, total, cap, o);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_fission_sites_out_mg_batch(const DevWorld* worlds, const RunParams* rps,
+                                              const unsigned long long* off, int P, unsigned long long N,
+                                              uint32_t max_yield, bool fast, const FissionRec* fis,
+                                              const uint32_t* count, const unsigned long long* offsets,
+                                              const unsigned long long* total, Site* out, cudaStream_t stream) {
+  const size_t smem = sites_out_smem(max_yield);
+  if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
+  const unsigned grid = static_cast<unsigned>((N + kSitesOutHist - 1) / kSitesOutHist);
+  const unsigned long long cap = N * max_yield;
+  auto* o = reinterpret_cast<uint4*>(out);
+  if (fast)
+    k_fission_sites_out_mg_batch<true><<<grid, kSitesOutHist, smem, stream>>>(worlds, rps, off, P, N, fis, count,
+                                                                               offsets, total, cap, o);
+  else
+    k_fission_sites_out_mg_batch<false><<<grid, kSitesOutHist, smem, stream>>>(worlds, rps, off, P, N, fis, count,
+                                                                                offsets, total, cap, o);
+  return cudaGetLastError();
+}
+
+cudaError_t sites_out_batch_prepare(uint32_t max_yield) {
+  const int smem = static_cast<int>(sites_out_smem(max_yield));
+  cudaError_t e = cudaFuncSetAttribute(k_fission_sites_out_mg_batch<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fission_sites_out_mg_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 cudaError_t launch_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,

@@ -116,6 +116,15 @@ bool sites_out_fits(uint32_t max_yield);
 cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream);
+// batched problems (Philox): histories concatenated, offsets off[0..P].
+// sites_out_batch_prepare sets the kernel's shared-memory limit (a host
+// call, made before a graph capture of the launch)
+cudaError_t sites_out_batch_prepare(uint32_t max_yield);
+cudaError_t launch_fission_sites_out_mg_batch(const DevWorld* worlds, const RunParams* rps,
+                                              const unsigned long long* off, int P, unsigned long long N,
+                                              uint32_t max_yield, bool fast, const FissionRec* fis,
+                                              const uint32_t* count, const unsigned long long* offsets,
+                                              const unsigned long long* total, Site* out, cudaStream_t stream);
 cudaError_t launch_fission_sites_out_ce(const RunParams& rp, int rng_mode, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream);

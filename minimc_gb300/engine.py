@@ -110,7 +110,8 @@ MLP_PARAMS = 35329  # FP32 parameters per surrogate network
 
 class BatchOpts(C.Structure):
     _fields_ = [("inactive", C.c_uint32), ("active", C.c_uint32), ("fast_math", C.c_int32), ("no_graph", C.c_int32),
-                ("variant", C.c_int32), ("max_events", C.c_uint32), ("reserved", C.c_uint64 * 4)]
+                ("variant", C.c_int32), ("max_events", C.c_uint32), ("bank_path", C.c_int32), ("pad", C.c_int32),
+                ("reserved", C.c_uint64 * 3)]
 
 
 class BatchOut(C.Structure):
@@ -775,14 +776,14 @@ class Batch:
         return rc
 
     def run(self, inactive: int, active: int, fast_math: int = 1, graph: bool = True, variant: int = 0,
-            max_events: int = 0, allow=()):
+            max_events: int = 0, bank_path: int = BANK_AUTO, allow=()):
         P = len(self.histories)
         ncyc = inactive + active
         k = np.zeros((P, ncyc))
         km = np.zeros(P)
         ks = np.zeros(P)
         o = BatchOpts(inactive=inactive, active=active, fast_math=fast_math, no_graph=0 if graph else 1,
-                      variant=variant, max_events=max_events)
+                      variant=variant, max_events=max_events, bank_path=bank_path)
         out = BatchOut()
         out.k_cycle = _dptr(k)
         out.k_mean = _dptr(km)

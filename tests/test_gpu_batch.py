@@ -4,7 +4,7 @@ seed and Philox streams, with and without the per-cycle CUDA graph."""
 import numpy as np
 import pytest
 
-from minimc_gb300 import RNG_PHILOX, Batch, Context, synth
+from minimc_gb300 import BANK_AUTO, BANK_SLOTS, RNG_PHILOX, Batch, Context, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -13,13 +13,15 @@ def problems(count, h_min, h_max):
     return synth.batch_problems(count=count, seed=11, h_min=h_min, h_max=h_max, inactive=2, active=4)
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_batch_equals_single_problem_runs(graph, built_library):
+@pytest.mark.parametrize("graph,bank_path", [(True, BANK_AUTO), (False, BANK_AUTO), (True, BANK_SLOTS)])
+def test_batch_equals_single_problem_runs(graph, bank_path, built_library):
+    """Both bank paths (sites sampled straight into the concatenated bank,
+    or slots and a compaction) give each problem its single-run k."""
     probs = problems(6, 2_000, 30_000)
     b = Batch(0)
     for p, h in probs:
         b.add(p.xml(), histories=h, seed=p.seed)
-    r = b.run(inactive=2, active=4, fast_math=1, graph=graph)
+    r = b.run(inactive=2, active=4, fast_math=1, graph=graph, bank_path=bank_path)
     assert r["graph"] == int(graph)
     for i, (p, h) in enumerate(probs):
         ctx = Context(0)
