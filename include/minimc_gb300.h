@@ -73,10 +73,11 @@ extern "C" {
  * the same bank, site for site. */
 #define MC_BANK_AUTO 0    /* direct where it applies, else slots          */
 #define MC_BANK_SLOTS 1   /* per-history slots, a scan, then a compaction */
-#define MC_BANK_DIRECT 2  /* counts known before sampling (multigroup,
-                             Philox streams, every chi cdf ending above the
-                             largest uniform drawn): a scan, then the sites
-                             sampled straight into their bank positions;
+#define MC_BANK_DIRECT 2  /* counts known before sampling (continuous
+                             energy always; multigroup with Philox streams
+                             and every chi cdf ending above the largest
+                             uniform drawn): a scan, then the sites sampled
+                             straight into their bank positions;
                              MC_ERR_INPUT where that does not hold        */
 
 typedef struct mc_ctx mc_ctx;
