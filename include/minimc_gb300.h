@@ -265,19 +265,25 @@ int mc_schedule_info(mc_ctx* ctx, int32_t* schedule, int32_t* variant, int32_t* 
 int mc_transport_bank(mc_ctx* ctx, const mc_site* sites, uint64_t n, const mc_run_opts* opts,
                       mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
 /* mc_transport_bank for callers that cannot allocate device memory when
- * they transport: code recording a CUDA graph (cudaMalloc is not allowed
- * during stream capture) and applications that fix their device-memory
- * budget at start-up.  No counterpart in the reference.  sites and
- * fission_sites are DEVICE pointers owned by the caller; *n_out (host) gets
- * the number of sites banked (at most cap are written).  Allocates nothing:
+ * they transport: applications that fix their device-memory budget at
+ * start-up and forbid allocation afterwards (e.g. a coupled code whose own
+ * pool owns the GPU's memory), or code that runs where the device allocator
+ * must not be entered.  No counterpart in the reference.  sites and
+ * fission_sites are caller-owned DEVICE (or managed, or page-locked host)
+ * pointers; pageable host memory is refused with MC_ERR_INPUT.  *n_out
+ * (host) gets the number of sites banked; at most cap are written, and
+ * MC_ERR_OVERFLOW is returned when the bank was larger.  Allocates nothing:
  * its scratch is a fixed 5.3 MB array that every GPU loading this library
  * holds until exit.  Limits: n <= 16384 sites per call, multigroup problems
  * whose fissions bank at most 4 sites; larger calls fail with MC_ERR_INPUT.
  * The first call on a device looks the array's address up (and loads the
- * kernels): make it before any stream capture.  All calls share the array,
- * so calls that overlap on the GPU (other streams, other contexts on the
- * same device) race; serialize them.  Tallies accumulate into the context's
- * estimators as with mc_transport_bank. */
+ * kernels): make it before any stream capture.  The address is kept for
+ * the life of the process, so a device reset invalidates it.  The call
+ * waits for its work before returning (it reads the bank size and the run
+ * counters back to the host).  All calls share the array, so calls that
+ * overlap on the GPU (other streams, other contexts on the same device)
+ * race; serialize them.  Tallies accumulate into the context's estimators
+ * as with mc_transport_bank. */
 int mc_transport_bank_noalloc(mc_ctx* ctx, const mc_site* sites, uint64_t n, const mc_run_opts* opts,
                               mc_site* fission_sites, uint64_t cap, uint64_t* n_out);
 int mc_tallies_reset(mc_ctx* ctx);

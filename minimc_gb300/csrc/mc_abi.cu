@@ -13,6 +13,7 @@
 #include <cstddef>
 #include <cstring>
 #include <exception>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -2294,15 +2295,16 @@ int mc_tsl_total(mc_ctx* c, int32_t tsl, const double* energy, const double* tem
 // Bank transport without allocation.
 //
 // Some callers cannot allocate device memory at the time they transport a
-// bank: code that is recording a CUDA graph (cudaMalloc is not allowed while
-// a stream is being captured), and host applications that fix their device
-// memory budget at start-up and forbid allocation afterwards (for example a
-// coupled multiphysics code that owns the GPU's memory pool).  For them,
-// mc_transport_bank_noalloc runs the same kernels as mc_transport_bank, but
-// all of its scratch memory -- run counters, fission records, per-history
-// site slots, scan sums -- lives in the fixed array below, which every GPU
-// that loads this library holds until the process exits.  The caller passes
-// its own device buffers for the input sites and the output bank.
+// bank: host applications that fix their device-memory budget at start-up
+// and forbid allocation afterwards (for example a coupled multiphysics code
+// whose own pool owns the GPU's memory), or code that runs where the device
+// allocator must not be entered.  For them, mc_transport_bank_noalloc runs
+// the same kernels as mc_transport_bank, but all of its scratch memory --
+// run counters, fission records, per-history site slots, scan sums -- lives
+// in the fixed array below, which every GPU that loads this library holds
+// until the process exits.  The caller passes its own device buffers for the
+// input sites and the output bank.  The call waits for its work before it
+// returns: it reads the bank size and the run counters back to the host.
 
 namespace {
 
@@ -2324,9 +2326,31 @@ static_assert(kNoAllocFission % 256 == 0 && kNoAllocSlots % 256 == 0 && kNoAlloc
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// device address of g_noalloc_scratch for each device, found once
+// device address of g_noalloc_scratch for each device, found once under the
+// mutex (two host threads may make their first call on a device together)
 constexpr int kMaxDevices = 64;
 void* g_noalloc_addr[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// the caller's buffer as a device address: device or managed memory as is,
+// page-locked host memory through its device mapping; anything else
+// (pageable host memory) is refused
+bool device_view(const void* p, void** out) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+    *out = a.devicePointer ? a.devicePointer : const_cast<void*>(p);
+    return true;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    *out = a.devicePointer;
+    return true;
+  }
+  return false;
+}
 
 }  // namespace
 
@@ -2349,16 +2373,30 @@ extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint
   if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (c->device < 0 || c->device >= kMaxDevices) return fail(c, MC_ERR_INPUT, "device index out of range");
   CUDA_TRY(c, cudaSetDevice(c->device));
+  // a dense-score commit that an earlier call left on the side stream
+  // must be ordered before this call's tally updates
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
+  void* in_dev = nullptr;
+  void* out_dev = nullptr;
+  if (!device_view(d_sites, &in_dev))
+    return fail(c, MC_ERR_INPUT, "mc_transport_bank_noalloc: sites is not device or page-locked memory");
+  if (d_fission_sites && cap && !device_view(d_fission_sites, &out_dev))
+    return fail(c, MC_ERR_INPUT, "mc_transport_bank_noalloc: fission_sites is not device or page-locked memory");
   // set-up, once per device with that device current: the host-side symbol
   // is not a device address, so ask the runtime for the array's address
-  if (!g_noalloc_addr[c->device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(c, MC_ERR_DEVICE, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-    g_noalloc_addr[c->device] = p;
+  char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[c->device]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return fail(c, MC_ERR_DEVICE,
+                    std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+      g_noalloc_addr[c->device] = p;
+    }
+    base = static_cast<char*>(g_noalloc_addr[c->device]);
   }
-  char* base = static_cast<char*>(g_noalloc_addr[c->device]);
   auto* ctr = reinterpret_cast<DevCounters*>(base);
   auto* fis = reinterpret_cast<mcd::FissionRec*>(base + kNoAllocCounters);
   auto* slots = reinterpret_cast<Site*>(base + kNoAllocCounters + kNoAllocFission);
@@ -2383,7 +2421,7 @@ extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint
   rp.from_bank = 1;
   rp.minstd_base = 0;
   rp.max_yield = kNoAllocMaxYield;
-  rp.src = reinterpret_cast<const Site*>(d_sites);
+  rp.src = static_cast<const Site*>(in_dev);
   rp.bank = slots;
   rp.bank_count = count;
   rp.ctr = ctr;
@@ -2398,9 +2436,9 @@ extern "C" int mc_transport_bank_noalloc(mc_ctx* c, const mc_site* d_sites, uint
   CUDA_TRY(c, mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant));
   CUDA_TRY(c, mcd::launch_fission_sites_mg(c->dw, rp, rng, sites_grid(rp.n), c->stream));
   CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
-  if (d_fission_sites && cap) {
+  if (out_dev) {
     k_compact_capped<<<static_cast<unsigned>((n + 255) / 256), 256, 0, c->stream>>>(
-        slots, count, offsets, n, kNoAllocMaxYield, reinterpret_cast<Site*>(d_fission_sites), cap);
+        slots, count, offsets, n, kNoAllocMaxYield, static_cast<Site*>(out_dev), cap);
     CUDA_TRY(c, cudaGetLastError());
   }
   c->launches += 6;

@@ -450,8 +450,8 @@ class Context:
 
     def transport_bank_noalloc(self, d_sites: int, n: int, d_out: int, cap: int, **kw) -> int:
         """mc_transport_bank_noalloc: device pointers in and out (for callers
-        that cannot allocate, e.g. while recording a CUDA graph); returns the
-        number of fission sites banked."""
+        that cannot allocate device memory, e.g. under a memory budget fixed
+        at start-up); returns the number of fission sites banked."""
         o = self.opts(**kw)
         n_out = C.c_uint64()
         self.check(self.lib.mc_transport_bank_noalloc(self.h, _P(d_sites), n, C.byref(o), _P(d_out), cap,

@@ -249,6 +249,53 @@ def two_zone_cubes(histories: int = 1_000_000, inactive: int = 20, active: int =
         estimators=[tracklength("fuel-flux", "fuel", groups), current("leak-xhi", "out-xhi", groups)], seed=1)
 
 
+def one_group_slab_sphere(histories: int = 10_000, inactive: int = 50, active: int = 100, half: float = 10.0,
+                          radius: float = 12.0, seed: int = 1) -> Problem:
+    """The one-group k-eigenvalue problem of ``one_group_cube`` in a geometry
+    the reference's own surfaces describe (it has no planey/planez): the
+    slab -half < x < half cut by a sphere of the given radius, vacuum
+    outside."""
+    fuel = MGNuclide("fuel", capture=np.array([0.1]), scatter=np.array([[0.7]]), fission=np.array([0.2]),
+                     nubar=np.array([2.5]), chi=np.array([[1.0]]))
+    surfaces = [f'  <planex name="xlo" x="{_fmt(-half)}"/>', f'  <planex name="xhi" x="{_fmt(half)}"/>',
+                f'  <sphere name="ball">\n    <center x="0" y="0" z="0"/>\n    <radius r="{_fmt(radius)}"/>\n  </sphere>']
+    cells = ['  <cell name="fuel" material="fuel">\n    <surface name="xlo" sense="+1"/>\n'
+             '    <surface name="xhi" sense="-1"/>\n    <surface name="ball" sense="-1"/>\n  </cell>',
+             '  <void>\n    <surface name="xlo" sense="-1"/>\n  </void>',
+             '  <void>\n    <surface name="xhi" sense="+1"/>\n  </void>',
+             '  <void>\n    <surface name="ball" sense="+1"/>\n  </void>']
+    return Problem(
+        groups=1, nuclides=[fuel], materials=[("fuel", 1.0, [("fuel", 1.0)])], surfaces=surfaces, cells=cells,
+        histories=histories, problem=f'keigenvalue inactive="{inactive}" active="{active}"',
+        estimators=[current("leak-xhi", "xhi"), current("leak-ball", "ball")], seed=seed)
+
+
+def two_zone_spheres(histories: int = 100_000, inactive: int = 20, active: int = 50, groups: int = 8,
+                     seed: int = 2026) -> Problem:
+    """The 8-group two-zone problem (same seeded cross sections as
+    ``two_zone_cubes``) in spheres of the cubes' volumes: a fuel sphere of
+    radius 18.6 cm inside a reflector sphere of radius 37.2 cm, vacuum
+    outside -- geometry the reference's own surfaces describe."""
+    rng = np.random.default_rng(seed)
+    fuel, _ = mg_data(rng, groups, True)
+    refl, _ = mg_data(rng, groups, False)
+    fuel.name, refl.name = "fuel", "reflector"
+    r_in = (3 * 30.0 ** 3 / (4 * np.pi)) ** (1 / 3)
+    r_out = (3 * 60.0 ** 3 / (4 * np.pi)) ** (1 / 3)
+    surfaces = [f'  <sphere name="{n}">\n    <center x="0" y="0" z="0"/>\n    <radius r="{_fmt(r)}"/>\n  </sphere>'
+                for n, r in (("inner", r_in), ("outer", r_out))]
+    cells = ['  <cell name="fuel" material="fuel">\n    <surface name="inner" sense="-1"/>\n  </cell>',
+             '  <cell name="reflector" material="reflector">\n    <surface name="inner" sense="+1"/>\n'
+             '    <surface name="outer" sense="-1"/>\n  </cell>',
+             '  <void>\n    <surface name="outer" sense="+1"/>\n  </void>']
+    return Problem(
+        groups=groups, nuclides=[fuel, refl],
+        materials=[("fuel", 1.0, [("fuel", 1.0)]), ("reflector", 1.0, [("reflector", 1.0)])],
+        surfaces=surfaces, cells=cells, histories=histories,
+        problem=f'keigenvalue inactive="{inactive}" active="{active}"',
+        estimators=[current("leak", "outer", groups)], seed=1)
+
+
 def sphere_fixed_source(radius: float = 1.0, capture: float = 1.0, histories: int = 1000) -> Problem:
     """Point source in a pure-absorber sphere (the reference's
     point-source-leakage check: leakage = exp(-capture*radius))."""

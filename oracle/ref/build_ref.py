@@ -7,7 +7,8 @@ it needs (pugixml, the HDF5 C++ API) and a replacement for its one
 Xerces-C++ user (XMLDocument.cpp, which only validates the XML schema).
 The stand-ins implement the calls the reference makes over the project's
 XML DOM and table container.  Needs the reference checkout; skipped (returns
-None) where it is absent.
+None) where it is absent.  The checkout is found at $MINIMC_REFERENCE, else at
+the path this recipe reads it from by default (REF_DEFAULT).
 """
 from __future__ import annotations
 
@@ -18,11 +19,14 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF_SRC = Path(os.environ.get("MINIMC_REFERENCE", "/root/reference")) / "src"
+REF_DEFAULT = "/root/reference"
+REF_SRC = Path(os.environ.get("MINIMC_REFERENCE", REF_DEFAULT)) / "src"
 OUT = ROOT / "oracle" / "_ref"
 LIB = OUT / "libminimc_ref.so"
 EXCLUDE = {"minimc.cpp", "XMLDocument.cpp"}
-FLAGS = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w", "-DNDEBUG"]
+# -O3 as the reference's own release build; no contraction, so every
+# product and sum rounds as the reference built for x86-64 rounds them
+FLAGS = ["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-w", "-DNDEBUG"]
 
 
 def sources() -> list[Path]:
@@ -30,11 +34,19 @@ def sources() -> list[Path]:
     return sorted(p for p in REF_SRC.glob("*.cpp") if p.name not in EXCLUDE) + own
 
 
+def available() -> bool:
+    """True where the reference's sources can be read."""
+    return REF_SRC.exists()
+
+
 def build(force: bool = False) -> Path | None:
-    if not REF_SRC.exists():
+    if not available():
         return None
     OUT.mkdir(parents=True, exist_ok=True)
     (OUT / "obj").mkdir(exist_ok=True)
+    stamp = OUT / "flags.txt"  # objects built with other flags are rebuilt
+    if not stamp.exists() or stamp.read_text() != " ".join(FLAGS):
+        force = True
     inc = [f"-I{REF_SRC}", f"-I{HERE / 'shim'}", f"-I{ROOT / 'minimc_gb300' / 'csrc'}"]
     headers = list((HERE / "shim").glob("*")) + list(REF_SRC.glob("*.hpp"))
     newest_header = max((h.stat().st_mtime for h in headers), default=0)
@@ -56,6 +68,7 @@ def build(force: bool = False) -> Path | None:
             list(ex.map(run, jobs))
     if force or jobs or not LIB.exists():
         run(["g++", "-shared", "-o", str(LIB), *map(str, objs), "-pthread"])
+    stamp.write_text(" ".join(FLAGS))
     return LIB
 
 

@@ -36,6 +36,11 @@ def ref():
     lib.ref_solve.argtypes = [C.c_char_p, C.c_char_p, C.c_uint64, C.POINTER(C.c_double), C.c_char_p, C.c_size_t,
                               C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t]
     lib.ref_solve.restype = C.c_int
+    lib.ref_keig.argtypes = [C.c_char_p, C.c_uint32, C.c_uint32, C.c_int, C.POINTER(C.c_double),
+                             C.POINTER(C.c_uint64), C.c_char_p, C.c_uint64, C.POINTER(C.c_double),
+                             C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_char_p, C.c_size_t, C.c_char_p,
+                             C.c_size_t]
+    lib.ref_keig.restype = C.c_int
     return lib
 
 
@@ -210,3 +215,69 @@ def test_sensitivity_input_errors(tmp_path, built_library, case):
     with pytest.raises(MCError) as e:
         format_output(xml, GOLDEN, [0.0] * 3, [0.0] * 3, 1)
     assert e.value.message.startswith(want), e.value.message
+
+
+def run_keig_both(ref, xml: str, tmp_path: Path, estimator: str, nbins: int, inactive: int, active: int,
+                  threads: int):
+    """The reference's own transport in the k-eigenvalue loop (oracle/ref/
+    harness.cpp: Particle::Transport per source particle, fission sites
+    through Particle::MoveSecondariesTo, k = M/N, uniform resampling) and
+    the oracle's loop on the same problem and seeds."""
+    n = int(re.search(r"<histories>(\d+)</histories>", xml).group(1))
+    o = Oracle(xml, tmp_path)
+    o.set_quirks(True)
+    path = tmp_path / "keig.xml"
+    path.write_text(xml)
+    cycles = inactive + active
+    k = np.zeros(cycles)
+    bank = np.zeros(cycles, np.uint64)
+    mean = np.zeros(nbins)  # the named estimator's bins
+    secs = C.c_double()
+    lost = C.c_uint64()
+    orders = C.create_string_buffer(1 << 16)
+    err = C.create_string_buffer(2048)
+    rc = ref.ref_keig(str(path).encode(), inactive, active, threads, k.ctypes.data_as(C.POINTER(C.c_double)),
+                      bank.ctypes.data_as(C.POINTER(C.c_uint64)), estimator.encode(), len(mean),
+                      mean.ctypes.data_as(C.POINTER(C.c_double)), C.byref(secs), C.byref(lost), orders, 1 << 16,
+                      err, 2048)
+    assert rc == 0, err.value.decode()
+    align_orders(o, orders.value.decode())
+    r = o.run_keigenvalue(n, 1, inactive, active, threads=threads)
+    return {"k": k, "bank": bank, "mean": mean, "seconds": secs.value, "lost": lost.value}, r, n
+
+
+@pytest.mark.parametrize("threads", [1, 4])
+def test_keigenvalue_loop_on_reference_code(ref, tmp_path, threads):
+    """k per cycle, bank sizes and (one thread: same summation order) the
+    estimator means of the oracle's k-eigenvalue loop equal the reference's
+    own transport run through the same loop, bit for bit: the one-group
+    problem in a planex slab cut by a sphere, 5 inactive + 5 active cycles
+    of 4,000 histories."""
+    from minimc_gb300 import synth
+
+    xml = synth.one_group_slab_sphere(histories=4000, inactive=5, active=5).xml()
+    got, want, n = run_keig_both(ref, xml, tmp_path, "leak-ball", 1, 5, 5, threads)
+    assert np.array_equal(got["bank"], want["bank_size"]), (got["bank"], want["bank_size"])
+    assert np.array_equal(got["k"], want["k_cycle"])
+    assert got["bank"].min() > 0
+    if threads == 1:
+        o_mean = want["sum"] / (n * 5)
+        # leak-ball is the second of the oracle's flattened bins
+        assert np.array_equal(got["mean"], o_mean[1:2])
+    # fission sites banked beyond a surface a particle grazed without
+    # crossing (the reference's fixed nudge) start in a void: lost in both
+    assert got["lost"] == want["lost"]
+
+
+def test_keigenvalue_two_zone_spheres_on_reference_code(ref, tmp_path):
+    """The 8-group two-zone problem (same seeded data as the GPU benchmark)
+    in concentric spheres: k per cycle and bank sizes of the oracle's loop
+    equal the reference's own transport, and the group-binned leakage means
+    too (one thread)."""
+    from minimc_gb300 import synth
+
+    xml = synth.two_zone_spheres(histories=3000, inactive=3, active=3).xml()
+    got, want, n = run_keig_both(ref, xml, tmp_path, "leak", 10, 3, 3, 1)  # 8 groups + 2 open ends
+    assert np.array_equal(got["bank"], want["bank_size"])
+    assert np.array_equal(got["k"], want["k_cycle"])
+    assert np.array_equal(got["mean"], want["sum"] / (n * 3))
