@@ -144,7 +144,10 @@ def cpu_baseline(xml: str, base: str, histories: int, threads: int, cycles: int)
     hps = histories * cycles / r["seconds"]
     return {"value": hps, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{cycles} cycles x {histories} histories of the same problem (CPU oracle, "
-                      f"{threads} threads), {r['seconds']:.1f} s"}
+                      f"{threads} threads), {r['seconds']:.1f} s",
+            "k_cycles": [round(float(k), 6) for k in r["k_cycle"]],
+            "reference_code_speed": "the restatement is 1.5-2.4x faster than the reference's own code at equal "
+                                    "threads (oracle/ref/calibrate.py), so speed-ups against it are conservative"}
 
 
 def run_reference(args) -> None:
@@ -219,8 +222,7 @@ def run_gpu(args) -> None:
 
     # ---- device-resident cycles
     ctx.keig_begin(**opts)
-    for _ in range(args.warmup):
-        ctx.keig_cycle(False)
+    k_warm = [ctx.keig_cycle(False) for _ in range(args.warmup)]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
     st0 = ctx.keig_status()
     clocks = ClockSampler(local)
@@ -303,6 +305,23 @@ def run_gpu(args) -> None:
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(xml, base, args.cpu_histories, os.cpu_count() or 1, args.cpu_cycles)
 
+    # the surrogate half of the metric: the thermal broomstick with the POD
+    # sampler and with the guided (surrogate) form, outside the timed region
+    surrogate = None
+    if rank == 0 and args.workload == "two_zone" and not args.no_surrogate:
+        f = thermal_forms(local, 1_000_000, 3, 1)
+        surrogate = {"workload": f["workload"], "histories_per_step": f["histories_per_step"],
+                     "pod_histories_per_s": f["pod"]["histories_per_s"],
+                     "pod_queue_histories_per_s": f["pod_queue"]["histories_per_s"],
+                     "surrogate_histories_per_s": f["guided"]["histories_per_s"],
+                     "surrogate_vs_pod": f["guided"]["vs_pod"],
+                     "surrogate_vs_pod_queue": f["guided"]["histories_per_s"] / f["pod_queue"]["histories_per_s"],
+                     "energy_chi2_vs_pod": f["guided"]["energy_chi2_vs_pod"],
+                     "cosine_chi2_vs_pod": f["guided"]["cosine_chi2_vs_pod"],
+                     "identical_tallies_same_seed": f["guided"]["identical_tallies_same_seed"],
+                     "form": "guided: the guide network starts each SampleAlpha CDF search, POD confirms it",
+                     "train": f["train"], "timed": "engine device time of each fixed-source run"}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -314,6 +333,12 @@ def run_gpu(args) -> None:
                        "parallelism": f"replicas{ws}" if ws > 1 else "single GPU",
                        "schedule": sched},
             "k_cycles": [round(k, 6) for k in k_steps],
+            "k": {"gpu_mean": float(np.mean(k_steps)),
+                  "gpu_std": float(np.std(k_steps, ddof=1) / np.sqrt(len(k_steps))) if len(k_steps) > 1 else None,
+                  "gpu_first_cycles": [round(k, 6) for k in (k_warm + k_steps)[:args.cpu_cycles]],
+                  "cpu_first_cycles": cpu["k_cycles"] if cpu else None,
+                  "note": "both runs start from the same point source; the 3-sigma k_eff test at 1e6 histories, "
+                          "30 + 30 cycles, is tests/test_gpu_c2_keff.py"},
             "events_per_history": e_h,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -327,7 +352,9 @@ def run_gpu(args) -> None:
                     "call": "mc_transport_bank (pinned host banks: the transport kernel reads the sites in host "
                             "memory over the chip-to-chip link; multigroup Philox fission sites are sampled "
                             "straight into the host bank, coalesced, while the score commit runs on a second "
-                            "stream)"},
+                            "stream); the caller's resampling of the next source (numpy) is outside the timed "
+                            "call"},
+            "surrogate": surrogate,
             "gpu_launches": int(launches),
             "clocks": clk,
             "wall_s": wall,
@@ -337,7 +364,7 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
-def tsl_problem(histories: int, seed: int = 1) -> dict:
+def tsl_problem(histories: int, seed: int = 1, energy: float = 1e-6, base: Path | None = None) -> dict:
     """Broomstick with the synthetic POD thermal library (1 eV beam, 450 K)."""
     import atexit
     import shutil
@@ -345,79 +372,150 @@ def tsl_problem(histories: int, seed: int = 1) -> dict:
 
     from minimc_gb300 import synth_tsl
 
-    base = Path(tempfile.mkdtemp(prefix="mc_tsl_"))
-    atexit.register(shutil.rmtree, base, True)
+    if base is None:
+        base = Path(tempfile.mkdtemp(prefix="mc_tsl_"))
+        atexit.register(shutil.rmtree, base, True)
     tsl = synth_tsl.write_tsl(base)
     nuc = synth_tsl.moderator_nuclide(base)
-    xml = synth_tsl.broomstick_xml(tsl, nuc, histories=histories, energy=1e-6, temperature=450.0)
+    xml = synth_tsl.broomstick_xml(tsl, nuc, histories=histories, energy=energy, temperature=450.0)
     return {"xml": xml.replace("<seed>1</seed>", f"<seed>{seed}</seed>"), "base": str(base)}
 
 
 TSL_WORKLOAD = ("thermal broomstick fixed source (POD S(alpha,beta,T) library rank 30, 4+4 partitions; "
                 "1 eV pencil beam on a 0.01 cm hydrogen-moderator cylinder at 450 K; cosine x energy leakage "
                 "tally 202 x 202 bins)")
+GUIDE_TRAIN = dict(E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096, samples_per_condition=512,
+                   batch=16384, steps=10000, lr=1e-3, seed=3)
+
+
+def chi2_two_sample(a, b) -> dict:
+    """Two-sample chi-square of two histograms (bins with >= 10 counts)."""
+    from scipy import stats
+
+    keep = (a + b) >= 10
+    a, b = a[keep], b[keep]
+    ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    chi2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
+    dof = int(keep.sum()) - 1
+    return {"chi2": chi2, "dof": dof, "p": float(stats.chi2.sf(chi2, dof))}
+
+
+def _spectra(ctx, r):
+    e = ctx.estimators()[0]
+    t = r.sum[e.offset:e.offset + e.n_bins].reshape(int(e.cosine_bins), int(e.energy_bins))
+    return t.sum(0), t.sum(1)
+
+
+def thermal_forms(local: int, hist: int, steps: int, warmup: int, quantile: bool = False) -> dict:
+    """The thermal broomstick (C4 shape) transported with each form of the
+    thermal sampler, histories/s from the engine's device timing of each
+    fixed-source run (a step = one run of `hist` histories):
+      pod        -- ThermalScattering's POD sampler inside the history kernel (FP32 form);
+      pod_queue  -- the same sampler as a batched launch over the thermal-scatter queue;
+      guided     -- the queue with the guide network starting each CDF search (the
+                    surrogate form: the POD sampler's samples, for less work);
+      quantile   -- (optional) the MLP inverse-CDF surrogate on the queue (approximate).
+    Spectrum chi-square of each form against the POD form at independent seeds."""
+    from minimc_gb300 import (RNG_PHILOX, THERMAL_GUIDED, THERMAL_POD, THERMAL_POD_QUEUE, THERMAL_SURROGATE,
+                              Context)
+
+    wl = tsl_problem(hist)
+    ctx = Context(local)
+    ctx.load_xml(wl["xml"], wl["base"])
+    t0 = time.perf_counter()
+    g = ctx.train_surrogate_guide(0, **GUIDE_TRAIN)
+    train = {"guide_s": time.perf_counter() - t0, "guide_loss": g.loss_alpha, "guide_rows": g.samples,
+             "guide_data_ms": g.data_ms, "guide_train_ms": g.train_ms}
+    forms = {"pod": THERMAL_POD, "pod_queue": THERMAL_POD_QUEUE, "guided": THERMAL_GUIDED}
+    if quantile:
+        t0 = time.perf_counter()
+        tq = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=16384,
+                                 samples_per_condition=1024, batch=16384, steps=12000, lr=1e-3, seed=3)
+        train.update({"quantile_s": time.perf_counter() - t0, "quantile_loss_beta": tq.loss_beta,
+                      "quantile_loss_alpha": tq.loss_alpha})
+        forms["quantile"] = THERMAL_SURROGATE
+    base = dict(rng=RNG_PHILOX, fast_math=1, histories=hist)
+    out = {}
+    for name, mode in forms.items():
+        for _ in range(warmup):
+            ctx.run_fixed_source(thermal=mode, **base)
+        ms = kms = 0.0
+        events = launches = 0
+        for i in range(steps):
+            r = ctx.run_fixed_source(thermal=mode, seed=1000 + i, **base)
+            ms += r.raw.transport_ms
+            kms += r.raw.kernel_ms
+            events += r.raw.events
+            launches += r.raw.launches
+        out[name] = {"histories_per_s": hist * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "events_per_history": events / (hist * steps), "launches_per_step": launches / steps}
+    ref = ctx.run_fixed_source(thermal=THERMAL_POD, seed=101, **base)
+    same = ctx.run_fixed_source(thermal=THERMAL_GUIDED, seed=101, **base)
+    out["guided"]["identical_tallies_same_seed"] = bool(np.allclose(same.sum, ref.sum, rtol=1e-12, atol=0))
+    for name, mode in forms.items():
+        if name == "pod":
+            continue
+        r = ctx.run_fixed_source(thermal=mode, seed=202, **base)
+        sp, sr = _spectra(ctx, r), _spectra(ctx, ref)
+        out[name]["energy_chi2_vs_pod"] = chi2_two_sample(sp[0], sr[0])
+        out[name]["cosine_chi2_vs_pod"] = chi2_two_sample(sp[1], sr[1])
+    for name in forms:
+        out[name]["vs_pod"] = out[name]["histories_per_s"] / out["pod"]["histories_per_s"]
+    out["train"] = train
+    out["workload"] = TSL_WORKLOAD
+    out["histories_per_step"] = hist
+    return out
 
 
 def run_gpu_tsl(args) -> None:
-    """Broomstick transport (histories/s, POD thermal sampling inside the
-    transport kernel) plus the sampler-level comparison of the POD forms and
-    the trained MLP surrogate on C4's incident energies with T uniform in
-    283.6-623.6 K per sample."""
+    """Broomstick transport (histories/s) with each thermal sampler form,
+    plus the sampler-level comparison of the POD forms, the guided sampler
+    and the MLP quantile surrogate on C4's incident energies with T uniform
+    in 283.6-623.6 K per sample."""
     import torch
 
-    from minimc_gb300 import RNG_PHILOX, THERMAL_SURROGATE, TSL_FAST, TSL_MLP, TSL_PHILOX, TSL_POD, Context
+    from minimc_gb300 import TSL_FAST, TSL_GUIDED, TSL_MLP, TSL_PHILOX, TSL_POD, Context
 
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     hist = args.histories
-    wl = tsl_problem(hist, seed=1 + rank)
-    ctx = Context(local)
     stream = torch.cuda.current_stream()
-    ctx.set_stream(stream.cuda_stream)
-    ctx.load_xml(wl["xml"], wl["base"])
-    opts = dict(rng=RNG_PHILOX, fast_math=int(args.fast), histories=hist)
     if args.mode == "kernel":
-        # profiling mode: train the surrogate, then each sampler form on 4e6
-        # samples, `steps` times; no transport
+        # profiling mode: each sampler form on 4e6 samples, `steps` times; no transport
+        wl = tsl_problem(hist)
+        ctx = Context(local)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.load_xml(wl["xml"], wl["base"])
         n = 4_000_000
         E = torch.full((n,), 1e-7, dtype=torch.float64, device="cuda")
         T = torch.full((n,), 450.0, dtype=torch.float64, device="cuda")
         b = torch.empty_like(E)
         a = torch.empty_like(E)
+        ctx.train_surrogate_guide(0, **GUIDE_TRAIN)
         ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
                             samples_per_condition=512, batch=8192, steps=3000, seed=3)
-        for method in (TSL_POD | TSL_PHILOX | TSL_FAST, TSL_MLP):
+        for method in (TSL_POD | TSL_PHILOX | TSL_FAST, TSL_GUIDED, TSL_MLP):
             for i in range(args.steps):
                 ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=1 + i,
                                       method=method)
         torch.cuda.synchronize()
         print(json.dumps({"mode": "kernel", "beta_mean": float(b.mean())}), flush=True)
         return
-    for _ in range(args.warmup):
-        ctx.run_fixed_source(**opts)
     clocks = ClockSampler(local)
     clocks.start()
-    torch.cuda.synchronize()
-    ms, kms, walls, events, launches = [], [], [], 0, 0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        r = ctx.run_fixed_source(**opts)
-        walls.append(time.perf_counter() - t0)
-        ms.append(r.raw.transport_ms)
-        kms.append(r.raw.kernel_ms)
-        events += r.raw.events
-        launches += r.raw.launches
-    torch.cuda.synchronize()
+    forms = thermal_forms(local, hist, args.steps, args.warmup, quantile=True)
     clk = clocks.stop()
-    value = hist * args.steps * ws / (sum(ms) / 1e3)
-    e2e_value = hist * args.steps * ws / sum(walls)
-    e_h = events / (hist * args.steps)
-    peak, peak_kind = peaks()
-    alg = e_h * BYTES_PER_EVENT * hist
-    achieved = alg / (sum(kms) / args.steps / 1e3) / 1e9
+    value = forms["guided"]["histories_per_s"] * ws
 
-    # sampler level: POD exact, POD FP32, MLP surrogate (trained here)
+    # sampler level: POD exact, POD FP32, guided, MLP quantile surrogate
+    wl = tsl_problem(hist)
+    ctx = Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_xml(wl["xml"], wl["base"])
+    ctx.train_surrogate_guide(0, **GUIDE_TRAIN)
+    tr = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=16384,
+                             samples_per_condition=1024, batch=16384, steps=12000, lr=1e-3, seed=3)
     n = 4_000_000
     g = torch.Generator(device="cuda")
     g.manual_seed(7)
@@ -426,13 +524,9 @@ def run_gpu_tsl(args) -> None:
     T = 283.6 + 340.0 * torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
     b = torch.empty(n, dtype=torch.float64, device="cuda")
     a = torch.empty_like(b)
-    t0 = time.perf_counter()
-    tr = ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=16384,
-                             samples_per_condition=1024, batch=16384, steps=12000, lr=1e-3, seed=3)
-    train_s = time.perf_counter() - t0
     rates, samples = {}, {}
     for name, method in (("pod_exact", TSL_POD | TSL_PHILOX), ("pod_fp32", TSL_POD | TSL_PHILOX | TSL_FAST),
-                         ("mlp", TSL_MLP)):
+                         ("guided", TSL_GUIDED), ("mlp_quantile", TSL_MLP)):
         for _ in range(2):
             ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=11, method=method)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -444,50 +538,15 @@ def run_gpu_tsl(args) -> None:
         e1.record(stream)
         torch.cuda.synchronize()
         rates[name] = n * reps / (e0.elapsed_time(e1) / 1e3)
-        samples[name] = (b[:200_000].cpu().numpy(), a[:200_000].cpu().numpy())
+        samples[name] = (b.cpu().numpy().copy(), a.cpu().numpy().copy())
     from scipy import stats
 
-    ks = {k: {"beta": float(stats.ks_2samp(samples[k][0], samples["pod_exact"][0]).statistic),
-              "alpha": float(stats.ks_2samp(samples[k][1], samples["pod_exact"][1]).statistic)}
-          for k in ("pod_fp32", "mlp")}
-    # transport with the surrogate: thermal scatters through the queue
-    # (one tensor-core sampler launch per round), same histories per step
-    sur_opts = dict(opts, thermal=THERMAL_SURROGATE)
-    pod_ref = ctx.run_fixed_source(**dict(opts, seed=101))
-    for _ in range(args.warmup):
-        ctx.run_fixed_source(**sur_opts)
-    sms, skms, slaunch = [], [], 0
-    for _ in range(args.steps):
-        r = ctx.run_fixed_source(**sur_opts)
-        sms.append(r.raw.transport_ms)
-        skms.append(r.raw.kernel_ms)
-        slaunch += r.raw.launches
-    sur_ref = ctx.run_fixed_source(**dict(sur_opts, seed=202))
-    sur_value = hist * args.steps * ws / (sum(sms) / 1e3)
-    spectra = {}
-    e0 = ctx.estimators()[0]
-    for name, rr in (("pod", pod_ref), ("surrogate", sur_ref)):
-        t = rr.sum[e0.offset:e0.offset + e0.n_bins].reshape(int(e0.cosine_bins), int(e0.energy_bins))
-        spectra[name] = (t.sum(0), t.sum(1))
-    from scipy import stats as sst
-
-    def chi2_two_sample(a, b):
-        keep = (a + b) >= 10
-        a, b = a[keep], b[keep]
-        ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
-        chi2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
-        dof = int(keep.sum()) - 1
-        return {"chi2": chi2, "dof": dof, "p": float(sst.chi2.sf(chi2, dof))}
-
-    surrogate_transport = {
-        "value": sur_value, "unit": UNIT, "vs_pod_transport": sur_value / value,
-        "ms_per_step": sum(sms) / args.steps, "kernel_ms_per_step": sum(skms) / args.steps,
-        "launches_per_step": slaunch / args.steps,
-        "energy_spectrum_chi2_vs_pod": chi2_two_sample(spectra["surrogate"][0], spectra["pod"][0]),
-        "cosine_spectrum_chi2_vs_pod": chi2_two_sample(spectra["surrogate"][1], spectra["pod"][1]),
-        "spectrum_histories": hist,
-    }
-    flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two networks, multiply-adds x 2
+    ks = {k: {"beta": float(stats.ks_2samp(samples[k][0][:200_000], samples["pod_exact"][0][:200_000]).statistic),
+              "alpha": float(stats.ks_2samp(samples[k][1][:200_000], samples["pod_exact"][1][:200_000]).statistic)}
+          for k in ("pod_fp32", "mlp_quantile")}
+    same = bool(np.array_equal(samples["guided"][0], samples["pod_fp32"][0], equal_nan=True) and
+                np.array_equal(samples["guided"][1], samples["pod_fp32"][1], equal_nan=True))
+    flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two network rows per sample, multiply-adds x 2
     bf16_peak = None
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -503,25 +562,28 @@ def run_gpu_tsl(args) -> None:
         cpu = {"value": nc / rc["seconds"], "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{nc} histories of the same broomstick (CPU oracle, {thr} threads), {rc['seconds']:.1f} s"}
     if rank == 0:
+        peak, peak_kind = peaks()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": sum(ms) / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": TSL_WORKLOAD, "histories_per_step": hist, "rng": "philox",
-                       "fast_math": bool(args.fast), "l2": "inputs generated on device; tallies 0.65 MB"},
-            "events_per_history": e_h,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "peak_kind": peak_kind, "kernel": "k_history_ce"},
-            "surrogate_transport": surrogate_transport,
-            "surrogate": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "train_s": train_s,
-                          "train": {"loss_beta": tr.loss_beta, "loss_alpha": tr.loss_alpha, "samples": tr.samples,
-                                    "data_ms": tr.data_ms, "train_ms": tr.train_ms},
-                          "mlp_tflops": rates["mlp"] * flops / 1e12, "bf16_peak_tflops": bf16_peak,
-                          "sample_n": n},
+            "ms_per_step": forms["guided"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": TSL_WORKLOAD, "histories_per_step": hist, "rng": "philox", "fast_math": True,
+                       "form": "guided (surrogate-started CDF searches, POD-exact samples)",
+                       "l2": "inputs generated on device; tallies 0.65 MB"},
+            "thermal_forms": forms,
+            "sampler": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "guided_equals_pod_fp32": same,
+                        "quantile_train": {"loss_beta": tr.loss_beta, "loss_alpha": tr.loss_alpha,
+                                           "samples": tr.samples, "data_ms": tr.data_ms, "train_ms": tr.train_ms},
+                        "mlp_quantile_tflops": rates["mlp_quantile"] * flops / 1e12,
+                        "guided_tflops": rates["guided"] * flops / 1e12, "bf16_peak_tflops": bf16_peak,
+                        "sample_n": n},
+            "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                         "traffic": None, "peak_kind": peak_kind, "kernel": "k_history_ce",
+                         "note": "see the default two-zone line; this workload is latency-bound"},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 2 * 8 * ctx.info.total_bins, "call": "mc_run_fixed_source"},
-            "gpu_launches": int(launches), "clocks": clk,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 2 * 8 * 40804,
+                    "call": "mc_run_fixed_source (tallies read back every step)"},
+            "gpu_launches": int(forms["guided"]["launches_per_step"] * args.steps), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
 
@@ -598,6 +660,7 @@ def main():
     ap.add_argument("--cpu-histories", type=int, default=1_000_000)
     ap.add_argument("--cpu-cycles", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the thermal surrogate leg of the default line")
     ap.add_argument("--variant", type=int, default=0, help="history-kernel variant + 1 (0: autotuned)")
     ap.add_argument("--mode", default="full", choices=["full", "kernel"],
                     help="kernel: only the k-eigenvalue cycles (for profiler captures)")

@@ -62,6 +62,16 @@ extern "C" {
  * streams, continuous energy); outside the box the POD sampler serves. */
 #define MC_THERMAL_POD 0
 #define MC_THERMAL_SURROGATE 1
+/* The guided sampler on the same queue: the trained guide network
+ * (mc_train_surrogate_guide) predicts where SampleAlpha's CDF search ends,
+ * the POD reconstructions confirm it, so every thermal scatter draws exactly
+ * the FP32 POD sampler's (beta, alpha) from the particle's own stream and the
+ * transport gives the same histories as MC_THERMAL_POD with fast_math, for
+ * less work (Philox streams, fast_math, continuous energy). */
+#define MC_THERMAL_GUIDED 2
+/* The FP32 POD sampler run as a batched launch over the same queue, without
+ * the network (the guided form's ablation; same histories). */
+#define MC_THERMAL_POD_QUEUE 3
 
 /* How the event loop is scheduled on the device. */
 #define MC_SCHEDULE_AUTO 0     /* autotuner's choice                      */
@@ -316,6 +326,9 @@ int mc_energy_index(mc_ctx* ctx, int32_t nuclide, const double* energy, uint64_t
 /* ---- thermal scattering (ThermalScattering.cpp) --------------------------- */
 #define MC_TSL_POD 0      /* POD reconstruction, SampleBeta/SampleAlpha     */
 #define MC_TSL_MLP 1      /* MLP surrogate (POD outside the trained box)    */
+#define MC_TSL_GUIDED 2   /* guided POD: the FP32 POD form's samples for the
+                             same Philox streams, CDF searches started where
+                             the guide network predicts (Philox only)      */
 #define MC_TSL_PHILOX 0x10 /* flag: Philox streams keyed by seed, counter i;
                               without it sample i draws from minstd seeded
                               seed + i, as the reference would            */
@@ -363,6 +376,15 @@ typedef struct mc_train_out {
 } mc_train_out;
 #define MC_MLP_PARAMS 35329     /* FP32 parameters per network              */
 int mc_train_surrogate(mc_ctx* ctx, int32_t tsl, const mc_train_desc* desc, mc_train_out* out);
+/* The guide network of the guided sampler (MC_TSL_GUIDED, MC_THERMAL_GUIDED;
+ * no reference counterpart): the same architecture, trained on the device to
+ * predict the CDF-grid position where ThermalScattering::SampleAlpha's
+ * find_cdf bisection ends (src/ThermalScattering.cpp:395-421) for each
+ * kinematic bound, from the bound, |beta| of the chosen grid point and T.
+ * Rows come from the FP32 POD sampler in the (E, T) box:
+ * conditions * samples_per_condition samples (defaults 8192 * 256), two
+ * rows each.  out->loss_alpha receives the guide's mean squared error. */
+int mc_train_surrogate_guide(mc_ctx* ctx, int32_t tsl, const mc_train_desc* desc, mc_train_out* out);
 /* Trained weights and box (net 0: beta, 1: alpha; MC_MLP_PARAMS floats each). */
 int mc_surrogate_get(mc_ctx* ctx, float* beta_params, float* alpha_params, mc_train_desc* box);
 int mc_surrogate_set(mc_ctx* ctx, int32_t tsl, const mc_train_desc* box, const float* beta_params,

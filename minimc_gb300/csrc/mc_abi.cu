@@ -29,6 +29,36 @@ struct DevBuffer {
   size_t bytes = 0;
 };
 
+// device scratch buffers of a context, grown on demand
+enum ScratchSlot {
+  kSrc = 0,
+  kSlots,
+  kCount,
+  kOffsets,
+  kScanSums,
+  kTotal,
+  kBank,
+  kHistEvents,
+  kHistFate,
+  kProbeIn,
+  kProbeIn2,
+  kProbeOut,
+  kEvState,
+  kEvQueues,
+  kEvCnt,
+  kEvPend,
+  kEvFis,
+  kTslFail,
+  kParkA,
+  kParkB,
+  kTqIn,
+  kTqOut,
+  kTqCnt,
+  kTqRows,
+  kTqRes,
+  kScratchSlots,  // number of slots
+};
+
 struct mc_ctx {
   int device = 0;
   int num_sms = 0;
@@ -62,7 +92,7 @@ struct mc_ctx {
   size_t pend_clean_bytes = 0;
   uint64_t launches = 0;
   // scratch, grown on demand
-  DevBuffer scratch[24];
+  DevBuffer scratch[kScratchSlots];
   int last_schedule = MC_SCHEDULE_HISTORY;
   // autotuner: history-kernel variant (occupancy target) chosen by timing
   int variant = 0;
@@ -76,6 +106,11 @@ struct mc_ctx {
   int mlp_batch_cap = 0;
   mcd::MlpBox mlp_box{};
   int32_t mlp_tsl = -1;          // library the networks were trained for
+  // guide network of the guided (POD-exact) thermal sampler
+  mcd::MlpNet guide;
+  mcd::MlpBox guide_box{};
+  int32_t guide_tsl = -1;
+  std::vector<bool> tsl_fast_ok;  // per library: every partition's rank fits the FP32 POD form
   std::vector<void*> mlp_allocs;
   // k-eigenvalue state
   struct {
@@ -119,31 +154,6 @@ __global__ void k_copy_bank_out(const uint4* bank, const unsigned long long* tot
 }
 
 
-enum ScratchSlot {
-  kSrc = 0,
-  kSlots,
-  kCount,
-  kOffsets,
-  kScanSums,
-  kTotal,
-  kBank,
-  kHistEvents,
-  kHistFate,
-  kProbeIn,
-  kProbeIn2,
-  kProbeOut,
-  kEvState,
-  kEvQueues,
-  kEvCnt,
-  kEvPend,
-  kEvFis,
-  kTslFail,
-  kParkA,
-  kParkB,
-  kTqIn,
-  kTqOut,
-  kTqCnt,
-};
 
 int fail(mc_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -244,6 +254,39 @@ int build_pod(mc_ctx* c, const mc::PODPartitionSet& P, mcd::DevPOD& d) {
   if ((rc = upload(c, g_off, &d.g_off)) != MC_OK) return rc;
   if ((rc = upload(c, g, &d.g)) != MC_OK) return rc;
   if ((rc = upload(c, gf, &d.gf)) != MC_OK) return rc;
+  // monotone flags of the FP32 form: at each tabulated temperature the
+  // reconstruction x_F = sum_o cs[F][o] gf[g][T][o] must rise from F to F + 1
+  // by more than four times the bound on the FP32 dot products' rounding
+  // (r * 2^-24 * sum_o |cs gf| for each); a convex combination of two
+  // such columns (the sampler's temperature interpolation) then rises too
+  std::vector<uint8_t> mono(P.concat.size(), 0);
+  for (size_t p = 0; p < np; p++) {
+    const size_t r = P.S[p].size(), nFp = P.F[p].size(), nTp = P.T[p].size();
+    const size_t first = p == 0 ? 0 : P.ends[p - 1];
+    const float* csp = cs.data() + cdf_off[p];
+    const float* gfp = gf.data() + g_off[p];
+    for (size_t gi = 0; first + gi < P.ends[p]; gi++) {
+      bool ok = true;
+      for (size_t t = 0; t < nTp && ok; t++) {
+        const float* v = gfp + (gi * nTp + t) * r;
+        double prev = 0, prev_err = 0;
+        for (size_t f = 0; f < nFp && ok; f++) {
+          double x = 0, a = 0;
+          for (size_t o = 0; o < r; o++) {
+            const double term = static_cast<double>(csp[f * r + o]) * v[o];
+            x += term;
+            a += std::fabs(term);
+          }
+          const double err = static_cast<double>(r) * 0x1p-24 * a;
+          if (f > 0 && !(x - prev > 4.0 * (err + prev_err))) ok = false;
+          prev = x;
+          prev_err = err;
+        }
+      }
+      mono[first + gi] = ok ? 1 : 0;
+    }
+  }
+  if ((rc = upload(c, mono, &d.mono)) != MC_OK) return rc;
   return MC_OK;
 }
 
@@ -251,6 +294,7 @@ int build_pod(mc_ctx* c, const mc::PODPartitionSet& P, mcd::DevPOD& d) {
 int build_tsl(mc_ctx* c) {
   const mc::Model& m = c->model;
   std::vector<mcd::DevTSL> libs;
+  c->tsl_fast_ok.clear();
   for (const mc::TSLData& t : m.tsl) {
     mcd::DevTSL d{};
     d.beta_cutoff = t.beta_cutoff;
@@ -286,6 +330,7 @@ int build_tsl(mc_ctx* c) {
     for (const auto& S : t.beta.S) fits &= S.size() <= static_cast<size_t>(mcd::kFastPodRank);
     for (const auto& S : t.alpha.S) fits &= S.size() <= static_cast<size_t>(mcd::kFastPodRank);
     d.fast_ok = fits ? 1 : 0;
+    c->tsl_fast_ok.push_back(fits);
     libs.push_back(d);
   }
   c->dw.n_tsl = static_cast<int32_t>(libs.size());
@@ -437,6 +482,21 @@ int build_world(mc_ctx* c) {
     UP(mtot, mat_mg_total)
     UP(mcdf, mat_mg_nuc_cdf)
     UP(mnsf, mat_mg_nusigf)
+    // FP32 copies (round to nearest) for the fast form
+    auto f32 = [](const std::vector<double>& v) {
+      std::vector<float> o(v.size());
+      for (size_t i = 0; i < v.size(); i++) o[i] = static_cast<float>(v[i]);
+      return o;
+    };
+    const std::vector<float> msig_f = f32(msig), mtot_f = f32(mtot), mcdf_f = f32(mcdf), total_f = f32(total),
+                             rx_f = f32(rx), scat_f = f32(scat), nubar_f = f32(nubar);
+    UP(msig_f, mat_mg_sigma_f)
+    UP(mtot_f, mat_mg_total_f)
+    UP(mcdf_f, mat_mg_nuc_cdf_f)
+    UP(total_f, mg_total_f)
+    UP(rx_f, mg_rx_cdf_f)
+    UP(scat_f, mg_scat_cdf_f)
+    UP(nubar_f, mg_nubar_f)
   }
   else {
     for (const auto& nuc : m.nuclides) {
@@ -778,8 +838,10 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   const int sched = resolve_schedule(c, schedule);
   if (sched < 0) return fail(c, MC_ERR_INPUT, "the event schedule supports multigroup problems with at most 64 tally bins");
   c->last_schedule = sched;
-  // dense per-history scores when the estimators are small, fission records
-  // for k-eigenvalue cycles
+  // dense per-history scores when the estimators are small (committed by
+  // a separate kernel: per-history sums kept in shared memory instead were
+  // measured slower, their commits contend on shared FP64 atomics), fission
+  // records for k-eigenvalue cycles
   const uint64_t n = rp.n;
   rp.nb = (rp.score && c->total_bins > 0 && c->total_bins <= static_cast<uint64_t>(mcd::kDenseBins))
               ? static_cast<int32_t>(c->total_bins)
@@ -862,16 +924,23 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
 // rounds need no host synchronisation; the last resume samples inline.
 int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
   const uint64_t n = rp.n;
+  const int mode = rp.tq_mode;  // 1 quantile surrogate, 2 guided, 3 plain POD queue
+  const bool exact_q = mode >= 2;
   auto* A = static_cast<mcd::ParkRec*>(scratch(c, kParkA, n * sizeof(mcd::ParkRec)));
   auto* B = static_cast<mcd::ParkRec*>(scratch(c, kParkB, n * sizeof(mcd::ParkRec)));
-  auto* qin = static_cast<float4*>(scratch(c, kTqIn, n * sizeof(float4)));
-  auto* qout = static_cast<float2*>(scratch(c, kTqOut, n * sizeof(float2)));
+  auto* qin = exact_q ? nullptr : static_cast<float4*>(scratch(c, kTqIn, n * sizeof(float4)));
+  auto* qout = exact_q ? nullptr : static_cast<float2*>(scratch(c, kTqOut, n * sizeof(float2)));
+  auto* rows = exact_q ? static_cast<mcd::GuideRow*>(scratch(c, kTqRows, n * sizeof(mcd::GuideRow))) : nullptr;
+  auto* res = exact_q ? static_cast<mcd::GuideOut*>(scratch(c, kTqRes, n * sizeof(mcd::GuideOut))) : nullptr;
   auto* cnt = static_cast<unsigned long long*>(scratch(c, kTqCnt, 2 * (mcd::kTqRounds + 1) * 8));
-  if (!A || !B || !qin || !qout || !cnt) return fail(c, MC_ERR_OOM, "thermal queue buffers");
+  if (!A || !B || !cnt || (exact_q ? !(rows && res) : !(qin && qout)))
+    return fail(c, MC_ERR_OOM, "thermal queue buffers");
   unsigned long long* heads = cnt + mcd::kTqRounds + 1;
   CUDA_TRY(c, cudaMemsetAsync(cnt, 0, 2 * (mcd::kTqRounds + 1) * 8, c->stream));
   rp.tq = 1;
-  rp.tq_tsl = c->mlp_tsl;
+  rp.tq_tsl = mode == 1 ? c->mlp_tsl : (c->guide_tsl >= 0 ? c->guide_tsl : 0);
+  rp.tq_rows = rows;
+  rp.tq_res = res;
   rp.tq_box[0] = std::exp(c->mlp_box.logE0);
   rp.tq_box[1] = std::exp(c->mlp_box.logE1);
   rp.tq_box[2] = c->mlp_box.T0;
@@ -890,9 +959,16 @@ int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
   for (int r = 0; r < mcd::kTqRounds; r++) {
     mcd::ParkRec* in = r % 2 == 0 ? A : B;
     mcd::ParkRec* out = r % 2 == 0 ? B : A;
-    e = mcd::launch_sample_tsl_mlp_queue(c->mlp[0], c->mlp[1], c->mlp_box, qin, cnt + r, n, qout, c->num_sms,
-                                         c->stream);
-    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("surrogate launch: ") + cudaGetErrorString(e));
+    if (mode == 2)
+      e = mcd::launch_sample_tsl_guided_queue(c->dw.tsl + rp.tq_tsl, c->guide, c->guide_box, rows, cnt + r, n,
+                                              rp.run_key, res, c->num_sms, c->stream);
+    else if (mode == 3)
+      e = mcd::launch_sample_tsl_pod_queue(c->dw.tsl + rp.tq_tsl, rows, cnt + r, n, rp.run_key, res, c->num_sms,
+                                           c->stream);
+    else
+      e = mcd::launch_sample_tsl_mlp_queue(c->mlp[0], c->mlp[1], c->mlp_box, qin, cnt + r, n, qout, c->num_sms,
+                                           c->stream);
+    if (e != cudaSuccess) return fail(c, MC_ERR_DEVICE, std::string("thermal sampler launch: ") + cudaGetErrorString(e));
     rp.tq = r + 1 < mcd::kTqRounds ? 1 : 0;
     rp.head = heads + r;
     rp.n_resume = cnt + r;
@@ -1181,13 +1257,22 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
   rp.from_bank = 0;
   rp.ref_source_seeds = 1;
   rp.max_yield = c->max_yield;
-  if (o && o->thermal == MC_THERMAL_SURROGATE) {
+  if (o && (o->thermal == MC_THERMAL_SURROGATE || o->thermal == MC_THERMAL_GUIDED ||
+            o->thermal == MC_THERMAL_POD_QUEUE)) {
     if (c->model.energy_mode != mc::kContinuous || rng != MC_RNG_PHILOX)
-      return fail(c, MC_ERR_INPUT, "the surrogate thermal sampler needs a continuous-energy problem and Philox streams");
-    if (c->mlp_tsl < 0) return fail(c, MC_ERR_STATE, "no trained surrogate (mc_train_surrogate)");
+      return fail(c, MC_ERR_INPUT, "the thermal-scatter queue needs a continuous-energy problem and Philox streams");
+    if (o->thermal == MC_THERMAL_SURROGATE && c->mlp_tsl < 0)
+      return fail(c, MC_ERR_STATE, "no trained surrogate (mc_train_surrogate)");
+    if (o->thermal == MC_THERMAL_GUIDED && c->guide_tsl < 0)
+      return fail(c, MC_ERR_STATE, "no trained guide network (mc_train_surrogate_guide)");
+    if (o->thermal != MC_THERMAL_SURROGATE && !rp.fast)
+      return fail(c, MC_ERR_INPUT, "the POD-exact thermal queue stands in for the FP32 POD sampler: set fast_math");
+    if (o->thermal != MC_THERMAL_SURROGATE && c->dw.n_tsl == 0)
+      return fail(c, MC_ERR_INPUT, "the problem has no thermal scattering library");
     if (!c->model.perturbations.empty())
-      return fail(c, MC_ERR_INPUT, "the surrogate thermal sampler does not carry indirect effects");
+      return fail(c, MC_ERR_INPUT, "the thermal-scatter queue does not carry indirect effects");
     rp.tq = 1;  // run_transport takes the queue form
+    rp.tq_mode = o->thermal == MC_THERMAL_SURROGATE ? 1 : (o->thermal == MC_THERMAL_GUIDED ? 2 : 3);
   }
   else if (o && o->thermal != MC_THERMAL_POD) {
     return fail(c, MC_ERR_INPUT, "unknown thermal sampler");
@@ -1997,6 +2082,24 @@ int sample_tsl_device(mc_ctx* c, int32_t tsl, const double* E, const double* T, 
   if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
   const int base = method & 0xF;
   if (base == MC_TSL_MLP) return sample_tsl_mlp(c, tsl, E, T, n, seed, method, beta, alpha, failures);
+  if (base == MC_TSL_GUIDED) {
+    if (c->guide_tsl != tsl) return fail(c, MC_ERR_STATE, "the guide network is not trained for this library");
+    if (!c->tsl_fast_ok[static_cast<size_t>(tsl)])
+      return fail(c, MC_ERR_INPUT, "the guided sampler needs the FP32 POD form (ranks up to 32)");
+    auto* d_fail = static_cast<unsigned long long*>(scratch(c, kTslFail, sizeof(unsigned long long)));
+    if (!d_fail) return fail(c, MC_ERR_OOM, "sampler counters");
+    CUDA_TRY(c, cudaMemsetAsync(d_fail, 0, sizeof(unsigned long long), c->stream));
+    // the POD sampler's stream keys (Philox), so that the samples are its own
+    CUDA_TRY(c, mcd::launch_sample_tsl_guided(c->dw.tsl + tsl, c->guide, c->guide_box, E, T, n,
+                                              run_key(seed, 0, 0x54534C00ull), beta, alpha, d_fail, c->num_sms,
+                                              c->stream));
+    c->launches++;
+    unsigned long long h = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&h, d_fail, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (failures) *failures = h;
+    return mlp_check(c);
+  }
   if (base != MC_TSL_POD) return fail(c, MC_ERR_INPUT, "unknown thermal scattering method");
   const bool philox = (method & MC_TSL_PHILOX) != 0;
   const bool fast = (method & MC_TSL_FAST) != 0;
@@ -2156,6 +2259,91 @@ int mc_train_surrogate(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_tra
   o.loss_beta = loss_b;
   o.loss_alpha = loss_a;
   o.samples = N;
+  if (out) *out = o;
+  return MC_OK;
+}
+
+// The guide network of the guided sampler: rows from the FP32 POD sampler
+// (per sample: (E, T) drawn in the box, SampleBeta, SampleAlpha's beta grid
+// choice, then for both kinematic bounds the features and the grid position
+// where find_cdf's bisection ends), then the same training loop as the
+// surrogate networks.  desc->conditions * desc->samples_per_condition
+// samples make twice as many rows.
+int mc_train_surrogate_guide(mc_ctx* c, int32_t tsl, const mc_train_desc* desc, mc_train_out* out) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  if (!desc) return fail(c, MC_ERR_INPUT, "null argument");
+  if (!c->tsl_fast_ok[static_cast<size_t>(tsl)])
+    return fail(c, MC_ERR_INPUT, "the guided sampler needs the FP32 POD form (ranks up to 32)");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  mc_train_desc d = *desc;
+  if (!d.conditions) d.conditions = 8192;
+  if (!d.samples_per_condition) d.samples_per_condition = 256;
+  if (!d.batch) d.batch = 8192;
+  if (!d.steps) d.steps = 4000;
+  if (!(d.lr > 0)) d.lr = 2e-3f;
+  if (d.batch % 128 || d.batch > (1u << 20)) return fail(c, MC_ERR_INPUT, "batch: a multiple of 128 up to 2^20");
+  const mc::TSLData& t = c->model.tsl[static_cast<size_t>(tsl)];
+  if (!(d.E_min > 0 && d.E_min < d.E_max && d.E_max < t.cutoff_energy()))
+    return fail(c, MC_ERR_INPUT, "energy box must lie inside (0, cutoff energy)");
+  if (!(d.T_min > 0 && d.T_min < d.T_max)) return fail(c, MC_ERR_INPUT, "temperature box");
+  mcd::MlpBox box;
+  box.logE0 = std::log(d.E_min);
+  box.logE1 = std::log(d.E_max);
+  box.T0 = d.T_min;
+  box.T1 = d.T_max;
+  box.beta_cutoff = t.beta_cutoff;
+  box.awr = t.awr;
+  box.beta_scale = std::log1p(std::max(t.beta_cutoff, d.E_max / (mcd::kBoltzmann * d.T_min)));
+  if (!mlp_net_alloc(c, c->guide) || !mlp_batch_alloc(c, static_cast<int>(d.batch)))
+    return fail(c, MC_ERR_OOM, "guide network buffers");
+  const uint64_t N = d.conditions * d.samples_per_condition, rows = 2 * N;
+  __half* X = nullptr;
+  float* y = nullptr;
+  unsigned long long* d_fail = nullptr;
+  if (cudaMalloc(&X, rows * mcd::kMlpIn * sizeof(__half)) != cudaSuccess ||
+      cudaMalloc(&y, rows * sizeof(float)) != cudaSuccess || cudaMalloc(&d_fail, 8) != cudaSuccess) {
+    cudaFree(X);
+    cudaFree(y);
+    cudaFree(d_fail);
+    return fail(c, MC_ERR_OOM, "guide training data");
+  }
+  mc_train_out o{};
+  double loss = 0;
+  int rc = MC_OK;
+  do {
+    cudaError_t e;
+    if ((e = cudaEventRecord(c->ev0, c->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d_fail, 0, 8, c->stream)) != cudaSuccess ||
+        (e = mcd::launch_guide_data(c->dw.tsl + tsl, box, run_key(d.seed, 1, 0x47554944ull), N, X, y, d_fail,
+                                    c->stream)) != cudaSuccess ||
+        (e = cudaEventRecord(c->ev1, c->stream)) != cudaSuccess || (e = cudaEventSynchronize(c->ev1)) != cudaSuccess) {
+      rc = fail(c, MC_ERR_DEVICE, std::string("guide training data: ") + cudaGetErrorString(e));
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.data_ms = ms;
+    CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if ((rc = mlp_train(c, c->guide, X, y, rows, 7, d, run_key(d.seed, 2, 0x47554944ull), &loss)) != MC_OK) break;
+    CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    o.train_ms = ms;
+    unsigned long long f = 0;
+    CUDA_TRY(c, cudaMemcpy(&f, d_fail, 8, cudaMemcpyDeviceToHost));
+    o.failures = f;
+  } while (false);
+  c->launches += 2;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(X);
+  cudaFree(y);
+  cudaFree(d_fail);
+  if (rc != MC_OK) return rc;
+  c->guide_box = box;
+  c->guide_tsl = tsl;
+  o.loss_alpha = loss;  // the guide's loss (one network)
+  o.samples = rows;
   if (out) *out = o;
   return MC_OK;
 }

@@ -112,6 +112,11 @@ struct DevPOD {
   const uint32_t* g_off;      // [n_parts] into g ([grid][nT][rank])
   const double* g;
   const float* gf;            // g in FP32 (fast form), same offsets
+  // [n_grid] 1 where the FP32 reconstruction of the grid point's inverse CDF
+  // rises along F at every tabulated temperature by more than its rounding
+  // bound (so it rises at every temperature between them too): a search
+  // over it may start anywhere and still find upper_bound's answer
+  const uint8_t* mono;
 };
 
 struct DevTSL {
@@ -129,6 +134,22 @@ struct DevTSL {
   const double* maj_x;        // majorant ContinuousMap
   const double* maj_y;
   DevPOD beta, alpha;
+};
+
+// A parked thermal scatter as the batched POD-exact samplers read it (the
+// guided sampler and the plain POD queue): incident energy, temperature and
+// the particle's own Philox stream position; and what they return: (beta,
+// alpha), the stream position after their draws, and whether the sampler
+// stayed within the resample limits.
+struct GuideRow {
+  double E, T;
+  unsigned long long rng_id;
+  uint32_t rng_pos, rng_tag;
+};
+struct GuideOut {
+  double beta, alpha;
+  uint32_t rng_pos;
+  int32_t ok;
 };
 
 constexpr int kMaxPert = 4;  // perturbations per problem
@@ -188,6 +209,16 @@ struct DevWorld {
   const int32_t* cell_box;        // [n_cells] index into boxes, or -1
   const struct BoxCell* boxes;
   const double* mat_mg_sigma;     // [T][M][G] number_density * microscopic total
+  // FP32 copies for the fast form (Philox streams, FP32 sampling
+  // arithmetic): flight lengths, nuclide / reaction / outgoing-group
+  // thresholds and fission yields are drawn against these
+  const float* mat_mg_sigma_f;    // [T][M][G]
+  const float* mat_mg_total_f;    // [T][M][G]
+  const float* mat_mg_nuc_cdf_f;  // [T][M][G][max_mat_nuc]
+  const float* mg_total_f;        // [T][N][G]
+  const float* mg_rx_cdf_f;       // [T][N][G][3]
+  const float* mg_scat_cdf_f;     // [T][N][G][G]
+  const float* mg_nubar_f;        // [T][N][G]
   DevCE ce;                       // continuous energy
   int32_t n_tsl;
   const DevTSL* tsl;              // [n_tsl] thermal scattering libraries
@@ -479,7 +510,7 @@ __device__ __forceinline__ bool dneg(double x) {
 // tiny or unusable FP32 values fall back to all exact divisions, so the
 // result always equals the exact computation.
 __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, int c, const double* pos,
-                                                   const double* dir, double& dist, int skip) {
+                                                   const double* dir, const float* dirf, double& dist, int skip) {
   const BoxCell& B = w.boxes[box];
   int cj[3];
   double cv[3];
@@ -498,7 +529,7 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
     const double v = dsub(__ldg(&B.c[j]), p);
     cv[a] = v;
     const bool ahead = __ldg(&B.s[j]) != skip && ((dpos(v) && dpos(d)) || (dneg(v) && dneg(d)));
-    tf[a] = ahead ? fabsf(__fdiv_rn(__double2float_rn(v), __double2float_rn(d))) : CUDART_INF_F;
+    tf[a] = ahead ? fabsf(__fdiv_rn(__double2float_rn(v), dirf[a])) : CUDART_INF_F;
   }
   int a0 = 0;
   if (tf[1] < tf[a0]) a0 = 1;
@@ -542,13 +573,31 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
 // surface order) with the least distance.  `skip` (robust crossing, see
 // below) is a surface the particle has just left and is moving away from;
 // it is treated as infinitely far.
+__device__ __forceinline__ int nearest_surface_general(const DevWorld& w, int c, double x, double y, double z,
+                                                       double u, double v, double ww, double& dist, int skip);
+
+// The same with the direction also given in FP32 (the box cells' preselection
+// reads it; callers that keep it avoid three conversions per event)
 __device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
-                                               double v, double ww, double& dist, int skip = -1) {
+                                               double v, double ww, float fu, float fv, float fw, double& dist,
+                                               int skip = -1) {
   const int box = __ldg(w.cell_box + c);
   if (box >= 0) {
     const double pos[3] = {x, y, z}, dir[3] = {u, v, ww};
-    return nearest_surface_box(w, box, c, pos, dir, dist, skip);
+    const float dirf[3] = {fu, fv, fw};
+    return nearest_surface_box(w, box, c, pos, dir, dirf, dist, skip);
   }
+  return nearest_surface_general(w, c, x, y, z, u, v, ww, dist, skip);
+}
+
+__device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
+                                               double v, double ww, double& dist, int skip = -1) {
+  return nearest_surface(w, c, x, y, z, u, v, ww, __double2float_rn(u), __double2float_rn(v), __double2float_rn(ww),
+                         dist, skip);
+}
+
+__device__ __forceinline__ int nearest_surface_general(const DevWorld& w, int c, double x, double y, double z,
+                                                       double u, double v, double ww, double& dist, int skip) {
   const int b = __ldg(w.cell_begin + c), e = __ldg(w.cell_begin + c + 1);
   int best = -1;
   double bd = CUDART_INF;
@@ -644,6 +693,19 @@ __device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, d
 // exponential flight length in FP32: -log(U) / sigma (U in (0,1))
 __device__ __forceinline__ double flight_fast(float u, double sigma) {
   return static_cast<double>(__fdiv_rn(-__logf(u), __double2float_rn(sigma)));
+}
+
+// the same on an FP32 table (fast form)
+__device__ __forceinline__ int cdf_first_above_f(const float* cdf, int n, float threshold) {
+  const int t = __float_as_int(threshold);
+  for (int k = 0; k < n; k++)
+    if (__float_as_int(__ldg(cdf + k)) > t) return k;
+  return -1;
+}
+
+// exponential flight length from an FP32 macroscopic total
+__device__ __forceinline__ double flight_fast_f(float u, float sigma) {
+  return static_cast<double>(__fdiv_rn(-__logf(u), sigma));
 }
 
 // first k in [0, n) with cdf[k] > threshold (both non-negative), or -1;

@@ -201,12 +201,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_mg(const DevWorld w, const E
       const int m = __ldg(w.cell_mat + cell);
       const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * w.G + g;
       const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
-      double dcol;
-      if (fast) {
-        if constexpr (std::is_same_v<Rng, PhiloxRng>) dcol = flight_fast(rng.u01f(), sigma);
-        else dcol = flight_fast(static_cast<float>(rng.u01()), sigma);
-      }
-      else dcol = ddiv(-log(dsub(1.0, rng.u01())), sigma);
+      const double dcol = mg_flight(w, rng, fast, mg, sigma);
       double dsurf;
       const int s = nearest_surface(w, cell, x, y, z, u, v, ww, dsurf, skip);
       const bool collide = w.tracking == 1 ? !(dsurf < dcol) : (dcol < dsurf);
@@ -222,18 +217,14 @@ __global__ void __launch_bounds__(256) k_ev_advance_mg(const DevWorld w, const E
       int event;
       if (collide) {
         track(dcol);
-        x = dadd(x, dmul(u, dcol));
-        y = dadd(y, dmul(v, dcol));
-        z = dadd(z, dmul(ww, dcol));
+        move(fast, x, y, z, u, v, ww, dcol);
         skip = -1;
         to_coll = true;
         event = kScatter;  // placeholder; the collide kernel decides
       }
       else if (__ldg(w.surf_refl + s)) {
         track(dsurf);
-        x = dadd(x, dmul(u, dsurf));
-        y = dadd(y, dmul(v, dsurf));
-        z = dadd(z, dmul(ww, dsurf));
+        move(fast, x, y, z, u, v, ww, dsurf);
         const int kind = __ldg(w.surf_kind + s);
         double nu = u, nv = v, nw = ww;
         if (kind == kPlaneX) nu = -u;
@@ -249,9 +240,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_mg(const DevWorld w, const E
       else {
         const double d = dadd(dsurf, kNudge);
         track(d);
-        x = dadd(x, dmul(u, d));
-        y = dadd(y, dmul(v, d));
-        z = dadd(z, dmul(ww, d));
+        move(fast, x, y, z, u, v, ww, d);
         if (w.quirks) {
           cell = find_cell(w, x, y, z);
         }
@@ -340,14 +329,10 @@ __global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const E
       const double micro = __ldg(w.mat_mg_total + mg);
       // CellDeltaTracking's real/virtual test; multigroup majorant == total
       if (w.tracking == 1) (void)uni(rng, fast);
-      const double thr_n = dmul(micro, uni(rng, fast));
       const int nb = __ldg(w.mat_begin + m), ne = __ldg(w.mat_begin + m + 1);
-      int kn = first_above(w.mat_mg_nuc_cdf + mg * w.max_mat_nuc, ne - nb, thr_n);
-      if (kn < 0) kn = ne - nb - 1;
-      const int nuc = __ldg(w.mat_nuc + nb + kn);
+      const int nuc = __ldg(w.mat_nuc + nb + mg_pick_nuclide(w, rng, fast, mg, ne - nb, micro));
       const size_t ng = (static_cast<size_t>(t) * w.n_nuclides + nuc) * G + g;
-      const double thr_r = dmul(uni(rng, fast), __ldg(w.mg_total + ng));
-      const int rx = first_above(w.mg_rx_cdf + ng * 3, 3, thr_r);
+      const int rx = mg_pick_reaction(w, rng, fast, ng);
       int event = kScatter;
       if (rx < 0) {
         // no reaction selected (threshold at the top of the CDF): the
@@ -359,8 +344,7 @@ __global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const E
         event = kCapture;
       }
       else if (rx == 1) {
-        const double thr = uni(rng, fast);
-        const int go = first_above(w.mg_scat_cdf + ng * G, G, thr);
+        const int go = mg_pick_outgoing(w, rng, fast, ng);
         if (go >= 0) {
           g = go;
           double u, v, ww;
@@ -374,8 +358,7 @@ __global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const E
       }
       else if (rx == 2) {
         event = kFission;
-        const double nubar = __ldg(w.mg_nubar + ng);
-        const unsigned yield = static_cast<unsigned>(dadd(nubar, uni(rng, fast)));
+        const unsigned yield = mg_yield(w, rng, fast, ng);
         if (ep.rp.keig) {
           FissionRec& f = ep.rp.fis[ep.st.hist[i]];
           f.x = ep.st.x[i];

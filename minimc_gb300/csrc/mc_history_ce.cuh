@@ -217,36 +217,50 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
             pend.overflow = ((R.pend_n >> 8) & 1) != 0;
             sc.dense = rp.nb ? rp.pend + hist : nullptr;
             const DevTSL& tl = w.tsl[R.tsl];
-            const float2 ba = rp.tq_out[qi];
             bool ok = false;
-            if (isfinite(ba.x) && isfinite(ba.y)) {
-              // ThermalScattering::Scatter's kinematics (src/ThermalScattering.cpp:159-171);
-              // the outgoing energy in FP64, the cosine and the rotation in
-              // FP32 in fast mode (the surrogate's (beta, alpha) are FP32)
-              const double kT = kBoltzmann * R.T;
-              const double Ep = p.E + static_cast<double>(ba.x) * kT;
-              if (Ep > 0) {
-                if (ffg) {
-                  const float num = __double2float_rn(p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT);
-                  const float mu = fminf(1.0f, fmaxf(-1.0f, __fdiv_rn(num, 2.0f * __fsqrt_rn(__double2float_rn(p.E * Ep)))));
-                  float dx = static_cast<float>(p.u), dy = static_cast<float>(p.v), dz = static_cast<float>(p.w);
-                  rotate_f(dx, dy, dz, mu, p.rng.u01f());
-                  p.u = dx;
-                  p.v = dy;
-                  p.w = dz;
-                }
-                else {
-                  const double mu = fmin(1.0, fmax(-1.0, (p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT) /
-                                                             (2.0 * sqrt(p.E * Ep))));
-                  rotate(p.u, p.v, p.w, mu, 2 * kPi * p.rng.u01());
-                }
-                p.E = Ep;
+            if (rp.tq_mode >= 2) {
+              // a POD-exact sample (guided or plain queue): continue the
+              // particle's stream after the sampler's draws and apply the
+              // kinematics exactly as the inline sampler does
+              const GuideOut go = rp.tq_res[qi];
+              p.rng.restore(rp.run_key, R.rng_id, R.rng_tag, go.rng_pos);
+              if (go.ok) {
+                tsl_apply<true>(tl, p.rng, R.T, go.beta, go.alpha, p.E, p.u, p.v, p.w);
                 ok = true;
               }
             }
-            if (!ok) {  // not representable: the POD sampler, inline
-              ok = tl.fast_ok && ffg ? tsl_scatter<true>(tl, p.rng, R.T, p.E, p.u, p.v, p.w)
-                                     : tsl_scatter<false>(tl, p.rng, R.T, p.E, p.u, p.v, p.w);
+            else {
+              const float2 ba = rp.tq_out[qi];
+              if (isfinite(ba.x) && isfinite(ba.y)) {
+                // ThermalScattering::Scatter's kinematics (src/ThermalScattering.cpp:159-171);
+                // the outgoing energy in FP64, the cosine and the rotation in
+                // FP32 in fast mode (the surrogate's (beta, alpha) are FP32)
+                const double kT = kBoltzmann * R.T;
+                const double Ep = p.E + static_cast<double>(ba.x) * kT;
+                if (Ep > 0) {
+                  if (ffg) {
+                    const float num = __double2float_rn(p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT);
+                    const float mu =
+                        fminf(1.0f, fmaxf(-1.0f, __fdiv_rn(num, 2.0f * __fsqrt_rn(__double2float_rn(p.E * Ep)))));
+                    float dx = static_cast<float>(p.u), dy = static_cast<float>(p.v), dz = static_cast<float>(p.w);
+                    rotate_f(dx, dy, dz, mu, p.rng.u01f());
+                    p.u = dx;
+                    p.v = dy;
+                    p.w = dz;
+                  }
+                  else {
+                    const double mu = fmin(1.0, fmax(-1.0, (p.E + Ep - static_cast<double>(ba.y) * tl.awr * kT) /
+                                                               (2.0 * sqrt(p.E * Ep))));
+                    rotate(p.u, p.v, p.w, mu, 2 * kPi * p.rng.u01());
+                  }
+                  p.E = Ep;
+                  ok = true;
+                }
+              }
+              if (!ok) {  // not representable: the POD sampler, inline
+                ok = tl.fast_ok && ffg ? tsl_scatter<true>(tl, p.rng, R.T, p.E, p.u, p.v, p.w)
+                                       : tsl_scatter<false>(tl, p.rng, R.T, p.E, p.u, p.v, p.w);
+              }
             }
             p.event = ok ? kScatter : kLostEvent;
             if (!ok) my_resample++;
@@ -366,8 +380,13 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
               // reference throws, here the history ends and is counted
               const DevTSL& tl = w.tsl[d.rx_tsl[r]];
               if constexpr (TQ) {
+                // the POD-exact forms (modes 2, 3) stand in for the FP32 POD
+                // sampler only, and need no trained box
+                const bool exact_q = rp.tq_mode >= 2;
                 if (rp.tq && d.rx_tsl[r] == rp.tq_tsl && sp == 0 && pend.n <= kParkPending &&
-                    p.E >= rp.tq_box[0] && p.E <= rp.tq_box[1] && T >= rp.tq_box[2] && T <= rp.tq_box[3]) {
+                    (exact_q ? (ffg && tl.fast_ok)
+                             : (p.E >= rp.tq_box[0] && p.E <= rp.tq_box[1] && T >= rp.tq_box[2] &&
+                                T <= rp.tq_box[3]))) {
                   // park for the batched surrogate sampler
                   const unsigned am = __activemask();
                   const int ld = __ffs(am) - 1;
@@ -377,8 +396,20 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
                   pb = __shfl_sync(am, pb, ld);
                   const unsigned long long slot = pb + __popc(am & ((1u << lane) - 1u));
                   if (slot < rp.park_cap) {
-                    const float u1 = p.rng.u01f(), u2 = p.rng.u01f();
-                    rp.tq_in[slot] = make_float4(static_cast<float>(p.E), static_cast<float>(T), u1, u2);
+                    if (exact_q) {
+                      GuideRow g;
+                      g.E = p.E;
+                      g.T = T;
+                      g.rng_id = static_cast<unsigned long long>(p.rng.h0) |
+                                 (static_cast<unsigned long long>(p.rng.h1) << 32);
+                      g.rng_pos = p.rng.save();
+                      g.rng_tag = p.rng.tag;
+                      rp.tq_rows[slot] = g;
+                    }
+                    else {
+                      const float u1 = p.rng.u01f(), u2 = p.rng.u01f();
+                      rp.tq_in[slot] = make_float4(static_cast<float>(p.E), static_cast<float>(T), u1, u2);
+                    }
                     ParkRec& R = rp.park_out[slot];
                     R.x = p.x;
                     R.y = p.y;

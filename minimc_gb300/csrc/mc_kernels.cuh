@@ -3,6 +3,8 @@
 
 #include "mc_device.cuh"
 
+#include <type_traits>
+
 namespace mcd {
 
 // mc_site layout (include/minimc_gb300.h)
@@ -92,6 +94,12 @@ struct RunParams {
   unsigned long long* park_count;      // records parked by this launch
   unsigned long long park_cap;
   int32_t direct_sites;  // k-eigenvalue: sites go straight into the bank (no slot kernel)
+  // thermal-scatter queue forms: 1 the quantile surrogate (tq_in / tq_out),
+  // 2 the guided sampler and 3 the plain POD queue (tq_rows / tq_res: POD-exact
+  // samples drawn from the particle's own stream)
+  int32_t tq_mode;
+  GuideRow* tq_rows;
+  const GuideOut* tq_res;
 };
 
 // k-eigenvalue sites from fission records and the per-history commit of
@@ -237,6 +245,88 @@ cudaError_t launch_material_xs_ce(const DevWorld& w, int32_t cell, const double*
                                   unsigned long long n, double* total, double* majorant, cudaStream_t stream);
 cudaError_t launch_energy_index(const DevWorld& w, int32_t nuclide, const double* energy, unsigned long long n,
                                 long long* out, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Multigroup collision choices, shared by the history and event schedules so
+// that both draw the same numbers and take the same decisions.  The exact
+// form follows the reference (FP64 thresholds against FP64 running sums);
+// the fast form (Philox streams, fast_math) forms the threshold in FP32 and
+// searches the FP32 copies of the same running sums.
+
+// Particle::SampleNuclide (src/Particle.cpp:110-124); a material of one
+// nuclide returns it whatever the threshold (micro * U < micro), so only
+// the draw is made
+template <class Rng>
+__device__ __forceinline__ int mg_pick_nuclide(const DevWorld& w, Rng& rng, bool fast, size_t mg, int count,
+                                               double micro) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) {
+      const float u = rng.u01f();
+      if (count == 1) return 0;
+      const int k = cdf_first_above_f(w.mat_mg_nuc_cdf_f + mg * w.max_mat_nuc, count,
+                                      __fmul_rn(__ldg(w.mat_mg_total_f + mg), u));
+      return k < 0 ? count - 1 : k;
+    }
+  }
+  const double u = rng.u01();
+  if (count == 1) return 0;
+  const int k = cdf_first_above(w.mat_mg_nuc_cdf + mg * w.max_mat_nuc, count, dmul(micro, u));
+  return k < 0 ? count - 1 : k;  // unreachable in the reference (assert)
+}
+
+// Multigroup::Interact's reaction (src/Multigroup.cpp:49-73): 0 capture,
+// 1 scatter, 2 fission, -1 none (threshold at the top of the CDF)
+template <class Rng>
+__device__ __forceinline__ int mg_pick_reaction(const DevWorld& w, Rng& rng, bool fast, size_t ng) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return cdf_first_above_f(w.mg_rx_cdf_f + ng * 3, 3, __fmul_rn(rng.u01f(), __ldg(w.mg_total_f + ng)));
+  }
+  return cdf_first_above(w.mg_rx_cdf + ng * 3, 3, dmul(rng.u01(), __ldg(w.mg_total + ng)));
+}
+
+// Multigroup::Scatter's outgoing group (src/Multigroup.cpp:249-265), or -1
+template <class Rng>
+__device__ __forceinline__ int mg_pick_outgoing(const DevWorld& w, Rng& rng, bool fast, size_t ng) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return cdf_first_above_f(w.mg_scat_cdf_f + ng * w.G, w.G, rng.u01f());
+  }
+  return cdf_first_above(w.mg_scat_cdf + ng * w.G, w.G, rng.u01());
+}
+
+// Multigroup::Fission's yield floor(nubar + U) (src/Multigroup.cpp:267-272)
+template <class Rng>
+__device__ __forceinline__ unsigned mg_yield(const DevWorld& w, Rng& rng, bool fast, size_t ng) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return static_cast<unsigned>(__fadd_rn(__ldg(w.mg_nubar_f + ng), rng.u01f()));
+  }
+  return static_cast<unsigned>(dadd(__ldg(w.mg_nubar + ng), rng.u01()));
+}
+
+// exponential flight in a multigroup material: -log(1 - U) / sigma, the
+// fast form from the FP32 macroscopic total
+template <class Rng>
+__device__ __forceinline__ double mg_flight(const DevWorld& w, Rng& rng, bool fast, size_t mg, double sigma) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) return flight_fast_f(rng.u01f(), __ldg(w.mat_mg_sigma_f + mg));
+  }
+  return ddiv(-log(dsub(1.0, rng.u01())), sigma);
+}
+
+// Particle::Stream: position += direction * d; the fast form rounds each
+// coordinate once (fused multiply-add)
+__device__ __forceinline__ void move(bool fast, double& x, double& y, double& z, double u, double v, double w,
+                                     double d) {
+  if (fast) {
+    x = fma(u, d, x);
+    y = fma(v, d, y);
+    z = fma(w, d, z);
+  }
+  else {
+    x = dadd(x, dmul(u, d));
+    y = dadd(y, dmul(v, d));
+    z = dadd(z, dmul(w, d));
+  }
+}
 
 // Philox helper shared with the host-side resampler description
 __host__ __device__ inline unsigned long long splitmix64(unsigned long long z) {

@@ -997,4 +997,326 @@ cudaError_t launch_sample_tsl_mlp_queue(const MlpNet& beta_net, const MlpNet& al
 
 int* mlp_error_flag() { return mlp_err_ptr(); }
 
+// ---------------------------------------------------------------------------
+// Learned brackets for SampleAlpha's CDF search (the guided sampler).
+//
+// ThermalScattering::SampleAlpha spends most of its time in find_cdf: a
+// bisection over the CDF grid whose every probe is a rank-r POD
+// reconstruction (src/ThermalScattering.cpp:395-421), twice per sample.  The
+// guide network predicts where that search ends -- the grid position of the
+// kinematic bound a, given |beta_s| and T -- and the search starts there:
+// two reconstructions confirm a right guess, a wrong one is walked out with
+// doubling steps and bisected (cdf_upper_guided).  Everything else is the
+// POD sampler itself, so for the same random numbers the guided sampler
+// returns exactly the POD sampler's (beta, alpha); only the work differs.
+
+namespace {
+
+// guide features of a bound a at |beta_s| and T (FP32, as in training):
+// ln a, ln(1 + |beta|), T, the log ratio of a to |beta|, and the free-gas
+// scaling variable (a - |beta|) / (2 sqrt a) -- for a free gas alpha given
+// beta is close to normal in it -- plain and squashed
+__device__ __forceinline__ void guide_features(const BoxF& b, float a, float abs_bs, float T, float (&f)[kMlpIn]) {
+#pragma unroll
+  for (int i = 0; i < kMlpIn; i++) f[i] = 0.0f;
+  const float aa = fmaxf(a, 1e-12f);
+  const float la = logf(aa);
+  f[0] = fmaf(la, 0.1f, 1.0f);
+  f[1] = fmaf(log1pf(abs_bs) * b.inv_beta_scale, 2.0f, -1.0f);
+  f[2] = fmaf(T, b.t_scale, b.t_shift);
+  f[3] = fminf(4.0f, fmaxf(-4.0f, (la - logf(abs_bs + 1e-3f)) * 0.125f));
+  f[4] = aa / (aa + abs_bs + 1.0f);
+  const float z = (aa - abs_bs) / (2.0f * sqrtf(aa));
+  f[5] = fminf(4.0f, fmaxf(-4.0f, 0.25f * z));
+  f[6] = tanhf(0.5f * z);
+}
+
+// training rows: per sample, (E, T) drawn in the box, beta from the POD
+// sampler, the beta grid point SampleAlpha picks, and for each of the two
+// bounds the features and the position where find_cdf's bisection ends
+__global__ void k_guide_data(const DevTSL* tsl, MlpBox box, unsigned long long key, unsigned long long n, f16* X,
+                             float* y, unsigned long long* failures) {
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BoxF bf = box_f(box);
+  const DevTSL& t = *tsl;
+  PhiloxRng rng;
+  rng.init(key, i, 6);
+  const double E = exp(box.logE0 + rng.u01() * (box.logE1 - box.logE0));
+  const double T = box.T0 + rng.u01() * (box.T1 - box.T0);
+  double b = 0;
+  AlphaCtx<true> x;
+  const bool ok = tsl_sample_beta<true>(t, rng, E, T, b) && alpha_begin<true>(t, rng, b, E, T, x);
+  float f[kMlpIn];
+#pragma unroll 1
+  for (int k = 0; k < 2; k++) {
+    float target = 0.5f, a = 1.0f, bs = 1.0f;
+    if (ok) {
+      const double av = k == 0 ? x.b_s_a_min : x.b_s_a_max;
+      target = cdf_position<true>(t, x, av, cdf_upper_bisect<true>(x, av));
+      a = static_cast<float>(av);
+      bs = fabsf(static_cast<float>(x.b_s));
+    }
+    guide_features(bf, a, bs, static_cast<float>(T), f);
+    store_features(f, X + (2 * i + k) * kMlpIn);
+    y[2 * i + k] = target;
+  }
+  if (!ok) atomicAdd(failures, 1ull);
+}
+
+constexpr int kGuideGroups = 4;  // warpgroups per CTA, each with its own tiles and accumulator
+constexpr uint32_t kGOffW1 = 0;
+constexpr uint32_t kGOffW2 = kGOffW1 + kTileW1;
+constexpr uint32_t kGOffW3 = kGOffW2 + kTileW;
+constexpr uint32_t kGOffG = kGOffW3 + kTileW;
+constexpr uint32_t kGOffF = kGOffG + kGuideGroups * kGroupBytes;
+constexpr uint32_t kGOffMisc = kGOffF + (4 * kMlpWidth + 4) * 4;
+constexpr uint32_t kGuideSmem = kGOffMisc + 64;
+static_assert(kGuideSmem <= 227 * 1024, "shared memory");
+
+struct GuideIO {
+  const DevTSL* tsl;
+  // array form: (E, T) per row, Philox streams keyed by the row
+  const double* E;
+  const double* T;
+  unsigned long long n;
+  unsigned long long key;
+  double* beta_out;
+  double* alpha_out;
+  unsigned long long* failures;
+  // queue form: parked particles with their own streams
+  const GuideRow* rows;
+  const unsigned long long* qcount;
+  unsigned long long qcap;
+  unsigned long long run_key;
+  GuideOut* qout;
+};
+
+// One thread per sample, 128-sample tiles per warpgroup: the POD SampleBeta
+// and the beta grid choice on the CUDA cores, the guide network for both
+// bounds on the tensor cores (one tcgen05 product per layer), then the
+// guided searches and SampleAlpha's resampling loop.
+template <bool QUEUE>
+__global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView nv, MlpBox box, GuideIO io, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  float* fw = reinterpret_cast<float*>(smem + kGOffF);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kGOffMisc);  // [0, 2G) mbarriers, [2G] tensor memory
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const unsigned long long n = QUEUE ? (*io.qcount < io.qcap ? *io.qcount : io.qcap) : io.n;
+  if (n == 0) return;  // uniform across the grid: nothing allocated yet
+  load_tile(smem + kGOffW1, nv.W1, kMlpIn);
+  load_tile(smem + kGOffW2, nv.W2, kMlpWidth);
+  load_tile(smem + kGOffW3, nv.W3, kMlpWidth);
+  for (int i = tid; i < kMlpWidth; i += blockDim.x) {  // hidden biases halved for the SiLU epilogues
+    fw[i] = 0.5f * nv.p[kMlpB1 + i];
+    fw[kMlpWidth + i] = 0.5f * nv.p[kMlpB2 + i];
+    fw[2 * kMlpWidth + i] = 0.5f * nv.p[kMlpB3 + i];
+    fw[3 * kMlpWidth + i] = nv.p[kMlpW4 + i];
+  }
+  if (tid == 0) {
+    fw[4 * kMlpWidth] = nv.p[kMlpB4];
+    for (int g = 0; g < kGuideGroups; g++) tc::mbar_init(tc::smem_addr(misc + 2 * g), 1);
+  }
+  if (warp == 0) tc::tmem_alloc(tc::smem_addr(misc + 2 * kGuideGroups), 128 * kGuideGroups);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  Group G;
+  G.base = smem;
+  G.g = tid >> 7;
+  G.lt = tid & 127;
+  G.X = kGOffG + G.g * kGroupBytes;
+  G.H = G.X + kTileW1;
+  G.tmem = misc[2 * kGuideGroups] + 128 * G.g;
+  G.mbar = tc::smem_addr(misc + 2 * G.g);
+  G.phase = 0;
+  G.ok = true;
+  const BoxF bf = box_f(box);
+  const DevTSL& t = *io.tsl;
+  unsigned long long my_fail = 0;
+  const unsigned long long tiles = (n + 127) / 128;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * kGuideGroups;
+  for (unsigned long long tile = static_cast<unsigned long long>(blockIdx.x) * kGuideGroups + G.g;
+       tile < tiles && G.ok; tile += stride) {
+    const unsigned long long i = tile * 128 + G.lt;
+    const bool valid = i < n;
+    PhiloxRng rng;
+    double E = 1e-7, T = 300.0;
+    if constexpr (QUEUE) {
+      if (valid) {
+        const GuideRow R = io.rows[i];
+        E = R.E;
+        T = R.T;
+        rng.restore(io.run_key, R.rng_id, R.rng_tag, R.rng_pos);
+      }
+    }
+    else {
+      if (valid) {
+        E = io.E[i];
+        T = io.T[i];
+      }
+      rng.init(io.key, i, 2);
+    }
+    double b = 0, a_min = 1.0, a_max = 1.0;
+    float abs_bs = 1.0f;
+    int b_s_i = -1;
+    bool ok = valid && tsl_sample_beta<true>(t, rng, E, T, b);
+    if (ok) {
+      AlphaCtx<true> x;
+      ok = alpha_begin<true>(t, rng, b, E, T, x);
+      if (ok) {
+        b_s_i = x.b_s_i;
+        a_min = x.b_s_a_min;
+        a_max = x.b_s_a_max;
+        abs_bs = fabsf(static_cast<float>(x.b_s));
+      }
+    }
+    // the guide network on both bounds (every row of the tile takes part)
+    float f[kMlpIn];
+    guide_features(bf, static_cast<float>(a_min), abs_bs, static_cast<float>(T), f);
+    write_x(G, f);
+    const float q0 = run_net(G, kGOffW1, kGOffW2, kGOffW3, fw);
+    guide_features(bf, static_cast<float>(a_max), abs_bs, static_cast<float>(T), f);
+    write_x(G, f);
+    const float q1 = run_net(G, kGOffW1, kGOffW2, kGOffW3, fw);
+    double alpha = 0;
+    if (ok) {
+      AlphaCtx<true> x;
+      alpha_setup<true>(t, b, E, T, b_s_i, x);  // the same context, rebuilt after the network
+      const float m = static_cast<float>(x.nF + 1);
+      const int g0 = static_cast<int>(floorf(fminf(1.0f, fmaxf(0.0f, q0)) * m));
+      const int g1 = static_cast<int>(floorf(fminf(1.0f, fmaxf(0.0f, q1)) * m));
+      // grid points whose reconstruction is not safely monotone, and
+      // temperatures outside the tabulated range (where Evaluate
+      // extrapolates), keep the bisection, so the answer is always the POD
+      // sampler's
+      const bool mono = __ldg(t.alpha.mono + b_s_i) != 0 && x.ev.c.Tl < x.ev.c.Th && x.ev.c.Tl <= T &&
+                        T <= x.ev.c.Th;
+      const int i_min = mono ? cdf_upper_guided<true>(x, x.b_s_a_min, g0) : cdf_upper_bisect<true>(x, x.b_s_a_min);
+      const int i_max = mono ? cdf_upper_guided<true>(x, x.b_s_a_max, g1) : cdf_upper_bisect<true>(x, x.b_s_a_max);
+      const double F_min = cdf_at<true>(t, x, x.b_s_a_min, i_min);
+      const double F_max = cdf_at<true>(t, x, x.b_s_a_max, i_max);
+      ok = alpha_end<true>(t, rng, x, F_min, F_max, alpha);
+    }
+    if (valid) {
+      if constexpr (QUEUE) {
+        GuideOut o;
+        o.beta = ok ? b : CUDART_NAN;
+        o.alpha = ok ? alpha : CUDART_NAN;
+        o.rng_pos = rng.save();
+        o.ok = ok ? 1 : 0;
+        io.qout[i] = o;
+      }
+      else {
+        io.beta_out[i] = ok ? b : CUDART_NAN;
+        io.alpha_out[i] = ok ? alpha : CUDART_NAN;
+        if (!ok) my_fail++;
+      }
+    }
+  }
+  if (!G.ok && G.lt == 0) atomicExch(err, 1);
+  if constexpr (!QUEUE) {
+    if (my_fail) atomicAdd(io.failures, my_fail);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(misc[2 * kGuideGroups], 128 * kGuideGroups);
+  }
+}
+
+// the POD sampler on the same queue, without the network (the ablation of
+// the guided form: same batching, find_cdf by plain bisection)
+__global__ void __launch_bounds__(256) k_pod_queue(const DevTSL* tsl, const GuideRow* rows,
+                                                   const unsigned long long* qcount, unsigned long long qcap,
+                                                   unsigned long long run_key, GuideOut* qout) {
+  const unsigned long long n = *qcount < qcap ? *qcount : qcap;
+  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const GuideRow R = rows[i];
+    PhiloxRng rng;
+    rng.restore(run_key, R.rng_id, R.rng_tag, R.rng_pos);
+    double b = 0, a = 0;
+    const bool ok = tsl_sample_beta<true>(*tsl, rng, R.E, R.T, b) && tsl_sample_alpha<true>(*tsl, rng, b, R.E, R.T, a);
+    GuideOut o;
+    o.beta = ok ? b : CUDART_NAN;
+    o.alpha = ok ? a : CUDART_NAN;
+    o.rng_pos = rng.save();
+    o.ok = ok ? 1 : 0;
+    qout[i] = o;
+  }
+}
+
+template <bool QUEUE>
+cudaError_t guided_attr() {
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_guided_sample<QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuideSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_guide_data(const DevTSL* tsl, const MlpBox& box, unsigned long long key, unsigned long long n,
+                              __half* X, float* y, unsigned long long* failures, cudaStream_t s) {
+  k_guide_data<<<blocks256(n), 256, 0, s>>>(tsl, box, key, n, X, y, failures);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, const double* E,
+                                     const double* T, unsigned long long n, unsigned long long key, double* beta,
+                                     double* alpha, unsigned long long* failures, int num_sms, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = guided_attr<false>();
+  if (e != cudaSuccess) return e;
+  const unsigned long long tiles = (n + 127) / 128;
+  const unsigned long long want = (tiles + kGuideGroups - 1) / kGuideGroups;
+  const unsigned grid = static_cast<unsigned>(want < static_cast<unsigned long long>(num_sms) ? want : num_sms);
+  NetView nv{guide.p, guide.W1, guide.W2, guide.W3};
+  GuideIO io{};
+  io.tsl = tsl;
+  io.E = E;
+  io.T = T;
+  io.n = n;
+  io.key = key;
+  io.beta_out = beta;
+  io.alpha_out = alpha;
+  io.failures = failures;
+  k_guided_sample<false><<<grid, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box,
+                                           const GuideRow* rows, const unsigned long long* count,
+                                           unsigned long long cap, unsigned long long run_key, GuideOut* out,
+                                           int num_sms, cudaStream_t s) {
+  if (cap == 0) return cudaSuccess;
+  cudaError_t e = guided_attr<true>();
+  if (e != cudaSuccess) return e;
+  NetView nv{guide.p, guide.W1, guide.W2, guide.W3};
+  GuideIO io{};
+  io.tsl = tsl;
+  io.rows = rows;
+  io.qcount = count;
+  io.qcap = cap;
+  io.run_key = run_key;
+  io.qout = out;
+  // the row count is known on the device only: one persistent CTA per SM
+  k_guided_sample<true><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, const GuideRow* rows, const unsigned long long* count,
+                                        unsigned long long cap, unsigned long long run_key, GuideOut* out,
+                                        int num_sms, cudaStream_t s) {
+  if (cap == 0) return cudaSuccess;
+  k_pod_queue<<<num_sms * 8, 256, 0, s>>>(tsl, rows, count, cap, run_key, out);
+  return cudaGetLastError();
+}
+
 }  // namespace mcd

@@ -111,6 +111,28 @@ cudaError_t launch_expand(const double* src, unsigned long long n, int K, double
 cudaError_t launch_quantile_u(double* u, unsigned long long n, int K, cudaStream_t s);
 // the device flag a timed-out tensor-core wait sets
 int* mlp_error_flag();
+
+// Guided sampler: the guide network (same layout as the surrogate networks:
+// 16 inputs, three hidden layers of 128, one output) predicts where
+// SampleAlpha's CDF bisection ends for each kinematic bound; the POD
+// sampler then confirms or walks from there, so the samples are exactly the
+// FP32 POD sampler's for the same random numbers.
+// training rows: 2 per sample (the two bounds), n samples
+cudaError_t launch_guide_data(const DevTSL* tsl, const MlpBox& box, unsigned long long key, unsigned long long n,
+                              __half* X, float* y, unsigned long long* failures, cudaStream_t s);
+// array form: Philox stream of row i keyed by (key, i), as the POD sampler's
+cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, const double* E,
+                                     const double* T, unsigned long long n, unsigned long long key, double* beta,
+                                     double* alpha, unsigned long long* failures, int num_sms, cudaStream_t s);
+// queue form: parked rows, *count of them (at most cap, read on the device)
+cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box,
+                                           const GuideRow* rows, const unsigned long long* count,
+                                           unsigned long long cap, unsigned long long run_key, GuideOut* out,
+                                           int num_sms, cudaStream_t s);
+// the POD sampler over the same queue, bisection without the network
+cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, const GuideRow* rows, const unsigned long long* count,
+                                        unsigned long long cap, unsigned long long run_key, GuideOut* out,
+                                        int num_sms, cudaStream_t s);
 // per-condition sort of K samples (K a power of two <= 1024) in place
 cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K, cudaStream_t s);
 // gathers a random batch (Philox key, step) of B rows of X / y into the

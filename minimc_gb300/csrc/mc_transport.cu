@@ -29,8 +29,7 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
                                            Emit&& emit) {
   const int G = w.G;
   const size_t base = (static_cast<size_t>(t) * w.n_nuclides + nuc) * G;
-  const double nubar = __ldg(w.mg_nubar + base + p.g);
-  const unsigned yield = static_cast<unsigned>(dadd(nubar, uniform(p.rng, fast)));
+  const unsigned yield = mg_yield(w, p.rng, fast, base + p.g);
   const double* chi = w.mg_chi_cdf + (base + p.g) * G;
   for (unsigned i = 0; i < yield; i++) {
     const double thr = uniform(p.rng, fast);
@@ -64,6 +63,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
   const unsigned lane = lane_id();
   const bool fast = rp.fast != 0;
   Particle<Rng> p;
+  float fu = 0, fv = 0, fw = 0;  // the direction in FP32, for the box cells' preselection
   Pending<kPending> pend;
   pend.clear();
   Scorer sc{&pend, nullptr, rp.n};
@@ -108,6 +108,9 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
         else {
           if (rp.from_bank) start_from_site(rp, hist, rp.src[hist], p, 0);
           else sample_source(w, rp, hist, p);
+          fu = __double2float_rn(p.u);
+          fv = __double2float_rn(p.v);
+          fw = __double2float_rn(p.w);
           p.cell = find_cell(w, p.x, p.y, p.z);
           p.event = kBirth;
           p.surf = -1;
@@ -146,9 +149,9 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       const size_t mg = (static_cast<size_t>(t) * w.n_materials + m) * w.G + p.g;
       const double micro = __ldg(w.mat_mg_total + mg);
       const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
-      const double dcol = sample_flight(p.rng, sigma, fast);
+      const double dcol = mg_flight(w, p.rng, fast, mg, sigma);
       double dsurf;
-      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
+      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, fu, fv, fw, dsurf, p.skip);
       const bool delta = w.tracking == 1;
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
       const bool refl = !collide && __ldg(w.surf_refl + s) != 0;
@@ -161,34 +164,31 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       if (rp.score) score_track(w, p, dmove, sc);
       if (KEIG) my_ktl += dmove * __ldg(w.mat_mg_nusigf + mg);
       indirect_stream<PERT>(w, p, m, micro, dmove);
-      stream(p.x, p.y, p.z, p.u, p.v, p.w, dmove);
+      move(fast, p.x, p.y, p.z, p.u, p.v, p.w, dmove);
       if (collide) {
         p.skip = -1;
         // multigroup majorant == total, so CellDeltaTracking's rejection
         // (src/TransportMethod.cpp:106-108) always accepts; it still draws
         if (delta) (void)uniform(p.rng, fast);
         // Particle::SampleNuclide (src/Particle.cpp:110-124)
-        const double thr_n = dmul(micro, uniform(p.rng, fast));
-        const double* ncdf = w.mat_mg_nuc_cdf + mg * w.max_mat_nuc;
         const int nb = __ldg(w.mat_begin + m), ne = __ldg(w.mat_begin + m + 1);
-        int k = cdf_search(ncdf, ne - nb, 1, thr_n);
-        if (k < 0) k = ne - nb - 1;  // unreachable in the reference (assert)
-        const int nuc = __ldg(w.mat_nuc + nb + k);
+        const int nuc = __ldg(w.mat_nuc + nb + mg_pick_nuclide(w, p.rng, fast, mg, ne - nb, micro));
         // Multigroup::Interact (src/Multigroup.cpp:49-73)
         const size_t ng = (static_cast<size_t>(t) * w.n_nuclides + nuc) * w.G + p.g;
-        const double thr_r = dmul(uniform(p.rng, fast), __ldg(w.mg_total + ng));
-        const int rx = cdf_search(w.mg_rx_cdf + ng * 3, 3, 1, thr_r);
+        const int rx = mg_pick_reaction(w, p.rng, fast, ng);
         if (rx == 0) {
           p.event = kCapture;
         }
         else if (rx == 1) {
           // Multigroup::Scatter (src/Multigroup.cpp:249-265)
           p.event = kScatter;
-          const double thr = uniform(p.rng, fast);
-          const int go = cdf_search(w.mg_scat_cdf + ng * w.G, w.G, 1, thr);
+          const int go = mg_pick_outgoing(w, p.rng, fast, ng);
           if (go >= 0) {
             p.g = go;
             sample_isotropic(p.rng, p.u, p.v, p.w, fast);
+            fu = __double2float_rn(p.u);
+            fv = __double2float_rn(p.v);
+            fw = __double2float_rn(p.w);
           }
         }
         else if (rx == 2) {
@@ -196,7 +196,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           if constexpr (KEIG) {
             // record the fission; its sites are drawn by the sites kernel
             // from the stream position after the yield draw
-            const unsigned yield = static_cast<unsigned>(dadd(__ldg(w.mg_nubar + ng), uniform(p.rng, fast)));
+            const unsigned yield = mg_yield(w, p.rng, fast, ng);
             FissionRec f;
             f.x = p.x;
             f.y = p.y;
@@ -233,9 +233,18 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           // reflective boundary (extension): stop on the plane, mirror the
           // normal component, stay in the cell
           const int kind = __ldg(w.surf_kind + s);
-          if (kind == kPlaneX) p.u = -p.u;
-          else if (kind == kPlaneY) p.v = -p.v;
-          else p.w = -p.w;
+          if (kind == kPlaneX) {
+            p.u = -p.u;
+            fu = -fu;
+          }
+          else if (kind == kPlaneY) {
+            p.v = -p.v;
+            fv = -fv;
+          }
+          else {
+            p.w = -p.w;
+            fw = -fw;
+          }
           p.event = kReflect;
           p.surf = s;
           p.skip = s;
@@ -283,6 +292,9 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           p.u = st.u;
           p.v = st.v;
           p.w = st.w;
+          fu = __double2float_rn(p.u);
+          fv = __double2float_rn(p.v);
+          fw = __double2float_rn(p.w);
           p.g = static_cast<int>(st.energy) - 1;
           p.type = 0;  // BankSecondaries creates neutrons
           if constexpr (std::is_same_v<Rng, PhiloxRng>) p.rng.init(rp.run_key, st.key, 1);

@@ -296,10 +296,44 @@ __device__ __forceinline__ void alpha_bounds(double sqrt_E, double E, double b, 
   a_max = sdiv<FAST>(dmul(hi, hi), akT);
 }
 
-// ThermalScattering::SampleAlpha
+// ThermalScattering::SampleAlpha (src/ThermalScattering.cpp:340-463), in
+// three steps so that a batched sampler can replace the CDF search between
+// them: alpha_begin (beta grid choice, kinematic bounds, partition), the
+// find_cdf of the two bounds, alpha_end (the resampling loop)
+template <bool FAST>
+struct AlphaCtx {
+  double b, E, T;
+  double sqrt_E, akT;
+  double b_s, b_s_a_min, b_s_a_max;
+  int b_s_i, nF;
+  const double* Fs;
+  PodEval<FAST> ev;
+};
+
+// everything of SampleAlpha that follows from the chosen beta grid point
+// b_s_i (no random draw), so a sampler may rebuild it after other work
+template <bool FAST>
+__device__ __forceinline__ void alpha_setup(const DevTSL& t, double b, double E, double T, int b_s_i,
+                                            AlphaCtx<FAST>& x) {
+  const DevPOD& P = t.alpha;
+  const int sgn_b = (0 < b) - (b < 0);
+  x.b = b;
+  x.E = E;
+  x.T = T;
+  x.b_s_i = b_s_i;
+  x.b_s = static_cast<double>(sgn_b) * __ldg(P.grid + b_s_i);
+  x.sqrt_E = ssqrt<FAST>(E);
+  x.akT = dmul(dmul(t.awr, kBoltzmann), T);
+  alpha_bounds<FAST>(x.sqrt_E, E, x.b_s, T, x.akT, x.b_s_a_min, x.b_s_a_max);
+  int local;
+  const int ps = pod_partition(P, b_s_i, local);
+  x.ev.init(P, ps, local, T);
+  x.nF = x.ev.c.nF;
+  x.Fs = x.ev.c.F;
+}
+
 template <bool FAST, class Rng>
-__device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, double b, double E, double T,
-                                                 double& alpha) {
+__device__ __forceinline__ bool alpha_begin(const DevTSL& t, Rng& rng, double b, double E, double T, AlphaCtx<FAST>& x) {
   const DevPOD& P = t.alpha;
   const double abs_b = fabs(b);
   const int sgn_b = (0 < b) - (b < 0);
@@ -321,71 +355,155 @@ __device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, doub
   }
   const int b_s_i = r <= su01<FAST>(rng) ? b_hi_i - 1 : b_hi_i;
   if (b_s_i < 0) return false;  // snapped below the first beta: betas.at() throws in the reference
-  const double b_s = static_cast<double>(sgn_b) * __ldg(P.grid + b_s_i);
-  const double sqrt_E = ssqrt<FAST>(E);
-  const double akT = dmul(dmul(t.awr, kBoltzmann), T);
-  double b_s_a_min, b_s_a_max;
-  alpha_bounds<FAST>(sqrt_E, E, b_s, T, akT, b_s_a_min, b_s_a_max);
-  int local;
-  const int ps = pod_partition(P, b_s_i, local);
-  PodEval<FAST> ev;
-  ev.init(P, ps, local, T);
-  const int nF = ev.c.nF;
-  const double* Fs = ev.c.F;
-  // find_cdf: std::upper_bound over CDF indices with a < Evaluate(i)
-  auto find_cdf = [&](double a) {
-    int first = 0, len = nF;
-    // the fast form compares in FP32 (its reconstructions are FP32 values)
-    const float af = __double2float_rn(a);
-    while (len > 0) {
-      const int half = len >> 1, mid = first + half;
-      bool below;
-      if constexpr (FAST) below = af < ev.f32(mid);
-      else below = a < ev(mid);
-      if (below) {
-        len = half;
-      }
-      else {
-        first = mid + 1;
-        len -= half + 1;
-      }
+  alpha_setup<FAST>(t, b, E, T, b_s_i, x);
+  return true;
+}
+
+// find_cdf's search: std::upper_bound over CDF indices with a < Evaluate(i)
+// (the fast form compares in FP32: its reconstructions are FP32 values)
+template <bool FAST>
+__device__ __forceinline__ bool cdf_pred(const AlphaCtx<FAST>& x, double a, float af, int i) {
+  if constexpr (FAST) return af < x.ev.f32(i);
+  else return a < x.ev(i);
+}
+
+template <bool FAST>
+__device__ __forceinline__ int cdf_upper_bisect(const AlphaCtx<FAST>& x, double a) {
+  int first = 0, len = x.nF;
+  const float af = __double2float_rn(a);
+  while (len > 0) {
+    const int half = len >> 1, mid = first + half;
+    if (cdf_pred(x, a, af, mid)) {
+      len = half;
     }
-    const int F_a_hi_i = first;
-    const double F_a_lo = F_a_hi_i != 0 ? __ldg(Fs + F_a_hi_i - 1) : 0.0;
-    const double F_a_hi = F_a_hi_i != nF ? __ldg(Fs + F_a_hi_i) : 1.0;
-    const double a_lo = F_a_hi_i != 0 ? ev(F_a_hi_i - 1) : 0.0;
-    const double a_hi = F_a_hi_i != nF ? ev(F_a_hi_i) : t.alpha_cutoff;
-    return dadd(F_a_lo, sdiv<FAST>(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
-  };
-  const double F_min = find_cdf(b_s_a_min);
-  const double F_max = find_cdf(b_s_a_max);
+    else {
+      first = mid + 1;
+      len -= half + 1;
+    }
+  }
+  return first;
+}
+
+// The same index from a starting guess i0 (a learned prediction): probe
+// i0 and its neighbour, walk away from them with doubling steps until the
+// answer is bracketed, then bisect the bracket.  For a non-decreasing
+// sequence of reconstructions (the POD pipeline removes CDFs that are not)
+// this is exactly upper_bound's answer, with 2 evaluations when the guess
+// is right instead of log2(nF).
+template <bool FAST>
+__device__ __forceinline__ int cdf_upper_guided(const AlphaCtx<FAST>& x, double a, int i0) {
+  const int nF = x.nF;
+  const float af = __double2float_rn(a);
+  int lo, hi;  // answer in [lo, hi]: pred false below lo, pred(hi) true or hi == nF
+  const int g = i0 < 0 ? 0 : (i0 > nF ? nF : i0);
+  if (g < nF && !cdf_pred(x, a, af, g)) {
+    lo = g + 1;
+    hi = nF;
+    for (int step = 1; lo < nF;) {
+      const int j = g + step < nF ? g + step : nF - 1;
+      if (cdf_pred(x, a, af, j)) {
+        hi = j;
+        break;
+      }
+      lo = j + 1;
+      if (j == nF - 1) break;
+      step <<= 1;
+    }
+  }
+  else {
+    hi = g;
+    lo = 0;
+    for (int step = 1; hi > 0;) {
+      const int j = g - step > 0 ? g - step : 0;
+      if (!cdf_pred(x, a, af, j)) {
+        lo = j + 1;
+        break;
+      }
+      hi = j;
+      if (j == 0) break;
+      step <<= 1;
+    }
+  }
+  // bisect [lo, hi): hi is known to satisfy the predicate (or be nF)
+  int first = lo, len = hi - lo;
+  while (len > 0) {
+    const int half = len >> 1, mid = first + half;
+    if (cdf_pred(x, a, af, mid)) {
+      len = half;
+    }
+    else {
+      first = mid + 1;
+      len -= half + 1;
+    }
+  }
+  return first;
+}
+
+// the CDF value of `a` from its bracket (assuming a histogram PDF)
+template <bool FAST>
+__device__ __forceinline__ double cdf_at(const DevTSL& t, const AlphaCtx<FAST>& x, double a, int F_a_hi_i) {
+  const int nF = x.nF;
+  const double F_a_lo = F_a_hi_i != 0 ? __ldg(x.Fs + F_a_hi_i - 1) : 0.0;
+  const double F_a_hi = F_a_hi_i != nF ? __ldg(x.Fs + F_a_hi_i) : 1.0;
+  const double a_lo = F_a_hi_i != 0 ? x.ev(F_a_hi_i - 1) : 0.0;
+  const double a_hi = F_a_hi_i != nF ? x.ev(F_a_hi_i) : t.alpha_cutoff;
+  return dadd(F_a_lo, sdiv<FAST>(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
+}
+
+// the fractional index position of `a` in [0, 1]: (upper index + where a
+// falls in its bracket) / (nF + 1) -- what the guide network learns
+template <bool FAST>
+__device__ __forceinline__ float cdf_position(const DevTSL& t, const AlphaCtx<FAST>& x, double a, int F_a_hi_i) {
+  const int nF = x.nF;
+  const double a_lo = F_a_hi_i != 0 ? x.ev(F_a_hi_i - 1) : 0.0;
+  const double a_hi = F_a_hi_i != nF ? x.ev(F_a_hi_i) : t.alpha_cutoff;
+  float th = static_cast<float>((a - a_lo) / (a_hi - a_lo));
+  th = th == th ? fminf(0.999f, fmaxf(0.0f, th)) : 0.5f;
+  return (static_cast<float>(F_a_hi_i) + th) / static_cast<float>(nF + 1);
+}
+
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool alpha_end(const DevTSL& t, Rng& rng, const AlphaCtx<FAST>& x, double F_min,
+                                          double F_max, double& alpha) {
+  const int nF = x.nF;
+  const double* Fs = x.Fs;
   for (int res = 0; res < kTslResampleLimit; res++) {
     const double F = dadd(F_min, dmul(su01<FAST>(rng), dsub(F_max, F_min)));
     const int F_hi_i = upper_index(Fs, nF, F);
     const double F_lo = F_hi_i != 0 ? __ldg(Fs + F_hi_i - 1) : 0.0;
     const double F_hi = F_hi_i != nF ? __ldg(Fs + F_hi_i) : 1.0;
-    const double a_lo = F_hi_i != 0 ? ev(F_hi_i - 1) : 0.0;
-    const double a_hi = F_hi_i != nF ? ev(F_hi_i) : t.alpha_cutoff;
+    const double a_lo = F_hi_i != 0 ? x.ev(F_hi_i - 1) : 0.0;
+    const double a_hi = F_hi_i != nF ? x.ev(F_hi_i) : t.alpha_cutoff;
     const double a_prime = dadd(a_lo, dmul(sdiv<FAST>(dsub(F, F_lo), dsub(F_hi, F_lo)), dsub(a_hi, a_lo)));
-    if (b_s_a_min < a_prime && a_prime < b_s_a_max) {
+    if (x.b_s_a_min < a_prime && a_prime < x.b_s_a_max) {
       double b_a_min, b_a_max;
-      alpha_bounds<FAST>(sqrt_E, E, b, T, akT, b_a_min, b_a_max);
-      alpha = dadd(b_a_min,
-                   sdiv<FAST>(dmul(dsub(a_prime, b_s_a_min), dsub(b_a_max, b_a_min)), dsub(b_s_a_max, b_s_a_min)));
+      alpha_bounds<FAST>(x.sqrt_E, x.E, x.b, x.T, x.akT, b_a_min, b_a_max);
+      alpha = dadd(b_a_min, sdiv<FAST>(dmul(dsub(a_prime, x.b_s_a_min), dsub(b_a_max, b_a_min)),
+                                       dsub(x.b_s_a_max, x.b_s_a_min)));
       return true;
     }
   }
   return false;
 }
 
+// ThermalScattering::SampleAlpha
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_sample_alpha(const DevTSL& t, Rng& rng, double b, double E, double T,
+                                                 double& alpha) {
+  AlphaCtx<FAST> x;
+  if (!alpha_begin<FAST>(t, rng, b, E, T, x)) return false;
+  const double F_min = cdf_at<FAST>(t, x, x.b_s_a_min, cdf_upper_bisect<FAST>(x, x.b_s_a_min));
+  const double F_max = cdf_at<FAST>(t, x, x.b_s_a_max, cdf_upper_bisect<FAST>(x, x.b_s_a_max));
+  return alpha_end<FAST>(t, rng, x, F_min, F_max, alpha);
+}
+
 // ThermalScattering::Scatter: beta, alpha -> E', mu; Particle::Scatter
 // rotates the direction by mu with a fresh azimuth
+// Scatter's kinematics for a sampled (beta, alpha): E' = E + beta kT and the
+// cosine, then Particle::Scatter's rotation with a fresh azimuth
 template <bool FAST, class Rng>
-__device__ __forceinline__ bool tsl_scatter_body(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
-                                            double& dw) {
-  double beta, alpha;
-  if (!tsl_sample_beta<FAST>(t, rng, E, T, beta)) return false;
-  if (!tsl_sample_alpha<FAST>(t, rng, beta, E, T, alpha)) return false;
+__device__ __forceinline__ void tsl_apply(const DevTSL& t, Rng& rng, double T, double beta, double alpha, double& E,
+                                          double& du, double& dv, double& dw) {
   const double E_p = dadd(E, dmul(dmul(beta, kBoltzmann), T));
   if constexpr (FAST && std::is_same_v<Rng, PhiloxRng>) {
     // E' and mu from the sampled pair, the direction in FP32
@@ -406,6 +524,15 @@ __device__ __forceinline__ bool tsl_scatter_body(const DevTSL& t, Rng& rng, doub
     rotate(du, dv, dw, mu, phi);
   }
   E = E_p;
+}
+
+template <bool FAST, class Rng>
+__device__ __forceinline__ bool tsl_scatter_body(const DevTSL& t, Rng& rng, double T, double& E, double& du, double& dv,
+                                            double& dw) {
+  double beta, alpha;
+  if (!tsl_sample_beta<FAST>(t, rng, E, T, beta)) return false;
+  if (!tsl_sample_alpha<FAST>(t, rng, beta, E, T, alpha)) return false;
+  tsl_apply<FAST>(t, rng, T, beta, alpha, E, du, dv, dw);
   return true;
 }
 

@@ -32,8 +32,10 @@ ERRORS = {
 }
 RNG_PHILOX, RNG_MINSTD = 0, 1
 SCHEDULE_AUTO, SCHEDULE_HISTORY, SCHEDULE_EVENT = 0, 1, 2
-TSL_POD, TSL_MLP = 0, 1
-THERMAL_POD, THERMAL_SURROGATE = 0, 1  # run option `thermal` (MC_THERMAL_*)
+TSL_POD, TSL_MLP, TSL_GUIDED = 0, 1, 2
+# run option `thermal` (MC_THERMAL_*): inline POD, quantile surrogate on the
+# thermal-scatter queue, guided POD-exact sampler on the queue, plain POD on it
+THERMAL_POD, THERMAL_SURROGATE, THERMAL_GUIDED, THERMAL_POD_QUEUE = 0, 1, 2, 3
 BANK_AUTO, BANK_SLOTS, BANK_DIRECT = 0, 1, 2  # run option `bank_path` (MC_BANK_*)
 TSL_PHILOX, TSL_FAST = 0x10, 0x20  # method flags: Philox streams, FP32 POD form
 GEOMETRY_ROBUST, GEOMETRY_REFERENCE = 0, 1
@@ -182,6 +184,7 @@ _SIGNATURES = {
     "mc_batch_run": (C.c_int, [_P, C.POINTER(BatchOpts), C.POINTER(BatchOut)]),
     "mc_batch_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
     "mc_train_surrogate": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), C.POINTER(TrainOut)]),
+    "mc_train_surrogate_guide": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), C.POINTER(TrainOut)]),
     "mc_surrogate_get": (C.c_int, [_P, _F, _F, C.POINTER(TrainDesc)]),
     "mc_surrogate_set": (C.c_int, [_P, C.c_int32, C.POINTER(TrainDesc), _F, _F]),
     "mc_surrogate_grad": (C.c_int, [_P, _F, _F, _F, C.c_uint64, _F, _F, _F]),
@@ -560,6 +563,18 @@ class Context:
                       steps=steps, lr=lr, seed=seed)
         out = TrainOut()
         self.check(self.lib.mc_train_surrogate(self.h, tsl, C.byref(d), C.byref(out)))
+        return out
+
+    def train_surrogate_guide(self, tsl: int = 0, E_range=(1e-9, 3e-6), T_range=(283.6, 623.6),
+                              conditions: int = 0, samples_per_condition: int = 0, batch: int = 0, steps: int = 0,
+                              lr: float = 0.0, seed: int = 1) -> TrainOut:
+        """Trains the guide network of the guided (POD-exact) thermal
+        sampler of library `tsl` (mc_train_surrogate_guide)."""
+        d = TrainDesc(E_min=E_range[0], E_max=E_range[1], T_min=T_range[0], T_max=T_range[1],
+                      conditions=conditions, samples_per_condition=samples_per_condition, batch=batch,
+                      steps=steps, lr=lr, seed=seed)
+        out = TrainOut()
+        self.check(self.lib.mc_train_surrogate_guide(self.h, tsl, C.byref(d), C.byref(out)))
         return out
 
     def surrogate_params(self):

@@ -251,3 +251,47 @@ def broomstick_xml(tsl: dict, nuc: dict, histories: int = 100_000, energy: float
             "  </fixedsource>\n</problemtype>\n"
             f'<temperature>\n  <constant c="{temperature!r}"/>\n</temperature>\n'
             f"<estimators>\n{est}\n</estimators>\n</minimc>\n")
+
+
+def continuous_temperature_slab_xml(tsl: dict, nuc: dict, histories: int = 100_000, energy: float = 0.56 * EV,
+                                    thickness: float = 4.33, t_lower: float = 300.0, t_upper: float = 600.0,
+                                    energy_bins: int = 60, aden: float = 0.066854, name: str = "Hmod",
+                                    seed: int = 1) -> str:
+    """The shape of the reference's continuous-temperature benchmark: a
+    slab of the bound moderator between planex -1e-6 and `thickness` cm,
+    cell delta tracking (the thermal library's majorant bounds the flights),
+    a linear temperature field rising from t_lower at x = 0 to t_upper at the
+    far face, a monoenergetic pencil beam along +x from the origin, and the
+    current through the far face binned in energy (log-spaced boundaries)."""
+    sc = (f'        <scatter>\n          <xs file="{nuc["elastic"]}" temperature="293.6"/>\n'
+          + tsl_xml(tsl, indent="          ") + "\n        </scatter>")
+    nucxml = (f'    <nuclide name="{name}" awr="{nuc["awr"]!r}">\n      <neutron>\n'
+              f'        <total file="{nuc["total"]}" temperature="293.6"/>\n'
+              f'        <capture file="{nuc["capture"]}" temperature="293.6"/>\n{sc}\n      </neutron>\n    </nuclide>')
+    edges = " ".join(repr(float(x)) for x in np.geomspace(1e-11, 2.5e-6, energy_bins + 1))
+    gradient = (t_upper - t_lower) / thickness
+    return ("<minimc>\n<general>\n  <particles>neutron</particles>\n"
+            f"  <histories>{histories}</histories>\n  <threads>1</threads>\n  <chunksize>1000</chunksize>\n"
+            f"  <seed>{seed}</seed>\n  <tracking>cell delta</tracking>\n</general>\n"
+            "<nuclides>\n  <continuous>\n" + nucxml + "\n  </continuous>\n</nuclides>\n"
+            f'<materials>\n  <material name="mod" aden="{aden!r}">\n    <nuclide name="{name}" afrac="1.0"/>\n'
+            "  </material>\n</materials>\n"
+            f'<surfaces>\n  <planex name="near" x="-1e-06"/>\n  <planex name="far" x="{thickness!r}"/>\n</surfaces>\n'
+            "<cells>\n"
+            '  <void>\n    <surface name="near" sense="-1"/>\n  </void>\n'
+            '  <cell name="slab" material="mod">\n    <surface name="near" sense="+1"/>\n'
+            '    <surface name="far" sense="-1"/>\n  </cell>\n'
+            '  <void>\n    <surface name="far" sense="+1"/>\n  </void>\n'
+            "</cells>\n"
+            "<problemtype>\n  <fixedsource>\n"
+            '    <position>\n      <constant x="0" y="0" z="0"/>\n    </position>\n'
+            '    <direction>\n      <constant x="1" y="0" z="0"/>\n    </direction>\n'
+            f'    <energy>\n      <constant energy="{energy!r}"/>\n    </energy>\n'
+            '    <particletype>\n      <constant type="neutron"/>\n    </particletype>\n'
+            "  </fixedsource>\n</problemtype>\n"
+            f'<temperature>\n  <linear>\n    <bounds lower="{t_lower!r}" upper="{t_upper!r}"/>\n'
+            f'    <intercept b="{t_lower!r}"/>\n    <gradient x="{gradient!r}" y="0" z="0"/>\n  </linear>\n'
+            "</temperature>\n"
+            f'<estimators>\n  <current name="leakage" surface="far">\n    <bins>\n      <energy>\n'
+            f"        <boundaries>{edges}</boundaries>\n      </energy>\n    </bins>\n  </current>\n"
+            "</estimators>\n</minimc>\n")

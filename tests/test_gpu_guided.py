@@ -1,0 +1,136 @@
+"""The guided thermal sampler, through the C ABI.
+
+The guide network (trained on the device from the FP32 POD sampler's own
+CDF searches) predicts where ThermalScattering::SampleAlpha's find_cdf
+bisection ends for each kinematic bound; the POD reconstructions confirm the
+guess or walk from it.  So, for the same random numbers:
+
+* at the sampler level (C4's incident energies 0.01, 0.1 and 1 eV, T uniform
+  in 283.6-623.6 K per sample) the guided sampler returns exactly the FP32
+  POD sampler's (beta, alpha), sample for sample;
+* in transport (the thermal-scatter queue), the broomstick's histories are
+  the ones the inline FP32 POD sampler gives: the same events and fate for
+  every history and the same leakage tallies -- and the same again for the
+  plain POD queue without the network;
+* with independent seeds, at 1e6 histories per energy, the leakage energy
+  and cosine spectra of the guided form pass a two-sample chi-square test
+  against the POD form (p > 0.01), the gate the surrogate is held to.
+"""
+import numpy as np
+import pytest
+from scipy import stats
+
+from minimc_gb300 import (RNG_PHILOX, THERMAL_GUIDED, THERMAL_POD, THERMAL_POD_QUEUE, TSL_FAST, TSL_GUIDED,
+                          TSL_PHILOX, TSL_POD, Context, synth_tsl)
+
+pytestmark = pytest.mark.gpu
+EV = 1e-6
+ENERGIES = [0.01 * EV, 0.1 * EV, 1.0 * EV]
+P_MIN = 0.01  # chi-square gate on the leakage spectra
+SUM_RTOL = 1e-12  # tallies of identical histories: summation order only
+
+
+@pytest.fixture(scope="module")
+def library(tmp_path_factory):
+    d = tmp_path_factory.mktemp("tsl_guided")
+    return d, synth_tsl.write_tsl(d), synth_tsl.moderator_nuclide(d)
+
+
+def guided_ctx(library, energy=1.0 * EV, histories=10):
+    d, tsl, nuc = library
+    ctx = Context(0)
+    ctx.load_xml(synth_tsl.broomstick_xml(tsl, nuc, histories=histories, energy=energy, temperature=450.0), d)
+    out = ctx.train_surrogate_guide(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
+                                    samples_per_condition=512, batch=16384, steps=10000, lr=1e-3, seed=3)
+    return ctx, out
+
+
+@pytest.fixture(scope="module")
+def ctx1(library):
+    return guided_ctx(library)
+
+
+def test_guide_training(ctx1):
+    """The guide learns where the CDF search ends to about a grid cell:
+    (nF + 1) = 161 cells span [0, 1]; an RMS error of two cells leaves the
+    walk from the guess far shorter than the bisection's 8 probes."""
+    _, out = ctx1
+    assert out.failures == 0
+    assert out.samples == 2 * 4096 * 512
+    assert np.sqrt(out.loss_alpha) < 2.0 / 161, out.loss_alpha
+
+
+@pytest.mark.parametrize("E", ENERGIES)
+def test_guided_samples_are_the_pod_samples(ctx1, E):
+    ctx, _ = ctx1
+    n = 300_000
+    T = np.random.default_rng(8).uniform(283.6, 623.6, n)
+    gb, ga, gf = ctx.sample_tsl(0, np.full(n, E), T, seed=21, method=TSL_GUIDED)
+    pb, pa, pf = ctx.sample_tsl(0, np.full(n, E), T, seed=21, method=TSL_POD | TSL_PHILOX | TSL_FAST)
+    assert gf == pf
+    assert np.array_equal(gb, pb, equal_nan=True)
+    assert np.array_equal(ga, pa, equal_nan=True)
+
+
+def test_guided_samples_outside_the_trained_box(ctx1):
+    """Outside the guide's (E, T) box the guesses are poorer, the samples
+    are still the POD sampler's."""
+    ctx, _ = ctx1
+    n = 100_000
+    E = np.full(n, 3.5e-6)
+    T = np.full(n, 700.0)
+    gb, ga, _ = ctx.sample_tsl(0, E, T, seed=4, method=TSL_GUIDED)
+    pb, pa, _ = ctx.sample_tsl(0, E, T, seed=4, method=TSL_POD | TSL_PHILOX | TSL_FAST)
+    assert np.array_equal(gb, pb, equal_nan=True) and np.array_equal(ga, pa, equal_nan=True)
+
+
+def test_guided_transport_is_pod_transport(ctx1):
+    """Same seed: every history of the broomstick has the same events and
+    fate with the inline FP32 POD sampler, the guided queue and the plain
+    POD queue; the tallies agree to summation order."""
+    ctx, _ = ctx1
+    n = 200_000
+    kw = dict(rng=RNG_PHILOX, fast_math=1, histories=n, seed=5, per_history=True)
+    pod = ctx.run_fixed_source(thermal=THERMAL_POD, **kw)
+    gui = ctx.run_fixed_source(thermal=THERMAL_GUIDED, **kw)
+    que = ctx.run_fixed_source(thermal=THERMAL_POD_QUEUE, **kw)
+    for r in (gui, que):
+        assert r.raw.lost == pod.raw.lost and r.raw.resample_failures == pod.raw.resample_failures
+        assert np.array_equal(r.history_events, pod.history_events)
+        assert np.array_equal(r.history_fate, pod.history_fate)
+        np.testing.assert_allclose(r.sum, pod.sum, rtol=SUM_RTOL, atol=0)
+        np.testing.assert_allclose(r.sum_sq, pod.sum_sq, rtol=SUM_RTOL, atol=0)
+    # the queue served the scatters (sampler and resume launches)
+    assert gui.raw.launches > pod.raw.launches
+
+
+def spectra(ctx, r):
+    """Leakage energy and cosine marginals (counts) of the broomstick tally."""
+    e = ctx.estimators()[0]
+    t = r.sum[e.offset:e.offset + e.n_bins].reshape(int(e.cosine_bins), int(e.energy_bins))
+    return t.sum(0), t.sum(1)
+
+
+def chi2_two_sample(a, b):
+    """Two-sample chi-square of two histograms (bins with >= 10 counts in
+    total; the samples' sizes may differ)."""
+    keep = (a + b) >= 10
+    a, b = a[keep], b[keep]
+    ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    chi2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
+    dof = int(keep.sum()) - 1
+    return chi2, dof, float(stats.chi2.sf(chi2, dof))
+
+
+@pytest.mark.parametrize("E", ENERGIES)
+def test_guided_spectra_pass_chi2_against_pod(library, E):
+    """Independent seeds, 1e6 histories each: the guided form's leakage
+    energy and cosine spectra against the inline POD form's."""
+    ctx, _ = guided_ctx(library, energy=E)
+    n = 1_000_000
+    pod = ctx.run_fixed_source(rng=RNG_PHILOX, fast_math=1, histories=n, seed=101, thermal=THERMAL_POD)
+    gui = ctx.run_fixed_source(rng=RNG_PHILOX, fast_math=1, histories=n, seed=202, thermal=THERMAL_GUIDED)
+    assert gui.raw.lost == 0 and gui.raw.resample_failures == pod.raw.resample_failures == 0
+    for name, a, b in zip(("energy", "cosine"), spectra(ctx, gui), spectra(ctx, pod)):
+        chi2, dof, p = chi2_two_sample(a, b)
+        assert p > P_MIN, (E, name, chi2, dof, p)

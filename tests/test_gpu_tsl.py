@@ -111,6 +111,46 @@ def test_broomstick_philox_fast_chi2(lib, built_library):
     assert p > 1e-3, p
 
 
+def test_continuous_temperature_delta_tracking(lib, built_library):
+    """The reference's continuous-temperature benchmark shape (oracle pinned
+    on the reference by tests/test_reference_cpu.py): cell delta tracking
+    with the thermal library's majorant (ThermalScattering::GetMajorant,
+    src/ThermalScattering.cpp:106-109), real/virtual rejection at the local
+    temperature of a linear 300-600 K field, POD thermal scattering.  With
+    reference streams the GPU's histories are the oracle's: the same events
+    and fate for at least 99.9 % of histories (the last bits of the CUDA and
+    C library erf/exp in the majorant and total may move a rejection), the
+    same leakage within 0.2 %."""
+    d, tsl, nuc = lib
+    n = 20_000
+    xml = synth_tsl.continuous_temperature_slab_xml(tsl, nuc, histories=n, thickness=1.0)
+    g = Context(0)
+    g.load_xml(xml, d)
+    r = g.run_fixed_source(rng=RNG_MINSTD, per_history=True, histories=n)
+    ro = Oracle(xml, d).run_fixed_source(n, 1, threads=8, per_history=True)
+    assert r.raw.lost == 0 and r.raw.resample_failures == ro["resample"]
+    assert r.raw.events > 3 * n  # virtual and real collisions, crossings
+    agree = np.mean((r.history_events == ro["history_events"]) & (r.history_fate == ro["history_fate"]))
+    assert agree > 0.999, agree
+    assert abs(r.sum.sum() - ro["sum"].sum()) <= 0.002 * n
+
+
+def test_continuous_temperature_philox_chi2(lib, built_library):
+    """The same problem with Philox streams and the FP32 forms (the
+    engine's fast path) against the oracle: leakage spectrum chi-square."""
+    d, tsl, nuc = lib
+    n = 200_000
+    xml = synth_tsl.continuous_temperature_slab_xml(tsl, nuc, histories=n, thickness=1.0, energy_bins=40)
+    g = Context(0)
+    g.load_xml(xml, d)
+    r = g.run_fixed_source(rng=RNG_PHILOX, fast_math=1, histories=n)
+    ro = Oracle(xml, d).run_fixed_source(n, 1, threads=8)
+    a, b = r.sum, ro["sum"]
+    keep = (a + b) >= 20
+    p = stats.chi2_contingency(np.vstack([a[keep], b[keep]]))[1]
+    assert p > 1e-3, p
+
+
 def test_pod_pipeline_library(lib, tmp_path, built_library):
     """A library built by the POD pipeline (adaptive ranks at a 1e-4
     relative Frobenius tolerance, decomposed on the GPU, non-monotone CDFs

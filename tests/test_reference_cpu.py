@@ -129,6 +129,23 @@ def test_thermal_scattering_broomstick(ref, tmp_path_factory, tmp_path):
     assert np.array_equal(got, want)
 
 
+def test_continuous_temperature_delta_tracking_thermal(ref, tmp_path_factory, tmp_path):
+    """The reference's continuous-temperature benchmark shape: cell delta
+    tracking through a slab of the bound moderator whose flights are bounded
+    by the thermal library's majorant (ThermalScattering::GetMajorant,
+    src/ThermalScattering.cpp:106-109; CellDeltaTracking::Transport,
+    src/TransportMethod.cpp:88-122), a linear temperature field 300-600 K,
+    POD SampleBeta/SampleAlpha at every real thermal collision: the oracle's
+    leakage means equal the reference's bit for bit."""
+    d = tmp_path_factory.mktemp("tsl_ct")
+    tsl = synth_tsl.write_tsl(d)
+    nuc = synth_tsl.moderator_nuclide(d)
+    xml = synth_tsl.continuous_temperature_slab_xml(tsl, nuc, histories=1500, thickness=1.0)
+    got, want, r = run_both(ref, xml, d, tmp_path, "leakage")
+    assert r["events"] > 3 * 1500  # real and virtual collisions happen
+    assert np.array_equal(got, want)
+
+
 def test_result_file_text(ref, ce_files, tmp_path, built_library):
     """The engine's result-file text (mc_output_format, the formatter behind
     Driver.write_output) for the oracle's tallies equals the reference's own
