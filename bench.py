@@ -495,7 +495,8 @@ def run_gpu_tsl(args) -> None:
         ctx.train_surrogate_guide(0, **GUIDE_TRAIN)
         ctx.train_surrogate(0, E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=4096,
                             samples_per_condition=512, batch=8192, steps=3000, seed=3)
-        for method in (TSL_POD | TSL_PHILOX | TSL_FAST, TSL_GUIDED, TSL_MLP):
+        for method in (TSL_POD | TSL_PHILOX | TSL_FAST, TSL_GUIDED | TSL_FAST, TSL_POD | TSL_PHILOX, TSL_GUIDED,
+                       TSL_MLP):
             for i in range(args.steps):
                 ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=1 + i,
                                       method=method)
@@ -525,8 +526,9 @@ def run_gpu_tsl(args) -> None:
     b = torch.empty(n, dtype=torch.float64, device="cuda")
     a = torch.empty_like(b)
     rates, samples = {}, {}
-    for name, method in (("pod_exact", TSL_POD | TSL_PHILOX), ("pod_fp32", TSL_POD | TSL_PHILOX | TSL_FAST),
-                         ("guided", TSL_GUIDED), ("mlp_quantile", TSL_MLP)):
+    for name, method in (("pod_exact", TSL_POD | TSL_PHILOX), ("guided_exact", TSL_GUIDED),
+                         ("pod_fp32", TSL_POD | TSL_PHILOX | TSL_FAST), ("guided_fp32", TSL_GUIDED | TSL_FAST),
+                         ("mlp_quantile", TSL_MLP)):
         for _ in range(2):
             ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=11, method=method)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -544,8 +546,9 @@ def run_gpu_tsl(args) -> None:
     ks = {k: {"beta": float(stats.ks_2samp(samples[k][0][:200_000], samples["pod_exact"][0][:200_000]).statistic),
               "alpha": float(stats.ks_2samp(samples[k][1][:200_000], samples["pod_exact"][1][:200_000]).statistic)}
           for k in ("pod_fp32", "mlp_quantile")}
-    same = bool(np.array_equal(samples["guided"][0], samples["pod_fp32"][0], equal_nan=True) and
-                np.array_equal(samples["guided"][1], samples["pod_fp32"][1], equal_nan=True))
+    same = {form: bool(np.array_equal(samples[f"guided_{form}"][0], samples[f"pod_{form}"][0], equal_nan=True) and
+                       np.array_equal(samples[f"guided_{form}"][1], samples[f"pod_{form}"][1], equal_nan=True))
+            for form in ("exact", "fp32")}
     flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two network rows per sample, multiply-adds x 2
     bf16_peak = None
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -571,11 +574,13 @@ def run_gpu_tsl(args) -> None:
                        "form": "guided (surrogate-started CDF searches, POD-exact samples)",
                        "l2": "inputs generated on device; tallies 0.65 MB"},
             "thermal_forms": forms,
-            "sampler": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "guided_equals_pod_fp32": same,
+            "sampler": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "guided_equals_pod": same,
+                        "guided_exact_vs_pod_exact": rates["guided_exact"] / rates["pod_exact"],
+                        "guided_fp32_vs_pod_fp32": rates["guided_fp32"] / rates["pod_fp32"],
                         "quantile_train": {"loss_beta": tr.loss_beta, "loss_alpha": tr.loss_alpha,
                                            "samples": tr.samples, "data_ms": tr.data_ms, "train_ms": tr.train_ms},
                         "mlp_quantile_tflops": rates["mlp_quantile"] * flops / 1e12,
-                        "guided_tflops": rates["guided"] * flops / 1e12, "bf16_peak_tflops": bf16_peak,
+                        "guided_tflops": rates["guided_fp32"] * flops / 1e12, "bf16_peak_tflops": bf16_peak,
                         "sample_n": n},
             "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
                          "traffic": None, "peak_kind": peak_kind, "kernel": "k_history_ce",

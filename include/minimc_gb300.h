@@ -326,9 +326,11 @@ int mc_energy_index(mc_ctx* ctx, int32_t nuclide, const double* energy, uint64_t
 /* ---- thermal scattering (ThermalScattering.cpp) --------------------------- */
 #define MC_TSL_POD 0      /* POD reconstruction, SampleBeta/SampleAlpha     */
 #define MC_TSL_MLP 1      /* MLP surrogate (POD outside the trained box)    */
-#define MC_TSL_GUIDED 2   /* guided POD: the FP32 POD form's samples for the
-                             same Philox streams, CDF searches started where
-                             the guide network predicts (Philox only)      */
+#define MC_TSL_GUIDED 2   /* guided POD: the POD sampler's samples for the
+                             same Philox streams (the FP32 form with
+                             MC_TSL_FAST, else the exact FP64 form), CDF
+                             searches started where the guide network
+                             predicts (Philox streams always)              */
 #define MC_TSL_PHILOX 0x10 /* flag: Philox streams keyed by seed, counter i;
                               without it sample i draws from minstd seeded
                               seed + i, as the reference would            */

@@ -259,31 +259,44 @@ int build_pod(mc_ctx* c, const mc::PODPartitionSet& P, mcd::DevPOD& d) {
   // by more than four times the bound on the FP32 dot products' rounding
   // (r * 2^-24 * sum_o |cs gf| for each); a convex combination of two
   // such columns (the sampler's temperature interpolation) then rises too
+  // (bit 0); the same for the exact form, from the FP64 tables with the
+  // FP64 rounding bound (bit 1)
   std::vector<uint8_t> mono(P.concat.size(), 0);
   for (size_t p = 0; p < np; p++) {
     const size_t r = P.S[p].size(), nFp = P.F[p].size(), nTp = P.T[p].size();
     const size_t first = p == 0 ? 0 : P.ends[p - 1];
     const float* csp = cs.data() + cdf_off[p];
     const float* gfp = gf.data() + g_off[p];
+    const double* cdp = cdf.data() + cdf_off[p];
+    const double* Sp = S.data() + S_off[p];
+    const double* gdp = g.data() + g_off[p];
     for (size_t gi = 0; first + gi < P.ends[p]; gi++) {
-      bool ok = true;
-      for (size_t t = 0; t < nTp && ok; t++) {
+      bool ok32 = true, ok64 = true;
+      for (size_t t = 0; t < nTp && (ok32 || ok64); t++) {
         const float* v = gfp + (gi * nTp + t) * r;
-        double prev = 0, prev_err = 0;
-        for (size_t f = 0; f < nFp && ok; f++) {
-          double x = 0, a = 0;
+        const double* vd = gdp + (gi * nTp + t) * r;
+        double prev = 0, prev_err = 0, prevd = 0, prevd_err = 0;
+        for (size_t f = 0; f < nFp; f++) {
+          double x = 0, a = 0, xd = 0, ad = 0;
           for (size_t o = 0; o < r; o++) {
             const double term = static_cast<double>(csp[f * r + o]) * v[o];
             x += term;
             a += std::fabs(term);
+            const double td = Sp[o] * cdp[f * r + o] * vd[o];
+            xd += td;
+            ad += std::fabs(td);
           }
           const double err = static_cast<double>(r) * 0x1p-24 * a;
-          if (f > 0 && !(x - prev > 4.0 * (err + prev_err))) ok = false;
+          const double errd = static_cast<double>(r) * 0x1p-52 * ad;
+          if (f > 0 && !(x - prev > 4.0 * (err + prev_err))) ok32 = false;
+          if (f > 0 && !(xd - prevd > 4.0 * (errd + prevd_err))) ok64 = false;
           prev = x;
           prev_err = err;
+          prevd = xd;
+          prevd_err = errd;
         }
       }
-      mono[first + gi] = ok ? 1 : 0;
+      mono[first + gi] = static_cast<uint8_t>((ok32 ? 1 : 0) | (ok64 ? 2 : 0));
     }
   }
   if ((rc = upload(c, mono, &d.mono)) != MC_OK) return rc;
@@ -2084,13 +2097,14 @@ int sample_tsl_device(mc_ctx* c, int32_t tsl, const double* E, const double* T, 
   if (base == MC_TSL_MLP) return sample_tsl_mlp(c, tsl, E, T, n, seed, method, beta, alpha, failures);
   if (base == MC_TSL_GUIDED) {
     if (c->guide_tsl != tsl) return fail(c, MC_ERR_STATE, "the guide network is not trained for this library");
-    if (!c->tsl_fast_ok[static_cast<size_t>(tsl)])
-      return fail(c, MC_ERR_INPUT, "the guided sampler needs the FP32 POD form (ranks up to 32)");
+    const bool gfast = (method & MC_TSL_FAST) != 0;
+    if (gfast && !c->tsl_fast_ok[static_cast<size_t>(tsl)])
+      return fail(c, MC_ERR_INPUT, "the FP32 POD form supports ranks up to " + std::to_string(mcd::kFastPodRank));
     auto* d_fail = static_cast<unsigned long long*>(scratch(c, kTslFail, sizeof(unsigned long long)));
     if (!d_fail) return fail(c, MC_ERR_OOM, "sampler counters");
     CUDA_TRY(c, cudaMemsetAsync(d_fail, 0, sizeof(unsigned long long), c->stream));
     // the POD sampler's stream keys (Philox), so that the samples are its own
-    CUDA_TRY(c, mcd::launch_sample_tsl_guided(c->dw.tsl + tsl, c->guide, c->guide_box, E, T, n,
+    CUDA_TRY(c, mcd::launch_sample_tsl_guided(c->dw.tsl + tsl, c->guide, c->guide_box, gfast, E, T, n,
                                               run_key(seed, 0, 0x54534C00ull), beta, alpha, d_fail, c->num_sms,
                                               c->stream));
     c->launches++;

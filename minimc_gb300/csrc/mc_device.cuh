@@ -112,10 +112,11 @@ struct DevPOD {
   const uint32_t* g_off;      // [n_parts] into g ([grid][nT][rank])
   const double* g;
   const float* gf;            // g in FP32 (fast form), same offsets
-  // [n_grid] 1 where the FP32 reconstruction of the grid point's inverse CDF
-  // rises along F at every tabulated temperature by more than its rounding
-  // bound (so it rises at every temperature between them too): a search
-  // over it may start anywhere and still find upper_bound's answer
+  // [n_grid] bit 0 where the FP32 reconstruction of the grid point's inverse
+  // CDF rises along F at every tabulated temperature by more than its
+  // rounding bound (so it rises at every temperature between them too), bit
+  // 1 the same for the exact FP64 reconstruction: a search over it may
+  // start anywhere and still find upper_bound's answer
   const uint8_t* mono;
 };
 
@@ -316,6 +317,17 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k
   }
 }
 
+// One Philox block as an out-of-line function: a stream's refill is reached
+// from every draw site of the transport kernels, and inlining its 10 rounds
+// at each of them makes the kernels large enough to miss the instruction
+// cache; arguments and result stay in registers.
+static __device__ __noinline__ uint4 philox_block(uint32_t ctr, uint32_t h0, uint32_t h1, uint32_t tag, uint32_t k0,
+                                                  uint32_t k1) {
+  uint32_t c[4] = {ctr, h0, h1, tag};
+  philox4x32_10(c, k0, k1);
+  return make_uint4(c[0], c[1], c[2], c[3]);
+}
+
 // Counter-based stream of one particle: key = the run (seed, cycle), counter
 // = (block index, particle id lo, particle id hi, tag).  Primaries use
 // their history index as id and tag 0; secondaries use 64 bits drawn from
@@ -335,12 +347,11 @@ struct PhiloxRng {
     idx = 4;
   }
   __device__ __forceinline__ void refill() {
-    uint32_t c[4] = {ctr++, h0, h1, tag};
-    philox4x32_10(c, k0, k1);
-    buf[0] = c[0];
-    buf[1] = c[1];
-    buf[2] = c[2];
-    buf[3] = c[3];
+    const uint4 b = philox_block(ctr++, h0, h1, tag, k0, k1);
+    buf[0] = b.x;
+    buf[1] = b.y;
+    buf[2] = b.z;
+    buf[3] = b.w;
     idx = 0;
   }
   __device__ __forceinline__ uint32_t next() {

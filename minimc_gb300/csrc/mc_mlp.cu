@@ -1096,7 +1096,7 @@ struct GuideIO {
 // and the beta grid choice on the CUDA cores, the guide network for both
 // bounds on the tensor cores (one tcgen05 product per layer), then the
 // guided searches and SampleAlpha's resampling loop.
-template <bool QUEUE>
+template <bool QUEUE, bool FAST>
 __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView nv, MlpBox box, GuideIO io, int* err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   float* fw = reinterpret_cast<float*>(smem + kGOffF);
@@ -1160,10 +1160,10 @@ __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView
     double b = 0, a_min = 1.0, a_max = 1.0;
     float abs_bs = 1.0f;
     int b_s_i = -1;
-    bool ok = valid && tsl_sample_beta<true>(t, rng, E, T, b);
+    bool ok = valid && tsl_sample_beta<FAST>(t, rng, E, T, b);
     if (ok) {
-      AlphaCtx<true> x;
-      ok = alpha_begin<true>(t, rng, b, E, T, x);
+      AlphaCtx<FAST> x;
+      ok = alpha_begin<FAST>(t, rng, b, E, T, x);
       if (ok) {
         b_s_i = x.b_s_i;
         a_min = x.b_s_a_min;
@@ -1181,8 +1181,8 @@ __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView
     const float q1 = run_net(G, kGOffW1, kGOffW2, kGOffW3, fw);
     double alpha = 0;
     if (ok) {
-      AlphaCtx<true> x;
-      alpha_setup<true>(t, b, E, T, b_s_i, x);  // the same context, rebuilt after the network
+      AlphaCtx<FAST> x;
+      alpha_setup<FAST>(t, b, E, T, b_s_i, x);  // the same context, rebuilt after the network
       const float m = static_cast<float>(x.nF + 1);
       const int g0 = static_cast<int>(floorf(fminf(1.0f, fmaxf(0.0f, q0)) * m));
       const int g1 = static_cast<int>(floorf(fminf(1.0f, fmaxf(0.0f, q1)) * m));
@@ -1190,13 +1190,13 @@ __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView
       // temperatures outside the tabulated range (where Evaluate
       // extrapolates), keep the bisection, so the answer is always the POD
       // sampler's
-      const bool mono = __ldg(t.alpha.mono + b_s_i) != 0 && x.ev.c.Tl < x.ev.c.Th && x.ev.c.Tl <= T &&
-                        T <= x.ev.c.Th;
-      const int i_min = mono ? cdf_upper_guided<true>(x, x.b_s_a_min, g0) : cdf_upper_bisect<true>(x, x.b_s_a_min);
-      const int i_max = mono ? cdf_upper_guided<true>(x, x.b_s_a_max, g1) : cdf_upper_bisect<true>(x, x.b_s_a_max);
-      const double F_min = cdf_at<true>(t, x, x.b_s_a_min, i_min);
-      const double F_max = cdf_at<true>(t, x, x.b_s_a_max, i_max);
-      ok = alpha_end<true>(t, rng, x, F_min, F_max, alpha);
+      const bool mono = (__ldg(t.alpha.mono + b_s_i) & (FAST ? 1 : 2)) != 0 && x.ev.c.Tl < x.ev.c.Th &&
+                        x.ev.c.Tl <= T && T <= x.ev.c.Th;
+      const int i_min = mono ? cdf_upper_guided<FAST>(x, x.b_s_a_min, g0) : cdf_upper_bisect<FAST>(x, x.b_s_a_min);
+      const int i_max = mono ? cdf_upper_guided<FAST>(x, x.b_s_a_max, g1) : cdf_upper_bisect<FAST>(x, x.b_s_a_max);
+      const double F_min = cdf_at<FAST>(t, x, x.b_s_a_min, i_min);
+      const double F_max = cdf_at<FAST>(t, x, x.b_s_a_max, i_max);
+      ok = alpha_end<FAST>(t, rng, x, F_min, F_max, alpha);
     }
     if (valid) {
       if constexpr (QUEUE) {
@@ -1248,12 +1248,12 @@ __global__ void __launch_bounds__(256) k_pod_queue(const DevTSL* tsl, const Guid
   }
 }
 
-template <bool QUEUE>
+template <bool QUEUE, bool FAST>
 cudaError_t guided_attr() {
   static bool attr = false;
   if (!attr) {
     const cudaError_t e =
-        cudaFuncSetAttribute(k_guided_sample<QUEUE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuideSmem);
+        cudaFuncSetAttribute(k_guided_sample<QUEUE, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGuideSmem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -1268,11 +1268,12 @@ cudaError_t launch_guide_data(const DevTSL* tsl, const MlpBox& box, unsigned lon
   return cudaGetLastError();
 }
 
-cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, const double* E,
-                                     const double* T, unsigned long long n, unsigned long long key, double* beta,
-                                     double* alpha, unsigned long long* failures, int num_sms, cudaStream_t s) {
+cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, bool fast,
+                                     const double* E, const double* T, unsigned long long n, unsigned long long key,
+                                     double* beta, double* alpha, unsigned long long* failures, int num_sms,
+                                     cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  cudaError_t e = guided_attr<false>();
+  cudaError_t e = fast ? guided_attr<false, true>() : guided_attr<false, false>();
   if (e != cudaSuccess) return e;
   const unsigned long long tiles = (n + 127) / 128;
   const unsigned long long want = (tiles + kGuideGroups - 1) / kGuideGroups;
@@ -1287,7 +1288,8 @@ cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, con
   io.beta_out = beta;
   io.alpha_out = alpha;
   io.failures = failures;
-  k_guided_sample<false><<<grid, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  if (fast) k_guided_sample<false, true><<<grid, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  else k_guided_sample<false, false><<<grid, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
   return cudaGetLastError();
 }
 
@@ -1296,7 +1298,7 @@ cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guid
                                            unsigned long long cap, unsigned long long run_key, GuideOut* out,
                                            int num_sms, cudaStream_t s) {
   if (cap == 0) return cudaSuccess;
-  cudaError_t e = guided_attr<true>();
+  cudaError_t e = guided_attr<true, true>();
   if (e != cudaSuccess) return e;
   NetView nv{guide.p, guide.W1, guide.W2, guide.W3};
   GuideIO io{};
@@ -1307,7 +1309,7 @@ cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guid
   io.run_key = run_key;
   io.qout = out;
   // the row count is known on the device only: one persistent CTA per SM
-  k_guided_sample<true><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  k_guided_sample<true, true><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
   return cudaGetLastError();
 }
 

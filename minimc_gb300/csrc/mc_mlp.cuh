@@ -120,10 +120,12 @@ int* mlp_error_flag();
 // training rows: 2 per sample (the two bounds), n samples
 cudaError_t launch_guide_data(const DevTSL* tsl, const MlpBox& box, unsigned long long key, unsigned long long n,
                               __half* X, float* y, unsigned long long* failures, cudaStream_t s);
-// array form: Philox stream of row i keyed by (key, i), as the POD sampler's
-cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, const double* E,
-                                     const double* T, unsigned long long n, unsigned long long key, double* beta,
-                                     double* alpha, unsigned long long* failures, int num_sms, cudaStream_t s);
+// array form: Philox stream of row i keyed by (key, i), as the POD sampler's;
+// `fast` selects the POD form reproduced (FP32 or exact FP64)
+cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, bool fast,
+                                     const double* E, const double* T, unsigned long long n, unsigned long long key,
+                                     double* beta, double* alpha, unsigned long long* failures, int num_sms,
+                                     cudaStream_t s);
 // queue form: parked rows, *count of them (at most cap, read on the device)
 cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box,
                                            const GuideRow* rows, const unsigned long long* count,

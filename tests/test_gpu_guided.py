@@ -65,11 +65,26 @@ def test_guided_samples_are_the_pod_samples(ctx1, E):
     ctx, _ = ctx1
     n = 300_000
     T = np.random.default_rng(8).uniform(283.6, 623.6, n)
-    gb, ga, gf = ctx.sample_tsl(0, np.full(n, E), T, seed=21, method=TSL_GUIDED)
+    gb, ga, gf = ctx.sample_tsl(0, np.full(n, E), T, seed=21, method=TSL_GUIDED | TSL_FAST)
     pb, pa, pf = ctx.sample_tsl(0, np.full(n, E), T, seed=21, method=TSL_POD | TSL_PHILOX | TSL_FAST)
     assert gf == pf
     assert np.array_equal(gb, pb, equal_nan=True)
     assert np.array_equal(ga, pa, equal_nan=True)
+
+
+def test_guided_exact_form_samples_are_the_exact_pod_samples(ctx1):
+    """The exact (FP64) POD form: the guide starts the same searches over
+    its reconstructions, the samples are the exact POD sampler's, bit for
+    bit, at C4's energies with T uniform per sample."""
+    ctx, _ = ctx1
+    n = 100_000
+    rng = np.random.default_rng(12)
+    E = np.asarray(ENERGIES)[rng.integers(0, 3, n)]
+    T = rng.uniform(283.6, 623.6, n)
+    gb, ga, gf = ctx.sample_tsl(0, E, T, seed=31, method=TSL_GUIDED)
+    pb, pa, pf = ctx.sample_tsl(0, E, T, seed=31, method=TSL_POD | TSL_PHILOX)
+    assert gf == pf
+    assert np.array_equal(gb, pb, equal_nan=True) and np.array_equal(ga, pa, equal_nan=True)
 
 
 def test_guided_samples_outside_the_trained_box(ctx1):
@@ -79,7 +94,7 @@ def test_guided_samples_outside_the_trained_box(ctx1):
     n = 100_000
     E = np.full(n, 3.5e-6)
     T = np.full(n, 700.0)
-    gb, ga, _ = ctx.sample_tsl(0, E, T, seed=4, method=TSL_GUIDED)
+    gb, ga, _ = ctx.sample_tsl(0, E, T, seed=4, method=TSL_GUIDED | TSL_FAST)
     pb, pa, _ = ctx.sample_tsl(0, E, T, seed=4, method=TSL_POD | TSL_PHILOX | TSL_FAST)
     assert np.array_equal(gb, pb, equal_nan=True) and np.array_equal(ga, pa, equal_nan=True)
 
