@@ -106,7 +106,12 @@ typedef struct {
   int32_t variant;      /* history-kernel variant + 1; 0 -> autotuned   */
   int32_t thermal;      /* MC_THERMAL_*: thermal scattering sampler      */
   int32_t bank_path;    /* MC_BANK_*: k-eigenvalue fission-site path     */
-  int32_t reserved[4];
+  uint32_t queue_sort_min; /* event schedule: sort a step's collision queue
+                           by (type, material, group) when it holds at
+                           least this many particles; 0 -> the value the
+                           autotuner chose (never before it has run);
+                           0xFFFFFFFF -> never                          */
+  int32_t reserved[3];
 } mc_run_opts;
 
 /* A particle in a bank: the state that Bank/Particle carry between
@@ -258,9 +263,13 @@ int mc_keig_resume(mc_ctx* ctx, const void* buf, uint64_t size);
 
 /* What the last transport ran: schedule (MC_SCHEDULE_*), the autotuned
  * history-kernel variant, grid and block, and the kernel times the tuner
- * measured per variant (tune_ms: n entries, may be NULL).  The tuner runs
- * on the first inactive k-eigenvalue cycle unless opts->block_size is set;
- * it has no counterpart in the reference. */
+ * measured per candidate (tune_ms: n entries, may be NULL): the history
+ * schedule's five occupancy variants at block 256, then at block 128, then
+ * (multigroup problems the event schedule serves) the event schedule with
+ * unsorted and with sorted collision queues.  With MC_SCHEDULE_AUTO and no
+ * fixed block size or variant, the tuner runs on the second inactive
+ * k-eigenvalue cycle and keeps the fastest candidate (schedule, block,
+ * variant, queue-sort threshold); it has no counterpart in the reference. */
 int mc_schedule_info(mc_ctx* ctx, int32_t* schedule, int32_t* variant, int32_t* grid, int32_t* block,
                      double* tune_ms, int32_t n);
 

@@ -97,7 +97,15 @@ struct mc_ctx {
   // autotuner: history-kernel variant (occupancy target) chosen by timing
   int variant = 0;
   bool tune_pending = false;
-  double tune_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_ms[16] = {};
+  // the tuner's other choices: schedule for MC_SCHEDULE_AUTO, block size
+  // (0: the run's own), event-schedule collision-queue sort threshold (0:
+  // never); and the caller's queue-sort request of the current run
+  // (mc_run_opts.queue_sort_min)
+  int tuned_schedule = MC_SCHEDULE_HISTORY;
+  int tuned_block = 0;
+  unsigned ev_sort_min = 0;
+  unsigned sort_min_req = 0;
   int last_grid = 0, last_block = 0;
   // MLP surrogate of the thermal scattering sampler
   mcd::MlpNet mlp[2];            // beta, alpha networks
@@ -746,11 +754,22 @@ int counters_status(mc_ctx* c, const DevCounters& h) {
 // pay a launch and a state round trip per event), so AUTO picks it; the
 // event schedule runs multigroup problems whose estimators fit the dense
 // per-history scores, without perturbations, when asked for.
+bool event_schedule_ok(const mc_ctx* c) {
+  return c->model.energy_mode == mc::kMultigroup && c->total_bins <= mcd::kEvDenseBins &&
+         c->model.perturbations.empty();
+}
+
 int resolve_schedule(mc_ctx* c, int requested) {
-  const bool event_ok = c->model.energy_mode == mc::kMultigroup && c->total_bins <= mcd::kEvDenseBins &&
-                        c->model.perturbations.empty();
+  const bool event_ok = event_schedule_ok(c);
   if (requested == MC_SCHEDULE_EVENT) return event_ok ? MC_SCHEDULE_EVENT : -1;
+  if (requested == MC_SCHEDULE_AUTO && event_ok) return c->tuned_schedule;
   return MC_SCHEDULE_HISTORY;
+}
+
+// the collision-queue sort threshold of an event-schedule run (0: never)
+unsigned event_sort_min(const mc_ctx* c) {
+  if (c->sort_min_req == 0) return c->ev_sort_min;
+  return c->sort_min_req == 0xFFFFFFFFu ? 0u : c->sort_min_req;
 }
 
 void count_launches(void* ctx, int n) { static_cast<mc_ctx*>(ctx)->launches += n; }
@@ -788,8 +807,8 @@ int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap) {
   // one allocation for the particle store: 6 f64 + E + 6 x u32 + u64 + u8
   const size_t bytes = cap * (8 * 7 + 4 * 6 + 8 + 1) + 256 * 16;
   char* base = static_cast<char*>(scratch(c, kEvState, bytes));
-  auto* q = static_cast<int32_t*>(scratch(c, kEvQueues, cap * 3 * sizeof(int32_t)));
-  auto* cnt = static_cast<unsigned*>(scratch(c, kEvCnt, 64));
+  auto* q = static_cast<int32_t*>(scratch(c, kEvQueues, cap * 4 * sizeof(int32_t)));
+  auto* cnt = static_cast<unsigned*>(scratch(c, kEvCnt, 64 + 2 * mcd::kEvSortKeys * sizeof(unsigned)));
   if (!base || !q || !cnt) return fail(c, MC_ERR_OOM, "event-schedule buffers");
   size_t off = 0;
   auto take = [&](size_t each) {
@@ -816,6 +835,12 @@ int run_event_once(mc_ctx* c, RunParams& rp, int rng, uint64_t cap) {
   ep.q_out = q + cap;
   ep.q_coll = q + 2 * cap;
   ep.cnt = cnt;
+  ep.q_sorted = q + 3 * cap;
+  ep.sort_hist = cnt + 16;
+  ep.sort_min = event_sort_min(c);
+  const size_t keys = 2 * static_cast<size_t>(c->model.materials.size()) * static_cast<size_t>(c->model.groups);
+  ep.sort_keys = ep.sort_min > 0 && keys <= static_cast<size_t>(mcd::kEvSortKeys) ? static_cast<int32_t>(keys) : 0;
+  if (ep.sort_keys > 0) CUDA_TRY(c, cudaMemsetAsync(ep.sort_hist, 0, mcd::kEvSortKeys * sizeof(unsigned), c->stream));
   if (rp.hist_events) CUDA_TRY(c, cudaMemsetAsync(rp.hist_events, 0, n * 4, c->stream));
   mcd::EvLaunch L{};
   L.grid = c->num_sms * 8;
@@ -1259,6 +1284,7 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
   if (rng != MC_RNG_PHILOX && rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   const int block = pick_block(o);
   if (o && o->variant > 0) c->variant = std::min(o->variant - 1, mcd::history_variants() - 1);
+  c->sort_min_req = o ? o->queue_sort_min : 0;
   RunParams rp{};
   rp.n = n;
   rp.seed = seed;
@@ -1347,9 +1373,11 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   k.max_events = o && o->max_events ? o->max_events : 1000000u;
   k.bank_path = o ? o->bank_path : MC_BANK_AUTO;
   k.launches0 = c->launches;
-  // tune the history kernel on the first inactive cycle unless the caller
-  // fixed the block size
-  c->tune_pending = !(o && (o->block_size > 0 || o->variant > 0)) && k.inactive > 0;
+  // tune on the second inactive cycle unless the caller fixed the block
+  // size, the variant or the schedule
+  c->tune_pending = !(o && (o->block_size > 0 || o->variant > 0)) && k.inactive > 0 &&
+                    k.schedule == MC_SCHEDULE_AUTO;
+  c->sort_min_req = o ? o->queue_sort_min : 0;
   if (o && o->variant > 0) c->variant = std::min(o->variant - 1, mcd::history_variants() - 1);
   if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_INPUT, "unknown rng mode");
   if (k.n == 0) return fail(c, MC_ERR_INPUT, "no histories");
@@ -1390,28 +1418,50 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   // the autotuner waits for the second inactive cycle when there is one:
   // the first cycle's source (Source::Sample) is not yet the fission
   // source the later cycles transport
-  if (!active && c->tune_pending && (k.cycle >= 1 || k.inactive < 2) &&
-      resolve_schedule(c, k.schedule) == MC_SCHEDULE_HISTORY) {
-    // Autotuner: every variant transports this (inactive, unscored) cycle,
-    // twice, interleaved, keeping each variant's shorter time; the variants
-    // draw the same numbers and give identical results, so only the timing
-    // differs.
+  if (!active && c->tune_pending && (k.cycle >= 1 || k.inactive < 2)) {
+    // Autotuner: every candidate transports this (inactive, unscored)
+    // cycle, twice, interleaved, keeping each candidate's shorter time of
+    // its transport kernels.  Candidates: the history schedule's occupancy
+    // variants at blocks of 256 and 128 threads, and -- where the event
+    // schedule serves the problem -- the event schedule with collision
+    // queues unsorted and sorted (threshold 2^15).  All draw the same
+    // numbers and give the same results; only the timing differs.
     c->tune_pending = false;
-    const int nv = std::min(mcd::history_variants(), 8);
-    for (int v = 0; v < nv; v++) c->tune_ms[v] = 1e300;
+    struct Candidate {
+      int schedule, variant, block;
+      unsigned sort_min;
+    };
+    std::vector<Candidate> cand;
+    const int nv = mcd::history_variants();
+    for (int b : {256, 128})
+      for (int v = 0; v < nv; v++) cand.push_back({MC_SCHEDULE_HISTORY, v, b, 0});
+    if (event_schedule_ok(c)) {
+      cand.push_back({MC_SCHEDULE_EVENT, 0, 256, 0});
+      cand.push_back({MC_SCHEDULE_EVENT, 0, 256, 1u << 15});
+    }
+    const int nc = std::min<int>(static_cast<int>(cand.size()), 16);
+    for (int i = 0; i < 16; i++) c->tune_ms[i] = i < nc ? 1e300 : 0;
+    const unsigned req = c->sort_min_req;
+    c->sort_min_req = 0;
     for (int pass = 0; pass < 2; pass++) {
-      for (int v = 0; v < nv; v++) {
-        c->variant = v;
+      for (int i = 0; i < nc; i++) {
+        c->variant = cand[i].variant;
+        c->ev_sort_min = cand[i].sort_min;
         double t = 0;
-        const int rc = run_transport(c, rp, k.rng, k.block, &t, k.schedule);
+        const int rc = run_transport(c, rp, k.rng, cand[i].block, &t, cand[i].schedule);
         if (rc != MC_OK) return rc;
-        c->tune_ms[v] = std::min(c->tune_ms[v], c->last_kernel_ms);
+        c->tune_ms[i] = std::min(c->tune_ms[i], c->last_kernel_ms);
       }
     }
+    c->sort_min_req = req;
     int best = 0;
-    for (int v = 1; v < nv; v++)
-      if (c->tune_ms[v] < c->tune_ms[best]) best = v;
-    c->variant = best;
+    for (int i = 1; i < nc; i++)
+      if (c->tune_ms[i] < c->tune_ms[best]) best = i;
+    c->tuned_schedule = cand[best].schedule;
+    c->variant = cand[best].variant;
+    c->ev_sort_min = cand[best].sort_min;
+    c->tuned_block = cand[best].block;
+    k.block = cand[best].block;
   }
   // transport, bank and read-back with one synchronisation; the cycle's
   // timing events have completed by then
@@ -1490,7 +1540,7 @@ int mc_schedule_info(mc_ctx* c, int32_t* schedule, int32_t* variant, int32_t* gr
   if (grid) *grid = c->last_grid;
   if (block) *block = c->last_block;
   if (tune_ms)
-    for (int32_t i = 0; i < n && i < 8; i++) tune_ms[i] = c->tune_ms[i];
+    for (int32_t i = 0; i < n && i < 16; i++) tune_ms[i] = c->tune_ms[i];
   return MC_OK;
 }
 
@@ -1695,6 +1745,7 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   // kernel (each site once, coalesced, when its history starts), so the
   // host-to-device transfer overlaps the transport instead of preceding it;
   // pageable memory is copied first.
+  c->sort_min_req = o ? o->queue_sort_min : 0;
   const Site* src = nullptr;
   cudaPointerAttributes pa{};
   if (cudaPointerGetAttributes(&pa, sites) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {

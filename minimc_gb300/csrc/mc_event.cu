@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256) k_ev_collide_mg(const DevWorld w, const E
     unsigned i = 0;
     Site sec[kMaxSec];
     if (have) {
-      i = static_cast<unsigned>(ep.q_coll[k]);
+      i = static_cast<unsigned>((ep.cnt[4] ? ep.q_sorted : ep.q_coll)[k]);
       Rng rng;
       load_rng(ep, i, rng);
       const int t = (ep.st.tag[i] >> 1) & 1;
@@ -749,6 +749,62 @@ __global__ void k_ev_reset(unsigned* cnt, unsigned slots) {
   cnt[1] = 0;
   cnt[2] = 0;
   cnt[3] = slots;
+  cnt[4] = 0;
+}
+
+// the collision queue's sort key of particle slot i
+__device__ __forceinline__ int ev_sort_key(const DevWorld& w, const EvParams& ep, unsigned i) {
+  const int t = (ep.st.tag[i] >> 1) & 1;
+  const int m = __ldg(w.cell_mat + ep.st.cell[i]);
+  return (t * w.n_materials + m) * w.G + ep.st.g[i];
+}
+
+// counting sort of the collision queue (when it is long enough): key counts
+__global__ void __launch_bounds__(256) k_ev_sort_count(const DevWorld w, const EvParams ep) {
+  __shared__ unsigned h[kEvSortKeys];
+  const unsigned n = ep.cnt[2];
+  if (n < ep.sort_min) return;  // the same for every block
+  for (int k = threadIdx.x; k < kEvSortKeys; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    atomicAdd(h + ev_sort_key(w, ep, static_cast<unsigned>(ep.q_coll[j])), 1u);
+  __syncthreads();
+  for (int k = threadIdx.x; k < ep.sort_keys; k += blockDim.x)
+    if (h[k]) atomicAdd(ep.sort_hist + k, h[k]);
+}
+
+// one block: exclusive scan of the counts into write positions, counts
+// cleared for the next step, and the flag that tells the collide kernel
+// which queue to read
+__global__ void __launch_bounds__(kEvSortKeys) k_ev_sort_offsets(EvParams ep) {
+  __shared__ unsigned s[kEvSortKeys];
+  const unsigned n = ep.cnt[2];
+  const bool sort = n >= ep.sort_min;
+  const int k = threadIdx.x;
+  const unsigned v = (sort && k < ep.sort_keys) ? ep.sort_hist[k] : 0;
+  s[k] = v;
+  __syncthreads();
+  for (int off = 1; off < kEvSortKeys; off <<= 1) {
+    const unsigned y = k >= off ? s[k - off] : 0;
+    __syncthreads();
+    s[k] += y;
+    __syncthreads();
+  }
+  if (k < ep.sort_keys) {
+    ep.sort_hist[kEvSortKeys + k] = s[k] - v;
+    ep.sort_hist[k] = 0;
+  }
+  if (k == 0) ep.cnt[4] = sort ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(256) k_ev_sort_scatter(const DevWorld w, const EvParams ep) {
+  if (!ep.cnt[4]) return;
+  const unsigned n = ep.cnt[2];
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int32_t i = ep.q_coll[j];
+    const unsigned pos = atomicAdd(ep.sort_hist + kEvSortKeys + ev_sort_key(w, ep, static_cast<unsigned>(i)), 1u);
+    ep.q_sorted[pos] = i;
+  }
 }
 
 template <class Rng>
@@ -775,6 +831,12 @@ static cudaError_t launch_all(const DevWorld& w, EvParams ep, const EvLaunch& L,
     ep.q_in = qa;
     ep.q_out = qb;
     k_ev_advance_mg<Rng><<<L.grid, block, 0, stream>>>(w, ep);
+    if (ep.sort_keys > 0) {
+      k_ev_sort_count<<<L.grid, 256, 0, stream>>>(w, ep);
+      k_ev_sort_offsets<<<1, kEvSortKeys, 0, stream>>>(ep);
+      k_ev_sort_scatter<<<L.grid, 256, 0, stream>>>(w, ep);
+      if (hook) hook(hook_ctx, 3);
+    }
     k_ev_collide_mg<Rng><<<L.grid, block, 0, stream>>>(w, ep);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (hook) hook(hook_ctx, 3);

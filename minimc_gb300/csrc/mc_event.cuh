@@ -30,8 +30,20 @@ struct EvParams {
   int32_t* q_in;
   int32_t* q_out;
   int32_t* q_coll;
-  unsigned* cnt;      // [0] in, [1] out, [2] collisions, [3] slots used
+  unsigned* cnt;      // [0] in, [1] out, [2] collisions, [3] slots used,
+                      // [4] 1 when this step's collision queue was sorted
+  // Collision-queue ordering: when sort_keys > 0 and a step's collision
+  // queue holds at least sort_min particles, it is counting-sorted by
+  // (particle type, material, group) into q_sorted before the collide
+  // kernel, so neighbouring lanes read the same cross-section rows.  Every
+  // particle draws from its own stream, so the order changes no result.
+  int32_t* q_sorted;
+  unsigned* sort_hist;  // [2 * kEvSortKeys]: counts, then write positions
+  unsigned sort_min;
+  int32_t sort_keys;
 };
+
+constexpr int kEvSortKeys = 256;  // most (type, material, group) keys the sort handles
 
 struct EvLaunch {
   int grid;

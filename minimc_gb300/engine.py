@@ -57,7 +57,7 @@ class RunOpts(C.Structure):
                 ("active", C.c_uint32), ("rng", C.c_int32), ("schedule", C.c_int32),
                 ("max_events", C.c_uint32), ("block_size", C.c_int32), ("fast_math", C.c_int32),
                 ("variant", C.c_int32), ("thermal", C.c_int32), ("bank_path", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("queue_sort_min", C.c_uint32), ("reserved", C.c_int32 * 3)]
 
 
 class Site(C.Structure):
@@ -420,8 +420,8 @@ class Context:
 
     def schedule_info(self) -> dict:
         s, v, g, b = (C.c_int32() for _ in range(4))
-        t = np.zeros(8)
-        self.check(self.lib.mc_schedule_info(self.h, C.byref(s), C.byref(v), C.byref(g), C.byref(b), _dptr(t), 8))
+        t = np.zeros(16)
+        self.check(self.lib.mc_schedule_info(self.h, C.byref(s), C.byref(v), C.byref(g), C.byref(b), _dptr(t), 16))
         names = {1: "history", 2: "event"}
         return {"schedule": names.get(s.value, s.value), "variant": v.value, "grid": g.value, "block": b.value,
                 "tune_kernel_ms": [round(x, 4) for x in t if x > 0]}

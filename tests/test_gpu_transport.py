@@ -147,6 +147,45 @@ def test_philox_reproducible_and_schedule_independent(built_library):
         np.testing.assert_allclose(r.sum, runs[0].sum, rtol=FP_RTOL)
 
 
+def test_event_schedule_sorted_queues_identical(built_library):
+    """Collision queues counting-sorted by (type, material, group) before
+    every collide step give the same banks and tallies as the unsorted
+    event schedule and the history schedule: each particle draws from its
+    own stream, so the processing order changes nothing."""
+    p = synth.two_zone_cubes(histories=200000, inactive=2, active=2)
+    xml = p.xml()
+    hist = gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_HISTORY)
+    for sort_min in (0xFFFFFFFF, 1, 50000):
+        ev = gpu_ctx(xml).run_keigenvalue(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_EVENT,
+                                          queue_sort_min=sort_min)
+        assert np.array_equal(ev.bank_size, hist.bank_size), sort_min
+        np.testing.assert_allclose(ev.sum, hist.sum, rtol=FP_RTOL)
+    # fixed source with secondaries in their history
+    fs = synth.one_group_cube(histories=20000, side=2.0)  # small: about one secondary per history
+    fs.problem = "fixedsource"
+    xf = fs.xml()
+    a = gpu_ctx(xf).run_fixed_source(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_EVENT, queue_sort_min=1)
+    b = gpu_ctx(xf).run_fixed_source(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_HISTORY)
+    assert a.raw.events == b.raw.events and a.raw.secondaries == b.raw.secondaries
+    np.testing.assert_allclose(a.sum, b.sum, rtol=FP_RTOL)
+
+
+def test_autotuner_candidates(built_library):
+    """MC_SCHEDULE_AUTO on a k-eigenvalue run: the tuner times the history
+    kernel's five occupancy variants at blocks of 256 and 128 and the event
+    schedule with unsorted and sorted collision queues, then keeps the
+    fastest; the run's results do not depend on the choice."""
+    p = synth.two_zone_cubes(histories=200000, inactive=3, active=2)
+    ctx = gpu_ctx(p.xml())
+    r = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=1)
+    info = ctx.schedule_info()
+    assert len(info["tune_kernel_ms"]) == 12, info
+    assert info["schedule"] in ("history", "event") and info["block"] in (128, 256)
+    ref = gpu_ctx(p.xml()).run_keigenvalue(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_HISTORY, variant=1)
+    assert np.array_equal(r.bank_size, ref.bank_size)
+    np.testing.assert_allclose(r.sum, ref.sum, rtol=FP_RTOL)
+
+
 def test_full_size_two_zone_invariants(built_library):
     """1e6 histories per cycle: no lost particles, fission bank = sum of
     per-history sites, tallies finite and non-negative, k in range."""
