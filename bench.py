@@ -467,6 +467,50 @@ def thermal_forms(local: int, hist: int, steps: int, warmup: int, quantile: bool
     return out
 
 
+def c4_scale(ctx, stream, n: int = 10_000_000, bins: int = 200) -> dict:
+    """C4 at its stated scale, per incident energy (0.01, 0.1, 1 eV): n
+    scatters with T uniform in 283.6-623.6 K per sample, outgoing beta and
+    alpha histograms of 200 equiprobable bins (edges from one exact-POD
+    sample), and the two-sample chi-square of the guided sampler (exact
+    form) and of the MLP quantile surrogate against an independent
+    exact-POD sample."""
+    import torch
+
+    from minimc_gb300 import TSL_GUIDED, TSL_MLP, TSL_PHILOX, TSL_POD
+
+    out = {"samples_per_energy": n, "bins": bins, "T": "uniform 283.6-623.6 K per sample"}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(13)
+    T = 283.6 + 340.0 * torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
+    E = torch.empty_like(T)
+    b = torch.empty_like(T)
+    a = torch.empty_like(T)
+
+    def draw(method, seed):
+        ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=seed, method=method)
+        torch.cuda.synchronize()
+        return b.clone(), a.clone()
+
+    def counts(x, edges):
+        x = x[~torch.isnan(x)]
+        return torch.bincount(torch.bucketize(x, edges), minlength=bins + 2).cpu().numpy().astype(np.float64)
+
+    for e_ev in (0.01, 0.1, 1.0):
+        E.fill_(e_ev * 1e-6)
+        ref = draw(TSL_POD | TSL_PHILOX, 101)
+        pod = draw(TSL_POD | TSL_PHILOX, 202)
+        res = {"guided": draw(TSL_GUIDED, 303), "mlp_quantile": draw(TSL_MLP, 404)}
+        row = {}
+        for v, name in ((0, "beta"), (1, "alpha")):
+            x = ref[v][~torch.isnan(ref[v])].sort().values
+            edges = x[torch.linspace(0, len(x) - 1, bins + 1, device="cuda").round().long()][1:-1].contiguous()
+            cp = counts(pod[v], edges)
+            for form, smp in res.items():
+                row.setdefault(form, {})[name] = chi2_two_sample(counts(smp[v], edges), cp)
+        out[f"{e_ev:g} eV"] = row
+    return out
+
+
 def run_gpu_tsl(args) -> None:
     """Broomstick transport (histories/s) with each thermal sampler form,
     plus the sampler-level comparison of the POD forms, the guided sampler
@@ -549,6 +593,7 @@ def run_gpu_tsl(args) -> None:
     same = {form: bool(np.array_equal(samples[f"guided_{form}"][0], samples[f"pod_{form}"][0], equal_nan=True) and
                        np.array_equal(samples[f"guided_{form}"][1], samples[f"pod_{form}"][1], equal_nan=True))
             for form in ("exact", "fp32")}
+    c4 = c4_scale(ctx, stream, n=10_000_000)
     flops = 2 * 2 * (16 * 128 + 2 * 128 * 128 + 128)  # two network rows per sample, multiply-adds x 2
     bf16_peak = None
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -574,6 +619,7 @@ def run_gpu_tsl(args) -> None:
                        "form": "guided (surrogate-started CDF searches, POD-exact samples)",
                        "l2": "inputs generated on device; tallies 0.65 MB"},
             "thermal_forms": forms,
+            "c4_scale": c4,
             "sampler": {"samples_per_s": rates, "ks_vs_pod_exact": ks, "guided_equals_pod": same,
                         "guided_exact_vs_pod_exact": rates["guided_exact"] / rates["pod_exact"],
                         "guided_fp32_vs_pod_fp32": rates["guided_fp32"] / rates["pod_fp32"],
@@ -594,57 +640,130 @@ def run_gpu_tsl(args) -> None:
 
 
 BATCH_WORKLOAD = ("64 independent 8-group two-zone k-eigenvalue problems (seeds 0..63, cube sides log-uniform "
-                  "10-80 cm, 1e4-1e6 histories/cycle log-uniform) in one batch: one transport launch per cycle, "
-                  "per-cycle CUDA graph")
+                  "10-80 cm, 1e4-1e6 histories/cycle log-uniform, material temperatures uniform 300-600 K with "
+                  "the two thermal groups' scatter transfer sampled from the MLP surrogate at each problem's "
+                  "temperature) in one batch: one persistent transport launch per cycle, per-cycle CUDA graph")
+QUANT_TRAIN = dict(E_range=(5e-9, 2e-6), T_range=(283.6, 623.6), conditions=16384, samples_per_condition=1024,
+                   batch=16384, steps=12000, lr=1e-3, seed=3)
+
+
+def batch_cpu_baseline(probs, rows, temps, threads: int, subset: int = 16, cycles: int = 6, seed: int = 21) -> dict:
+    """The CPU oracle (reference algorithm, minstd streams) on a seeded
+    subset of the batch's problems, each run alone for `cycles` cycles of
+    its own histories per cycle (capped at 2e5): total histories over total
+    time."""
+    from minimc_gb300 import thermal_groups
+    from oracle.build import Oracle
+
+    pick = sorted(np.random.default_rng(seed).choice(len(probs), size=min(subset, len(probs)), replace=False))
+    hist = secs = 0.0
+    for i in pick:
+        p, h = probs[i]
+        n = min(int(h), 200_000)
+        q = thermal_groups.with_thermal_rows(p, temps[i], rows[i])
+        r = Oracle(q.xml()).run_keigenvalue(n, p.seed, 1, cycles - 1, threads=threads)
+        hist += n * cycles
+        secs += r["seconds"]
+    return {"value": hist / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"problems {[int(i) for i in pick]} of the batch (seeded subset), each alone on the CPU "
+                      f"oracle: {cycles} cycles x min(its histories, 2e5), {threads} threads, {secs:.1f} s"}
 
 
 def run_gpu_batch(args) -> None:
-    """C5: the batch against the same problems run one after another
-    (single-problem k-eigenvalue path, same seeds: identical k per cycle)."""
+    """C5: 64 uneven problems whose thermal groups scatter by transfer rows
+    sampled from the MLP surrogate at each problem's temperature, in one
+    batch; against (a) the same problems with the POD sampler's rows
+    (per-problem k within sigma: the plain form), (b) the same problems run
+    one after another through the single-problem path (identical k; the
+    batching gain) and (c) the CPU oracle on a seeded subset."""
     import torch
+    from scipy import stats
 
-    from minimc_gb300 import RNG_PHILOX, Batch, Context, synth
+    from minimc_gb300 import RNG_PHILOX, TSL_MLP, TSL_PHILOX, TSL_POD, Batch, Context, synth, thermal_groups
 
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     probs = synth.batch_problems(count=64, seed=7 + rank)
-    b = Batch(local)
-    for p, h in probs:
-        b.add(p.xml(), histories=h, seed=p.seed)
+    temps = thermal_groups.problem_temperatures(len(probs), seed=11 + rank)
+    # transfer rows of the thermal groups: surrogate and POD sampler
+    wl = tsl_problem(10)
+    tctx = Context(local)
+    tctx.load_xml(wl["xml"], wl["base"])
+    t0 = time.perf_counter()
+    tr = tctx.train_surrogate(0, **QUANT_TRAIN)
+    train_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rows_s, fail_s = thermal_groups.transfer_rows(tctx, 0, temps, seed=3, method=TSL_MLP)
+    rows_ms = 1e3 * (time.perf_counter() - t0)
+    rows_p, fail_p = thermal_groups.transfer_rows(tctx, 0, temps, seed=4, method=TSL_POD | TSL_PHILOX)
+    thermal = [thermal_groups.with_thermal_rows(p, T, r) for (p, _), T, r in zip(probs, temps, rows_s)]
+    plain = [thermal_groups.with_thermal_rows(p, T, r) for (p, _), T, r in zip(probs, temps, rows_p)]
+
+    def make(problems, seed_offset=0):
+        b = Batch(local)
+        for q, (p, h) in zip(problems, probs):
+            b.add(q.xml(), histories=h, seed=p.seed + seed_offset)
+        return b
+
     clocks = ClockSampler(local)
     clocks.start()
-    r = b.run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
+    r = make(thermal).run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
     clk = clocks.stop()
     cycles = args.warmup + args.steps
-    value = r["histories"] * ws / (r["transport_ms"] / 1e3)
-    # the plain form: each problem alone, the same cycles
+    n_cycle = int(sum(h for _, h in probs))
+    value = n_cycle * args.steps * ws / (r["active_ms"] / 1e3)
+    rp = make(plain, 1000).run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
+    z = (r["k_mean"] - rp["k_mean"]) / np.hypot(r["k_std"], rp["k_std"])
+    chi2 = float(np.sum(z ** 2))
+    # the plain path: each problem alone, the same cycles
     seq_ms = 0.0
     agree = True
-    for i, (p, h) in enumerate(probs):
+    for i, (q, (p, h)) in enumerate(zip(thermal, probs)):
         ctx = Context(local)
-        ctx.load_xml(p.xml())
+        ctx.load_xml(q.xml())
         s = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=int(args.fast), histories=h, seed=p.seed,
                                 inactive=args.warmup, active=args.steps, variant=r["variant"] + 1)
         seq_ms += s.raw.transport_ms
         agree &= bool(np.array_equal(s.k_cycle, r["k_cycle"][i]))
-    seq_value = r["histories"] / (seq_ms / 1e3)
+    seq_value = n_cycle * cycles / (seq_ms / 1e3)
+    all_value = n_cycle * cycles / (r["transport_ms"] / 1e3)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = batch_cpu_baseline(probs, rows_s, temps, os.cpu_count() or 1)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": r["transport_ms"] / cycles, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": r["active_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOAD, "problems": len(probs),
-                       "histories_per_cycle": int(sum(h for _, h in probs)), "rng": "philox",
-                       "fast_math": bool(args.fast), "timed": "all cycles of the batch run (warm-up included)"},
+            "config": {"workload": BATCH_WORKLOAD, "problems": len(probs), "histories_per_cycle": n_cycle,
+                       "rng": "philox", "fast_math": bool(args.fast),
+                       "timed": "the active cycles (a step = one cycle of all problems); the warm-up cycles "
+                                "and the autotuner's runs before them are outside",
+                       "l2": "working set (sources, banks, records of 1.4e7 histories) far above L2"},
             "batch": {"variant": r["variant"], "graph": bool(r["graph"]), "launches": r["launches"],
                       "tune_ms": [round(x, 3) for x in r["tune_ms"] if x > 0],
-                      "sequential_histories_per_s": seq_value, "speedup_vs_sequential": value / seq_value,
+                      "all_cycles_histories_per_s": all_value,
+                      "sequential_histories_per_s": seq_value, "speedup_vs_sequential": all_value / seq_value,
                       "k_identical_to_single_runs": agree,
                       "k_mean_range": [float(r["k_mean"].min()), float(r["k_mean"].max())]},
-            "cpu_baseline": None,
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
-                    "call": "mc_batch_run (results copied back once)"},
+            "thermal_groups": {
+                "temperatures_K": [round(float(t), 1) for t in temps],
+                "rows": "surrogate (MLP quantile networks, tcgen05) at each temperature, 2^20 scatters per "
+                        "thermal group, binned on the device",
+                "rows_ms": rows_ms, "train_s": train_s, "train_loss": [tr.loss_beta, tr.loss_alpha],
+                "sampler_failures": [int(fail_s), int(fail_p)],
+                "max_row_diff_vs_pod": float(np.abs(rows_s - rows_p).max()),
+                "k_vs_pod_rows": {"chi2": chi2, "dof": len(z), "p": float(stats.chi2.sf(chi2, len(z))),
+                                  "max_abs_z": float(np.abs(z).max()),
+                                  "within_3_sigma": int((np.abs(z) < 3).sum()),
+                                  "k_surrogate": [round(float(k), 6) for k in r["k_mean"]],
+                                  "k_pod": [round(float(k), 6) for k in rp["k_mean"]],
+                                  "note": "independent seeds; z = dk / combined standard error"}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": all_value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "call": "mc_batch_run over all cycles, warm-up included (problems loaded before; k read back "
+                            "once at the end)"},
             "gpu_launches": int(r["launches"]), "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -427,8 +427,9 @@ int mc_output_format(const char* xml_text, const char* base_dir, const double* s
 /* ---- batched problems -------------------------------------------------------
  * No reference counterpart: the reference runs one problem per process.
  * Many independent multigroup k-eigenvalue problems of uneven sizes run
- * together: one transport launch per cycle serves all of them (each CTA
- * one problem), one prefix sum, compaction and resampling over their
+ * together: one persistent transport launch per cycle serves all of them
+ * (each CTA starts on one problem and, its queue drained, helps drain the
+ * others'), one prefix sum, compaction and resampling over their
  * concatenated fission banks, and one cycle's launches are captured once
  * as a CUDA graph and replayed every cycle.  Per problem the k per cycle
  * equals mc_run_keigenvalue's with Philox streams and the same seed. */
@@ -454,7 +455,8 @@ typedef struct mc_batch_out {
   uint64_t launches;          /* kernel launches (graph: one per cycle)      */
   int32_t variant;            /* chosen variant                              */
   int32_t graph;              /* 1 if the cycles ran as a CUDA graph         */
-  uint64_t reserved[4];
+  double active_ms;           /* device time of the active cycles            */
+  uint64_t reserved[3];
 } mc_batch_out;
 int mc_batch_create(mc_batch** out, int device);
 void mc_batch_destroy(mc_batch* b);
@@ -464,6 +466,23 @@ int mc_batch_set_stream(mc_batch* b, void* cuda_stream);
 int mc_batch_add(mc_batch* b, const char* xml_text, const char* base_dir, uint64_t histories, uint64_t seed);
 int mc_batch_run(mc_batch* b, const mc_batch_opts* opts, mc_batch_out* out);
 int mc_batch_last_error(mc_batch* b, char* buf, size_t n);
+
+/* Multigroup transfer of thermal scatters: for each of `rows` (energy MeV,
+ * temperature K) pairs, n scatters are sampled on the device with `method`
+ * (any mc_sample_tsl method: MC_TSL_MLP is the surrogate, MC_TSL_POD |
+ * MC_TSL_PHILOX [| MC_TSL_FAST] the POD sampler), each outgoing energy
+ * E' = E + beta k T formed as ThermalScattering::Scatter does
+ * (src/ThermalScattering.cpp:159-171) and binned into the groups whose
+ * boundaries (MeV, `groups` + 1 values, descending, group 1 the fastest)
+ * are given: group g holds bounds[g] <= E' < bounds[g - 1]; energies above
+ * the first bound count in group 1, below the last in the last group.
+ * probs[r * groups + g] = the fraction of row r's binned samples in group
+ * g + 1.  Samples whose resampling failed (NaN) are not binned; their
+ * number is returned in *failures.  The samples stay on the device.
+ * groups <= 64, n <= 2^26. */
+int mc_tsl_group_transfer(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
+                          uint32_t rows, uint64_t n, const double* bounds, uint32_t groups, uint64_t seed,
+                          int32_t method, double* probs, uint64_t* failures);
 
 /* ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157). */
 int mc_tsl_total(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,

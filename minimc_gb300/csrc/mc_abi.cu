@@ -56,6 +56,8 @@ enum ScratchSlot {
   kTqCnt,
   kTqRows,
   kTqRes,
+  kGroupRows,     // thermal group transfer: rows, bounds, counts
+  kGroupSamples,  // thermal group transfer: one chunk's samples
   kScratchSlots,  // number of slots
 };
 
@@ -2542,6 +2544,67 @@ int mc_tsl_total(mc_ctx* c, int32_t tsl, const double* energy, const double* tem
   return MC_OK;
 }
 
+int mc_tsl_group_transfer(mc_ctx* c, int32_t tsl, const double* energy, const double* temperature, uint32_t rows,
+                          uint64_t n, const double* bounds, uint32_t groups, uint64_t seed, int32_t method,
+                          double* probs, uint64_t* failures) {
+  if (!check_ctx(c)) return MC_ERR_STATE;
+  if (tsl < 0 || tsl >= c->dw.n_tsl) return fail(c, MC_ERR_INPUT, "thermal scattering library index out of range");
+  if (rows == 0) return MC_OK;
+  if (!energy || !temperature || !bounds || !probs) return fail(c, MC_ERR_INPUT, "null argument");
+  if (groups < 1 || groups > static_cast<uint32_t>(mcd::kMaxTransferGroups))
+    return fail(c, MC_ERR_INPUT, "groups must be 1.." + std::to_string(mcd::kMaxTransferGroups));
+  if (n == 0 || n > (1ull << 26)) return fail(c, MC_ERR_INPUT, "samples per row must be 1..2^26");
+  for (uint32_t g = 0; g < groups; g++)
+    if (!(bounds[g] > bounds[g + 1])) return fail(c, MC_ERR_INPUT, "group boundaries must be descending");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  // rows per chunk: about 2^24 samples (E, T, beta, alpha: 512 MB) at a time
+  const uint64_t per_chunk =
+      std::max<uint64_t>(1, std::min<uint64_t>({static_cast<uint64_t>(rows), 65535ull, std::max<uint64_t>(1, (1ull << 24) / n)}));
+  const size_t row_bytes = (2 * static_cast<size_t>(rows) + groups + 1) * 8 + static_cast<size_t>(rows) * groups * 8;
+  auto* rb = static_cast<double*>(scratch(c, kGroupRows, row_bytes));
+  auto* sb = static_cast<double*>(scratch(c, kGroupSamples, per_chunk * n * 32));
+  if (!rb || !sb) return fail(c, MC_ERR_OOM, "thermal group transfer buffers");
+  double* d_E = rb;
+  double* d_T = rb + rows;
+  double* d_bounds = rb + 2 * static_cast<size_t>(rows);
+  auto* d_counts = reinterpret_cast<unsigned long long*>(d_bounds + groups + 1);
+  CUDA_TRY(c, cudaMemcpyAsync(d_E, energy, rows * 8ull, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d_T, temperature, rows * 8ull, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d_bounds, bounds, (groups + 1) * 8ull, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(d_counts, 0, static_cast<size_t>(rows) * groups * 8, c->stream));
+  uint64_t fails = 0;
+  for (uint64_t r0 = 0, chunk = 0; r0 < rows; r0 += per_chunk, chunk++) {
+    const unsigned nr = static_cast<unsigned>(std::min<uint64_t>(per_chunk, rows - r0));
+    const uint64_t m = nr * n;
+    double* E = sb;
+    double* T = sb + m;
+    double* beta = sb + 2 * m;
+    double* alpha = sb + 3 * m;
+    CUDA_TRY(c, mcd::launch_expand_rows(d_E + r0, d_T + r0, nr, n, E, T, c->stream));
+    c->launches++;
+    // every chunk its own streams
+    uint64_t f = 0;
+    const int rc = sample_tsl_device(c, tsl, E, T, m, seed ^ (chunk * 0x9E3779B97F4A7C15ull), method, beta, alpha, &f);
+    if (rc != MC_OK) return rc;
+    fails += f;
+    CUDA_TRY(c, mcd::launch_group_bins(beta, nr, n, d_E + r0, d_T + r0, d_bounds, static_cast<int>(groups),
+                                       d_counts + r0 * groups, c->stream));
+    c->launches++;
+  }
+  std::vector<unsigned long long> counts(static_cast<size_t>(rows) * groups);
+  CUDA_TRY(c, cudaMemcpyAsync(counts.data(), d_counts, counts.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t r = 0; r < rows; r++) {
+    unsigned long long tot = 0;
+    for (uint32_t g = 0; g < groups; g++) tot += counts[static_cast<size_t>(r) * groups + g];
+    for (uint32_t g = 0; g < groups; g++)
+      probs[static_cast<size_t>(r) * groups + g] =
+          tot ? static_cast<double>(counts[static_cast<size_t>(r) * groups + g]) / static_cast<double>(tot) : 0.0;
+  }
+  if (failures) *failures = fails;
+  return MC_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -2941,7 +3004,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
       if (rc != MC_OK) return rc;
       BATCH_TRY(b, mcd::launch_batch_begin(bc, src0, s));
       BATCH_TRY(b, cudaEventRecord(e0, s));
-      BATCH_TRY(b, mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, static_cast<int>(bp.size()), s, v));
+      BATCH_TRY(b, mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, static_cast<int>(bp.size()), P, s, v));
       BATCH_TRY(b, cudaEventRecord(e1, s));
       BATCH_TRY(b, cudaEventSynchronize(e1));
       float ms = 0;
@@ -2971,7 +3034,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
   auto cycle_launches = [&](const Site* from, Site* to) -> cudaError_t {
     cudaError_t e;
     if ((e = mcd::launch_batch_begin(bc, from, s)) != cudaSuccess) return e;
-    if ((e = mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, grid, s, variant)) != cudaSuccess) return e;
+    if ((e = mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, grid, P, s, variant)) != cudaSuccess) return e;
     if (direct) {
       if ((e = mcd::launch_fission_counts(all, s)) != cudaSuccess) return e;
       if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
@@ -3013,8 +3076,15 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
       if (ie != cudaSuccess) return bfail(b, MC_ERR_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(ie));
     }
   }
+  cudaEvent_t em;  // start of the active cycles
+  BATCH_TRY(b, cudaEventCreate(&em));
+  struct EvGuard1 {
+    cudaEvent_t e;
+    ~EvGuard1() { cudaEventDestroy(e); }
+  } evm{em};
   BATCH_TRY(b, cudaEventRecord(e0, s));
   for (uint32_t cyc = 0; cyc < cycles; cyc++) {
+    if (cyc == o->inactive) BATCH_TRY(b, cudaEventRecord(em, s));
     if (graph) {
       BATCH_TRY(b, cudaGraphLaunch(exec[cyc & 1], s));
       res.launches += 1;
@@ -3026,8 +3096,9 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
   }
   BATCH_TRY(b, cudaEventRecord(e1, s));
   BATCH_TRY(b, cudaEventSynchronize(e1));
-  float ms = 0;
+  float ms = 0, ms_active = 0;
   cudaEventElapsedTime(&ms, e0, e1);
+  if (o->active > 0) cudaEventElapsedTime(&ms_active, em, e1);
   std::vector<double> k(static_cast<size_t>(P) * cycles);
   std::vector<unsigned long long> stats(4 * static_cast<size_t>(P));
   int died = 0;
@@ -3035,6 +3106,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
   BATCH_TRY(b, cudaMemcpy(stats.data(), d_stats, stats.size() * 8, cudaMemcpyDeviceToHost));
   BATCH_TRY(b, cudaMemcpy(&died, d_died, 4, cudaMemcpyDeviceToHost));
   res.transport_ms = ms;
+  res.active_ms = ms_active;
   res.histories = N * cycles;
   res.variant = variant;
   res.graph = graph ? 1 : 0;

@@ -172,10 +172,11 @@ cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mo
                               cudaStream_t stream, int variant);
 int history_blocks_per_sm(int energy_mode, int rng_mode, int block, bool keig, bool fast, int variant);
 
-// batched multigroup k-eigenvalue transport (mc_transport.cu): CTA b serves
-// problem block_problem[b]
+// batched multigroup k-eigenvalue transport (mc_transport.cu): CTA b starts
+// on problem block_problem[b], then helps drain the other P - 1 problems'
+// queues
 cudaError_t launch_history_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
-                                    int grid, cudaStream_t stream, int variant);
+                                    int grid, int P, cudaStream_t stream, int variant);
 int history_batch_blocks_per_sm(int variant);
 cudaError_t launch_fission_sites_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
                                           const uint32_t* block_first, int grid, cudaStream_t stream);
@@ -221,6 +222,14 @@ cudaError_t launch_sample_tsl(const DevTSL* tsl, bool fast, int rng_mode, const 
                               double* alpha, unsigned long long* failures, cudaStream_t stream);
 cudaError_t launch_tsl_total(const DevTSL* tsl, const double* E, const double* T, unsigned long long n, double* out,
                              cudaStream_t stream);
+// multigroup transfer of thermal scatters (mc_tsl.cu): rows of (E, T)
+// repeated over n samples, and the samples' outgoing groups counted per row
+constexpr int kMaxTransferGroups = 64;
+cudaError_t launch_expand_rows(const double* E_rows, const double* T_rows, unsigned rows, unsigned long long n,
+                               double* E, double* T, cudaStream_t stream);
+cudaError_t launch_group_bins(const double* beta, unsigned rows, unsigned long long n, const double* E_rows,
+                              const double* T_rows, const double* bounds, int G, unsigned long long* counts,
+                              cudaStream_t stream);
 
 // bank compaction and resampling (mc_transport.cu)
 cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,

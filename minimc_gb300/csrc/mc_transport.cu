@@ -359,22 +359,45 @@ __global__ void __launch_bounds__(256, 1) k_history_mg_pert(const DevWorld w, co
   history_mg<Rng, false, true>(w, rp, smem);
 }
 
-// batched k-eigenvalue transport: every CTA serves one problem (its world
-// and run parameters copied to shared memory); the problems' histories
-// take their own global queues
+// batched k-eigenvalue transport, a persistent grid over all problems:
+// each problem's histories form its own global queue; a CTA starts on the
+// problem its block table assigns (CTAs in proportion to the histories),
+// drains that queue, then visits the other problems in turn and helps
+// drain any queue that still holds histories, so small problems' CTAs do
+// not idle while large ones run.  The world and run parameters of the
+// problem a CTA serves sit in shared memory.  A history's result depends
+// only on its problem, index and stream, not on the CTA that runs it.
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) k_history_mg_batch(const DevWorld* worlds, const RunParams* rps,
-                                                                const uint32_t* block_problem) {
+                                                                const uint32_t* block_problem, int P) {
   extern __shared__ double smem[];
   __shared__ DevWorld w;
   __shared__ RunParams rp;
-  const uint32_t p = block_problem[blockIdx.x];
-  if (threadIdx.x == 0) {
-    w = worlds[p];
-    rp = rps[p];
+  __shared__ int q_serve;
+  const uint32_t p0 = block_problem[blockIdx.x];
+  int q = 0;  // problems visited: p0, p0 + 1, ... (mod P)
+  for (;;) {
+    if (threadIdx.x == 0) {
+      // the next problem whose queue still holds histories (a stale read
+      // costs one empty visit); the CTA's own problem is always served
+      while (q > 0 && q < P) {
+        const uint32_t p = (p0 + static_cast<uint32_t>(q)) % static_cast<uint32_t>(P);
+        if (*reinterpret_cast<volatile unsigned long long*>(&rps[p].ctr->next) < rps[p].n) break;
+        q++;
+      }
+      q_serve = q;
+      if (q < P) {
+        const uint32_t p = (p0 + static_cast<uint32_t>(q)) % static_cast<uint32_t>(P);
+        w = worlds[p];
+        rp = rps[p];
+      }
+    }
+    __syncthreads();
+    if (q_serve >= P) break;
+    history_mg<PhiloxRng, true>(w, rp, smem);
+    q = q_serve + 1;
+    __syncthreads();  // every warp is done with this problem's parameters
   }
-  __syncthreads();
-  history_mg<PhiloxRng, true>(w, rp, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -415,9 +438,9 @@ void launch_mg(const DevWorld& w, const RunParams& rp, int rng_mode, int grid, i
 
 namespace {
 template <int MINB>
-void launch_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem, int grid,
+void launch_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem, int grid, int P,
                      cudaStream_t stream) {
-  k_history_mg_batch<MINB><<<grid, 256, 2 * kSharedBins * sizeof(double), stream>>>(worlds, rps, block_problem);
+  k_history_mg_batch<MINB><<<grid, 256, 2 * kSharedBins * sizeof(double), stream>>>(worlds, rps, block_problem, P);
 }
 template <int MINB>
 int occupancy_mg_batch() {
@@ -426,13 +449,14 @@ int occupancy_mg_batch() {
 }  // namespace
 
 cudaError_t launch_history_mg_batch(const DevWorld* worlds, const RunParams* rps, const uint32_t* block_problem,
-                                    int grid, cudaStream_t stream, int variant) {
+                                    int grid, int P, cudaStream_t stream, int variant) {
+  if (P < 1) return cudaErrorInvalidValue;
   switch (variant) {
-  case 1: launch_mg_batch<3>(worlds, rps, block_problem, grid, stream); break;
-  case 2: launch_mg_batch<4>(worlds, rps, block_problem, grid, stream); break;
-  case 3: launch_mg_batch<5>(worlds, rps, block_problem, grid, stream); break;
-  case 4: launch_mg_batch<6>(worlds, rps, block_problem, grid, stream); break;
-  default: launch_mg_batch<1>(worlds, rps, block_problem, grid, stream); break;
+  case 1: launch_mg_batch<3>(worlds, rps, block_problem, grid, P, stream); break;
+  case 2: launch_mg_batch<4>(worlds, rps, block_problem, grid, P, stream); break;
+  case 3: launch_mg_batch<5>(worlds, rps, block_problem, grid, P, stream); break;
+  case 4: launch_mg_batch<6>(worlds, rps, block_problem, grid, P, stream); break;
+  default: launch_mg_batch<1>(worlds, rps, block_problem, grid, P, stream); break;
   }
   return cudaGetLastError();
 }

@@ -121,7 +121,7 @@ class BatchOut(C.Structure):
                 ("k_std", C.POINTER(C.c_double)), ("transport_ms", C.c_double), ("tune_ms", C.c_double * 8),
                 ("histories", C.c_uint64), ("events", C.c_uint64), ("lost", C.c_uint64), ("capped", C.c_uint64),
                 ("overflow", C.c_uint64), ("launches", C.c_uint64), ("variant", C.c_int32), ("graph", C.c_int32),
-                ("reserved", C.c_uint64 * 4)]
+                ("active_ms", C.c_double), ("reserved", C.c_uint64 * 3)]
 
 
 class KeigOut(C.Structure):
@@ -173,6 +173,8 @@ _SIGNATURES = {
     "mc_sample_tsl_device": (C.c_int, [_P, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_int32,
                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
+    "mc_tsl_group_transfer": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint32, C.c_uint64, _D, C.c_uint32, C.c_uint64,
+                                        C.c_int32, _D, C.POINTER(C.c_uint64)]),
     "mc_output_text": (C.c_int, [_P, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
                                  C.POINTER(C.c_size_t)]),
     "mc_output_format": (C.c_int, [C.c_char_p, C.c_char_p, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
@@ -544,6 +546,22 @@ class Context:
                                           C.byref(f)))
         return b, a, int(f.value)
 
+    def tsl_group_transfer(self, tsl: int, energy, temperature, n: int, bounds, seed: int = 1,
+                           method: int = TSL_POD):
+        """Multigroup transfer of thermal scatters (mc_tsl_group_transfer):
+        for each (E, T) row, the fractions of n sampled outgoing energies
+        E' = E + beta k T in each group of `bounds` (MeV, descending); returns
+        (probs [rows, groups], failures)."""
+        e = _arr(np.atleast_1d(energy), np.float64)
+        t = _arr(np.broadcast_to(temperature, e.shape), np.float64)
+        b = _arr(np.asarray(bounds), np.float64)
+        G = len(b) - 1
+        out = np.zeros((len(e), G))
+        f = C.c_uint64()
+        self.check(self.lib.mc_tsl_group_transfer(self.h, tsl, _dptr(e), _dptr(t), len(e), n, _dptr(b), G, seed,
+                                                  method, _dptr(out), C.byref(f)))
+        return out, int(f.value)
+
     def sample_tsl_device(self, tsl: int, d_energy: int, d_temperature: int, n: int, d_beta: int, d_alpha: int,
                           seed: int = 1, method: int = TSL_POD) -> int:
         """The sampler on device arrays (raw device addresses); returns the
@@ -807,5 +825,5 @@ class Batch:
         if rc != MC_OK and rc not in allow:
             raise MCError(rc, self.error())
         return {"k_cycle": k, "k_mean": km, "k_std": ks, "transport_ms": out.transport_ms,
-                "histories": out.histories, "events": out.events, "launches": out.launches,
+                "active_ms": out.active_ms, "histories": out.histories, "events": out.events, "launches": out.launches,
                 "variant": out.variant, "graph": out.graph, "tune_ms": list(out.tune_ms), "status": rc}

@@ -12,9 +12,12 @@ guess or walk from it.  So, for the same random numbers:
   the ones the inline FP32 POD sampler gives: the same events and fate for
   every history and the same leakage tallies -- and the same again for the
   plain POD queue without the network;
-* with independent seeds, at 1e6 histories per energy, the leakage energy
-  and cosine spectra of the guided form pass a two-sample chi-square test
-  against the POD form (p > 0.01), the gate the surrogate is held to.
+* with independent seeds, at 1e7 histories per energy (C4's scale), the
+  leakage energy and cosine spectra of the guided form pass a two-sample
+  chi-square test against the POD form (p > 0.01), the gate the surrogate
+  is held to; and at the sampler level, 1e7 scatters per energy with T
+  uniform per sample, its outgoing beta and alpha histograms (200 bins)
+  pass the same test against an independent exact-POD sample.
 """
 import numpy as np
 import pytest
@@ -139,13 +142,34 @@ def chi2_two_sample(a, b):
 
 @pytest.mark.parametrize("E", ENERGIES)
 def test_guided_spectra_pass_chi2_against_pod(library, E):
-    """Independent seeds, 1e6 histories each: the guided form's leakage
+    """Independent seeds, 1e7 histories each: the guided form's leakage
     energy and cosine spectra against the inline POD form's."""
     ctx, _ = guided_ctx(library, energy=E)
-    n = 1_000_000
+    n = 10_000_000
     pod = ctx.run_fixed_source(rng=RNG_PHILOX, fast_math=1, histories=n, seed=101, thermal=THERMAL_POD)
     gui = ctx.run_fixed_source(rng=RNG_PHILOX, fast_math=1, histories=n, seed=202, thermal=THERMAL_GUIDED)
     assert gui.raw.lost == 0 and gui.raw.resample_failures == pod.raw.resample_failures == 0
     for name, a, b in zip(("energy", "cosine"), spectra(ctx, gui), spectra(ctx, pod)):
         chi2, dof, p = chi2_two_sample(a, b)
         assert p > P_MIN, (E, name, chi2, dof, p)
+
+
+@pytest.mark.parametrize("E", ENERGIES)
+def test_c4_scale_beta_alpha_histograms(ctx1, E):
+    """1e7 scatters at one incident energy, T uniform in 283.6-623.6 K per
+    sample: 200-bin beta and alpha histograms (equiprobable edges from one
+    exact-POD sample) of the exact guided sampler against an independent
+    exact-POD sample."""
+    ctx, _ = ctx1
+    n = 10_000_000
+    T = np.random.default_rng(19).uniform(283.6, 623.6, n)
+    ref = ctx.sample_tsl(0, np.full(n, E), T, seed=101, method=TSL_POD | TSL_PHILOX)
+    pod = ctx.sample_tsl(0, np.full(n, E), T, seed=202, method=TSL_POD | TSL_PHILOX)
+    gui = ctx.sample_tsl(0, np.full(n, E), T, seed=303, method=TSL_GUIDED)
+    assert gui[2] == 0 and pod[2] == 0
+    for v, name in ((0, "beta"), (1, "alpha")):
+        edges = np.quantile(ref[v], np.linspace(0, 1, 201)[1:-1])
+        a = np.bincount(np.searchsorted(edges, gui[v]), minlength=200).astype(float)
+        b = np.bincount(np.searchsorted(edges, pod[v]), minlength=200).astype(float)
+        chi2, dof, p = chi2_two_sample(a, b)
+        assert dof >= 150 and p > P_MIN, (E, name, chi2, dof, p)

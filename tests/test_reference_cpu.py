@@ -298,3 +298,23 @@ def test_keigenvalue_two_zone_spheres_on_reference_code(ref, tmp_path):
     assert np.array_equal(got["bank"], want["bank_size"])
     assert np.array_equal(got["k"], want["k_cycle"])
     assert np.array_equal(got["mean"], want["sum"] / (n * 3))
+
+
+def test_keigenvalue_thermal_group_rows_on_reference_code(ref, tmp_path):
+    """The two-zone problem with thermal transfer rows in its two lowest
+    groups (up- and downscatter between them and into group 6, as the
+    batched workload's thermal groups make them) and a cell temperature:
+    the oracle's k per cycle, bank sizes and leakage means equal the
+    reference's own transport (Multigroup::Scatter samples the full
+    column, src/Multigroup.cpp:249-265)."""
+    from minimc_gb300 import synth, thermal_groups
+
+    rows = np.random.default_rng(5).dirichlet(np.ones(8) * 0.5, size=2)
+    rows[:, :5] = 0.0  # thermal scatters stay in groups 6-8
+    base = synth.two_zone_spheres(histories=3000, inactive=3, active=3)
+    xml = thermal_groups.with_thermal_rows(base, 451.5, rows).xml()
+    assert 'temperature="451.5"' in xml
+    got, want, n = run_keig_both(ref, xml, tmp_path, "leak", 10, 3, 3, 1)
+    assert np.array_equal(got["bank"], want["bank_size"])
+    assert np.array_equal(got["k"], want["k_cycle"])
+    assert np.array_equal(got["mean"], want["sum"] / (n * 3))
