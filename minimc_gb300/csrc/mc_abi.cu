@@ -134,6 +134,12 @@ struct mc_ctx {
     double transport_ms = 0, kernel_ms = 0;
     uint64_t events = 0, lost = 0, capped = 0, overflow = 0;
     uint64_t launches0 = 0;
+    // the next cycle's source is still the resampling of the last bank
+    // (scratch kBank, size in kTotal): the next transport draws it as it
+    // reads its sources; anything else that needs the source, or that
+    // would overwrite the bank first, writes it out (materialize_source)
+    bool src_pending = false;
+    unsigned long long src_key = 0;
   } keig;
 };
 
@@ -1039,6 +1045,18 @@ int bank_direct(const mc_ctx* c, int rng, bool fast, int path) {
   return ok ? 1 : 0;
 }
 
+// writes a pending resampled k-eigenvalue source into scratch kSrc
+int materialize_source(mc_ctx* c) {
+  auto& k = c->keig;
+  if (!k.src_pending) return MC_OK;
+  k.src_pending = false;
+  CUDA_TRY(c, mcd::launch_resample(static_cast<const Site*>(c->scratch[kBank].p),
+                                   static_cast<unsigned long long*>(c->scratch[kTotal].p), k.n, k.src_key,
+                                   static_cast<Site*>(c->scratch[kSrc].p), c->stream));
+  c->launches++;
+  return MC_OK;
+}
+
 // The cycle's fission sites as a compacted bank in history order.  Slot
 // path: the slot kernel has run; a scan of its counts places each history's
 // sites and a compaction copies them into the device bank.  Direct path:
@@ -1049,6 +1067,8 @@ int bank_direct(const mc_ctx* c, int rng, bool fast, int path) {
 // kTotal) unless read_size, which reads it into *m_out.
 int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap, Site** bank_out, uint64_t* m_out,
               bool read_size = true) {
+  // the bank about to be written may still hold a pending source
+  if (materialize_source(c) != MC_OK) return MC_ERR_DEVICE;
   const uint64_t n = rp.n;
   auto* count = static_cast<uint32_t*>(c->scratch[kCount].p);
   auto* offsets = static_cast<unsigned long long*>(scratch(c, kOffsets, n * 8));
@@ -1414,6 +1434,11 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.minstd_base = k.seed + static_cast<unsigned long long>(k.cycle) * k.n;
   rp.max_yield = c->max_yield;
   rp.src = static_cast<const Site*>(c->scratch[kSrc].p);
+  if (k.src_pending) {
+    rp.resample_bank = static_cast<const Site*>(c->scratch[kBank].p);
+    rp.resample_m = static_cast<const unsigned long long*>(c->scratch[kTotal].p);
+    rp.resample_key = k.src_key;
+  }
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
   rp.direct_sites = bank_direct(c, k.rng, k.fast != 0, k.bank_path) > 0 ? 1 : 0;
@@ -1469,6 +1494,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   // timing events have completed by then
   int rc = run_transport(c, rp, k.rng, k.block, nullptr, k.schedule, /*side_commit=*/true);
   if (rc != MC_OK) return rc;
+  k.src_pending = false;  // read by the transport, which precedes any write of the bank
   Site* bank = nullptr;
   uint64_t m = 0;
   rc = emit_bank(c, rp, k.rng, nullptr, 0, &bank, &m, /*read_size=*/false);
@@ -1492,11 +1518,11 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   k.bank.push_back(m);
   if (kout) *kout = kc;
   if (m == 0) return fail(c, MC_ERR_INPUT, "fission bank is empty: the source died out");
-  // next cycle's source
-  CUDA_TRY(c, mcd::launch_resample(bank, static_cast<unsigned long long*>(c->scratch[kTotal].p), k.n,
-                                   run_key(k.seed, k.cycle, 0x52455341ull), static_cast<Site*>(c->scratch[kSrc].p),
-                                   c->stream));
-  c->launches++;
+  // next cycle's source: resampled from this bank as the next transport
+  // reads it (the same draw as the resampling kernel)
+  if (bank != c->scratch[kBank].p) return fail(c, MC_ERR_STATE, "fission bank outside its buffer");
+  k.src_pending = true;
+  k.src_key = run_key(k.seed, k.cycle, 0x52455341ull);
   k.cycle++;
   return counters_status(c, h);
 }
@@ -1645,6 +1671,7 @@ int mc_keig_checkpoint(mc_ctx* c, void* buf, uint64_t cap, uint64_t* size) {
   out += tb * 8;
   CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sq, tb * 8, cudaMemcpyDeviceToHost, c->stream));
   out += tb * 8;
+  if (materialize_source(c) != MC_OK) return MC_ERR_DEVICE;
   CUDA_TRY(c, cudaMemcpyAsync(out, c->scratch[kSrc].p, k.n * sizeof(Site), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return MC_OK;

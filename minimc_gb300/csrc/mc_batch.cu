@@ -68,12 +68,7 @@ __global__ void k_batch_resample(const BatchCycle b, const Site* bank, Site* nex
   const unsigned long long m = b.M[p];
   if (m == 0) return;
   const unsigned long long key = dev_run_key(b.seeds[p], *b.cycle, 0x52455341ull);
-  uint32_t c[4] = {static_cast<uint32_t>(jj), static_cast<uint32_t>(jj >> 32), 0x72657361u, 0};
-  philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
-  const double u = ((c[0] >> 5) * 67108864.0 + (c[1] >> 6)) * (1.0 / 9007199254740992.0);
-  unsigned long long idx = static_cast<unsigned long long>(u * static_cast<double>(m));
-  if (idx >= m) idx = m - 1;
-  next[j] = bank[b.start[p] + idx];
+  next[j] = bank[b.start[p] + resample_index(key, jj, m)];
 }
 
 __global__ void k_batch_next_cycle(const BatchCycle b) { *b.cycle += 1; }

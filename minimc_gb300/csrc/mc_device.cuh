@@ -520,8 +520,21 @@ __device__ __forceinline__ bool dneg(double x) {
 // than 4e-6 relative, only its exact FP64 distance is needed.  Near ties,
 // tiny or unusable FP32 values fall back to all exact divisions, so the
 // result always equals the exact computation.
+// c / d without a division, for the Philox fast form's plane distances:
+// the FP32 reciprocal of d refined by one Newton-Raphson step (relative
+// error about 2^-46), the quotient, and one residual correction
+// q + r (c - d q), which leaves it within an ulp or two of the correctly
+// rounded quotient.  df is d in FP32 and must be a normal number.
+__device__ __forceinline__ double quot_nr(double c, double d, float df) {
+  const double r0 = static_cast<double>(__frcp_rn(df));
+  const double r1 = __fma_rn(r0, __fma_rn(-d, r0, 1.0), r0);
+  const double q0 = __dmul_rn(c, r1);
+  return __fma_rn(r1, __fma_rn(-d, q0, c), q0);
+}
+
 __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, int c, const double* pos,
-                                                   const double* dir, const float* dirf, double& dist, int skip) {
+                                                   const double* dir, const float* dirf, double& dist, int skip,
+                                                   bool fast_div) {
   const BoxCell& B = w.boxes[box];
   int cj[3];
   double cv[3];
@@ -550,7 +563,8 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
   for (int a = 0; a < 3; a++)
     if (a != a0) second = fminf(second, tf[a]);
   if (tf[a0] < CUDART_INF_F && tf[a0] > 1e-30f && !(second <= __fmul_rn(tf[a0], 1.000004f))) {
-    const double t = ddiv(cv[a0], dir[a0]);
+    const double t = fast_div && fabsf(dirf[a0]) >= 1.17549435e-38f ? quot_nr(cv[a0], dir[a0], dirf[a0])
+                                                                    : ddiv(cv[a0], dir[a0]);
     if (t > 0 && t < CUDART_INF) {
       dist = t;
       return __ldg(&B.s[cj[a0]]);
@@ -588,23 +602,25 @@ __device__ __forceinline__ int nearest_surface_general(const DevWorld& w, int c,
                                                        double u, double v, double ww, double& dist, int skip);
 
 // The same with the direction also given in FP32 (the box cells' preselection
-// reads it; callers that keep it avoid three conversions per event)
+// reads it; callers that keep it avoid three conversions per event).
+// fast_div (Philox fast form only): a box cell's plane distance by quot_nr.
 __device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
                                                double v, double ww, float fu, float fv, float fw, double& dist,
-                                               int skip = -1) {
+                                               int skip = -1, bool fast_div = false) {
   const int box = __ldg(w.cell_box + c);
   if (box >= 0) {
     const double pos[3] = {x, y, z}, dir[3] = {u, v, ww};
     const float dirf[3] = {fu, fv, fw};
-    return nearest_surface_box(w, box, c, pos, dir, dirf, dist, skip);
+    return nearest_surface_box(w, box, c, pos, dir, dirf, dist, skip, fast_div);
   }
   return nearest_surface_general(w, c, x, y, z, u, v, ww, dist, skip);
 }
 
 __device__ __forceinline__ int nearest_surface(const DevWorld& w, int c, double x, double y, double z, double u,
-                                               double v, double ww, double& dist, int skip = -1) {
+                                               double v, double ww, double& dist, int skip = -1,
+                                               bool fast_div = false) {
   return nearest_surface(w, c, x, y, z, u, v, ww, __double2float_rn(u), __double2float_rn(v), __double2float_rn(ww),
-                         dist, skip);
+                         dist, skip, fast_div);
 }
 
 __device__ __forceinline__ int nearest_surface_general(const DevWorld& w, int c, double x, double y, double z,
@@ -699,6 +715,23 @@ __device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, d
   u = mu;
   v = __fmul_rn(st, c);
   w = __fmul_rn(st, s);
+}
+
+// the same, also returning the direction's FP32 values (exactly the
+// FP64 ones rounded back: they were FP32 numbers)
+template <class Rng>
+__device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, double& w, float& fu, float& fv,
+                                               float& fw) {
+  const float mu = __fmaf_rn(2.0f, rng.u01f(), -1.0f);
+  float s, c;
+  __sincosf(__fmul_rn(__fsub_rn(rng.u01f(), 0.5f), 6.28318530717958647692f), &s, &c);
+  const float st = __fsqrt_rn(fmaxf(0.0f, __fmaf_rn(-mu, mu, 1.0f)));
+  fu = mu;
+  fv = __fmul_rn(st, c);
+  fw = __fmul_rn(st, s);
+  u = fu;
+  v = fv;
+  w = fw;
 }
 
 // exponential flight length in FP32: -log(U) / sigma (U in (0,1))

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_ev_init(const DevWorld w, const EvParam
     unsigned long long id = i;
     uint8_t tag = 0;
     if (ep.rp.from_bank) {
-      const Site& s = ep.rp.src[i];
+      const Site s = source_site(ep.rp, i);
       x = s.x; y = s.y; z = s.z; u = s.u; v = s.v; ww = s.w;
       g = static_cast<int>(s.energy) - 1;
       if constexpr (std::is_same_v<Rng, MinstdRng>) {
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(256) k_ev_advance_mg(const DevWorld w, const E
       const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
       const double dcol = mg_flight(w, rng, fast, mg, sigma);
       double dsurf;
-      const int s = nearest_surface(w, cell, x, y, z, u, v, ww, dsurf, skip);
+      const int s = nearest_surface(w, cell, x, y, z, u, v, ww, dsurf, skip, std::is_same_v<Rng, PhiloxRng> && fast);
       const bool collide = w.tracking == 1 ? !(dsurf < dcol) : (dcol < dsurf);
       const bool score = ep.rp.score != 0;
       auto track = [&](double d) {

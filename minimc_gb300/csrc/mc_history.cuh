@@ -137,6 +137,22 @@ __device__ __forceinline__ void sample_isotropic(Rng& rng, double& u, double& v,
   isotropic(rng, u, v, w);
 }
 
+// the same with the direction's FP32 copy (no conversions in the fast form)
+template <class Rng>
+__device__ __forceinline__ void sample_isotropic(Rng& rng, double& u, double& v, double& w, float& fu, float& fv,
+                                                 float& fw, bool fast) {
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    if (fast) {
+      isotropic_fast(rng, u, v, w, fu, fv, fw);
+      return;
+    }
+  }
+  isotropic(rng, u, v, w);
+  fu = __double2float_rn(u);
+  fv = __double2float_rn(v);
+  fw = __double2float_rn(w);
+}
+
 // first index k in [0, n) with cdf[k] > threshold, or -1
 __device__ __forceinline__ int cdf_search(const double* cdf, int n, int, double threshold) {
   return cdf_first_above(cdf, n, threshold);

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
           }
         }
         else {
-          if (rp.from_bank) start_from_site(rp, hist, rp.src[hist], p, 1);
+          if (rp.from_bank) start_from_site(rp, hist, source_site(rp, hist), p, 1);
           else sample_source(w, rp, hist, p);
           p.cell = find_cell(w, p.x, p.y, p.z);
           p.j = ce_search(w.ce, p.E);
@@ -338,7 +338,8 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
       }
       const double dcol = sample_flight(p.rng, sigma, fast);
       double dsurf;
-      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip);
+      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, dsurf, p.skip,
+                                    std::is_same_v<Rng, PhiloxRng> && fast);
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
       const bool refl = !collide && __ldg(w.surf_refl + s) != 0;
       bool real = true;

@@ -100,7 +100,32 @@ struct RunParams {
   int32_t tq_mode;
   GuideRow* tq_rows;
   const GuideOut* tq_res;
+  // resampling fused into the source read (k-eigenvalue cycles after the
+  // first): with resample_m set, source i is the bank entry the resampling
+  // draw picks -- resample_bank[resample_index(resample_key, i, *resample_m)]
+  // -- and src is not read
+  const Site* resample_bank;
+  const unsigned long long* resample_m;
+  unsigned long long resample_key;
 };
+
+// KEigenvalue's next source, uniform over the bank: source j is bank entry
+// floor(U_j * M), U_j a 53-bit uniform from Philox(key; j, "resa").  The
+// resampling kernels and the fused source read share this draw.
+__device__ __forceinline__ unsigned long long resample_index(unsigned long long key, unsigned long long j,
+                                                             unsigned long long m) {
+  const uint4 c = philox_block(static_cast<uint32_t>(j), static_cast<uint32_t>(j >> 32), 0x72657361u, 0u,
+                               static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
+  const double u = ((c.x >> 5) * 67108864.0 + (c.y >> 6)) * (1.0 / 9007199254740992.0);
+  const unsigned long long idx = static_cast<unsigned long long>(u * static_cast<double>(m));
+  return idx < m ? idx : m - 1;
+}
+
+// source site i of a run from a bank
+__device__ __forceinline__ Site source_site(const RunParams& rp, unsigned long long i) {
+  if (rp.resample_m) return rp.resample_bank[resample_index(rp.resample_key, i, *rp.resample_m)];
+  return rp.src[i];
+}
 
 // k-eigenvalue sites from fission records and the per-history commit of
 // dense scores (mc_event.cu)

@@ -106,7 +106,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           done = true;
         }
         else {
-          if (rp.from_bank) start_from_site(rp, hist, rp.src[hist], p, 0);
+          if (rp.from_bank) start_from_site(rp, hist, source_site(rp, hist), p, 0);
           else sample_source(w, rp, hist, p);
           fu = __double2float_rn(p.u);
           fv = __double2float_rn(p.v);
@@ -151,7 +151,8 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       const double sigma = __ldg(w.mat_mg_sigma + mg);  // number_density * micro, tabulated
       const double dcol = mg_flight(w, p.rng, fast, mg, sigma);
       double dsurf;
-      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, fu, fv, fw, dsurf, p.skip);
+      const int s = nearest_surface(w, p.cell, p.x, p.y, p.z, p.u, p.v, p.w, fu, fv, fw, dsurf, p.skip,
+                                    std::is_same_v<Rng, PhiloxRng> && fast);
       const bool delta = w.tracking == 1;
       const bool collide = delta ? !(dsurf < dcol) : (dcol < dsurf);
       const bool refl = !collide && __ldg(w.surf_refl + s) != 0;
@@ -185,10 +186,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           const int go = mg_pick_outgoing(w, p.rng, fast, ng);
           if (go >= 0) {
             p.g = go;
-            sample_isotropic(p.rng, p.u, p.v, p.w, fast);
-            fu = __double2float_rn(p.u);
-            fv = __double2float_rn(p.v);
-            fw = __double2float_rn(p.w);
+            sample_isotropic(p.rng, p.u, p.v, p.w, fu, fv, fw, fast);
           }
         }
         else if (rx == 2) {
@@ -586,12 +584,7 @@ __global__ void k_resample(const Site* bank, const unsigned long long* total, un
   if (j >= n) return;
   const unsigned long long m = *total;
   if (m == 0) return;
-  uint32_t c[4] = {static_cast<uint32_t>(j), static_cast<uint32_t>(j >> 32), 0x72657361u, 0};
-  philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
-  const double u = ((c[0] >> 5) * 67108864.0 + (c[1] >> 6)) * (1.0 / 9007199254740992.0);
-  unsigned long long idx = static_cast<unsigned long long>(u * static_cast<double>(m));
-  if (idx >= m) idx = m - 1;
-  next[j] = bank[idx];
+  next[j] = bank[resample_index(key, j, m)];
 }
 }  // namespace
 
