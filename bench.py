@@ -685,6 +685,15 @@ def run_gpu_batch(args) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     probs = synth.batch_problems(count=64, seed=7 + rank)
+    if args.mode == "kernel":
+        # profiling mode: the batch's cycles only (no thermal rows, no
+        # surrogate training, no comparisons)
+        b = Batch(local)
+        for p, h in probs:
+            b.add(p.xml(), histories=h, seed=p.seed)
+        r = b.run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
+        print(json.dumps({"mode": "kernel", "variant": r["variant"], "active_ms": r["active_ms"]}), flush=True)
+        return
     temps = thermal_groups.problem_temperatures(len(probs), seed=11 + rank)
     # transfer rows of the thermal groups: surrogate and POD sampler
     wl = tsl_problem(10)

@@ -36,7 +36,7 @@ enum ScratchSlot {
   kCount,
   kOffsets,
   kScanSums,
-  kTotal,
+  kTotal,        // (unused: the bank size lives after the run counters)
   kBank,
   kHistEvents,
   kHistFate,
@@ -82,6 +82,7 @@ struct mc_ctx {
   void* h_small = nullptr;
   uint64_t total_bins = 0;
   DevCounters* d_ctr = nullptr;
+  unsigned long long* d_total = nullptr;  // bank size, right after the counters (one read-back)
   double* d_sum = nullptr;
   double* d_sq = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
@@ -135,7 +136,7 @@ struct mc_ctx {
     uint64_t events = 0, lost = 0, capped = 0, overflow = 0;
     uint64_t launches0 = 0;
     // the next cycle's source is still the resampling of the last bank
-    // (scratch kBank, size in kTotal): the next transport draws it as it
+    // (scratch kBank, size in d_total): the next transport draws it as it
     // reads its sources; anything else that needs the source, or that
     // would overwrite the bank first, writes it out (materialize_source)
     bool src_pending = false;
@@ -692,9 +693,11 @@ int build_world(mc_ctx* c) {
 
   // run buffers
   void* p = nullptr;
-  if (cudaMalloc(&p, sizeof(DevCounters)) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc counters");
+  static_assert(sizeof(DevCounters) % 8 == 0, "the bank size follows the counters");
+  if (cudaMalloc(&p, sizeof(DevCounters) + 64) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc counters");
   c->world_allocs.push_back(p);
   c->d_ctr = static_cast<DevCounters*>(p);
+  c->d_total = reinterpret_cast<unsigned long long*>(c->d_ctr + 1);
   const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
   if (cudaMalloc(&p, tb) != cudaSuccess) return fail(c, MC_ERR_OOM, "cudaMalloc tallies");
   c->world_allocs.push_back(p);
@@ -908,6 +911,7 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   const double* pend_before = c->pend_clean;
   c->pend_clean = nullptr;  // dirty until the commit has run
   CUDA_TRY(c, cudaEventRecord(c->evk0, c->stream));
+  rp.write_counts = 0;
   if (sched == MC_SCHEDULE_EVENT) {
     const int rc = run_event(c, rp, rng);
     if (rc != MC_OK) return rc;
@@ -922,6 +926,9 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     }
     else {
       cudaError_t e;
+      // the multigroup history kernel writes the direct path's site counts
+      rp.write_counts = keig && rp.direct_sites && c->model.energy_mode == mc::kMultigroup &&
+                        rp.bank_count == c->scratch[kCount].p;
       if (c->model.energy_mode == mc::kMultigroup)
         e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
       else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream, c->variant);
@@ -1051,7 +1058,7 @@ int materialize_source(mc_ctx* c) {
   if (!k.src_pending) return MC_OK;
   k.src_pending = false;
   CUDA_TRY(c, mcd::launch_resample(static_cast<const Site*>(c->scratch[kBank].p),
-                                   static_cast<unsigned long long*>(c->scratch[kTotal].p), k.n, k.src_key,
+                                   c->d_total, k.n, k.src_key,
                                    static_cast<Site*>(c->scratch[kSrc].p), c->stream));
   c->launches++;
   return MC_OK;
@@ -1060,11 +1067,12 @@ int materialize_source(mc_ctx* c) {
 // The cycle's fission sites as a compacted bank in history order.  Slot
 // path: the slot kernel has run; a scan of its counts places each history's
 // sites and a compaction copies them into the device bank.  Direct path:
-// counts from the fission records, their scan, then the sites sampled
+// counts from the fission records (written by the multigroup history kernel
+// itself, else by a count kernel), their scan, then the sites sampled
 // straight into `dest` (16-byte aligned page-locked host memory, `cap`
 // sites) or else into the device bank.  *bank_out is the device bank (null
-// when the sites went to `dest`); the size stays on the device (scratch
-// kTotal) unless read_size, which reads it into *m_out.
+// when the sites went to `dest`); the size stays on the device (d_total,
+// after the counters) unless read_size, which reads it into *m_out.
 int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap, Site** bank_out, uint64_t* m_out,
               bool read_size = true) {
   // the bank about to be written may still hold a pending source
@@ -1073,20 +1081,23 @@ int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap,
   auto* count = static_cast<uint32_t*>(c->scratch[kCount].p);
   auto* offsets = static_cast<unsigned long long*>(scratch(c, kOffsets, n * 8));
   auto* sums = static_cast<unsigned long long*>(scratch(c, kScanSums, ((n + 1023) / 1024 + 1) * 8));
-  auto* total = static_cast<unsigned long long*>(scratch(c, kTotal, 8));
+  unsigned long long* total = c->d_total;
   Site* bank = dest ? nullptr : static_cast<Site*>(scratch(c, kBank, n * c->max_yield * sizeof(Site)));
   if (!offsets || !sums || !total || (!dest && !bank)) return fail(c, MC_ERR_OOM, "bank scratch allocation failed");
   if (rp.direct_sites) {
     RunParams q = rp;
     q.ctr = c->d_ctr;
     q.bank_count = count;
-    CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
+    if (!(rp.write_counts && rp.bank_count == count)) {
+      CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
+      c->launches++;
+    }
     CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
     const uint64_t qcap = dest ? cap : n * c->max_yield;
     if (c->model.energy_mode == mc::kMultigroup)
       CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, qcap, dest ? dest : bank, c->stream));
     else CUDA_TRY(c, mcd::launch_fission_sites_out_ce(q, rng, offsets, total, qcap, dest ? dest : bank, c->stream));
-    c->launches += 5;
+    c->launches += 4;
   }
   else {
     auto* slots = static_cast<Site*>(c->scratch[kSlots].p);
@@ -1107,12 +1118,11 @@ int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap,
 // bank size (when m) and counters, read back with one synchronisation
 int read_back(mc_ctx* c, uint64_t* m, DevCounters* h) {
   if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
-  auto* hm = static_cast<unsigned long long*>(c->h_small);
+  // the counters and the bank size that follows them, in one copy
   auto* hc = reinterpret_cast<DevCounters*>(static_cast<char*>(c->h_small) + 64);
-  if (m) CUDA_TRY(c, cudaMemcpyAsync(hm, c->scratch[kTotal].p, 8, cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(c, cudaMemcpyAsync(hc, c->d_ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(hc, c->d_ctr, sizeof(DevCounters) + (m ? 8 : 0), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  if (m) *m = *hm;
+  if (m) *m = *reinterpret_cast<const unsigned long long*>(hc + 1);
   *h = *hc;
   return MC_OK;
 }
@@ -1436,7 +1446,7 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.src = static_cast<const Site*>(c->scratch[kSrc].p);
   if (k.src_pending) {
     rp.resample_bank = static_cast<const Site*>(c->scratch[kBank].p);
-    rp.resample_m = static_cast<const unsigned long long*>(c->scratch[kTotal].p);
+    rp.resample_m = c->d_total;
     rp.resample_key = k.src_key;
   }
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
@@ -1827,7 +1837,7 @@ int mc_transport_bank(mc_ctx* c, const mc_site* sites, uint64_t n, const mc_run_
   if (rc != MC_OK) return rc;
   if (out_mapped && bank) {
     k_copy_bank_out<<<c->num_sms * 8, 256, 0, c->stream>>>(
-        reinterpret_cast<const uint4*>(bank), static_cast<const unsigned long long*>(c->scratch[kTotal].p), cap,
+        reinterpret_cast<const uint4*>(bank), c->d_total, cap,
         reinterpret_cast<uint4*>(out_mapped));
     CUDA_TRY(c, cudaGetLastError());
     c->launches++;

@@ -536,8 +536,10 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
                                                    const double* dir, const float* dirf, double& dist, int skip,
                                                    bool fast_div) {
   const BoxCell& B = w.boxes[box];
-  int cj[3];
-  double cv[3];
+  // per axis: the plane ahead (3 bits each in `js`) and its FP32 distance;
+  // the FP64 differences c - p are formed again for the chosen plane only,
+  // so fewer values stay live through the selection
+  unsigned js = 0;
   float tf[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) {
@@ -548,10 +550,9 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
     // the skipped surface reads as infinitely far; the axis' other plane
     // then is the only candidate
     if (__ldg(&B.s[j]) == skip) j ^= 1;
-    cj[a] = j;
+    js |= static_cast<unsigned>(j) << (3 * a);
     // PlaneX::Distance: v = c - p, positive iff v and d have the same sign
     const double v = dsub(__ldg(&B.c[j]), p);
-    cv[a] = v;
     const bool ahead = __ldg(&B.s[j]) != skip && ((dpos(v) && dpos(d)) || (dneg(v) && dneg(d)));
     tf[a] = ahead ? fabsf(__fdiv_rn(__double2float_rn(v), dirf[a])) : CUDART_INF_F;
   }
@@ -563,11 +564,13 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
   for (int a = 0; a < 3; a++)
     if (a != a0) second = fminf(second, tf[a]);
   if (tf[a0] < CUDART_INF_F && tf[a0] > 1e-30f && !(second <= __fmul_rn(tf[a0], 1.000004f))) {
-    const double t = fast_div && fabsf(dirf[a0]) >= 1.17549435e-38f ? quot_nr(cv[a0], dir[a0], dirf[a0])
-                                                                    : ddiv(cv[a0], dir[a0]);
+    const int j = (js >> (3 * a0)) & 7u;
+    const double v = dsub(__ldg(&B.c[j]), pos[a0]);
+    const double t = fast_div && fabsf(dirf[a0]) >= 1.17549435e-38f ? quot_nr(v, dir[a0], dirf[a0])
+                                                                    : ddiv(v, dir[a0]);
     if (t > 0 && t < CUDART_INF) {
       dist = t;
-      return __ldg(&B.s[cj[a0]]);
+      return __ldg(&B.s[j]);
     }
   }
   // exact path: every candidate divided, reference tie-breaking
@@ -576,12 +579,12 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
   double bd = CUDART_INF;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const int j = cj[a];
+    const int j = (js >> (3 * a)) & 7u;
     const int s = __ldg(&B.s[j]);
     const int o = __ldg(&B.order[j]);
     double t = CUDART_INF;
     if (s != skip) {
-      const double q = ddiv(cv[a], dir[a]);
+      const double q = ddiv(dsub(__ldg(&B.c[j]), pos[a]), dir[a]);
       t = q > 0 ? q : CUDART_INF;
     }
     if (t < bd || (t == bd && t != CUDART_INF && o < best_o)) {

@@ -107,6 +107,10 @@ struct RunParams {
   const Site* resample_bank;
   const unsigned long long* resample_m;
   unsigned long long resample_key;
+  // k-eigenvalue direct path: the multigroup history kernel writes each
+  // history's site count, min(yield, max_yield), into bank_count as the
+  // history ends (no separate count kernel)
+  int32_t write_counts;
 };
 
 // KEigenvalue's next source, uniform over the bank: source j is bank entry
