@@ -180,3 +180,39 @@ def test_c4_scale_beta_alpha_histograms(ctx1, E):
         b = np.bincount(np.searchsorted(edges, ok(pod[v])), minlength=200).astype(float)
         chi2, dof, p = chi2_two_sample(a, b)
         assert dof >= 150 and p > P_MIN, (E, name, chi2, dof, p)
+
+
+def test_guide_gains_over_the_bisection(ctx1):
+    """What the trained network gains over the method without it: the exact
+    (FP64) POD sampler with the guide starting its CDF searches against the
+    same sampler bisecting them, on the same 2e6 (E, T) rows on the device
+    -- the same samples (tested above), less time.  (In the FP32 form the
+    bisection's reconstructions are cheap enough that the network's cost
+    outweighs them; the bench line reports both forms.)"""
+    torch = pytest.importorskip("torch")
+    ctx, _ = ctx1
+    n = 2_000_000
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    E = torch.tensor(ENERGIES, dtype=torch.float64, device="cuda")[torch.randint(0, 3, (n,), device="cuda",
+                                                                                 generator=g)]
+    T = 283.6 + 340.0 * torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
+    b = torch.empty_like(E)
+    a = torch.empty_like(E)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def ms(method):
+        for _ in range(2):
+            ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=9, method=method)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(3):
+            ctx.sample_tsl_device(0, E.data_ptr(), T.data_ptr(), n, b.data_ptr(), a.data_ptr(), seed=10 + i,
+                                  method=method)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    pod, guided = ms(TSL_POD | TSL_PHILOX), ms(TSL_GUIDED)
+    assert pod / guided > 1.05, (pod, guided)
