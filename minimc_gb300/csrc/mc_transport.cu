@@ -51,10 +51,13 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 // ---------------------------------------------------------------------------
 // multigroup history loop of one CTA: the body of the single-problem kernel
 // (world and run parameters in the kernel's parameter space) and of the
-// batched kernel (copied into shared memory per CTA)
-template <class Rng, bool KEIG, bool PERT = false>
+// batched kernel (copied into shared memory per CTA).  SCORE = false
+// compiles the estimator scoring out (runs without tallies: the batched
+// problems), which leaves the loop fewer live registers.
+template <class Rng, bool KEIG, bool PERT = false, bool SCORE = true>
 __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& rp, double* smem) {
-  const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
+  const bool score = SCORE && rp.score != 0;
+  const bool use_smem = rp.total_bins <= kSharedBins && score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
   if (use_smem) {
     for (int i = threadIdx.x; i < 2 * kSharedBins; i += blockDim.x) smem[i] = 0;
@@ -84,7 +87,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
 
   // history complete: ScorableProxy::CommitHistory (src/Scorable.cpp:101-106)
   auto finish_history = [&]() {
-    if (rp.score && !rp.nb) {
+    if (score && !rp.nb) {
       sink.commit(pend);
       if (pend.overflow) my_overflow++;
     }
@@ -172,7 +175,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       // active lanes), before the branch-specific work.
       const double dcross = dadd(dsurf, kNudge);
       const double dmove = collide ? dcol : (refl ? dsurf : dcross);
-      if (rp.score) score_track(w, p, dmove, sc);
+      if (score) score_track(w, p, dmove, sc);
       if (KEIG) my_ktl += dmove * __ldg(w.mat_mg_nusigf + mg);
       indirect_stream<PERT>(w, p, m, micro, dmove);
       move(fast, p.x, p.y, p.z, p.u, p.v, p.w, dmove);
@@ -279,7 +282,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           }
         }
       }
-      if (rp.score) score_event<false, PERT>(w, p, sc);
+      if (score) score_event<false, PERT>(w, p, sc);
       p.nev++;
       hist_nev++;
       my_events++;
@@ -403,7 +406,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_mg_batch(const DevWorld* 
     }
     __syncthreads();
     if (q_serve >= P) break;
-    history_mg<PhiloxRng, true>(w, rp, smem);
+    history_mg<PhiloxRng, true, false, false>(w, rp, smem);  // batched problems keep no tallies
     q = q_serve + 1;
     __syncthreads();  // every warp is done with this problem's parameters
   }
