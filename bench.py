@@ -320,6 +320,8 @@ def run_gpu(args) -> None:
                      "cosine_chi2_vs_pod": f["guided"]["cosine_chi2_vs_pod"],
                      "identical_tallies_same_seed": f["guided"]["identical_tallies_same_seed"],
                      "form": "guided: the guide network starts each SampleAlpha CDF search, POD confirms it",
+                     "exact_form": {k: (v["histories_per_s"] if isinstance(v, dict) else v)
+                                    for k, v in f["exact_form"].items()},
                      "train": f["train"], "timed": "engine device time of each fixed-source run"}
 
     if rank == 0:
@@ -436,19 +438,31 @@ def thermal_forms(local: int, hist: int, steps: int, warmup: int, quantile: bool
         forms["quantile"] = THERMAL_SURROGATE
     base = dict(rng=RNG_PHILOX, fast_math=1, histories=hist)
     out = {}
-    for name, mode in forms.items():
+
+    def timed(mode, fast_math):
+        kw = dict(base, fast_math=fast_math)
         for _ in range(warmup):
-            ctx.run_fixed_source(thermal=mode, **base)
+            ctx.run_fixed_source(thermal=mode, **kw)
         ms = kms = 0.0
         events = launches = 0
         for i in range(steps):
-            r = ctx.run_fixed_source(thermal=mode, seed=1000 + i, **base)
+            r = ctx.run_fixed_source(thermal=mode, seed=1000 + i, **kw)
             ms += r.raw.transport_ms
             kms += r.raw.kernel_ms
             events += r.raw.events
             launches += r.raw.launches
-        out[name] = {"histories_per_s": hist * steps / (ms / 1e3), "ms_per_step": ms / steps,
-                     "events_per_history": events / (hist * steps), "launches_per_step": launches / steps}
+        return {"histories_per_s": hist * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                "events_per_history": events / (hist * steps), "launches_per_step": launches / steps}
+
+    for name, mode in forms.items():
+        out[name] = timed(mode, 1)
+    # the exact (FP64) sampler throughout (fast_math off): where the
+    # network's saving -- FP64 reconstructions -- is largest
+    exact = {f"{k}_exact": timed(v, 0) for k, v in (("pod", THERMAL_POD), ("pod_queue", THERMAL_POD_QUEUE),
+                                                      ("guided", THERMAL_GUIDED))}
+    for k in exact:
+        exact[k]["vs_pod_exact"] = exact[k]["histories_per_s"] / exact["pod_exact"]["histories_per_s"]
+    out["exact_form"] = exact
     ref = ctx.run_fixed_source(thermal=THERMAL_POD, seed=101, **base)
     same = ctx.run_fixed_source(thermal=THERMAL_GUIDED, seed=101, **base)
     out["guided"]["identical_tallies_same_seed"] = bool(np.allclose(same.sum, ref.sum, rtol=1e-12, atol=0))
@@ -461,6 +475,8 @@ def thermal_forms(local: int, hist: int, steps: int, warmup: int, quantile: bool
         out[name]["cosine_chi2_vs_pod"] = chi2_two_sample(sp[1], sr[1])
     for name in forms:
         out[name]["vs_pod"] = out[name]["histories_per_s"] / out["pod"]["histories_per_s"]
+    out["exact_form"]["guided_vs_pod_queue"] = (out["exact_form"]["guided_exact"]["histories_per_s"] /
+                                                out["exact_form"]["pod_queue_exact"]["histories_per_s"])
     out["train"] = train
     out["workload"] = TSL_WORKLOAD
     out["histories_per_step"] = hist

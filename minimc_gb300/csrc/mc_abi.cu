@@ -992,6 +992,9 @@ int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
   CUDA_TRY(c, cudaMemsetAsync(cnt, 0, 2 * (mcd::kTqRounds + 1) * 8, c->stream));
   rp.tq = 1;
   rp.tq_tsl = mode == 1 ? c->mlp_tsl : (c->guide_tsl >= 0 ? c->guide_tsl : 0);
+  // the POD-exact queue forms sample what the inline sampler would: its
+  // FP32 form in fast mode when the library's ranks allow it, else FP64
+  rp.tq_fast = rp.fast && c->tsl_fast_ok[static_cast<size_t>(rp.tq_tsl)] ? 1 : 0;
   rp.tq_rows = rows;
   rp.tq_res = res;
   rp.tq_box[0] = std::exp(c->mlp_box.logE0);
@@ -1013,11 +1016,11 @@ int run_tq(mc_ctx* c, RunParams rp, int grid, int block) {
     mcd::ParkRec* in = r % 2 == 0 ? A : B;
     mcd::ParkRec* out = r % 2 == 0 ? B : A;
     if (mode == 2)
-      e = mcd::launch_sample_tsl_guided_queue(c->dw.tsl + rp.tq_tsl, c->guide, c->guide_box, rows, cnt + r, n,
-                                              rp.run_key, res, c->num_sms, c->stream);
+      e = mcd::launch_sample_tsl_guided_queue(c->dw.tsl + rp.tq_tsl, c->guide, c->guide_box, rp.tq_fast != 0, rows,
+                                              cnt + r, n, rp.run_key, res, c->num_sms, c->stream);
     else if (mode == 3)
-      e = mcd::launch_sample_tsl_pod_queue(c->dw.tsl + rp.tq_tsl, rows, cnt + r, n, rp.run_key, res, c->num_sms,
-                                           c->stream);
+      e = mcd::launch_sample_tsl_pod_queue(c->dw.tsl + rp.tq_tsl, rp.tq_fast != 0, rows, cnt + r, n, rp.run_key,
+                                           res, c->num_sms, c->stream);
     else
       e = mcd::launch_sample_tsl_mlp_queue(c->mlp[0], c->mlp[1], c->mlp_box, qin, cnt + r, n, qout, c->num_sms,
                                            c->stream);
@@ -1336,8 +1339,6 @@ int mc_run_fixed_source(mc_ctx* c, const mc_run_opts* o, mc_tally_out* out) {
       return fail(c, MC_ERR_STATE, "no trained surrogate (mc_train_surrogate)");
     if (o->thermal == MC_THERMAL_GUIDED && c->guide_tsl < 0)
       return fail(c, MC_ERR_STATE, "no trained guide network (mc_train_surrogate_guide)");
-    if (o->thermal != MC_THERMAL_SURROGATE && !rp.fast)
-      return fail(c, MC_ERR_INPUT, "the POD-exact thermal queue stands in for the FP32 POD sampler: set fast_math");
     if (o->thermal != MC_THERMAL_SURROGATE && c->dw.n_tsl == 0)
       return fail(c, MC_ERR_INPUT, "the problem has no thermal scattering library");
     if (!c->model.perturbations.empty())

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
               const GuideOut go = rp.tq_res[qi];
               p.rng.restore(rp.run_key, R.rng_id, R.rng_tag, go.rng_pos);
               if (go.ok) {
-                tsl_apply<true>(tl, p.rng, R.T, go.beta, go.alpha, p.E, p.u, p.v, p.w);
+                if (rp.tq_fast) tsl_apply<true>(tl, p.rng, R.T, go.beta, go.alpha, p.E, p.u, p.v, p.w);
+                else tsl_apply<false>(tl, p.rng, R.T, go.beta, go.alpha, p.E, p.u, p.v, p.w);
                 ok = true;
               }
             }
@@ -381,11 +382,12 @@ __global__ void __launch_bounds__(256, MINB) k_history_ce(const DevWorld w, cons
               // reference throws, here the history ends and is counted
               const DevTSL& tl = w.tsl[d.rx_tsl[r]];
               if constexpr (TQ) {
-                // the POD-exact forms (modes 2, 3) stand in for the FP32 POD
-                // sampler only, and need no trained box
+                // the POD-exact forms (modes 2, 3) sample what the inline
+                // sampler below would (the FP32 form when ffg and the
+                // library allow it, else FP64) and need no trained box
                 const bool exact_q = rp.tq_mode >= 2;
                 if (rp.tq && d.rx_tsl[r] == rp.tq_tsl && sp == 0 && pend.n <= kParkPending &&
-                    (exact_q ? (ffg && tl.fast_ok)
+                    (exact_q ? ((ffg && tl.fast_ok) == (rp.tq_fast != 0))
                              : (p.E >= rp.tq_box[0] && p.E <= rp.tq_box[1] && T >= rp.tq_box[2] &&
                                 T <= rp.tq_box[3]))) {
                   // park for the batched surrogate sampler

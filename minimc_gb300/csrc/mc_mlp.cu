@@ -1228,6 +1228,7 @@ __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView
 
 // the POD sampler on the same queue, without the network (the ablation of
 // the guided form: same batching, find_cdf by plain bisection)
+template <bool FAST>
 __global__ void __launch_bounds__(256) k_pod_queue(const DevTSL* tsl, const GuideRow* rows,
                                                    const unsigned long long* qcount, unsigned long long qcap,
                                                    unsigned long long run_key, GuideOut* qout) {
@@ -1238,7 +1239,8 @@ __global__ void __launch_bounds__(256) k_pod_queue(const DevTSL* tsl, const Guid
     PhiloxRng rng;
     rng.restore(run_key, R.rng_id, R.rng_tag, R.rng_pos);
     double b = 0, a = 0;
-    const bool ok = tsl_sample_beta<true>(*tsl, rng, R.E, R.T, b) && tsl_sample_alpha<true>(*tsl, rng, b, R.E, R.T, a);
+    const bool ok =
+        tsl_sample_beta<FAST>(*tsl, rng, R.E, R.T, b) && tsl_sample_alpha<FAST>(*tsl, rng, b, R.E, R.T, a);
     GuideOut o;
     o.beta = ok ? b : CUDART_NAN;
     o.alpha = ok ? a : CUDART_NAN;
@@ -1293,12 +1295,12 @@ cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, con
   return cudaGetLastError();
 }
 
-cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box,
+cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, bool fast,
                                            const GuideRow* rows, const unsigned long long* count,
                                            unsigned long long cap, unsigned long long run_key, GuideOut* out,
                                            int num_sms, cudaStream_t s) {
   if (cap == 0) return cudaSuccess;
-  cudaError_t e = guided_attr<true, true>();
+  cudaError_t e = fast ? guided_attr<true, true>() : guided_attr<true, false>();
   if (e != cudaSuccess) return e;
   NetView nv{guide.p, guide.W1, guide.W2, guide.W3};
   GuideIO io{};
@@ -1309,15 +1311,17 @@ cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guid
   io.run_key = run_key;
   io.qout = out;
   // the row count is known on the device only: one persistent CTA per SM
-  k_guided_sample<true, true><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  if (fast) k_guided_sample<true, true><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
+  else k_guided_sample<true, false><<<num_sms, 128 * kGuideGroups, kGuideSmem, s>>>(nv, box, io, mlp_err_ptr());
   return cudaGetLastError();
 }
 
-cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, const GuideRow* rows, const unsigned long long* count,
-                                        unsigned long long cap, unsigned long long run_key, GuideOut* out,
-                                        int num_sms, cudaStream_t s) {
+cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, bool fast, const GuideRow* rows,
+                                        const unsigned long long* count, unsigned long long cap,
+                                        unsigned long long run_key, GuideOut* out, int num_sms, cudaStream_t s) {
   if (cap == 0) return cudaSuccess;
-  k_pod_queue<<<num_sms * 8, 256, 0, s>>>(tsl, rows, count, cap, run_key, out);
+  if (fast) k_pod_queue<true><<<num_sms * 8, 256, 0, s>>>(tsl, rows, count, cap, run_key, out);
+  else k_pod_queue<false><<<num_sms * 8, 256, 0, s>>>(tsl, rows, count, cap, run_key, out);
   return cudaGetLastError();
 }
 

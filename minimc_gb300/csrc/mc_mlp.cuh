@@ -126,15 +126,16 @@ cudaError_t launch_sample_tsl_guided(const DevTSL* tsl, const MlpNet& guide, con
                                      const double* E, const double* T, unsigned long long n, unsigned long long key,
                                      double* beta, double* alpha, unsigned long long* failures, int num_sms,
                                      cudaStream_t s);
-// queue form: parked rows, *count of them (at most cap, read on the device)
-cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box,
+// queue form: parked rows, *count of them (at most cap, read on the device);
+// fast: the FP32 POD form, else the exact (FP64) one
+cudaError_t launch_sample_tsl_guided_queue(const DevTSL* tsl, const MlpNet& guide, const MlpBox& box, bool fast,
                                            const GuideRow* rows, const unsigned long long* count,
                                            unsigned long long cap, unsigned long long run_key, GuideOut* out,
                                            int num_sms, cudaStream_t s);
 // the POD sampler over the same queue, bisection without the network
-cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, const GuideRow* rows, const unsigned long long* count,
-                                        unsigned long long cap, unsigned long long run_key, GuideOut* out,
-                                        int num_sms, cudaStream_t s);
+cudaError_t launch_sample_tsl_pod_queue(const DevTSL* tsl, bool fast, const GuideRow* rows,
+                                        const unsigned long long* count, unsigned long long cap,
+                                        unsigned long long run_key, GuideOut* out, int num_sms, cudaStream_t s);
 // per-condition sort of K samples (K a power of two <= 1024) in place
 cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K, cudaStream_t s);
 // gathers a random batch (Philox key, step) of B rows of X / y into the

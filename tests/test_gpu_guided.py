@@ -123,6 +123,24 @@ def test_guided_transport_is_pod_transport(ctx1):
     assert gui.raw.launches > pod.raw.launches
 
 
+def test_guided_transport_exact_form_is_pod_transport(ctx1):
+    """The exact (FP64) form throughout (fast_math off): the guided queue and
+    the plain POD queue give every history the inline exact POD sampler's
+    events and fate, tallies to summation order."""
+    ctx, _ = ctx1
+    n = 200_000
+    kw = dict(rng=RNG_PHILOX, fast_math=0, histories=n, seed=7, per_history=True)
+    pod = ctx.run_fixed_source(thermal=THERMAL_POD, **kw)
+    gui = ctx.run_fixed_source(thermal=THERMAL_GUIDED, **kw)
+    que = ctx.run_fixed_source(thermal=THERMAL_POD_QUEUE, **kw)
+    for r in (gui, que):
+        assert r.raw.lost == pod.raw.lost and r.raw.resample_failures == pod.raw.resample_failures
+        assert np.array_equal(r.history_events, pod.history_events)
+        assert np.array_equal(r.history_fate, pod.history_fate)
+        np.testing.assert_allclose(r.sum, pod.sum, rtol=SUM_RTOL, atol=0)
+    assert gui.raw.launches > pod.raw.launches
+
+
 def spectra(ctx, r):
     """Leakage energy and cosine marginals (counts) of the broomstick tally."""
     e = ctx.estimators()[0]
