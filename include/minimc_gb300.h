@@ -65,12 +65,13 @@ extern "C" {
 /* The guided sampler on the same queue: the trained guide network
  * (mc_train_surrogate_guide) predicts where SampleAlpha's CDF search ends,
  * the POD reconstructions confirm it, so every thermal scatter draws exactly
- * the FP32 POD sampler's (beta, alpha) from the particle's own stream and the
- * transport gives the same histories as MC_THERMAL_POD with fast_math, for
- * less work (Philox streams, fast_math, continuous energy). */
+ * the POD sampler's (beta, alpha) from the particle's own stream -- its FP32
+ * form with fast_math, its exact FP64 form without -- and the transport
+ * gives the same histories as MC_THERMAL_POD, for less work (Philox
+ * streams, continuous energy). */
 #define MC_THERMAL_GUIDED 2
-/* The FP32 POD sampler run as a batched launch over the same queue, without
- * the network (the guided form's ablation; same histories). */
+/* The POD sampler run as a batched launch over the same queue, without the
+ * network (the guided form's ablation; same histories). */
 #define MC_THERMAL_POD_QUEUE 3
 
 /* How the event loop is scheduled on the device. */
