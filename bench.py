@@ -7,9 +7,11 @@ continuous-energy plain method instead: three synthetic nuclides on 5e4-point
 log grids (1/v capture, 200 SLBW resonances, potential scattering), free-gas
 scattering at 293.6 K, a homogeneous mixture in a reflected 40 cm box,
 1e6 histories per cycle.  A step is one active k-eigenvalue
-cycle: transport of 1e6 source particles, fission-bank compaction and
-resampling of the next source.  ``value`` times the steps with CUDA events
-on the engine's stream, with the bank resident in HBM; ``e2e`` times the
+cycle: transport of 1e6 source particles (each drawn from the previous
+cycle's bank), fission-bank sites and their prefix sum, k of the cycle.
+``value`` times the K steps with CUDA events on the engine's stream around
+one mc_keig_cycles call (one host synchronisation, k per cycle returned),
+with the bank resident in HBM; ``e2e`` times the
 same workload through the C ABI's host-buffer call (mc_transport_bank), with
 the source copied in from pinned host memory and the fission bank copied
 back every step.
@@ -227,21 +229,23 @@ def run_gpu(args) -> None:
     st0 = ctx.keig_status()
     clocks = ClockSampler(local)
     clocks.start()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    k_steps = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.zero_()  # L2 flushed before the timed cycles (outside the event pair)
     barrier()
     t_wall = time.perf_counter()
-    for i in range(args.steps):
-        ev[i][0].record(stream)
-        k_steps.append(ctx.keig_cycle(True))
-        ev[i][1].record(stream)
-        flush.zero_()  # L2 flush between timed steps (outside the event pair)
+    # the K active cycles in one call: each cycle transports the sources it
+    # draws from the previous cycle's bank, with one host synchronisation
+    # at the end (mc_keig_cycles); a cycle streams its ~310 MB working set
+    # (source bank 64 MB, fission records 64 MB, per-history scores 128 MB,
+    # bank written 57 MB) through the 129 MB L2
+    e0.record(stream)
+    k_steps = [float(k) for k in ctx.keig_cycles(args.steps, True)]
+    e1.record(stream)
     barrier()
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     st1 = ctx.keig_status()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
+    total_ms = e0.elapsed_time(e1)
     sched = ctx.schedule_info()
     k_out = ctx.keig_end()
     events = st1.events - st0.events
@@ -331,7 +335,12 @@ def run_gpu(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOADS[args.workload], "histories_per_cycle": hist, **wl["config"],
                        "rng": "philox",
-                       "fast_math": bool(args.fast), "l2": "flushed between steps (256 MB write)",
+                       "fast_math": bool(args.fast),
+                       "l2": "flushed (256 MB write) before the timed cycles; inside them each cycle's working set "
+                             "(~310 MB: source bank, fission records, per-history scores, bank written) is larger "
+                             "than L2",
+                       "timed": "the K active cycles through one mc_keig_cycles call (one host synchronisation; "
+                                "k per cycle returned)",
                        "parallelism": f"replicas{ws}" if ws > 1 else "single GPU",
                        "schedule": sched},
             "k_cycles": [round(k, 6) for k in k_steps],

@@ -245,6 +245,13 @@ int mc_run_keigenvalue(mc_ctx* ctx, const mc_run_opts* opts, mc_keig_out* out);
  * fills out. */
 int mc_keig_begin(mc_ctx* ctx, const mc_run_opts* opts);
 int mc_keig_cycle(mc_ctx* ctx, int32_t active, double* k);
+/* n cycles (all active or all inactive) with one host synchronisation at
+ * the end: each cycle's bank size, k and counters stay on the device until
+ * then, and each cycle draws its sources from the previous bank in place.
+ * The same k per cycle and tallies as n calls of mc_keig_cycle; k (NULL or
+ * n values) receives them.  The first cycle and an autotuning cycle run on
+ * their own. */
+int mc_keig_cycles(mc_ctx* ctx, uint32_t n, int32_t active, double* k);
 int mc_keig_end(mc_ctx* ctx, mc_keig_out* out);
 /* Running totals of the cycles run so far (events, transport_ms, launches,
  * counters); k_cycle/bank_size/sum/sum_sq are filled when non-NULL. */

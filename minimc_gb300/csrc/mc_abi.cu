@@ -58,6 +58,7 @@ enum ScratchSlot {
   kTqRes,
   kGroupRows,     // thermal group transfer: rows, bounds, counts
   kGroupSamples,  // thermal group transfer: one chunk's samples
+  kCycleRec,      // mc_keig_cycles: per-cycle records and counters
   kScratchSlots,  // number of slots
 };
 
@@ -86,6 +87,7 @@ struct mc_ctx {
   double* d_sum = nullptr;
   double* d_sq = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  std::vector<cudaEvent_t> ev_pool;  // per-cycle timing events of mc_keig_cycles
   // second stream: the dense-score commit overlaps the bank kernels there
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -1177,6 +1179,7 @@ void mc_destroy(mc_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->evk0) cudaEventDestroy(c->evk0);
   if (c->evk1) cudaEventDestroy(c->evk1);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->h_small) cudaFreeHost(c->h_small);
   if (c->side) {
     cudaStreamSynchronize(c->side);
@@ -1428,8 +1431,11 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   return MC_OK;
 }
 
-int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
-  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
+}  // extern "C"
+
+namespace {
+// the run parameters of the k-eigenvalue cycle about to run
+RunParams keig_params(mc_ctx* c, int32_t active) {
   auto& k = c->keig;
   RunParams rp{};
   rp.n = k.n;
@@ -1453,10 +1459,25 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   rp.bank = static_cast<Site*>(c->scratch[kSlots].p);
   rp.bank_count = static_cast<uint32_t*>(c->scratch[kCount].p);
   rp.direct_sites = bank_direct(c, k.rng, k.fast != 0, k.bank_path) > 0 ? 1 : 0;
+  return rp;
+}
+
+// the autotuner runs in this cycle
+bool keig_tunes(const mc_ctx* c, int32_t active) {
+  return !active && c->tune_pending && (c->keig.cycle >= 1 || c->keig.inactive < 2);
+}
+}  // namespace
+
+extern "C" {
+
+int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
+  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
+  auto& k = c->keig;
+  RunParams rp = keig_params(c, active);
   // the autotuner waits for the second inactive cycle when there is one:
   // the first cycle's source (Source::Sample) is not yet the fission
   // source the later cycles transport
-  if (!active && c->tune_pending && (k.cycle >= 1 || k.inactive < 2)) {
+  if (keig_tunes(c, active)) {
     // Autotuner: every candidate transports this (inactive, unscored)
     // cycle, twice, interleaved, keeping each candidate's shorter time of
     // its transport kernels.  Candidates: the history schedule's occupancy
@@ -1536,6 +1557,93 @@ int mc_keig_cycle(mc_ctx* c, int32_t active, double* kout) {
   k.src_key = run_key(k.seed, k.cycle, 0x52455341ull);
   k.cycle++;
   return counters_status(c, h);
+}
+
+int mc_keig_cycles(mc_ctx* c, uint32_t ncyc, int32_t active, double* kout) {
+  if (!check_ctx(c) || !c->keig.active) return fail(c, MC_ERR_STATE, "mc_keig_begin not called");
+  auto& k = c->keig;
+  uint32_t done = 0;
+  int status = MC_OK;  // the first non-fatal status (lost, overflow, cap, resample) of the cycles run
+  // the first cycle (its source is Source::Sample's) and a tuning cycle run
+  // on their own
+  while (done < ncyc && (k.cycle == 0 || keig_tunes(c, active))) {
+    const int rc = mc_keig_cycle(c, active, kout ? kout + done : nullptr);
+    if (rc == MC_ERR_DEVICE || rc == MC_ERR_OOM || rc == MC_ERR_STATE || rc == MC_ERR_INPUT) return rc;
+    if (rc != MC_OK && status == MC_OK) status = rc;
+    done++;
+  }
+  const uint32_t m = ncyc - done;
+  if (m == 0) return status;
+  if (k.rng != MC_RNG_PHILOX && k.rng != MC_RNG_MINSTD) return fail(c, MC_ERR_STATE, "unknown rng mode");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  // per cycle (k, M, k_tracklength), then the counters of all m cycles
+  const size_t rec_bytes = 3 * sizeof(double) * m;
+  auto* rec = static_cast<double*>(scratch(c, kCycleRec, rec_bytes + sizeof(DevCounters)));
+  if (!rec) return fail(c, MC_ERR_OOM, "cycle records");
+  auto* acc = reinterpret_cast<DevCounters*>(reinterpret_cast<char*>(rec) + rec_bytes);
+  CUDA_TRY(c, cudaMemsetAsync(acc, 0, sizeof(DevCounters), c->stream));
+  while (c->ev_pool.size() < 4 * static_cast<size_t>(m)) {
+    cudaEvent_t e = nullptr;
+    CUDA_TRY(c, cudaEventCreate(&e));
+    c->ev_pool.push_back(e);
+  }
+  cudaEvent_t keep[4] = {c->ev0, c->ev1, c->evk0, c->evk1};
+  auto restore = [&]() {
+    c->ev0 = keep[0];
+    c->ev1 = keep[1];
+    c->evk0 = keep[2];
+    c->evk1 = keep[3];
+  };
+  for (uint32_t i = 0; i < m; i++) {
+    RunParams rp = keig_params(c, active);
+    // this cycle's timing events (read after the one synchronisation)
+    c->ev0 = c->ev_pool[4 * i];
+    c->ev1 = c->ev_pool[4 * i + 1];
+    c->evk0 = c->ev_pool[4 * i + 2];
+    c->evk1 = c->ev_pool[4 * i + 3];
+    int rc = run_transport(c, rp, k.rng, k.block, nullptr, k.schedule, /*side_commit=*/true);
+    restore();
+    if (rc != MC_OK) return rc;
+    k.src_pending = false;
+    Site* bank = nullptr;
+    uint64_t mm = 0;
+    rc = emit_bank(c, rp, k.rng, nullptr, 0, &bank, &mm, /*read_size=*/false);
+    if (rc != MC_OK) return rc;
+    if (bank != c->scratch[kBank].p) return fail(c, MC_ERR_STATE, "fission bank outside its buffer");
+    CUDA_TRY(c, mcd::launch_keig_record(c->d_ctr, c->d_total, k.n, rec + 3 * i, acc, c->stream));
+    c->launches++;
+    // the next cycle draws its sources from this bank (an empty bank is
+    // reported below; the next transport then reads only entry 0)
+    k.src_pending = true;
+    k.src_key = run_key(k.seed, k.cycle, 0x52455341ull);
+    k.cycle++;
+  }
+  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
+  std::vector<double> h(3 * static_cast<size_t>(m));
+  DevCounters tot{};
+  CUDA_TRY(c, cudaMemcpyAsync(h.data(), rec, rec_bytes, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(&tot, acc, sizeof tot, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t i = 0; i < m; i++) {
+    float f = 0;
+    CUDA_TRY(c, cudaEventElapsedTime(&f, c->ev_pool[4 * i], c->ev_pool[4 * i + 1]));
+    k.transport_ms += f;
+    CUDA_TRY(c, cudaEventElapsedTime(&f, c->ev_pool[4 * i + 2], c->ev_pool[4 * i + 3]));
+    c->last_kernel_ms = f;
+    k.kernel_ms += f;
+    k.k.push_back(h[3 * i]);
+    k.bank.push_back(static_cast<uint64_t>(h[3 * i + 1]));
+    k.ktl.push_back(h[3 * i + 2]);
+    if (kout) kout[done + i] = h[3 * i];
+    if (h[3 * i + 1] == 0) break;  // the source died out: later cycles are void
+  }
+  k.events += tot.events;
+  k.lost += tot.lost;
+  k.capped += tot.capped;
+  k.overflow += tot.overflow;
+  if (tot.next) return fail(c, MC_ERR_INPUT, "fission bank is empty: the source died out");
+  if (status != MC_OK) return status;
+  return counters_status(c, tot);
 }
 
 int mc_keig_status(mc_ctx* c, mc_keig_out* out) {
@@ -1747,10 +1855,13 @@ int mc_keig_resume(mc_ctx* c, const void* buf, uint64_t size) {
 int mc_run_keigenvalue(mc_ctx* c, const mc_run_opts* o, mc_keig_out* out) {
   int rc = mc_keig_begin(c, o);
   if (rc != MC_OK) return rc;
-  const uint32_t total = c->keig.inactive + c->keig.act;
   int status = MC_OK;
-  for (uint32_t i = 0; i < total; i++) {
-    rc = mc_keig_cycle(c, i >= c->keig.inactive ? 1 : 0, nullptr);
+  // the inactive cycles, then the active ones, each phase with one host
+  // synchronisation (mc_keig_cycles)
+  for (int phase = 0; phase < 2; phase++) {
+    const uint32_t n = phase == 0 ? c->keig.inactive : c->keig.act;
+    if (n == 0) continue;
+    rc = mc_keig_cycles(c, n, phase, nullptr);
     if (rc == MC_ERR_DEVICE || rc == MC_ERR_OOM || rc == MC_ERR_STATE || (rc == MC_ERR_INPUT)) {
       mc_keig_end(c, out);
       return rc;

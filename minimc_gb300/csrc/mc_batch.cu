@@ -73,6 +73,28 @@ __global__ void k_batch_resample(const BatchCycle b, const Site* bank, Site* nex
 
 __global__ void k_batch_next_cycle(const BatchCycle b) { *b.cycle += 1; }
 
+__global__ void k_keig_record(const DevCounters* ctr, const unsigned long long* total, unsigned long long n,
+                              double* out, DevCounters* acc) {
+  const DevCounters& c = *ctr;
+  const unsigned long long m = *total;
+  out[0] = static_cast<double>(m) / static_cast<double>(n);
+  out[1] = static_cast<double>(m);
+  out[2] = c.k_tracklength / static_cast<double>(n);
+  if (c.lost && !acc->lost) {
+    for (int i = 0; i < 3; i++) acc->lost_xyz[i] = c.lost_xyz[i];
+    for (int i = 0; i < 4; i++) acc->pad[i] = c.pad[i];
+  }
+  acc->events += c.events;
+  acc->secondaries += c.secondaries;
+  acc->lost += c.lost;
+  acc->capped += c.capped;
+  acc->overflow += c.overflow;
+  acc->resample += c.resample;
+  acc->banked += c.banked;
+  acc->k_tracklength += c.k_tracklength;
+  if (m == 0) acc->next = 1;  // a cycle's bank came out empty
+}
+
 unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
 
 }  // namespace
@@ -85,6 +107,12 @@ cudaError_t launch_batch_begin(const BatchCycle& b, const Site* src, cudaStream_
 cudaError_t launch_batch_tally(const BatchCycle& b, const unsigned long long* offsets,
                                const unsigned long long* total, cudaStream_t s) {
   k_batch_tally<<<blocks_for(b.P), 256, 0, s>>>(b, offsets, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_keig_record(const DevCounters* ctr, const unsigned long long* total, unsigned long long n,
+                               double* out, DevCounters* acc, cudaStream_t stream) {
+  k_keig_record<<<1, 1, 0, stream>>>(ctr, total, n, out, acc);
   return cudaGetLastError();
 }
 

@@ -151,6 +151,7 @@ _SIGNATURES = {
     "mc_run_keigenvalue": (C.c_int, [_P, C.POINTER(RunOpts), C.POINTER(KeigOut)]),
     "mc_keig_begin": (C.c_int, [_P, C.POINTER(RunOpts)]),
     "mc_keig_cycle": (C.c_int, [_P, C.c_int32, _D]),
+    "mc_keig_cycles": (C.c_int, [_P, C.c_uint32, C.c_int32, _D]),
     "mc_keig_end": (C.c_int, [_P, C.POINTER(KeigOut)]),
     "mc_keig_status": (C.c_int, [_P, C.POINTER(KeigOut)]),
     "mc_keig_checkpoint": (C.c_int, [_P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -367,6 +368,12 @@ class Context:
         k = C.c_double()
         self.check(self.lib.mc_keig_cycle(self.h, int(active), C.byref(k)))
         return k.value
+
+    def keig_cycles(self, n: int, active: bool) -> np.ndarray:
+        """n cycles with one synchronisation (mc_keig_cycles): k per cycle."""
+        k = np.zeros(max(1, n))
+        self.check(self.lib.mc_keig_cycles(self.h, n, int(active), _dptr(k)))
+        return k[:n]
 
     def keig_status(self) -> KeigOut:
         out = KeigOut()

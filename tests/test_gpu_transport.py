@@ -359,3 +359,42 @@ def test_bank_direct_path_rejected_where_counts_are_unknown(built_library):
     assert np.array_equal(a.bank_size, b.bank_size)
     r = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=0)
     assert (np.asarray(r.bank_size) > 0).all()
+
+
+@pytest.mark.parametrize("rng,fast", [(RNG_PHILOX, 1), (RNG_MINSTD, 0)])
+def test_keig_cycles_equal_cycle_by_cycle(rng, fast, built_library):
+    """mc_keig_cycles (one synchronisation for many cycles, bank sizes and k
+    kept on the device, sources drawn from the bank in place) gives the
+    cycle-by-cycle loop's k per cycle, bank sizes and tallies, with both
+    stream kinds (Philox: direct bank path; minstd: slots)."""
+    xml = synth.two_zone_cubes(histories=40_000, inactive=3, active=4).xml()
+    a, b = gpu_ctx(xml), gpu_ctx(xml)
+    for ctx in (a, b):
+        ctx.keig_begin(rng=rng, fast_math=fast, variant=2)
+    ka = [a.keig_cycle(False) for _ in range(3)] + [a.keig_cycle(True) for _ in range(4)]
+    kb = list(b.keig_cycles(3, False)) + list(b.keig_cycles(4, True))
+    assert ka == kb
+    oa, ob = a.keig_status(), b.keig_status()
+    assert oa.events == ob.events
+    ra, rb = a.keig_end(), b.keig_end()
+    assert ra.k_mean == rb.k_mean and ra.k_std == rb.k_std
+
+
+def test_run_keigenvalue_uses_cycles_and_checkpoint(built_library, tmp_path):
+    """The full-run call (inactive and active phases through mc_keig_cycles)
+    equals the cycle-by-cycle loop; a checkpoint taken after cycles run in
+    one call writes the pending source out and resumes to the same k."""
+    xml = synth.two_zone_cubes(histories=30_000, inactive=2, active=3).xml()
+    a = gpu_ctx(xml)
+    r = a.run_keigenvalue(rng=RNG_PHILOX, fast_math=1, variant=2)
+    b = gpu_ctx(xml)
+    b.keig_begin(rng=RNG_PHILOX, fast_math=1, variant=2)
+    kb = [b.keig_cycle(i >= 2) for i in range(5)]
+    assert list(r.k_cycle) == kb
+    c = gpu_ctx(xml)
+    c.keig_begin(rng=RNG_PHILOX, fast_math=1, variant=2)
+    c.keig_cycles(2, False)
+    blob = c.keig_checkpoint()
+    d = gpu_ctx(xml)
+    d.keig_resume(blob)
+    assert list(d.keig_cycles(3, True)) == kb[2:]
