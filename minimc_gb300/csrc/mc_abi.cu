@@ -521,7 +521,17 @@ int build_world(mc_ctx* c) {
       return o;
     };
     const std::vector<float> msig_f = f32(msig), mtot_f = f32(mtot), mcdf_f = f32(mcdf), total_f = f32(total),
-                             rx_f = f32(rx), scat_f = f32(scat), nubar_f = f32(nubar);
+                             nubar_f = f32(nubar);
+    // the reaction and outgoing-group cdfs as 16-byte aligned rows padded
+    // to a multiple of 4 entries with -1 (never above a threshold), read
+    // 4 entries per load by the fast form's searches
+    const size_t G4 = (G + 3) / 4, rows = rx.size() / 3;
+    w.G4 = static_cast<int32_t>(G4);
+    std::vector<float> rx_f(rows * 4, -1.0f), scat_f(rows * 4 * G4, -1.0f);
+    for (size_t i = 0; i < rows; i++) {
+      for (size_t r = 0; r < 3; r++) rx_f[4 * i + r] = static_cast<float>(rx[3 * i + r]);
+      for (size_t go = 0; go < G; go++) scat_f[4 * G4 * i + go] = static_cast<float>(scat[G * i + go]);
+    }
     UP(msig_f, mat_mg_sigma_f)
     UP(mtot_f, mat_mg_total_f)
     UP(mcdf_f, mat_mg_nuc_cdf_f)

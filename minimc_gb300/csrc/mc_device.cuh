@@ -160,6 +160,7 @@ constexpr int kMaxSens = 4;  // sensitivities per estimator
 struct DevWorld {
   int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
   int32_t energy_mode, tracking, quirks, G, max_mat_nuc;
+  int32_t G4;  // 16-byte chunks per row of the FP32 scatter cdfs (G padded to a multiple of 4)
   // surfaces
   const int32_t* surf_kind;
   const int32_t* surf_refl;
@@ -217,8 +218,8 @@ struct DevWorld {
   const float* mat_mg_total_f;    // [T][M][G]
   const float* mat_mg_nuc_cdf_f;  // [T][M][G][max_mat_nuc]
   const float* mg_total_f;        // [T][N][G]
-  const float* mg_rx_cdf_f;       // [T][N][G][3]
-  const float* mg_scat_cdf_f;     // [T][N][G][G]
+  const float* mg_rx_cdf_f;       // [T][N][G][4], the fourth entry a negative pad
+  const float* mg_scat_cdf_f;     // [T][N][G][4 G4], padded with negative entries
   const float* mg_nubar_f;        // [T][N][G]
   DevCE ce;                       // continuous energy
   int32_t n_tsl;
@@ -740,6 +741,33 @@ __device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, d
 // exponential flight length in FP32: -log(U) / sigma (U in (0,1))
 __device__ __forceinline__ double flight_fast(float u, double sigma) {
   return static_cast<double>(__fdiv_rn(-__logf(u), __double2float_rn(sigma)));
+}
+
+// The same on a 16-byte aligned FP32 row of n4 chunks of 4 entries, padded
+// past its end with negative values (which never exceed a non-negative
+// threshold): the chunks are read as 16-byte words, the first two before
+// any comparison, so a row of up to 8 entries costs one dependent load.
+__device__ __forceinline__ int cdf_first_above_f4(const float* row, int n4, float threshold) {
+  const int t = __float_as_int(threshold);
+  const int4* r = reinterpret_cast<const int4*>(row);
+  const int4 a = __ldg(r);
+  const int4 b = n4 > 1 ? __ldg(r + 1) : make_int4(-1, -1, -1, -1);
+  if (a.x > t) return 0;
+  if (a.y > t) return 1;
+  if (a.z > t) return 2;
+  if (a.w > t) return 3;
+  if (b.x > t) return 4;
+  if (b.y > t) return 5;
+  if (b.z > t) return 6;
+  if (b.w > t) return 7;
+  for (int q = 2; q < n4; q++) {
+    const int4 v = __ldg(r + q);
+    if (v.x > t) return 4 * q;
+    if (v.y > t) return 4 * q + 1;
+    if (v.z > t) return 4 * q + 2;
+    if (v.w > t) return 4 * q + 3;
+  }
+  return -1;
 }
 
 // the same on an FP32 table (fast form)
