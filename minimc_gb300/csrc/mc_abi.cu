@@ -521,17 +521,7 @@ int build_world(mc_ctx* c) {
       return o;
     };
     const std::vector<float> msig_f = f32(msig), mtot_f = f32(mtot), mcdf_f = f32(mcdf), total_f = f32(total),
-                             nubar_f = f32(nubar);
-    // the reaction and outgoing-group cdfs as 16-byte aligned rows padded
-    // to a multiple of 4 entries with -1 (never above a threshold), read
-    // 4 entries per load by the fast form's searches
-    const size_t G4 = (G + 3) / 4, rows = rx.size() / 3;
-    w.G4 = static_cast<int32_t>(G4);
-    std::vector<float> rx_f(rows * 4, -1.0f), scat_f(rows * 4 * G4, -1.0f);
-    for (size_t i = 0; i < rows; i++) {
-      for (size_t r = 0; r < 3; r++) rx_f[4 * i + r] = static_cast<float>(rx[3 * i + r]);
-      for (size_t go = 0; go < G; go++) scat_f[4 * G4 * i + go] = static_cast<float>(scat[G * i + go]);
-    }
+                             rx_f = f32(rx), scat_f = f32(scat), nubar_f = f32(nubar);
     UP(msig_f, mat_mg_sigma_f)
     UP(mtot_f, mat_mg_total_f)
     UP(mcdf_f, mat_mg_nuc_cdf_f)
@@ -923,7 +913,6 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   const double* pend_before = c->pend_clean;
   c->pend_clean = nullptr;  // dirty until the commit has run
   CUDA_TRY(c, cudaEventRecord(c->evk0, c->stream));
-  rp.write_counts = 0;
   if (sched == MC_SCHEDULE_EVENT) {
     const int rc = run_event(c, rp, rng);
     if (rc != MC_OK) return rc;
@@ -938,9 +927,6 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     }
     else {
       cudaError_t e;
-      // the multigroup history kernel writes the direct path's site counts
-      rp.write_counts = keig && rp.direct_sites && c->model.energy_mode == mc::kMultigroup &&
-                        rp.bank_count == c->scratch[kCount].p;
       if (c->model.energy_mode == mc::kMultigroup)
         e = mcd::launch_history_mg(c->dw, rp, rng, grid, block, c->stream, c->variant);
       else e = mcd::launch_history_ce(c->dw, rp, rng, grid, block, c->stream, c->variant);
@@ -1082,8 +1068,7 @@ int materialize_source(mc_ctx* c) {
 // The cycle's fission sites as a compacted bank in history order.  Slot
 // path: the slot kernel has run; a scan of its counts places each history's
 // sites and a compaction copies them into the device bank.  Direct path:
-// counts from the fission records (written by the multigroup history kernel
-// itself, else by a count kernel), their scan, then the sites sampled
+// counts from the fission records, their scan, then the sites sampled
 // straight into `dest` (16-byte aligned page-locked host memory, `cap`
 // sites) or else into the device bank.  *bank_out is the device bank (null
 // when the sites went to `dest`); the size stays on the device (d_total,
@@ -1103,16 +1088,13 @@ int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap,
     RunParams q = rp;
     q.ctr = c->d_ctr;
     q.bank_count = count;
-    if (!(rp.write_counts && rp.bank_count == count)) {
-      CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
-      c->launches++;
-    }
+    CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
     CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
     const uint64_t qcap = dest ? cap : n * c->max_yield;
     if (c->model.energy_mode == mc::kMultigroup)
       CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, qcap, dest ? dest : bank, c->stream));
     else CUDA_TRY(c, mcd::launch_fission_sites_out_ce(q, rng, offsets, total, qcap, dest ? dest : bank, c->stream));
-    c->launches += 4;
+    c->launches += 5;
   }
   else {
     auto* slots = static_cast<Site*>(c->scratch[kSlots].p);

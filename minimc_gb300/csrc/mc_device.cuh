@@ -160,7 +160,6 @@ constexpr int kMaxSens = 4;  // sensitivities per estimator
 struct DevWorld {
   int32_t n_surfaces, n_cells, n_materials, n_nuclides, n_types;
   int32_t energy_mode, tracking, quirks, G, max_mat_nuc;
-  int32_t G4;  // 16-byte chunks per row of the FP32 scatter cdfs (G padded to a multiple of 4)
   // surfaces
   const int32_t* surf_kind;
   const int32_t* surf_refl;
@@ -218,8 +217,8 @@ struct DevWorld {
   const float* mat_mg_total_f;    // [T][M][G]
   const float* mat_mg_nuc_cdf_f;  // [T][M][G][max_mat_nuc]
   const float* mg_total_f;        // [T][N][G]
-  const float* mg_rx_cdf_f;       // [T][N][G][4], the fourth entry a negative pad
-  const float* mg_scat_cdf_f;     // [T][N][G][4 G4], padded with negative entries
+  const float* mg_rx_cdf_f;       // [T][N][G][3]
+  const float* mg_scat_cdf_f;     // [T][N][G][G]
   const float* mg_nubar_f;        // [T][N][G]
   DevCE ce;                       // continuous energy
   int32_t n_tsl;
@@ -537,10 +536,8 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
                                                    const double* dir, const float* dirf, double& dist, int skip,
                                                    bool fast_div) {
   const BoxCell& B = w.boxes[box];
-  // per axis: the plane ahead (3 bits each in `js`) and its FP32 distance;
-  // the FP64 differences c - p are formed again for the chosen plane only,
-  // so fewer values stay live through the selection
-  unsigned js = 0;
+  int cj[3];
+  double cv[3];
   float tf[3];
 #pragma unroll
   for (int a = 0; a < 3; a++) {
@@ -551,9 +548,10 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
     // the skipped surface reads as infinitely far; the axis' other plane
     // then is the only candidate
     if (__ldg(&B.s[j]) == skip) j ^= 1;
-    js |= static_cast<unsigned>(j) << (3 * a);
+    cj[a] = j;
     // PlaneX::Distance: v = c - p, positive iff v and d have the same sign
     const double v = dsub(__ldg(&B.c[j]), p);
+    cv[a] = v;
     const bool ahead = __ldg(&B.s[j]) != skip && ((dpos(v) && dpos(d)) || (dneg(v) && dneg(d)));
     tf[a] = ahead ? fabsf(__fdiv_rn(__double2float_rn(v), dirf[a])) : CUDART_INF_F;
   }
@@ -565,13 +563,11 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
   for (int a = 0; a < 3; a++)
     if (a != a0) second = fminf(second, tf[a]);
   if (tf[a0] < CUDART_INF_F && tf[a0] > 1e-30f && !(second <= __fmul_rn(tf[a0], 1.000004f))) {
-    const int j = (js >> (3 * a0)) & 7u;
-    const double v = dsub(__ldg(&B.c[j]), pos[a0]);
-    const double t = fast_div && fabsf(dirf[a0]) >= 1.17549435e-38f ? quot_nr(v, dir[a0], dirf[a0])
-                                                                    : ddiv(v, dir[a0]);
+    const double t = fast_div && fabsf(dirf[a0]) >= 1.17549435e-38f ? quot_nr(cv[a0], dir[a0], dirf[a0])
+                                                                    : ddiv(cv[a0], dir[a0]);
     if (t > 0 && t < CUDART_INF) {
       dist = t;
-      return __ldg(&B.s[j]);
+      return __ldg(&B.s[cj[a0]]);
     }
   }
   // exact path: every candidate divided, reference tie-breaking
@@ -580,12 +576,12 @@ __device__ __forceinline__ int nearest_surface_box(const DevWorld& w, int box, i
   double bd = CUDART_INF;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const int j = (js >> (3 * a)) & 7u;
+    const int j = cj[a];
     const int s = __ldg(&B.s[j]);
     const int o = __ldg(&B.order[j]);
     double t = CUDART_INF;
     if (s != skip) {
-      const double q = ddiv(dsub(__ldg(&B.c[j]), pos[a]), dir[a]);
+      const double q = ddiv(cv[a], dir[a]);
       t = q > 0 ? q : CUDART_INF;
     }
     if (t < bd || (t == bd && t != CUDART_INF && o < best_o)) {
@@ -741,33 +737,6 @@ __device__ __forceinline__ void isotropic_fast(Rng& rng, double& u, double& v, d
 // exponential flight length in FP32: -log(U) / sigma (U in (0,1))
 __device__ __forceinline__ double flight_fast(float u, double sigma) {
   return static_cast<double>(__fdiv_rn(-__logf(u), __double2float_rn(sigma)));
-}
-
-// The same on a 16-byte aligned FP32 row of n4 chunks of 4 entries, padded
-// past its end with negative values (which never exceed a non-negative
-// threshold): the chunks are read as 16-byte words, the first two before
-// any comparison, so a row of up to 8 entries costs one dependent load.
-__device__ __forceinline__ int cdf_first_above_f4(const float* row, int n4, float threshold) {
-  const int t = __float_as_int(threshold);
-  const int4* r = reinterpret_cast<const int4*>(row);
-  const int4 a = __ldg(r);
-  const int4 b = n4 > 1 ? __ldg(r + 1) : make_int4(-1, -1, -1, -1);
-  if (a.x > t) return 0;
-  if (a.y > t) return 1;
-  if (a.z > t) return 2;
-  if (a.w > t) return 3;
-  if (b.x > t) return 4;
-  if (b.y > t) return 5;
-  if (b.z > t) return 6;
-  if (b.w > t) return 7;
-  for (int q = 2; q < n4; q++) {
-    const int4 v = __ldg(r + q);
-    if (v.x > t) return 4 * q;
-    if (v.y > t) return 4 * q + 1;
-    if (v.z > t) return 4 * q + 2;
-    if (v.w > t) return 4 * q + 3;
-  }
-  return -1;
 }
 
 // the same on an FP32 table (fast form)

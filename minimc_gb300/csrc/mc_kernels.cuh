@@ -108,10 +108,6 @@ struct RunParams {
   const Site* resample_bank;
   const unsigned long long* resample_m;
   unsigned long long resample_key;
-  // k-eigenvalue direct path: the multigroup history kernel writes each
-  // history's site count, min(yield, max_yield), into bank_count as the
-  // history ends (no separate count kernel)
-  int32_t write_counts;
 };
 
 // KEigenvalue's next source, uniform over the bank: source j is bank entry
@@ -329,7 +325,7 @@ __device__ __forceinline__ int mg_pick_nuclide(const DevWorld& w, Rng& rng, bool
 template <class Rng>
 __device__ __forceinline__ int mg_pick_reaction(const DevWorld& w, Rng& rng, bool fast, size_t ng) {
   if constexpr (std::is_same_v<Rng, PhiloxRng>) {
-    if (fast) return cdf_first_above_f4(w.mg_rx_cdf_f + ng * 4, 1, __fmul_rn(rng.u01f(), __ldg(w.mg_total_f + ng)));
+    if (fast) return cdf_first_above_f(w.mg_rx_cdf_f + ng * 3, 3, __fmul_rn(rng.u01f(), __ldg(w.mg_total_f + ng)));
   }
   return cdf_first_above(w.mg_rx_cdf + ng * 3, 3, dmul(rng.u01(), __ldg(w.mg_total + ng)));
 }
@@ -338,7 +334,7 @@ __device__ __forceinline__ int mg_pick_reaction(const DevWorld& w, Rng& rng, boo
 template <class Rng>
 __device__ __forceinline__ int mg_pick_outgoing(const DevWorld& w, Rng& rng, bool fast, size_t ng) {
   if constexpr (std::is_same_v<Rng, PhiloxRng>) {
-    if (fast) return cdf_first_above_f4(w.mg_scat_cdf_f + ng * (4 * static_cast<size_t>(w.G4)), w.G4, rng.u01f());
+    if (fast) return cdf_first_above_f(w.mg_scat_cdf_f + ng * w.G, w.G, rng.u01f());
   }
   return cdf_first_above(w.mg_scat_cdf + ng * w.G, w.G, rng.u01());
 }

@@ -74,11 +74,9 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
   int sp = 0;
   bool alive = false, done = false;
   unsigned long long hist = 0;
-  // per-thread counts (a thread runs far fewer than 2^32 events)
-  uint32_t my_events = 0, my_lost = 0, my_capped = 0, my_overflow = 0, my_sec = 0;
+  unsigned long long my_events = 0, my_lost = 0, my_capped = 0, my_overflow = 0, my_sec = 0;
   double my_ktl = 0;
   uint32_t hist_nev = 0;
-  uint32_t hist_yield = 0;  // k-eigenvalue: this history's fission yield
   int8_t fate = 0;
   // a secondary did not fit the stack: the history's result is invalid
   // (reported as an overflow), so its remaining particles are dropped,
@@ -94,13 +92,6 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
     pend.clear();
     if (rp.hist_events) rp.hist_events[hist] = hist_nev;
     if (rp.hist_fate) rp.hist_fate[hist] = fate;
-    if constexpr (KEIG) {
-      if (rp.write_counts) {
-        // the count kernel's rule: sites past max_yield are dropped and counted
-        rp.bank_count[hist] = hist_yield < rp.max_yield ? hist_yield : rp.max_yield;
-        if (hist_yield > rp.max_yield) my_overflow += hist_yield - rp.max_yield;
-      }
-    }
   };
 
   for (;;) {
@@ -130,7 +121,6 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           p.nev = 0;
           reset_indirect<PERT>(p);
           hist_nev = 0;
-          hist_yield = 0;
           fate = kBirth;
           dropped = false;
           alive = true;
@@ -208,7 +198,6 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
             // record the fission; its sites are drawn by the sites kernel
             // from the stream position after the yield draw
             const unsigned yield = mg_yield(w, p.rng, fast, ng);
-            hist_yield = yield;
             FissionRec f;
             f.x = p.x;
             f.y = p.y;
@@ -338,11 +327,11 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
     my_ktl += __shfl_down_sync(0xffffffffu, my_ktl, off);
   }
   if (lane == 0) {
-    atomicAdd(&rp.ctr->events, static_cast<unsigned long long>(my_events));
-    if (my_lost) atomicAdd(&rp.ctr->lost, static_cast<unsigned long long>(my_lost));
-    if (my_capped) atomicAdd(&rp.ctr->capped, static_cast<unsigned long long>(my_capped));
-    if (my_overflow) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(my_overflow));
-    if (my_sec) atomicAdd(&rp.ctr->secondaries, static_cast<unsigned long long>(my_sec));
+    atomicAdd(&rp.ctr->events, my_events);
+    if (my_lost) atomicAdd(&rp.ctr->lost, my_lost);
+    if (my_capped) atomicAdd(&rp.ctr->capped, my_capped);
+    if (my_overflow) atomicAdd(&rp.ctr->overflow, my_overflow);
+    if (my_sec) atomicAdd(&rp.ctr->secondaries, my_sec);
     if (KEIG) atomicAdd(&rp.ctr->k_tracklength, my_ktl);
   }
   if (use_smem) {
