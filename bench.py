@@ -224,7 +224,9 @@ def run_gpu(args) -> None:
 
     # ---- device-resident cycles
     ctx.keig_begin(**opts)
-    k_warm = [ctx.keig_cycle(False) for _ in range(args.warmup)]
+    # warm-up through the same call as the timed cycles (the first cycle and
+    # the autotuner's cycle run on their own inside it)
+    k_warm = [float(k) for k in ctx.keig_cycles(args.warmup, False)]
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
     st0 = ctx.keig_status()
     clocks = ClockSampler(local)

@@ -1416,6 +1416,16 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
       !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
     return fail(c, MC_ERR_OOM, "k-eigenvalue bank allocation failed");
+  // mc_keig_cycles' per-cycle records and timing events for the longer of
+  // the two phases, so that its calls neither allocate nor create events
+  const uint32_t phase = std::max<uint32_t>({k.inactive, k.act, 1u});
+  if (!scratch(c, kCycleRec, 3 * sizeof(double) * phase + sizeof(DevCounters)))
+    return fail(c, MC_ERR_OOM, "cycle records");
+  while (c->ev_pool.size() < 4 * static_cast<size_t>(phase)) {
+    cudaEvent_t e = nullptr;
+    CUDA_TRY(c, cudaEventCreate(&e));
+    c->ev_pool.push_back(e);
+  }
   const size_t tb = std::max<uint64_t>(1, c->total_bins) * sizeof(double);
   CUDA_TRY(c, cudaMemsetAsync(c->d_sum, 0, tb, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(c->d_sq, 0, tb, c->stream));
