@@ -59,6 +59,7 @@ enum ScratchSlot {
   kGroupRows,     // thermal group transfer: rows, bounds, counts
   kGroupSamples,  // thermal group transfer: one chunk's samples
   kCycleRec,      // mc_keig_cycles: per-cycle records and counters
+  kEvPend2,       // second dense per-history score array (alternate runs)
   kScratchSlots,  // number of slots
 };
 
@@ -93,8 +94,15 @@ struct mc_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool side_pending = false;  // the main stream has not yet waited for ev_join
   double last_kernel_ms = 0;  // main transport kernel(s) of the last run_transport
-  const double* pend_clean = nullptr;  // dense score array known to be all zero
-  size_t pend_clean_bytes = 0;
+  // Two dense per-history score arrays (scratch kEvPend, kEvPend2) used by
+  // alternate scored runs, so that the commit of one run (side stream) can
+  // overlap the next run's transport: a run waits only for the commit that
+  // last read the array it is about to fill.  A commit zeroes what it reads.
+  int pend_next = 0;
+  bool pend_zero[2] = {false, false};  // known to be all zero (of pend_zero_bytes)
+  size_t pend_zero_bytes[2] = {0, 0};
+  cudaEvent_t ev_commit[2] = {nullptr, nullptr};
+  bool commit_pending[2] = {false, false};
   uint64_t launches = 0;
   // scratch, grown on demand
   DevBuffer scratch[kScratchSlots];
@@ -870,6 +878,7 @@ int join_side(mc_ctx* c) {
   if (c->side_pending) {
     CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     c->side_pending = false;
+    c->commit_pending[0] = c->commit_pending[1] = false;
   }
   return MC_OK;
 }
@@ -879,7 +888,22 @@ int join_side(mc_ctx* c) {
 // orders it before anything that reads the tallies or the score array.
 int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int schedule = MC_SCHEDULE_AUTO,
                   bool side_commit = false) {
-  if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
+  // dense per-history scores when the estimators are small (committed by
+  // a separate kernel: per-history sums kept in shared memory instead were
+  // measured slower, their commits contend on shared FP64 atomics)
+  const bool dense = rp.score && c->total_bins > 0 && c->total_bins <= static_cast<uint64_t>(mcd::kDenseBins);
+  const int pb = c->pend_next;
+  if (dense && side_commit) {
+    // only the commit that last read this run's score array must be done;
+    // the other array's commit may still run beside this transport
+    if (c->commit_pending[pb]) {
+      CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_commit[pb], 0));
+      c->commit_pending[pb] = false;
+    }
+  }
+  else if (join_side(c) != MC_OK) {
+    return MC_ERR_DEVICE;
+  }
   CUDA_TRY(c, cudaMemsetAsync(c->d_ctr, 0, sizeof(DevCounters), c->stream));
   rp.ctr = c->d_ctr;
   rp.tally_sum = c->d_sum;
@@ -889,29 +913,24 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
   const int sched = resolve_schedule(c, schedule);
   if (sched < 0) return fail(c, MC_ERR_INPUT, "the event schedule supports multigroup problems with at most 64 tally bins");
   c->last_schedule = sched;
-  // dense per-history scores when the estimators are small (committed by
-  // a separate kernel: per-history sums kept in shared memory instead were
-  // measured slower, their commits contend on shared FP64 atomics), fission
-  // records for k-eigenvalue cycles
+  // fission records for k-eigenvalue cycles
   const uint64_t n = rp.n;
-  rp.nb = (rp.score && c->total_bins > 0 && c->total_bins <= static_cast<uint64_t>(mcd::kDenseBins))
-              ? static_cast<int32_t>(c->total_bins)
-              : 0;
-  rp.pend = rp.nb ? static_cast<double*>(scratch(c, kEvPend, n * rp.nb * sizeof(double))) : nullptr;
+  rp.nb = dense ? static_cast<int32_t>(c->total_bins) : 0;
+  const int pslot = pb == 0 ? kEvPend : kEvPend2;
+  if (dense) c->pend_next = 1 - pb;
+  rp.pend = rp.nb ? static_cast<double*>(scratch(c, pslot, n * rp.nb * sizeof(double))) : nullptr;
   rp.fis = keig ? static_cast<mcd::FissionRec*>(scratch(c, kEvFis, n * sizeof(mcd::FissionRec))) : nullptr;
   if ((rp.nb && !rp.pend) || (keig && !rp.fis)) return fail(c, MC_ERR_OOM, "score/fission buffers");
   CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-  // the commit kernel zeroes what it reads, so the dense array only needs a
-  // memset when it is new or a previous run did not reach the commit
+  // the commit kernel zeroes what it reads, so a dense array only needs a
+  // memset when it is new or a previous run did not reach its commit
   const size_t pend_bytes = n * rp.nb * sizeof(double);
-  if (rp.pend && (rp.pend != c->pend_clean || c->pend_clean_bytes < pend_bytes)) {
-    const size_t all = c->scratch[kEvPend].bytes;
+  if (rp.pend && (!c->pend_zero[pb] || c->pend_zero_bytes[pb] < pend_bytes)) {
+    const size_t all = c->scratch[pslot].bytes;
     CUDA_TRY(c, cudaMemsetAsync(rp.pend, 0, all, c->stream));
-    c->pend_clean = rp.pend;
-    c->pend_clean_bytes = all;
+    c->pend_zero_bytes[pb] = all;
   }
-  const double* pend_before = c->pend_clean;
-  c->pend_clean = nullptr;  // dirty until the commit has run
+  if (rp.pend) c->pend_zero[pb] = false;  // dirty until the commit has run
   CUDA_TRY(c, cudaEventRecord(c->evk0, c->stream));
   if (sched == MC_SCHEDULE_EVENT) {
     const int rc = run_event(c, rp, rng);
@@ -950,12 +969,14 @@ int run_transport(mc_ctx* c, RunParams& rp, int rng, int block, double* ms, int 
     }
     CUDA_TRY(c, mcd::launch_commit_dense(rp, c->num_sms * 8, cs));
     c->launches++;
+    c->pend_zero[pb] = true;
     if (side_commit) {
+      CUDA_TRY(c, cudaEventRecord(c->ev_commit[pb], c->side));
+      c->commit_pending[pb] = true;
       CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
       c->side_pending = true;
     }
   }
-  c->pend_clean = pend_before;
   CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
   if (ms) {
     CUDA_TRY(c, cudaEventSynchronize(c->ev1));
@@ -1150,6 +1171,8 @@ int mc_create(mc_ctx** out, int device) {
   }
   cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->ev_commit[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->ev_commit[1], cudaEventDisableTiming);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
@@ -1179,6 +1202,8 @@ void mc_destroy(mc_ctx* c) {
   }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  for (cudaEvent_t e : c->ev_commit)
+    if (e) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1416,6 +1441,22 @@ int mc_keig_begin(mc_ctx* c, const mc_run_opts* o) {
   if (!scratch(c, kSrc, k.n * sizeof(Site)) || !scratch(c, kSlots, k.n * c->max_yield * sizeof(Site)) ||
       !scratch(c, kCount, k.n * 4) || !scratch(c, kOffsets, k.n * 8) || !scratch(c, kBank, k.n * c->max_yield * sizeof(Site)))
     return fail(c, MC_ERR_OOM, "k-eigenvalue bank allocation failed");
+  // the two dense per-history score arrays of the active cycles, zeroed
+  // here so that no cycle allocates
+  if (c->total_bins > 0 && c->total_bins <= static_cast<uint64_t>(mcd::kDenseBins)) {
+    for (int b = 0; b < 2; b++) {
+      const int slot = b == 0 ? kEvPend : kEvPend2;
+      const size_t bytes = k.n * c->total_bins * sizeof(double);
+      if (c->scratch[slot].bytes < bytes || !c->pend_zero[b]) {
+        if (join_side(c) != MC_OK) return MC_ERR_DEVICE;
+        void* pp = scratch(c, slot, bytes);
+        if (!pp) return fail(c, MC_ERR_OOM, "score buffers");
+        CUDA_TRY(c, cudaMemsetAsync(pp, 0, c->scratch[slot].bytes, c->stream));
+        c->pend_zero[b] = true;
+        c->pend_zero_bytes[b] = c->scratch[slot].bytes;
+      }
+    }
+  }
   // mc_keig_cycles' per-cycle records and timing events for the longer of
   // the two phases, so that its calls neither allocate nor create events
   const uint32_t phase = std::max<uint32_t>({k.inactive, k.act, 1u});

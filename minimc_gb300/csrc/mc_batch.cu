@@ -73,7 +73,7 @@ __global__ void k_batch_resample(const BatchCycle b, const Site* bank, Site* nex
 
 __global__ void k_batch_next_cycle(const BatchCycle b) { *b.cycle += 1; }
 
-__global__ void k_keig_record(const DevCounters* ctr, const unsigned long long* total, unsigned long long n,
+__global__ void k_keig_record(const DevCounters* ctr, unsigned long long* total, unsigned long long n,
                               double* out, DevCounters* acc) {
   const DevCounters& c = *ctr;
   const unsigned long long m = *total;
@@ -92,7 +92,10 @@ __global__ void k_keig_record(const DevCounters* ctr, const unsigned long long* 
   acc->resample += c.resample;
   acc->banked += c.banked;
   acc->k_tracklength += c.k_tracklength;
-  if (m == 0) acc->next = 1;  // a cycle's bank came out empty
+  if (m == 0) {  // a cycle's bank came out empty
+    acc->next = 1;
+    *total = 1;
+  }
 }
 
 unsigned blocks_for(unsigned long long n) { return static_cast<unsigned>((n + 255) / 256); }
@@ -110,7 +113,7 @@ cudaError_t launch_batch_tally(const BatchCycle& b, const unsigned long long* of
   return cudaGetLastError();
 }
 
-cudaError_t launch_keig_record(const DevCounters* ctr, const unsigned long long* total, unsigned long long n,
+cudaError_t launch_keig_record(const DevCounters* ctr, unsigned long long* total, unsigned long long n,
                                double* out, DevCounters* acc, cudaStream_t stream) {
   k_keig_record<<<1, 1, 0, stream>>>(ctr, total, n, out, acc);
   return cudaGetLastError();

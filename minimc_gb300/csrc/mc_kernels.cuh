@@ -122,13 +122,10 @@ __device__ __forceinline__ unsigned long long resample_index(unsigned long long 
   return idx < m ? idx : m - 1;
 }
 
-// source site i of a run from a bank (an empty bank -- a source that died
-// out, reported by the caller -- reads entry 0 and is never indexed past)
+// source site i of a run from a bank (*resample_m >= 1: callers never
+// resample an empty bank)
 __device__ __forceinline__ Site source_site(const RunParams& rp, unsigned long long i) {
-  if (rp.resample_m) {
-    const unsigned long long m = *rp.resample_m;
-    return rp.resample_bank[m ? resample_index(rp.resample_key, i, m) : 0];
-  }
+  if (rp.resample_m) return rp.resample_bank[resample_index(rp.resample_key, i, *rp.resample_m)];
   return rp.src[i];
 }
 
@@ -214,8 +211,11 @@ cudaError_t launch_fission_sites_mg_batch(const DevWorld* worlds, const RunParam
 // one k-eigenvalue cycle's results kept on the device (mc_batch.cu): bank
 // size M and k = M / n into out[3 * i .. 3 * i + 2] = (k, M, k_tracklength),
 // the run counters added into acc (lost_xyz and pad kept from the first
-// cycle that lost a particle)
-cudaError_t launch_keig_record(const DevCounters* ctr, const unsigned long long* total, unsigned long long n,
+// cycle that lost a particle); an empty bank sets acc->next and leaves
+// *total = 1, so that the cycles queued behind it read bank entry 0 -- a
+// site some earlier cycle wrote (mc_keig_cycles runs the first cycle on its
+// own and checks its bank) -- until the caller reports the error
+cudaError_t launch_keig_record(const DevCounters* ctr, unsigned long long* total, unsigned long long n,
                                double* out, DevCounters* acc, cudaStream_t stream);
 
 // batched k-eigenvalue cycle bookkeeping (mc_batch.cu)
