@@ -98,7 +98,6 @@ struct RunParams {
   // 2 the guided sampler and 3 the plain POD queue (tq_rows / tq_res: POD-exact
   // samples drawn from the particle's own stream)
   int32_t tq_mode;
-  int32_t tq_fast;  // modes 2, 3: the queue samples the FP32 POD form (else the exact one)
   GuideRow* tq_rows;
   const GuideOut* tq_res;
   // resampling fused into the source read (k-eigenvalue cycles after the
@@ -108,6 +107,7 @@ struct RunParams {
   const Site* resample_bank;
   const unsigned long long* resample_m;
   unsigned long long resample_key;
+  int32_t tq_fast;  // thermal queue modes 2, 3: the queue samples the FP32 POD form (else the exact one)
 };
 
 // KEigenvalue's next source, uniform over the bank: source j is bank entry

@@ -51,12 +51,10 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 // ---------------------------------------------------------------------------
 // multigroup history loop of one CTA: the body of the single-problem kernel
 // (world and run parameters in the kernel's parameter space) and of the
-// batched kernel (copied into shared memory per CTA).  SCORE = false
-// compiles the estimator scoring out (runs without tallies: the batched
-// problems), which leaves the loop fewer live registers.
-template <class Rng, bool KEIG, bool PERT = false, bool SCORE = true>
+// batched kernel (copied into shared memory per CTA)
+template <class Rng, bool KEIG, bool PERT = false>
 __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& rp, double* smem) {
-  const bool score = SCORE && rp.score != 0;
+  const bool score = rp.score != 0;
   const bool use_smem = rp.total_bins <= kSharedBins && score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
   if (use_smem) {
@@ -395,7 +393,7 @@ __global__ void __launch_bounds__(256, MINB) k_history_mg_batch(const DevWorld* 
     }
     __syncthreads();
     if (q_serve >= P) break;
-    history_mg<PhiloxRng, true, false, false>(w, rp, smem);  // batched problems keep no tallies
+    history_mg<PhiloxRng, true>(w, rp, smem);
     q = q_serve + 1;
     __syncthreads();  // every warp is done with this problem's parameters
   }
