@@ -7,8 +7,8 @@ it needs (pugixml, the HDF5 C++ API) and a replacement for its one
 Xerces-C++ user (XMLDocument.cpp, which only validates the XML schema).
 The stand-ins implement the calls the reference makes over the project's
 XML DOM and table container.  Needs the reference checkout; skipped (returns
-None) where it is absent.  The checkout is found at $MINIMC_REFERENCE, else at
-the path this recipe reads it from by default (REF_DEFAULT).
+None) where it is absent.  The checkout is found at $MINIMC_REFERENCE, else
+in a directory named `reference` beside this repository's root.
 """
 from __future__ import annotations
 
@@ -19,8 +19,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REF_DEFAULT = "/root/reference"
-REF_SRC = Path(os.environ.get("MINIMC_REFERENCE", REF_DEFAULT)) / "src"
+REF_SRC = Path(os.environ.get("MINIMC_REFERENCE", ROOT.parent / "reference")) / "src"
 OUT = ROOT / "oracle" / "_ref"
 LIB = OUT / "libminimc_ref.so"
 EXCLUDE = {"minimc.cpp", "XMLDocument.cpp"}
