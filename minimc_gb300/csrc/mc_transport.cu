@@ -54,8 +54,7 @@ __device__ __forceinline__ void mg_fission(const DevWorld& w, Particle<Rng>& p, 
 // batched kernel (copied into shared memory per CTA)
 template <class Rng, bool KEIG, bool PERT = false>
 __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& rp, double* smem) {
-  const bool score = rp.score != 0;
-  const bool use_smem = rp.total_bins <= kSharedBins && score && !rp.nb;
+  const bool use_smem = rp.total_bins <= kSharedBins && rp.score && !rp.nb;
   TallySink sink{use_smem ? smem : nullptr, use_smem ? smem + kSharedBins : nullptr, rp.tally_sum, rp.tally_sq};
   if (use_smem) {
     for (int i = threadIdx.x; i < 2 * kSharedBins; i += blockDim.x) smem[i] = 0;
@@ -83,7 +82,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
 
   // history complete: ScorableProxy::CommitHistory (src/Scorable.cpp:101-106)
   auto finish_history = [&]() {
-    if (score && !rp.nb) {
+    if (rp.score && !rp.nb) {
       sink.commit(pend);
       if (pend.overflow) my_overflow++;
     }
@@ -163,7 +162,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
       // active lanes), before the branch-specific work.
       const double dcross = dadd(dsurf, kNudge);
       const double dmove = collide ? dcol : (refl ? dsurf : dcross);
-      if (score) score_track(w, p, dmove, sc);
+      if (rp.score) score_track(w, p, dmove, sc);
       if (KEIG) my_ktl += dmove * __ldg(w.mat_mg_nusigf + mg);
       indirect_stream<PERT>(w, p, m, micro, dmove);
       move(fast, p.x, p.y, p.z, p.u, p.v, p.w, dmove);
@@ -269,7 +268,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
           }
         }
       }
-      if (score) score_event<false, PERT>(w, p, sc);
+      if (rp.score) score_event<false, PERT>(w, p, sc);
       p.nev++;
       hist_nev++;
       my_events++;
