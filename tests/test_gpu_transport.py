@@ -398,3 +398,25 @@ def test_run_keigenvalue_uses_cycles_and_checkpoint(built_library, tmp_path):
     d = gpu_ctx(xml)
     d.keig_resume(blob)
     assert list(d.keig_cycles(3, True)) == kb[2:]
+
+
+@pytest.mark.parametrize("multi", [False, True])
+def test_source_dying_out_is_reported(multi, built_library):
+    """A strongly subcritical medium (k_inf = 0.04, 50 histories per cycle:
+    a cycle banks no site with probability ~e^-2) loses its fission source
+    within a few cycles: the per-cycle call and the multi-cycle call both
+    report it ("source died out"), without reading past the empty bank, and
+    the context stays usable."""
+    xml = synth.infinite_medium(c=0.25, capture=0.72, fission=0.03, nubar=1.0, histories=50, keig=(60, 0)).xml()
+    ctx = gpu_ctx(xml)
+    ctx.keig_begin(rng=RNG_PHILOX, fast_math=1, variant=2)
+    with pytest.raises(MCError, match="died out"):
+        if multi:
+            ctx.keig_cycles(60, False)
+        else:
+            for _ in range(60):
+                ctx.keig_cycle(False)
+    ctx.keig_end()
+    ctx.load_xml(synth.one_group_cube(histories=5000, inactive=1, active=2).xml())
+    r = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=1, variant=2)
+    assert (np.asarray(r.k_cycle) > 0.5).all()
