@@ -1192,10 +1192,13 @@ __global__ void __launch_bounds__(128 * kGuideGroups, 1) k_guided_sample(NetView
       // sampler's
       const bool mono = (__ldg(t.alpha.mono + b_s_i) & (FAST ? 1 : 2)) != 0 && x.ev.c.Tl < x.ev.c.Th &&
                         x.ev.c.Tl <= T && T <= x.ev.c.Th;
-      const int i_min = mono ? cdf_upper_guided<FAST>(x, x.b_s_a_min, g0) : cdf_upper_bisect<FAST>(x, x.b_s_a_min);
-      const int i_max = mono ? cdf_upper_guided<FAST>(x, x.b_s_a_max, g1) : cdf_upper_bisect<FAST>(x, x.b_s_a_max);
-      const double F_min = cdf_at<FAST>(t, x, x.b_s_a_min, i_min);
-      const double F_max = cdf_at<FAST>(t, x, x.b_s_a_max, i_max);
+      Probes p0, p1;  // each guided search's last reconstructions, reused by cdf_at
+      const int i_min =
+          mono ? cdf_upper_guided_kept<FAST>(x, x.b_s_a_min, g0, p0) : cdf_upper_bisect<FAST>(x, x.b_s_a_min);
+      const int i_max =
+          mono ? cdf_upper_guided_kept<FAST>(x, x.b_s_a_max, g1, p1) : cdf_upper_bisect<FAST>(x, x.b_s_a_max);
+      const double F_min = cdf_at_kept<FAST>(t, x, x.b_s_a_min, i_min, p0);
+      const double F_max = cdf_at_kept<FAST>(t, x, x.b_s_a_max, i_max, p1);
       ok = alpha_end<FAST>(t, rng, x, F_min, F_max, alpha);
     }
     if (valid) {

@@ -439,6 +439,96 @@ __device__ __forceinline__ int cdf_upper_guided(const AlphaCtx<FAST>& x, double 
   return first;
 }
 
+// The last two reconstructions a search evaluated, (index, value): the
+// guided search's confirming probes are the bracket that cdf_at reads, so
+// keeping them saves two reconstructions per bound (the values are the
+// same ones cdf_at would compute).
+struct Probes {
+  int i0 = -1, i1 = -1;
+  double v0 = 0, v1 = 0;
+  __device__ __forceinline__ void put(int i, double v) {
+    i1 = i0;
+    v1 = v0;
+    i0 = i;
+    v0 = v;
+  }
+  __device__ __forceinline__ bool get(int i, double& v) const {
+    if (i == i0) {
+      v = v0;
+      return true;
+    }
+    if (i == i1) {
+      v = v1;
+      return true;
+    }
+    return false;
+  }
+};
+
+// cdf_pred, keeping the reconstruction it evaluates
+template <bool FAST>
+__device__ __forceinline__ bool cdf_pred_kept(const AlphaCtx<FAST>& x, double a, float af, int i, Probes& pr) {
+  if constexpr (FAST) {
+    const float v = x.ev.f32(i);
+    pr.put(i, static_cast<double>(v));
+    return af < v;
+  }
+  else {
+    const double v = x.ev(i);
+    pr.put(i, v);
+    return a < v;
+  }
+}
+
+// cdf_upper_guided, keeping its last two reconstructions in pr
+template <bool FAST>
+__device__ __forceinline__ int cdf_upper_guided_kept(const AlphaCtx<FAST>& x, double a, int i0, Probes& pr) {
+  const int nF = x.nF;
+  const float af = __double2float_rn(a);
+  int lo, hi;
+  const int g = i0 < 0 ? 0 : (i0 > nF ? nF : i0);
+  if (g < nF && !cdf_pred_kept(x, a, af, g, pr)) {
+    lo = g + 1;
+    hi = nF;
+    for (int step = 1; lo < nF;) {
+      const int j = g + step < nF ? g + step : nF - 1;
+      if (cdf_pred_kept(x, a, af, j, pr)) {
+        hi = j;
+        break;
+      }
+      lo = j + 1;
+      if (j == nF - 1) break;
+      step <<= 1;
+    }
+  }
+  else {
+    hi = g;
+    lo = 0;
+    for (int step = 1; hi > 0;) {
+      const int j = g - step > 0 ? g - step : 0;
+      if (!cdf_pred_kept(x, a, af, j, pr)) {
+        lo = j + 1;
+        break;
+      }
+      hi = j;
+      if (j == 0) break;
+      step <<= 1;
+    }
+  }
+  int first = lo, len = hi - lo;
+  while (len > 0) {
+    const int half = len >> 1, mid = first + half;
+    if (cdf_pred_kept(x, a, af, mid, pr)) {
+      len = half;
+    }
+    else {
+      first = mid + 1;
+      len -= half + 1;
+    }
+  }
+  return first;
+}
+
 // the CDF value of `a` from its bracket (assuming a histogram PDF)
 template <bool FAST>
 __device__ __forceinline__ double cdf_at(const DevTSL& t, const AlphaCtx<FAST>& x, double a, int F_a_hi_i) {
@@ -447,6 +537,19 @@ __device__ __forceinline__ double cdf_at(const DevTSL& t, const AlphaCtx<FAST>& 
   const double F_a_hi = F_a_hi_i != nF ? __ldg(x.Fs + F_a_hi_i) : 1.0;
   const double a_lo = F_a_hi_i != 0 ? x.ev(F_a_hi_i - 1) : 0.0;
   const double a_hi = F_a_hi_i != nF ? x.ev(F_a_hi_i) : t.alpha_cutoff;
+  return dadd(F_a_lo, sdiv<FAST>(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
+}
+
+// cdf_at with the bracket's reconstructions taken from pr where it holds them
+template <bool FAST>
+__device__ __forceinline__ double cdf_at_kept(const DevTSL& t, const AlphaCtx<FAST>& x, double a, int F_a_hi_i,
+                                              const Probes& pr) {
+  const int nF = x.nF;
+  const double F_a_lo = F_a_hi_i != 0 ? __ldg(x.Fs + F_a_hi_i - 1) : 0.0;
+  const double F_a_hi = F_a_hi_i != nF ? __ldg(x.Fs + F_a_hi_i) : 1.0;
+  double a_lo = 0.0, a_hi = t.alpha_cutoff;
+  if (F_a_hi_i != 0 && !pr.get(F_a_hi_i - 1, a_lo)) a_lo = x.ev(F_a_hi_i - 1);
+  if (F_a_hi_i != nF && !pr.get(F_a_hi_i, a_hi)) a_hi = x.ev(F_a_hi_i);
   return dadd(F_a_lo, sdiv<FAST>(dmul(dsub(a, a_lo), dsub(F_a_hi, F_a_lo)), dsub(a_hi, a_lo)));
 }
 
