@@ -512,33 +512,35 @@ __global__ void __launch_bounds__(256) k_fission_counts(const RunParams rp) {
 }
 
 // The multigroup direct-bank CTA: the draws are those of fission_sites_mg,
-// site for site.
+// site for site.  A site draws a fixed number of 32-bit words -- the chi
+// threshold (1 in the FP32 form, 2 in FP64), the isotropic direction (2, 4)
+// and the secondary's key (2) -- so site y of a record starts y times that
+// many words into the record's stream, and each site is sampled by a thread
+// of its own.
 template <bool FAST>
 __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_mg(const DevWorld w, const RunParams rp,
                                                                         const unsigned long long* offsets,
                                                                         const unsigned long long* total,
                                                                         unsigned long long cap, uint4* out) {
   extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
-  sites_out_cta(rp.n, rp.bank_count, offsets, total, cap, out, stage,
-                [&](unsigned long long h, uint32_t c, Site* dst) {
-                  const FissionRec f = rp.fis[h];
-                  PhiloxRng rng;
-                  rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
-                  const int G = w.G;
-                  const double* chi = w.mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
-                  for (uint32_t y = 0; y < c; y++) {
-                    // go >= 0: the cdf ends above every threshold this stream draws
-                    const int go = first_above(chi, G, uni(rng, FAST));
-                    Site s;
-                    iso(rng, s.u, s.v, s.w, FAST);
-                    s.x = f.x;
-                    s.y = f.y;
-                    s.z = f.z;
-                    s.energy = static_cast<double>(go + 1);
-                    s.key = rng.child_key();
-                    dst[y] = s;
-                  }
-                });
+  constexpr uint32_t kWordsPerSite = FAST ? 1u + 2u + 2u : 2u + 4u + 2u;
+  sites_out_cta_by_site(rp.n, offsets, total, cap, out, stage, [&](unsigned long long h, uint32_t y, Site* dst) {
+    const FissionRec f = rp.fis[h];
+    PhiloxRng rng;
+    rng.restore(rp.run_key, f.id, f.tag & 1u, philox_skip(f.rng, y * kWordsPerSite));
+    const int G = w.G;
+    const double* chi = w.mg_chi_cdf + static_cast<size_t>(f.chi_index) * G;
+    // go >= 0: the cdf ends above every threshold this stream draws
+    const int go = first_above(chi, G, uni(rng, FAST));
+    Site s;
+    iso(rng, s.u, s.v, s.w, FAST);
+    s.x = f.x;
+    s.y = f.y;
+    s.z = f.z;
+    s.energy = static_cast<double>(go + 1);
+    s.key = rng.child_key();
+    *dst = s;
+  });
 }
 
 // Batched problems on the direct bank path: CTAs run over the concatenated

@@ -191,6 +191,48 @@ __device__ __forceinline__ void sites_out_cta(unsigned long long n, const uint32
   for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[base * kWords + i] = stage[i];
 }
 
+// The same CTA with one thread per site instead of one per history: the
+// CTA's histories' bank offsets go to shared memory, each thread finds the
+// history and the index y of its site there, and site(h, y, dst) writes
+// that one site (a history's sites are then sampled by neighbouring
+// threads side by side, not one after another by one thread).
+template <class SiteFn>
+__device__ __forceinline__ void sites_out_cta_by_site(unsigned long long n, const unsigned long long* offsets,
+                                                      const unsigned long long* total, unsigned long long cap,
+                                                      uint4* out, uint4* stage, SiteFn&& site) {
+  static_assert(sizeof(Site) % sizeof(uint4) == 0, "sites are stored as 16-byte words");
+  __shared__ unsigned long long s_off[kSitesOutHist + 1];
+  const unsigned long long first = static_cast<unsigned long long>(blockIdx.x) * kSitesOutHist;
+  const unsigned long long last = first + kSitesOutHist < n ? first + kSitesOutHist : n;
+  const int H = static_cast<int>(last - first);
+  const unsigned long long base = offsets[first];
+  const unsigned long long end = last < n ? offsets[last] : *total;
+  for (int i = threadIdx.x; i < H; i += blockDim.x) s_off[i] = offsets[first + i] - base;
+  if (threadIdx.x == 0) s_off[H] = end - base;
+  __syncthreads();
+  const unsigned long long m = end - base;
+  for (unsigned long long j = threadIdx.x; j < m; j += blockDim.x) {
+    // the history whose sites hold j: the last k with s_off[k] <= j
+    int lo = 0, hi = H;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (s_off[mid] <= j) lo = mid;
+      else hi = mid;
+    }
+    site(first + lo, static_cast<uint32_t>(j - s_off[lo]), reinterpret_cast<Site*>(stage) + j);
+  }
+  __syncthreads();
+  const unsigned long long keep = base >= cap ? 0 : (m < cap - base ? m : cap - base);
+  constexpr unsigned kWords = sizeof(Site) / sizeof(uint4);
+  for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[base * kWords + i] = stage[i];
+}
+
+// A Philox stream position (PhiloxRng::save's packing) s words further on
+__device__ __forceinline__ uint32_t philox_skip(uint32_t packed, uint32_t s) {
+  const uint32_t p = 4u * (packed >> 3) + (packed & 7u) - 4u + s;  // word index of the next draw
+  return ((p / 4u + 1u) << 3) | (p % 4u);
+}
+
 // launches (mc_transport.cu)
 // history-schedule kernel variants differ only in their occupancy target
 // (register budget); results are identical, the autotuner times them
