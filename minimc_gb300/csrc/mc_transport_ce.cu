@@ -49,23 +49,44 @@ __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_ce(const Ru
                                                                         unsigned long long cap, uint4* out) {
   extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
   const bool fast = rp.fast != 0;
-  sites_out_cta(rp.n, rp.bank_count, offsets, total, cap, out, stage,
-                [&](unsigned long long h, uint32_t c, Site* dst) {
-                  const FissionRec f = rp.fis[h];
-                  Rng rng;
-                  rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
-                  const double E = record_energy(f);
-                  for (uint32_t y = 0; y < c; y++) {
-                    Site s;
-                    sample_isotropic(rng, s.u, s.v, s.w, fast);
-                    s.x = f.x;
-                    s.y = f.y;
-                    s.z = f.z;
-                    s.energy = E;
-                    s.key = rng.child_key();
-                    dst[y] = s;
-                  }
-                });
+  if constexpr (std::is_same_v<Rng, PhiloxRng>) {
+    // a site draws a fixed number of 32-bit words -- the isotropic direction
+    // (2 in the FP32 form, 4 in FP64) and the secondary's key (2) -- so each
+    // site starts at a known stream position and has a thread of its own
+    const uint32_t words = (fast ? 2u : 4u) + 2u;
+    sites_out_cta_by_site(rp.n, offsets, total, cap, out, stage, [&](unsigned long long h, uint32_t y, Site* dst) {
+      const FissionRec f = rp.fis[h];
+      PhiloxRng rng;
+      rng.restore(rp.run_key, f.id, f.tag & 1u, philox_skip(f.rng, y * words));
+      Site s;
+      sample_isotropic(rng, s.u, s.v, s.w, fast);
+      s.x = f.x;
+      s.y = f.y;
+      s.z = f.z;
+      s.energy = record_energy(f);
+      s.key = rng.child_key();
+      *dst = s;
+    });
+  }
+  else {
+    sites_out_cta(rp.n, rp.bank_count, offsets, total, cap, out, stage,
+                  [&](unsigned long long h, uint32_t c, Site* dst) {
+                    const FissionRec f = rp.fis[h];
+                    Rng rng;
+                    rng.restore(rp.run_key, f.id, f.tag & 1u, f.rng);
+                    const double E = record_energy(f);
+                    for (uint32_t y = 0; y < c; y++) {
+                      Site s;
+                      sample_isotropic(rng, s.u, s.v, s.w, fast);
+                      s.x = f.x;
+                      s.y = f.y;
+                      s.z = f.z;
+                      s.energy = E;
+                      s.key = rng.child_key();
+                      dst[y] = s;
+                    }
+                  });
+  }
 }
 
 constexpr int kMinb[5] = {1, 3, 4, 5, 6};  // occupancy variants (autotuner index)
