@@ -55,6 +55,51 @@ def _dist():
     return ws, rank
 
 
+class Replicas:
+    """The N>1 path: one process per GPU, each running an independent replica
+    of the workload (its own seed), with no collective on the data path.
+    The process group serves only the timing contract: a barrier on both
+    sides of the timed region and the whole-job figure, i.e. the units all
+    ranks processed divided by the slowest rank's time.  ``backend`` is
+    "nccl" under torchrun on GPUs ("gloo" runs the same logic on the CPU)."""
+
+    def __init__(self, backend: str = "nccl"):
+        self.ws, self.rank = _dist()
+        self.backend = backend
+        self.dist = None
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def _device(self):
+        return "cuda" if self.backend == "nccl" else "cpu"
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def total_rate(self, units: float, ms: float) -> tuple[float, float]:
+        """(units of all ranks per second over the slowest rank's time, that
+        time in ms).  With one rank: units / ms."""
+        if self.dist is None:
+            return units / (ms / 1e3), ms
+        import torch
+
+        t = torch.tensor([ms], dtype=torch.float64, device=self._device())
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        u = torch.tensor([units], dtype=torch.float64, device=self._device())
+        self.dist.all_reduce(u, op=self.dist.ReduceOp.SUM)
+        ms_max = float(t.item())
+        return float(u.item()) / (ms_max / 1e3), ms_max
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi during the timed
     region."""
@@ -190,11 +235,7 @@ def run_gpu(args) -> None:
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    rep = Replicas("nccl")
     from minimc_gb300 import RNG_PHILOX, SITE_DTYPE, Context
 
     hist = args.histories
@@ -215,11 +256,11 @@ def run_gpu(args) -> None:
         torch.cuda.synchronize()
         print(json.dumps({"mode": "kernel", "k_last": k, "schedule": ctx.schedule_info()}), flush=True)
         ctx.keig_end()
+        rep.close()
         return
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        rep.barrier()
         torch.cuda.synchronize()
 
     # ---- device-resident cycles
@@ -253,12 +294,8 @@ def run_gpu(args) -> None:
     events = st1.events - st0.events
     kernel_ms = st1.kernel_ms - st0.kernel_ms
     launches = st1.launches - st0.launches
-    # max over ranks
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = hist * args.steps * ws / (total_ms / 1e3)
+    # histories of all ranks over the slowest rank's time
+    value, total_ms = rep.total_rate(hist * args.steps, total_ms)
     e_h = events / (hist * args.steps)
     peak, peak_kind = peaks()
     alg_bytes = e_h * BYTES_PER_EVENT * hist  # per transport launch (one per step)
@@ -304,8 +341,7 @@ def run_gpu(args) -> None:
         nxt = bank[idx]
         src[:] = nxt
         src["key"] = np.arange(n_sites, dtype=np.uint64) + (i + 1) * n_sites
-    e2e_s = sum(e2e_times)
-    e2e_value = hist * args.steps * ws / e2e_s
+    e2e_value, _ = rep.total_rate(hist * args.steps, 1e3 * sum(e2e_times))
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -373,8 +409,7 @@ def run_gpu(args) -> None:
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
 
 
 def tsl_problem(histories: int, seed: int = 1, energy: float = 1e-6, base: Path | None = None) -> dict:
@@ -550,6 +585,7 @@ def run_gpu_tsl(args) -> None:
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    rep = Replicas("nccl")
     hist = args.histories
     stream = torch.cuda.current_stream()
     if args.mode == "kernel":
@@ -573,12 +609,14 @@ def run_gpu_tsl(args) -> None:
                                       method=method)
         torch.cuda.synchronize()
         print(json.dumps({"mode": "kernel", "beta_mean": float(b.mean())}), flush=True)
+        rep.close()
         return
     clocks = ClockSampler(local)
     clocks.start()
+    rep.barrier()
     forms = thermal_forms(local, hist, args.steps, args.warmup, quantile=True)
     clk = clocks.stop()
-    value = forms["guided"]["histories_per_s"] * ws
+    value, _ = rep.total_rate(hist * args.steps, forms["guided"]["ms_per_step"] * args.steps)
 
     # sampler level: POD exact, POD FP32, guided, MLP quantile surrogate
     wl = tsl_problem(hist)
@@ -664,6 +702,7 @@ def run_gpu_tsl(args) -> None:
             "gpu_launches": int(forms["guided"]["launches_per_step"] * args.steps), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
+    rep.close()
 
 
 BATCH_WORKLOAD = ("64 independent 8-group two-zone k-eigenvalue problems (seeds 0..63, cube sides log-uniform "
@@ -711,6 +750,7 @@ def run_gpu_batch(args) -> None:
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    rep = Replicas("nccl")
     probs = synth.batch_problems(count=64, seed=7 + rank)
     if args.mode == "kernel":
         # profiling mode: the batch's cycles only (no thermal rows, no
@@ -720,6 +760,7 @@ def run_gpu_batch(args) -> None:
             b.add(p.xml(), histories=h, seed=p.seed)
         r = b.run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
         print(json.dumps({"mode": "kernel", "variant": r["variant"], "active_ms": r["active_ms"]}), flush=True)
+        rep.close()
         return
     temps = thermal_groups.problem_temperatures(len(probs), seed=11 + rank)
     # transfer rows of the thermal groups: surrogate and POD sampler
@@ -744,11 +785,12 @@ def run_gpu_batch(args) -> None:
 
     clocks = ClockSampler(local)
     clocks.start()
+    rep.barrier()
     r = make(thermal).run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
     clk = clocks.stop()
     cycles = args.warmup + args.steps
     n_cycle = int(sum(h for _, h in probs))
-    value = n_cycle * args.steps * ws / (r["active_ms"] / 1e3)
+    value, _ = rep.total_rate(n_cycle * args.steps, r["active_ms"])
     rp = make(plain, 1000).run(inactive=args.warmup, active=args.steps, fast_math=int(args.fast))
     z = (r["k_mean"] - rp["k_mean"]) / np.hypot(r["k_std"], rp["k_std"])
     chi2 = float(np.sum(z ** 2))
@@ -803,6 +845,7 @@ def run_gpu_batch(args) -> None:
             "gpu_launches": int(r["launches"]), "clocks": clk,
         }
         print(json.dumps(line), flush=True)
+    rep.close()
 
 
 def main():
