@@ -13,6 +13,9 @@
 #include "mc_tc.cuh"
 #include "mc_tsl.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <type_traits>
 
 namespace mcd {
@@ -57,85 +60,117 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // ---------------------------------------------------------------------------
-// generic GEMM: one CTA (128 threads) computes rows [m0, m0 + 128) x N of
-// C = A[M x K] * B[N x K]^T over the K range of its split (blockIdx.z),
-// KC columns at a time through shared memory; the accumulator lives in
-// tensor memory and is handed to the epilogue row by row.
+// generic GEMM: one CTA (128 threads) computes rows [m0, m0 + 128) x columns
+// [n0, n0 + NT) of C = A[M x K] * B[N x K]^T over the K range of its split
+// (blockIdx.z, at most kGemmMaxK columns).  Thread 0 issues every operand
+// copy of that range up front as TMA boxes of R rows x 8 columns (16 bytes
+// a row), one mbarrier per kGemmStageK columns, then issues each stage's
+// MMAs as soon as its copies have landed, so the second stage's copies
+// overlap the first stage's products.  A box lands as R * 16 contiguous
+// bytes, so the element (row, k) of the K range sits at byte
+//     (k / 8) * R * 16 + row * 16 + (k % 8) * 2
+// -- the canonical K-major layout without swizzling, core matrices (8 rows
+// x 16 B) 128 B apart along the rows (SBO) and R * 16 B apart along K
+// (LBO).  The accumulator lives in tensor memory; the epilogue reads it 32
+// columns at a time, and each warp turns its 32 x 32 block around in shared
+// memory (the operand tiles' space, free once the products are done) so
+// that the epilogues' row-major stores, transposed stores and atomics all
+// run along contiguous addresses.
+constexpr int kGemmStageK = 64;
+constexpr int kGemmMaxK = 128;
+constexpr int kGemmMaxStages = kGemmMaxK / kGemmStageK;
+constexpr int kStagePitch = 33;  // floats per row of a warp's 32 x 32 block (conflict-free both ways)
+constexpr size_t kGemmEpiBytes = 4 * 32 * kStagePitch * sizeof(float);
+
 struct GemmArgs {
-  const uint16_t* A;  // 16-bit operands: FP16 (forward) or BF16 (backward)
-  int lda;
-  const uint16_t* B;
-  int ldb;
-  int k_split;  // K per CTA (multiple of KC)
-  int* err;     // set when an MMA wait timed out
+  int k_split;  // K per CTA (a multiple of 16, at most kGemmMaxK)
+  int* err;     // set when a copy or an MMA wait timed out
 };
 
-template <int N, int KC, class Epi, bool F16>
-__global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
-  static_assert(N % 16 == 0 && N >= 16 && N <= 128, "N");
-  static_assert(KC % 16 == 0 && KC <= 64, "KC");
-  constexpr int kCols = N < 32 ? 32 : N;  // tensor-memory columns (power of two >= 32)
-  __shared__ __align__(1024) uint8_t sA[128 * KC * 2];
-  __shared__ __align__(1024) uint8_t sB[N * KC * 2];
-  __shared__ __align__(8) unsigned long long mbar;
+__host__ __device__ constexpr size_t gemm_smem_bytes(int NT, int k_split) {
+  const size_t ops = static_cast<size_t>(128 + NT) * k_split * 2;
+  return ops > kGemmEpiBytes ? ops : kGemmEpiBytes;
+}
+
+template <int NT, class Epi, bool F16>
+__global__ void __launch_bounds__(128) k_gemm(const __grid_constant__ CUtensorMap tmA,
+                                              const __grid_constant__ CUtensorMap tmB, const GemmArgs a,
+                                              const Epi epi) {
+  static_assert(NT % 16 == 0 && NT >= 16 && NT <= 128, "NT");
+  constexpr int kCols = NT < 32 ? 32 : NT;  // tensor-memory columns (power of two >= 32)
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) unsigned long long full[kGemmMaxStages];
+  __shared__ __align__(8) unsigned long long done;
   __shared__ uint32_t tmem_slot;
+  __shared__ int issue_ok;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * 128;
+  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * NT;
   const int k_begin = blockIdx.z * a.k_split;
+  const int stages = (a.k_split + kGemmStageK - 1) / kGemmStageK;
+  const uint32_t sA = tc::smem_addr(smem);
+  const uint32_t sB = sA + 128u * static_cast<uint32_t>(a.k_split) * 2u;
   if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_slot), kCols);
-  if (tid == 0) tc::mbar_init(tc::smem_addr(&mbar), 1);
+  if (tid == 0) {
+    for (int s = 0; s < stages; s++) tc::mbar_init(tc::smem_addr(&full[s]), 1);
+    tc::mbar_init(tc::smem_addr(&done), 1);
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  const uint32_t mb = tc::smem_addr(&mbar);
-  constexpr uint32_t idesc = F16 ? tc::idesc_f16_f32(128, N) : tc::idesc_bf16_f32(128, N);
-  uint32_t phase = 0;
-  bool ok = true;
-  for (int k0 = 0; k0 < a.k_split && ok; k0 += KC) {
-    // operand tiles: one 16-byte chunk (8 values of one row) per step,
-    // consecutive threads on consecutive rows
-    for (int c = tid; c < 128 * (KC / 8); c += 128) {
-      const int row = c & 127, kc = c >> 7;
-      const uint4 v = *reinterpret_cast<const uint4*>(a.A + static_cast<size_t>(m0 + row) * a.lda + k_begin + k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sA + tc::tile_offset(row, kc * 8, KC)) = v;
-    }
-    for (int c = tid; c < N * (KC / 8); c += 128) {
-      const int row = c % N, kc = c / N;
-      const uint4 v = *reinterpret_cast<const uint4*>(a.B + static_cast<size_t>(row) * a.ldb + k_begin + k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sB + tc::tile_offset(row, kc * 8, KC)) = v;
-    }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after_sync();
-      const uint32_t a0 = tc::smem_addr(sA), b0 = tc::smem_addr(sB);
-#pragma unroll
-      for (int s = 0; s < KC / 16; s++) {
-        const uint64_t ad = tc::smem_desc(a0 + s * 256, 128, KC * 16);
-        const uint64_t bd = tc::smem_desc(b0 + s * 256, 128, KC * 16);
-        tc::mma_bf16(tmem, ad, bd, idesc, (k0 > 0 || s > 0) ? 1u : 0u);
+  if (tid == 0) {
+    constexpr uint32_t idesc = F16 ? tc::idesc_f16_f32(128, NT) : tc::idesc_bf16_f32(128, NT);
+    for (int s = 0; s < stages; s++) {
+      const int kw = min(kGemmStageK, a.k_split - s * kGemmStageK);
+      const uint32_t fb = tc::smem_addr(&full[s]);
+      tc::mbar_expect_tx(fb, static_cast<uint32_t>((128 + NT) * kw * 2));
+      for (int k = s * kGemmStageK; k < s * kGemmStageK + kw; k += 8) {
+        tc::tma_load_2d(sA + static_cast<uint32_t>(k / 8) * 128u * 16u, &tmA, fb, k_begin + k, m0);
+        tc::tma_load_2d(sB + static_cast<uint32_t>(k / 8) * NT * 16u, &tmB, fb, k_begin + k, n0);
       }
-      tc::mma_commit(mb);
     }
-    // the verdict is taken by the whole CTA so that every thread leaves the
-    // loop at the same trip
-    ok = __syncthreads_and(tc::mbar_wait(mb, phase, kWaitCycles) ? 1 : 0) != 0;
-    phase ^= 1;
-    tc::fence_after_sync();
+    int landed = 0;
+    for (; landed < stages; landed++) {
+      if (!tc::mbar_wait(tc::smem_addr(&full[landed]), 0, kWaitCycles)) break;
+      tc::fence_after_sync();
+      const int kw = min(kGemmStageK, a.k_split - landed * kGemmStageK);
+      for (int k = landed * kGemmStageK; k < landed * kGemmStageK + kw; k += 16) {
+        const uint64_t ad = tc::smem_desc(sA + static_cast<uint32_t>(k / 8) * 128u * 16u, 128u * 16u, 128u);
+        const uint64_t bd = tc::smem_desc(sB + static_cast<uint32_t>(k / 8) * NT * 16u, NT * 16u, 128u);
+        tc::mma_bf16(tmem, ad, bd, idesc, k > 0 ? 1u : 0u);
+      }
+    }
+    tc::mma_commit(tc::smem_addr(&done));
+    issue_ok = landed == stages;
+    // copies still in flight after a timed-out wait finish before the CTA
+    // leaves (bounded again)
+    for (int s = landed; s < stages; s++) tc::mbar_wait(tc::smem_addr(&full[s]), 0, kWaitCycles);
   }
-  if (!ok) {
-    if (tid == 0) atomicExch(a.err, 1);
-    tc::mbar_wait(mb, phase ^ 1, kWaitCycles);  // the MMAs in flight, bounded again
+  // the verdict is taken by the whole CTA so that every thread takes the
+  // same branch
+  const int fine = __syncthreads_and(tc::mbar_wait(tc::smem_addr(&done), 0, kWaitCycles) ? 1 : 0);
+  tc::fence_after_sync();
+  if (!fine || !issue_ok) {
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      if (!fine) tc::mbar_wait(tc::smem_addr(&done), 0, kWaitCycles);  // the MMAs in flight, bounded again
+    }
   }
   else {
     // epilogue: warp w owns tensor-memory lanes (rows) 32 w .. 32 w + 31
-    const int row = m0 + warp * 32 + lane;
+    float* st = reinterpret_cast<float*>(smem) + warp * 32 * kStagePitch;
+    const int row0 = m0 + warp * 32;
 #pragma unroll 1
-    for (int c = 0; c < (N + 31) / 32; c++) {
+    for (int c = 0; c < (NT + 31) / 32; c++) {
       float v[32];
       tc::tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c * 32, v);
-      epi(row, c * 32, v, N - c * 32 < 32 ? N - c * 32 : 32);
+#pragma unroll
+      for (int j = 0; j < 32; j++) st[lane * kStagePitch + j] = v[j];
+      __syncwarp();
+      epi(row0, n0 + c * 32, st, NT - c * 32 < 32 ? NT - c * 32 : 32, lane);
+      __syncwarp();
     }
   }
   tc::fence_before_sync();
@@ -146,6 +181,9 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs a, const Epi epi) {
   }
 }
 
+// The epilogues see one warp's 32 x 32 block of the accumulator in shared
+// memory: st[i * kStagePitch + j] = acc(row0 + i, col0 + j), j < ncol.
+
 // z = acc + bias; keeps Z (FP32) and optionally H = SiLU(z) (FP16, the next
 // forward operand) and H^T (BF16, for the weight gradients)
 struct EpiForward {
@@ -154,23 +192,29 @@ struct EpiForward {
   f16* H;
   bf16* Ht;
   int B;
-  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
-#pragma unroll
-    for (int j = 0; j < 32; j += 2) {
-      if (j < ncol) {  // ncol is even (N = 128)
-        const int c = col0 + j;
-        const float z0 = v[j] + bias[c], z1 = v[j + 1] + bias[c + 1];
-        Z[static_cast<size_t>(row) * kMlpWidth + c] = z0;
-        Z[static_cast<size_t>(row) * kMlpWidth + c + 1] = z1;
-        if (H) {
-          const __half2 h = silu2_f16(0.5f * z0, 0.5f * z1);
-          *reinterpret_cast<__half2*>(H + static_cast<size_t>(row) * kMlpWidth + c) = h;
-          if (Ht) {
-            Ht[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(__low2float(h));
-            Ht[static_cast<size_t>(c + 1) * B + row] = __float2bfloat16_rn(__high2float(h));
-          }
-        }
+  __device__ __forceinline__ void operator()(int row0, int col0, float* st, int, int lane) const {
+    // lanes 0-15 take column pairs of row i, lanes 16-31 those of row i + 1
+    const int cp = 2 * (lane & 15), half = lane >> 4;
+    const float b0 = bias[col0 + cp], b1 = bias[col0 + cp + 1];
+#pragma unroll 4
+    for (int i = 0; i < 32; i += 2) {
+      const int r = i + half;
+      float* e = st + r * kStagePitch + cp;
+      const float z0 = e[0] + b0, z1 = e[1] + b1;
+      const size_t o = static_cast<size_t>(row0 + r) * kMlpWidth + col0 + cp;
+      *reinterpret_cast<float2*>(Z + o) = make_float2(z0, z1);
+      if (H) {
+        const __half2 h = silu2_f16(0.5f * z0, 0.5f * z1);
+        *reinterpret_cast<__half2*>(H + o) = h;
+        e[0] = __low2float(h);
+        e[1] = __high2float(h);
       }
+    }
+    if (Ht) {
+      __syncwarp();
+#pragma unroll 4
+      for (int j = 0; j < 32; j++)
+        Ht[static_cast<size_t>(col0 + j) * B + row0 + lane] = __float2bfloat16_rn(st[lane * kStagePitch + j]);
     }
   }
 };
@@ -183,39 +227,90 @@ struct EpiBackward {
   bf16* dZt;
   float* db;
   int B;
-  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
+  __device__ __forceinline__ void operator()(int row0, int col0, float* st, int, int lane) const {
+    // lane = column: Zp and dZ along rows, the column sum in a register;
+    // the block's 32 Zp loads are all issued before the first is used
+    float zp[32];
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
-      if (j < ncol) {
-        const int c = col0 + j;
-        const float dz = v[j] * dsilu(Zp[static_cast<size_t>(row) * kMlpWidth + c]);
-        if (dZ) dZ[static_cast<size_t>(row) * kMlpWidth + c] = __float2bfloat16_rn(dz);
-        dZt[static_cast<size_t>(c) * B + row] = __float2bfloat16_rn(dz);
-        const float s = warp_sum(dz);
-        if ((threadIdx.x & 31) == 0) atomicAdd(db + c, s);
-      }
+    for (int i = 0; i < 32; i++) zp[i] = Zp[static_cast<size_t>(row0 + i) * kMlpWidth + col0 + lane];
+    float sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; i++) {
+      const float dz = st[i * kStagePitch + lane] * dsilu(zp[i]);
+      if (dZ) dZ[static_cast<size_t>(row0 + i) * kMlpWidth + col0 + lane] = __float2bfloat16_rn(dz);
+      st[i * kStagePitch + lane] = dz;
+      sum += dz;
     }
+    atomicAdd(db + col0 + lane, sum);
+    __syncwarp();
+    // lane = row: dZ^T along rows
+#pragma unroll 4
+    for (int j = 0; j < 32; j++)
+      dZt[static_cast<size_t>(col0 + j) * B + row0 + lane] = __float2bfloat16_rn(st[lane * kStagePitch + j]);
   }
 };
 
-// C[row][col] += acc (split-K weight gradients)
+// C[row][col] += acc (split-K weight gradients); lane = column, so a warp's
+// atomics of one row share cache lines
 struct EpiAtomic {
   float* C;
   int ldc;
-  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32], int ncol) const {
-#pragma unroll
-    for (int j = 0; j < 32; j++)
-      if (j < ncol) atomicAdd(C + static_cast<size_t>(row) * ldc + col0 + j, v[j]);
+  __device__ __forceinline__ void operator()(int row0, int col0, float* st, int ncol, int lane) const {
+    if (lane >= ncol) return;
+#pragma unroll 4
+    for (int i = 0; i < 32; i++)
+      atomicAdd(C + static_cast<size_t>(row0 + i) * ldc + col0 + lane, st[i * kStagePitch + lane]);
   }
 };
 
-template <int N, int KC, class Epi, class T>
-cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int K, int splits, int* err, const Epi& epi,
+// cuTensorMapEncodeTiled from the driver, found through the runtime (no
+// link against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<PFN_cuTensorMapEncodeTiled_v12000>(nullptr);
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// tensor map of a row-major [rows x K] 16-bit operand (row pitch ld
+// elements) whose boxes are `box_rows` rows x 8 columns
+bool operand_map(CUtensorMap* m, const void* base, int ld, int rows, int K, int box_rows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+  const cuuint32_t box[2] = {8, static_cast<cuuint32_t>(box_rows)};
+  const cuuint32_t step[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base), dims, strides, box, step,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// C = A[M x K] B[N x K]^T in tiles of 128 x NT, K split over `splits` CTAs
+template <int NT, class Epi, class T>
+cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int N, int K, int splits, int* err, const Epi& epi,
                  cudaStream_t s) {
   static_assert(sizeof(T) == 2, "16-bit operands");
   constexpr bool kF16 = std::is_same_v<T, f16>;
-  GemmArgs a{reinterpret_cast<const uint16_t*>(A), lda, reinterpret_cast<const uint16_t*>(B), ldb, K / splits, err};
-  k_gemm<N, KC, Epi, kF16><<<dim3(M / 128, 1, splits), 128, 0, s>>>(a, epi);
+  if (M % 128 || N % NT || splits < 1 || K % splits) return cudaErrorInvalidValue;
+  const int k_split = K / splits;
+  if (k_split % 16 || k_split > kGemmMaxK || K > lda || K > ldb) return cudaErrorInvalidValue;
+  if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15 || (lda | ldb) & 7)
+    return cudaErrorInvalidValue;
+  CUtensorMap ta, tb;
+  if (!operand_map(&ta, A, lda, M, K, 128) || !operand_map(&tb, B, ldb, N, K, NT)) return cudaErrorInvalidValue;
+  auto* kern = &k_gemm<NT, Epi, kF16>;
+  const size_t smem = gemm_smem_bytes(NT, k_split);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(gemm_smem_bytes(NT, kGemmMaxK)));
+  if (e != cudaSuccess) return e;
+  kern<<<dim3(M / 128, N / NT, splits), 128, smem, s>>>(ta, tb, GemmArgs{k_split, err}, epi);
   return cudaGetLastError();
 }
 
@@ -311,13 +406,13 @@ int* mlp_err_ptr() {
 cudaError_t mlp_forward(const MlpNet& net, const MlpBatch& b, float* out, cudaStream_t s) {
   int* err = mlp_err_ptr();
   cudaError_t e;
-  if ((e = gemm<128, 16>(b.X, kMlpIn, net.W1, kMlpIn, b.B, kMlpIn, 1, err,
+  if ((e = gemm<64>(b.X, kMlpIn, net.W1, kMlpIn, b.B, kMlpWidth, kMlpIn, 1, err,
                          EpiForward{net.p + kMlpB1, b.Z1, b.H1, nullptr, b.B}, s)) != cudaSuccess)
     return e;
-  if ((e = gemm<128, 64>(b.H1, kMlpWidth, net.W2, kMlpWidth, b.B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.H1, kMlpWidth, net.W2, kMlpWidth, b.B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB2, b.Z2, b.H2, nullptr, b.B}, s)) != cudaSuccess)
     return e;
-  if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, b.B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.H2, kMlpWidth, net.W3, kMlpWidth, b.B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, b.B}, s)) != cudaSuccess)
     return e;
   k_head_forward<<<(b.B + 127) / 128, 128, 0, s>>>(b.Z3, net.p, b.B, out);
@@ -332,34 +427,34 @@ cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStrea
   cudaError_t e;
   if ((e = cudaMemsetAsync(net.g, 0, kMlpParams * sizeof(float), s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(b.loss, 0, sizeof(float), s)) != cudaSuccess) return e;
-  if ((e = gemm<128, 16>(b.X, kMlpIn, net.W1, kMlpIn, B, kMlpIn, 1, err,
+  if ((e = gemm<64>(b.X, kMlpIn, net.W1, kMlpIn, B, kMlpWidth, kMlpIn, 1, err,
                          EpiForward{net.p + kMlpB1, b.Z1, b.H1, b.H1t, B}, s)) != cudaSuccess)
     return e;
-  if ((e = gemm<128, 64>(b.H1, kMlpWidth, net.W2, kMlpWidth, B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.H1, kMlpWidth, net.W2, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB2, b.Z2, b.H2, b.H2t, B}, s)) != cudaSuccess)
     return e;
   // Z3 only (H3 is recomputed from Z3 by the head)
-  if ((e = gemm<128, 64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, B}, s)) != cudaSuccess)
     return e;
   k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // layer 3: dW3 = dZ3^T H2; dH2 = dZ3 W3 -> dZ2
-  if ((e = gemm<128, 64>(b.dZ3t, B, b.H2t, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW3, kMlpWidth}, s)) !=
+  if ((e = gemm<64>(b.dZ3t, B, b.H2t, B, kMlpWidth, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW3, kMlpWidth}, s)) !=
       cudaSuccess)
     return e;
-  if ((e = gemm<128, 64>(b.dZ3, kMlpWidth, net.W3t, kMlpWidth, B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.dZ3, kMlpWidth, net.W3t, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiBackward{b.Z2, b.dZ2, b.dZ2t, net.g + kMlpB2, B}, s)) != cudaSuccess)
     return e;
   // layer 2: dW2 = dZ2^T H1; dH1 = dZ2 W2 -> dZ1 (transposed only)
-  if ((e = gemm<128, 64>(b.dZ2t, B, b.H1t, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW2, kMlpWidth}, s)) !=
+  if ((e = gemm<64>(b.dZ2t, B, b.H1t, B, kMlpWidth, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW2, kMlpWidth}, s)) !=
       cudaSuccess)
     return e;
-  if ((e = gemm<128, 64>(b.dZ2, kMlpWidth, net.W2t, kMlpWidth, B, kMlpWidth, 1, err,
+  if ((e = gemm<64>(b.dZ2, kMlpWidth, net.W2t, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiBackward{b.Z1, nullptr, b.dZ1t, net.g + kMlpB1, B}, s)) != cudaSuccess)
     return e;
   // layer 1: dW1 = dZ1^T X
-  return gemm<16, 64>(b.dZ1t, B, b.Xt, B, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW1, kMlpIn}, s);
+  return gemm<16>(b.dZ1t, B, b.Xt, B, kMlpWidth, kMlpIn, B, splits, err, EpiAtomic{net.g + kMlpW1, kMlpIn}, s);
 }
 
 cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s) {

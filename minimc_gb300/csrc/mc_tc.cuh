@@ -1,17 +1,18 @@
 // Blackwell tensor-core primitives (tcgen05, sm_100 family) in inline PTX:
 // tensor-memory allocation, shared-memory matrix descriptors, BF16 MMA with
-// FP32 accumulation in tensor memory, completion through an mbarrier, and
-// tensor-memory loads.
+// FP32 accumulation in tensor memory, completion through an mbarrier,
+// tensor-memory loads, and TMA tile copies into shared memory.
 //
 // Operand tiles use the canonical K-major layout without swizzling: a
-// "core matrix" is 8 rows x 16 bytes (8 BF16 values of one row) stored as
+// "core matrix" is 8 rows x 16 bytes (8 16-bit values of one row) stored as
 // 128 contiguous bytes; core matrices adjacent in K are LBO bytes apart,
-// adjacent 8-row groups SBO bytes apart.  Tiles here are R rows x KC
-// columns with LBO = 128 B and SBO = KC * 16 B, so the element (row, k)
-// lives at byte
+// adjacent 8-row groups SBO bytes apart.  The sampler's tiles (R rows x KC
+// columns, written by the threads) use LBO = 128 B and SBO = KC * 16 B, so
+// the element (row, k) lives at byte
 //     (k / 8) * 128 + (row / 8) * KC * 16 + (row % 8) * 16 + (k % 8) * 2
 // and the 16-column slice s that one MMA (K = 16) consumes starts at
-// byte s * 256.
+// byte s * 256.  The training products' tiles arrive by TMA as R-row x
+// 8-column slabs (LBO = R * 16 B, SBO = 128 B; mc_mlp.cu).
 #pragma once
 
 #include <cstdint>
@@ -100,6 +101,25 @@ __device__ __forceinline__ void tmem_alloc(uint32_t dst, uint32_t ncols) {
 }
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- TMA (the tensor memory accelerator)
+// the next phase of the mbarrier also waits for `bytes` bytes of copies
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+// copies the box at (x, y) (x innermost, in elements) of a 2-D tensor map
+// to shared memory at `dst`; completion is counted in bytes on the mbarrier.
+// The tensor map lives in kernel parameter space (__grid_constant__).
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, uint32_t mbar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(mbar), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void prefetch_tmap(const void* tmap) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
 }
 
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

@@ -115,7 +115,7 @@ def random_case(n, seed):
     return p, x, y
 
 
-@pytest.mark.parametrize("n", [128, 1024])
+@pytest.mark.parametrize("n", [128, 1024, 8192])
 def test_gradient_matches_cpu_reference(n, built_library):
     p, x, y = random_case(n, seed=n)
     g, loss, out = Context(0).surrogate_grad(p, x, y)
