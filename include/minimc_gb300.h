@@ -492,6 +492,20 @@ int mc_tsl_group_transfer(mc_ctx* ctx, int32_t tsl, const double* energy, const 
                           uint32_t rows, uint64_t n, const double* bounds, uint32_t groups, uint64_t seed,
                           int32_t method, double* probs, uint64_t* failures);
 
+/* Thin SVD of the POD table pipeline's decomposition step (truncate /
+ * adaptive_coarsen in the pipeline that writes the partition files the
+ * reference reads in ThermalScattering.cpp:183-463; the pipeline's own source
+ * is not in the reference, its call site is
+ * scripts/tolerance_vs_spectrum_error/tolerance_vs_spectrum_error.py:16-41):
+ * A = U diag(S) V^T for a column-major m x n host matrix, m >= n, in FP64 on
+ * the device by one-sided Jacobi rotations.  Outputs (host): S[n] descending,
+ * U m x n and V n x n column-major; a column of U whose singular value is 0
+ * is zero.  *sweeps (may be NULL) = sweeps over the column pairs until one
+ * made no rotation.  Needs no loaded problem.  n <= 2^16, m * n <= 2^30,
+ * finite entries. */
+int mc_pod_svd(mc_ctx* ctx, const double* A, uint64_t m, uint64_t n, double* U, double* S, double* V,
+               uint32_t* sweeps);
+
 /* ThermalScattering::GetTotal (src/ThermalScattering.cpp:111-157). */
 int mc_tsl_total(mc_ctx* ctx, int32_t tsl, const double* energy, const double* temperature,
                  uint64_t n, double* xs);

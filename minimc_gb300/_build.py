@@ -24,7 +24,7 @@ LIB = OUT_DIR / "libminimc_gb300.so"
 HOST_SOURCES = ["mc_xml.cpp", "mc_model.cpp", "mc_ce_tables.cpp", "mc_output.cpp"]
 CUDA_SOURCES = ["mc_abi.cu", "mc_transport.cu", "mc_transport_ce.cu", "mc_transport_ce_fx1.cu", "mc_transport_ce_fx2.cu",
                 "mc_transport_ce_exact.cu", "mc_transport_ce_ext.cu", "mc_event.cu", "mc_probe.cu", "mc_tsl.cu",
-                "mc_mlp.cu", "mc_batch.cu"]
+                "mc_mlp.cu", "mc_batch.cu", "mc_pod.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

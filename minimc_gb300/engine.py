@@ -176,6 +176,7 @@ _SIGNATURES = {
     "mc_tsl_total": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint64, _D]),
     "mc_tsl_group_transfer": (C.c_int, [_P, C.c_int32, _D, _D, C.c_uint32, C.c_uint64, _D, C.c_uint32, C.c_uint64,
                                         C.c_int32, _D, C.POINTER(C.c_uint64)]),
+    "mc_pod_svd": (C.c_int, [_P, _D, C.c_uint64, C.c_uint64, _D, _D, _D, C.POINTER(C.c_uint32)]),
     "mc_output_text": (C.c_int, [_P, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
                                  C.POINTER(C.c_size_t)]),
     "mc_output_format": (C.c_int, [C.c_char_p, C.c_char_p, _D, _D, C.c_uint64, C.c_double, C.c_char_p, C.c_size_t,
@@ -568,6 +569,29 @@ class Context:
         self.check(self.lib.mc_tsl_group_transfer(self.h, tsl, _dptr(e), _dptr(t), len(e), n, _dptr(b), G, seed,
                                                   method, _dptr(out), C.byref(f)))
         return out, int(f.value)
+
+    def pod_svd(self, M):
+        """Thin SVD of a real matrix on the device (mc_pod_svd, FP64,
+        one-sided Jacobi): returns (U, S, Vh, sweeps) with M = U diag(S) Vh,
+        S descending, U [rows, k], Vh [k, cols], k = min(rows, cols)."""
+        M = np.asarray(M, dtype=np.float64)
+        if M.ndim != 2 or M.size == 0:
+            raise ValueError("pod_svd needs a non-empty 2-D matrix")
+        rows, cols = M.shape
+        tall = rows >= cols
+        # the column-major buffer of A (m >= n): A = M when tall, M^T when wide
+        A = _arr(M.T if tall else M, np.float64)
+        m, n = (rows, cols) if tall else (cols, rows)
+        U = np.zeros(m * n)
+        S = np.zeros(n)
+        V = np.zeros(n * n)
+        sw = C.c_uint32()
+        self.check(self.lib.mc_pod_svd(self.h, _dptr(A), m, n, _dptr(U), _dptr(S), _dptr(V), C.byref(sw)))
+        Ua = U.reshape(n, m).T  # A's left vectors [m, n]
+        Va = V.reshape(n, n).T  # A's right vectors [n, n]
+        if tall:
+            return Ua, S, Va.T, int(sw.value)
+        return Va, S, Ua.T, int(sw.value)
 
     def sample_tsl_device(self, tsl: int, d_energy: int, d_temperature: int, n: int, d_beta: int, d_alpha: int,
                           seed: int = 1, method: int = TSL_POD) -> int:

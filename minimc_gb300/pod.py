@@ -24,8 +24,9 @@ their names and the layout the reference reads:
   values, sum_{k>r} S_k^2 <= tol^2 sum_k S_k^2), optionally from complete
   decompositions made once for a sweep over tolerances.
 
-The decompositions run on the GPU when one is present (torch.linalg on the
-device, FP64); the results are written as ``.mctab`` files
+The decompositions run on the GPU when one is present: a one-sided Jacobi
+SVD in FP64 (minimc_gb300/csrc/mc_pod.cu, C ABI mc_pod_svd), with LAPACK
+on hosts without one; the results are written as ``.mctab`` files
 (synth_ce.write_table) named like synth_tsl's.
 """
 from __future__ import annotations
@@ -77,22 +78,41 @@ class Pod:
         return float(np.sqrt(max(0.0, tot - float(np.sum(self.S ** 2))) / tot)) if tot > 0 else 0.0
 
 
-def _svd(M: np.ndarray, device: str | None):
-    """Thin SVD in FP64: on the GPU when available (device None), on a
-    given torch device, or with LAPACK through numpy (device "numpy")."""
-    torch = None
-    if device != "numpy":
-        try:
-            import torch
-        except ImportError:
-            torch = None
-    if torch is not None:
-        dev = device or ("cuda" if torch.cuda.is_available() else "cpu")
-        t = torch.as_tensor(M, dtype=torch.float64, device=dev)
-        U, S, Vh = torch.linalg.svd(t, full_matrices=False)
-        return U.cpu().numpy(), S.cpu().numpy(), Vh.cpu().numpy()
-    U, S, Vh = np.linalg.svd(M, full_matrices=False)
+_SVD_CTX = None
+
+
+def _device_svd(M: np.ndarray):
+    """Thin SVD on the GPU: the project's one-sided Jacobi kernel
+    (Context.pod_svd, C ABI mc_pod_svd), FP64."""
+    global _SVD_CTX
+    if _SVD_CTX is None:
+        from .engine import Context
+
+        _SVD_CTX = Context(0)
+    U, S, Vh, _ = _SVD_CTX.pod_svd(M)
     return U, S, Vh
+
+
+def _gpu_present() -> bool:
+    try:
+        import torch
+
+        return bool(torch.cuda.is_available())
+    except ImportError:
+        return False
+
+
+def _svd(M: np.ndarray, device: str | None):
+    """Thin SVD in FP64: device "cuda" runs the project's Jacobi kernel on
+    the GPU, "numpy" LAPACK on the host; None picks the GPU when one is
+    present."""
+    if device is None:
+        device = "cuda" if _gpu_present() else "numpy"
+    if device == "cuda":
+        return _device_svd(M)
+    if device == "numpy":
+        return np.linalg.svd(M, full_matrices=False)
+    raise ValueError(f"unknown SVD device {device!r} (\"cuda\" or \"numpy\")")
 
 
 def split(table: Table, boundaries) -> list[Table]:

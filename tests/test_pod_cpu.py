@@ -28,7 +28,7 @@ def test_split():
         pod.split(t, [5, 5])
 
 
-@pytest.mark.parametrize("device", ["numpy", "cpu"])
+@pytest.mark.parametrize("device", ["numpy"])
 def test_truncate_exact_and_tail(device):
     t = table()
     full = pod.truncate(t, 10**6, device)
@@ -88,7 +88,7 @@ def test_pipeline_library_loads(tmp_path, built_library):
     from minimc_gb300.engine import format_output
 
     tsl = synth_tsl.write_tsl(tmp_path, n_E=16, n_beta_grid=40, n_F_beta=40, n_F_alpha=40,
-                              temperatures=np.linspace(283.6, 623.6, 4), rel_tol=1e-3, device="cpu")
+                              temperatures=np.linspace(283.6, 623.6, 4), rel_tol=1e-3, device="numpy")
     nuc = synth_tsl.moderator_nuclide(tmp_path)
     xml = synth_tsl.broomstick_xml(tsl, nuc, histories=10, cosine_bins=4, energy_bins=4)
     text = format_output(xml, tmp_path, np.zeros(36), np.zeros(36), 10)
