@@ -60,6 +60,8 @@ enum ScratchSlot {
   kGroupSamples,  // thermal group transfer: one chunk's samples
   kCycleRec,      // mc_keig_cycles: per-cycle records and counters
   kEvPend2,       // second dense per-history score array (alternate runs)
+  kPodA,          // mc_pod_svd: the matrix being orthogonalised
+  kPodV,          // mc_pod_svd: V, the singular values and the rotation count
   kScratchSlots,  // number of slots
 };
 
@@ -2794,6 +2796,61 @@ int mc_tsl_group_transfer(mc_ctx* c, int32_t tsl, const double* energy, const do
           tot ? static_cast<double>(counts[static_cast<size_t>(r) * groups + g]) / static_cast<double>(tot) : 0.0;
   }
   if (failures) *failures = fails;
+  return MC_OK;
+}
+
+int mc_pod_svd(mc_ctx* c, const double* A, uint64_t m, uint64_t n, double* U, double* S, double* V,
+               uint32_t* sweeps) {
+  if (!check_ctx(c, false)) return MC_ERR_STATE;
+  if (!A || !U || !S || !V) return fail(c, MC_ERR_INPUT, "null argument");
+  if (n == 0 || m < n) return fail(c, MC_ERR_INPUT, "mc_pod_svd: needs m >= n >= 1");
+  if (n > (1u << 16) || m > (1ull << 31) || m * n > (1ull << 30))
+    return fail(c, MC_ERR_INPUT, "mc_pod_svd: at most 2^16 columns, 2^31 rows and 2^30 entries");
+  for (uint64_t k = 0; k < m * n; k++)
+    if (!std::isfinite(A[k])) return fail(c, MC_ERR_INPUT, "mc_pod_svd: the matrix holds a non-finite value");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  auto* dA = static_cast<double*>(scratch(c, kPodA, m * n * 8));
+  auto* dV = static_cast<double*>(scratch(c, kPodV, (n * n + n + 1) * 8));
+  if (!dA || !dV) return fail(c, MC_ERR_OOM, "mc_pod_svd buffers");
+  double* dS = dV + n * n;
+  auto* d_rot = reinterpret_cast<unsigned*>(dS + n);
+  const int mi = static_cast<int>(m), ni = static_cast<int>(n);
+  CUDA_TRY(c, cudaMemcpyAsync(dA, A, m * n * 8, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, mcd::launch_jacobi_init(dV, ni, c->stream));
+  // a pair counts as orthogonal when |a_i . a_j| <= sqrt(m) eps |a_i| |a_j|
+  const double tol = std::sqrt(static_cast<double>(m)) * 2.220446049250313e-16;
+  constexpr uint32_t kMaxSweeps = 60;
+  uint32_t done = 0;
+  unsigned rot = 1;
+  while (rot && done < kMaxSweeps) {
+    CUDA_TRY(c, cudaMemsetAsync(d_rot, 0, sizeof(unsigned), c->stream));
+    CUDA_TRY(c, mcd::launch_jacobi_sweep(dA, dV, mi, ni, tol, d_rot, c->stream));
+    c->launches += static_cast<uint64_t>(ni + (ni & 1) - 1);
+    CUDA_TRY(c, cudaMemcpyAsync(&rot, d_rot, sizeof rot, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    done++;
+  }
+  if (rot) return fail(c, MC_ERR_INPUT, "mc_pod_svd: no convergence in " + std::to_string(kMaxSweeps) + " sweeps");
+  CUDA_TRY(c, mcd::launch_column_norms(dA, mi, ni, dS, c->stream));
+  c->launches++;
+  std::vector<double> hA(m * n), hV(n * n), hS(n);
+  CUDA_TRY(c, cudaMemcpyAsync(hA.data(), dA, m * n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(hV.data(), dV, n * n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(hS.data(), dS, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  // descending singular values (ties keep column order); U's columns
+  // normalised, zero where the singular value is zero
+  std::vector<uint64_t> order(n);
+  for (uint64_t k = 0; k < n; k++) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return hS[a] > hS[b]; });
+  for (uint64_t k = 0; k < n; k++) {
+    const uint64_t j = order[k];
+    S[k] = hS[j];
+    const double inv = hS[j] > 0.0 ? 1.0 / hS[j] : 0.0;
+    for (uint64_t r = 0; r < m; r++) U[k * m + r] = hA[j * m + r] * inv;
+    for (uint64_t r = 0; r < n; r++) V[k * n + r] = hV[j * n + r];
+  }
+  if (sweeps) *sweeps = done;
   return MC_OK;
 }
 

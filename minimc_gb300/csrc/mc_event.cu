@@ -522,9 +522,8 @@ __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_mg(const De
                                                                         const unsigned long long* offsets,
                                                                         const unsigned long long* total,
                                                                         unsigned long long cap, uint4* out) {
-  extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
   constexpr uint32_t kWordsPerSite = FAST ? 1u + 2u + 2u : 2u + 4u + 2u;
-  sites_out_cta_by_site(rp.n, offsets, total, cap, out, stage, [&](unsigned long long h, uint32_t y, Site* dst) {
+  sites_out_cta_by_site(rp.n, offsets, total, cap, out, [&](unsigned long long h, uint32_t y, Site* dst) {
     const FissionRec f = rp.fis[h];
     PhiloxRng rng;
     rng.restore(rp.run_key, f.id, f.tag & 1u, philox_skip(f.rng, y * kWordsPerSite));
@@ -672,24 +671,10 @@ bool sites_out_fits(uint32_t max_yield) { return sites_out_smem(max_yield) <= kS
 cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream) {
-  const size_t smem = sites_out_smem(rp.max_yield);
-  if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
   const unsigned grid = static_cast<unsigned>((rp.n + kSitesOutHist - 1) / kSitesOutHist);
   auto* o = reinterpret_cast<uint4*>(out);
-  // the attribute is per device, so it is set at every launch (a host-side call)
-  cudaError_t e;
-  if (rp.fast) {
-    e = cudaFuncSetAttribute(k_fission_sites_out_mg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    k_fission_sites_out_mg<true><<<grid, kSitesOutHist, smem, stream>>>(w, rp, offsets, total, cap, o);
-  }
-  else {
-    e = cudaFuncSetAttribute(k_fission_sites_out_mg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    k_fission_sites_out_mg<false><<<grid, kSitesOutHist, smem, stream>>>(w, rp, offsets, total, cap, o);
-  }
+  if (rp.fast) k_fission_sites_out_mg<true><<<grid, kSitesOutHist, 0, stream>>>(w, rp, offsets, total, cap, o);
+  else k_fission_sites_out_mg<false><<<grid, kSitesOutHist, 0, stream>>>(w, rp, offsets, total, cap, o);
   return cudaGetLastError();
 }
 

@@ -195,13 +195,19 @@ __device__ __forceinline__ void sites_out_cta(unsigned long long n, const uint32
 // CTA's histories' bank offsets go to shared memory, each thread finds the
 // history and the index y of its site there, and site(h, y, dst) writes
 // that one site (a history's sites are then sampled by neighbouring
-// threads side by side, not one after another by one thread).
+// threads side by side, not one after another by one thread).  The CTA's
+// sites pass through a window of kSitesOutHist sites in shared memory, one
+// window after another, so its footprint (9 KB) does not grow with the
+// largest yield and the kernel keeps its occupancy; each window is stored
+// with coalesced 16-byte writes.  blockDim.x must be kSitesOutHist.
 template <class SiteFn>
 __device__ __forceinline__ void sites_out_cta_by_site(unsigned long long n, const unsigned long long* offsets,
                                                       const unsigned long long* total, unsigned long long cap,
-                                                      uint4* out, uint4* stage, SiteFn&& site) {
+                                                      uint4* out, SiteFn&& site) {
   static_assert(sizeof(Site) % sizeof(uint4) == 0, "sites are stored as 16-byte words");
+  constexpr unsigned kWords = sizeof(Site) / sizeof(uint4);
   __shared__ unsigned long long s_off[kSitesOutHist + 1];
+  __shared__ uint4 win[kSitesOutHist * kWords];
   const unsigned long long first = static_cast<unsigned long long>(blockIdx.x) * kSitesOutHist;
   const unsigned long long last = first + kSitesOutHist < n ? first + kSitesOutHist : n;
   const int H = static_cast<int>(last - first);
@@ -211,20 +217,25 @@ __device__ __forceinline__ void sites_out_cta_by_site(unsigned long long n, cons
   if (threadIdx.x == 0) s_off[H] = end - base;
   __syncthreads();
   const unsigned long long m = end - base;
-  for (unsigned long long j = threadIdx.x; j < m; j += blockDim.x) {
-    // the history whose sites hold j: the last k with s_off[k] <= j
-    int lo = 0, hi = H;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (s_off[mid] <= j) lo = mid;
-      else hi = mid;
+  for (unsigned long long w0 = 0; w0 < m; w0 += kSitesOutHist) {
+    const unsigned long long j = w0 + threadIdx.x;
+    if (j < m) {
+      // the history whose sites hold j: the last k with s_off[k] <= j
+      int lo = 0, hi = H;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (s_off[mid] <= j) lo = mid;
+        else hi = mid;
+      }
+      site(first + lo, static_cast<uint32_t>(j - s_off[lo]), reinterpret_cast<Site*>(win) + threadIdx.x);
     }
-    site(first + lo, static_cast<uint32_t>(j - s_off[lo]), reinterpret_cast<Site*>(stage) + j);
+    __syncthreads();
+    const unsigned long long at = base + w0;
+    const unsigned long long cnt = m - w0 < kSitesOutHist ? m - w0 : kSitesOutHist;
+    const unsigned long long keep = at >= cap ? 0 : (cnt < cap - at ? cnt : cap - at);
+    for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[at * kWords + i] = win[i];
+    __syncthreads();
   }
-  __syncthreads();
-  const unsigned long long keep = base >= cap ? 0 : (m < cap - base ? m : cap - base);
-  constexpr unsigned kWords = sizeof(Site) / sizeof(uint4);
-  for (unsigned long long i = threadIdx.x; i < keep * kWords; i += kSitesOutHist) out[base * kWords + i] = stage[i];
 }
 
 // A Philox stream position (PhiloxRng::save's packing) s words further on
@@ -309,6 +320,14 @@ cudaError_t launch_expand_rows(const double* E_rows, const double* T_rows, unsig
 cudaError_t launch_group_bins(const double* beta, unsigned rows, unsigned long long n, const double* E_rows,
                               const double* T_rows, const double* bounds, int G, unsigned long long* counts,
                               cudaStream_t stream);
+
+// thin SVD of the POD table pipeline by one-sided Jacobi rotations
+// (mc_pod.cu): V = I, then sweeps until one makes no rotation, then the
+// column norms of A V
+cudaError_t launch_jacobi_init(double* V, int n, cudaStream_t stream);
+cudaError_t launch_jacobi_sweep(double* A, double* V, int m, int n, double tol, unsigned* rotations,
+                                cudaStream_t stream);
+cudaError_t launch_column_norms(const double* A, int m, int n, double* S, cudaStream_t stream);
 
 // bank compaction and resampling (mc_transport.cu)
 cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,

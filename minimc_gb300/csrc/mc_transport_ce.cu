@@ -47,14 +47,14 @@ __global__ void __launch_bounds__(kSitesOutHist) k_fission_sites_out_ce(const Ru
                                                                         const unsigned long long* offsets,
                                                                         const unsigned long long* total,
                                                                         unsigned long long cap, uint4* out) {
-  extern __shared__ uint4 stage[];  // [kSitesOutHist * max_yield] sites
+  extern __shared__ uint4 stage[];  // minstd: [kSitesOutHist * max_yield] sites
   const bool fast = rp.fast != 0;
   if constexpr (std::is_same_v<Rng, PhiloxRng>) {
     // a site draws a fixed number of 32-bit words -- the isotropic direction
     // (2 in the FP32 form, 4 in FP64) and the secondary's key (2) -- so each
     // site starts at a known stream position and has a thread of its own
     const uint32_t words = (fast ? 2u : 4u) + 2u;
-    sites_out_cta_by_site(rp.n, offsets, total, cap, out, stage, [&](unsigned long long h, uint32_t y, Site* dst) {
+    sites_out_cta_by_site(rp.n, offsets, total, cap, out, [&](unsigned long long h, uint32_t y, Site* dst) {
       const FissionRec f = rp.fis[h];
       PhiloxRng rng;
       rng.restore(rp.run_key, f.id, f.tag & 1u, philox_skip(f.rng, y * words));
@@ -95,23 +95,21 @@ constexpr int kMinb[5] = {1, 3, 4, 5, 6};  // occupancy variants (autotuner inde
 cudaError_t launch_fission_sites_out_ce(const RunParams& rp, int rng_mode, const unsigned long long* offsets,
                                         const unsigned long long* total, unsigned long long cap, Site* out,
                                         cudaStream_t stream) {
-  const size_t smem = sites_out_smem(rp.max_yield);
-  if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
   const unsigned grid = static_cast<unsigned>((rp.n + kSitesOutHist - 1) / kSitesOutHist);
   auto* o = reinterpret_cast<uint4*>(out);
-  // the attribute is per device, so it is set at every launch (a host-side call)
-  cudaError_t e;
   if (rng_mode == 1) {
-    e = cudaFuncSetAttribute(k_fission_sites_out_ce<MinstdRng>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
+    // minstd: one thread per history, its sites staged whole
+    const size_t smem = sites_out_smem(rp.max_yield);
+    if (smem > kSitesOutMaxSmem) return cudaErrorInvalidValue;
+    // the attribute is per device, so it is set at every launch (a host-side call)
+    const cudaError_t e = cudaFuncSetAttribute(k_fission_sites_out_ce<MinstdRng>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     k_fission_sites_out_ce<MinstdRng><<<grid, kSitesOutHist, smem, stream>>>(rp, offsets, total, cap, o);
   }
   else {
-    e = cudaFuncSetAttribute(k_fission_sites_out_ce<PhiloxRng>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    k_fission_sites_out_ce<PhiloxRng><<<grid, kSitesOutHist, smem, stream>>>(rp, offsets, total, cap, o);
+    // Philox: one thread per site through a fixed window (no dynamic shared memory)
+    k_fission_sites_out_ce<PhiloxRng><<<grid, kSitesOutHist, 0, stream>>>(rp, offsets, total, cap, o);
   }
   return cudaGetLastError();
 }
