@@ -1111,13 +1111,12 @@ int emit_bank(mc_ctx* c, const RunParams& rp, int rng, Site* dest, uint64_t cap,
     RunParams q = rp;
     q.ctr = c->d_ctr;
     q.bank_count = count;
-    CUDA_TRY(c, mcd::launch_fission_counts(q, c->stream));
-    CUDA_TRY(c, mcd::launch_bank_scan(count, n, offsets, sums, total, c->stream));
+    CUDA_TRY(c, mcd::launch_direct_bank_scan(q, offsets, sums, total, c->stream));
     const uint64_t qcap = dest ? cap : n * c->max_yield;
     if (c->model.energy_mode == mc::kMultigroup)
       CUDA_TRY(c, mcd::launch_fission_sites_out_mg(c->dw, q, offsets, total, qcap, dest ? dest : bank, c->stream));
     else CUDA_TRY(c, mcd::launch_fission_sites_out_ce(q, rng, offsets, total, qcap, dest ? dest : bank, c->stream));
-    c->launches += 5;
+    c->launches += 4;
   }
   else {
     auto* slots = static_cast<Site*>(c->scratch[kSlots].p);
@@ -3285,8 +3284,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
     if ((e = mcd::launch_batch_begin(bc, from, s)) != cudaSuccess) return e;
     if ((e = mcd::launch_history_mg_batch(d_worlds, d_rps, d_bp, grid, P, s, variant)) != cudaSuccess) return e;
     if (direct) {
-      if ((e = mcd::launch_fission_counts(all, s)) != cudaSuccess) return e;
-      if ((e = mcd::launch_bank_scan(count, N, offsets, sums, total, s)) != cudaSuccess) return e;
+      if ((e = mcd::launch_direct_bank_scan(all, offsets, sums, total, s)) != cudaSuccess) return e;
       if ((e = mcd::launch_fission_sites_out_mg_batch(d_worlds, d_rps, d_off, P, N, max_yield, o->fast_math != 0,
                                                       fis, count, offsets, total, bank, s)) != cudaSuccess)
         return e;
@@ -3299,7 +3297,7 @@ int mc_batch_run(mc_batch* b, const mc_batch_opts* o, mc_batch_out* out) {
     if ((e = mcd::launch_batch_tally(bc, offsets, total, s)) != cudaSuccess) return e;
     return mcd::launch_batch_resample(bc, bank, to, s);
   };
-  constexpr int kLaunchesPerCycle = 10;
+  const int kLaunchesPerCycle = direct ? 9 : 10;  // begin, transport, bank (4 or 5), tally, resample (2)
   BATCH_TRY(b, cudaMemsetAsync(d_cycle, 0, 4, s));
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   struct GraphGuard {

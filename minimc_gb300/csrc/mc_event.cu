@@ -501,15 +501,8 @@ __global__ void __launch_bounds__(256) k_fission_sites_mg(const DevWorld w, cons
 // min(n, max_yield) sites (multigroup: no chi draw can fall past the end of
 // its cdf, which the caller checks against the largest uniform the stream
 // draws; continuous energy: always), the counts are known before sampling
-// and a scan of them gives every history its place in the bank.
-__global__ void __launch_bounds__(256) k_fission_counts(const RunParams rp) {
-  const unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (h >= rp.n) return;
-  const uint32_t f = rp.fis[h].n;
-  rp.bank_count[h] = f < rp.max_yield ? f : rp.max_yield;
-  // sites past max_yield are dropped and counted, as the slot kernel does
-  if (f > rp.max_yield) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(f - rp.max_yield));
-}
+// and a scan of them (launch_direct_bank_scan, mc_transport.cu) gives every
+// history its place in the bank.
 
 // The multigroup direct-bank CTA: the draws are those of fission_sites_mg,
 // site for site.  A site draws a fixed number of 32-bit words -- the chi
@@ -656,11 +649,6 @@ cudaError_t launch_fission_sites_mg(const DevWorld& w, const RunParams& rp, int 
                                     cudaStream_t stream) {
   if (rng_mode == 1) k_fission_sites_mg<MinstdRng><<<grid, 256, 0, stream>>>(w, rp);
   else k_fission_sites_mg<PhiloxRng><<<grid, 256, 0, stream>>>(w, rp);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_fission_counts(const RunParams& rp, cudaStream_t stream) {
-  k_fission_counts<<<static_cast<unsigned>((rp.n + 255) / 256), 256, 0, stream>>>(rp);
   return cudaGetLastError();
 }
 

@@ -139,13 +139,13 @@ cudaError_t launch_commit_dense(const RunParams& rp, int grid, cudaStream_t stre
 // record's site count is known before sampling (multigroup: Philox streams
 // and chi cdfs that all end above the largest uniform the stream draws;
 // continuous energy: always): per-history counts min(n, max_yield) into
-// bank_count, then (after a scan of the counts) the sites, staged per CTA of
-// kSitesOutHist histories in shared memory and stored to `out` (device or
+// bank_count with their scan (launch_direct_bank_scan), then the sites,
+// staged per CTA of kSitesOutHist histories in shared memory and stored to
+// `out` (device or
 // page-locked host memory, 16-byte aligned) with coalesced 16-byte writes;
 // sites at or past `cap` are not written
 constexpr int kSitesOutHist = 128;
 constexpr size_t kSitesOutMaxSmem = 192 * 1024;
-cudaError_t launch_fission_counts(const RunParams& rp, cudaStream_t stream);
 size_t sites_out_smem(uint32_t max_yield);
 bool sites_out_fits(uint32_t max_yield);
 cudaError_t launch_fission_sites_out_mg(const DevWorld& w, const RunParams& rp, const unsigned long long* offsets,
@@ -332,6 +332,11 @@ cudaError_t launch_column_norms(const double* A, int m, int n, double* S, cudaSt
 // bank compaction and resampling (mc_transport.cu)
 cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
                              unsigned long long* scratch_sums, unsigned long long* total, cudaStream_t stream);
+// the direct bank path's counts (min(n, max_yield) per fission record, into
+// rp.bank_count, overflow counted in rp.ctr), their exclusive prefix sum and
+// the bank size, in three launches
+cudaError_t launch_direct_bank_scan(const RunParams& rp, unsigned long long* offsets, unsigned long long* scratch_sums,
+                                    unsigned long long* total, cudaStream_t stream);
 cudaError_t launch_bank_compact(const Site* slots, const uint32_t* count, const unsigned long long* offsets,
                                 unsigned long long n, uint32_t max_yield, Site* out, cudaStream_t stream);
 cudaError_t launch_resample(const Site* bank, const unsigned long long* total, unsigned long long n,

@@ -510,12 +510,10 @@ cudaError_t launch_history_mg(const DevWorld& w, const RunParams& rp, int rng_mo
 namespace {
 constexpr int kScanBlock = 1024;
 
-__global__ void k_scan_blocks(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
-                              unsigned long long* block_sums) {
-  __shared__ unsigned long long warp_sums[32];
-  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
-  unsigned long long v = i < n ? count[i] : 0;
-  // inclusive warp scan
+// inclusive scan of v over a CTA of kScanBlock threads; *cta_total (every
+// thread) = the CTA's sum
+__device__ __forceinline__ unsigned long long cta_scan(unsigned long long v, unsigned long long* warp_sums,
+                                                      unsigned long long* cta_total) {
   const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long x = v;
   for (int off = 1; off < 32; off <<= 1) {
@@ -533,9 +531,64 @@ __global__ void k_scan_blocks(const uint32_t* count, unsigned long long n, unsig
     warp_sums[lane] = s;
   }
   __syncthreads();
-  const unsigned long long warp_base = wid ? warp_sums[wid - 1] : 0;
-  if (i < n) offsets[i] = warp_base + x - v;
-  if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = warp_base + x;
+  *cta_total = warp_sums[31];
+  return (wid ? warp_sums[wid - 1] : 0) + x;
+}
+
+__global__ void k_scan_blocks(const uint32_t* count, unsigned long long n, unsigned long long* offsets,
+                              unsigned long long* block_sums) {
+  __shared__ unsigned long long warp_sums[32];
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
+  const unsigned long long v = i < n ? count[i] : 0;
+  unsigned long long tot;
+  const unsigned long long x = cta_scan(v, warp_sums, &tot);
+  if (i < n) offsets[i] = x - v;
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// The direct bank path's prefix sum, from the fission records themselves:
+// history h yields min(n_h, max_yield) sites (sites past max_yield are
+// dropped and counted, as the slot kernel does).  Pass 1 sums each CTA's
+// counts; the one-CTA scan turns the sums into CTA prefixes and the bank
+// size; pass 2 scans each CTA's counts again and writes the counts and the
+// finished offsets.
+__device__ __forceinline__ uint32_t record_sites(const RunParams& rp, unsigned long long i, uint32_t* f_out) {
+  const uint32_t f = i < rp.n ? rp.fis[i].n : 0u;
+  *f_out = f;
+  return f < rp.max_yield ? f : rp.max_yield;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_count_block_sums(const RunParams rp, unsigned long long* block_sums) {
+  __shared__ unsigned long long warp_sums[32];
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
+  uint32_t f;
+  unsigned long long v = record_sites(rp, i, &f);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned long long s = warp_sums[threadIdx.x];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_count_offsets(const RunParams rp,
+                                                              const unsigned long long* block_prefix,
+                                                              unsigned long long* offsets) {
+  __shared__ unsigned long long warp_sums[32];
+  const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
+  uint32_t f;
+  const uint32_t c = record_sites(rp, i, &f);
+  unsigned long long tot;
+  const unsigned long long x = cta_scan(c, warp_sums, &tot);
+  if (i < rp.n) {
+    offsets[i] = block_prefix[blockIdx.x] + x - c;
+    rp.bank_count[i] = c;
+    if (f > rp.max_yield) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(f - rp.max_yield));
+  }
 }
 
 __global__ void k_scan_sums(unsigned long long* block_sums, unsigned long long nb, unsigned long long* total) {
@@ -594,6 +647,15 @@ cudaError_t launch_bank_scan(const uint32_t* count, unsigned long long n, unsign
   k_scan_blocks<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(count, n, offsets, scratch_sums);
   k_scan_sums<<<1, 1024, 0, stream>>>(scratch_sums, nb, total);
   k_scan_add<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(offsets, n, scratch_sums);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_direct_bank_scan(const RunParams& rp, unsigned long long* offsets, unsigned long long* scratch_sums,
+                                    unsigned long long* total, cudaStream_t stream) {
+  const unsigned long long nb = (rp.n + kScanBlock - 1) / kScanBlock;
+  k_count_block_sums<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(rp, scratch_sums);
+  k_scan_sums<<<1, 1024, 0, stream>>>(scratch_sums, nb, total);
+  k_count_offsets<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(rp, scratch_sums, offsets);
   return cudaGetLastError();
 }
 
