@@ -2288,24 +2288,93 @@ std::vector<float> mlp_init_params(uint64_t seed, int used_inputs) {
 }
 
 // one network trained on (X, y) by Adam with a cosine-decayed rate; returns
-// the mean squared error over the last 5 % of the steps
+// the mean squared error over the last 5 % of the steps.  The step number,
+// each step's learning rate and Adam's bias corrections live on the device,
+// so after an eager first step (which also sets the products' launch
+// attributes) one captured CUDA graph of kGraphSteps steps is replayed;
+// the steps left over run eagerly with the same device state.
 int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __half* X, const float* y, uint64_t n, int used_inputs,
               const mc_train_desc& d, uint64_t key, double* loss_out) {
+  constexpr uint32_t kGraphSteps = 8;
   const std::vector<float> p0 = mlp_init_params(key, used_inputs);
   CUDA_TRY(c, cudaMemcpyAsync(net.p, p0.data(), p0.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(net.m, 0, mcd::kMlpParams * sizeof(float), c->stream));
   CUDA_TRY(c, cudaMemsetAsync(net.v, 0, mcd::kMlpParams * sizeof(float), c->stream));
   CUDA_TRY(c, mcd::mlp_refresh_weights(net, c->stream));
   float* losses = mlp_alloc<float>(c, d.steps);
-  if (!losses) return fail(c, MC_ERR_OOM, "surrogate loss buffer");
+  float* sched = mlp_alloc<float>(c, 3ull * d.steps);
+  int* step = mlp_alloc<int>(c, 1);
+  if (!losses || !sched || !step) return fail(c, MC_ERR_OOM, "surrogate training buffers");
+  std::vector<float> hs(3ull * d.steps);
+  for (uint32_t t = 1; t <= d.steps; t++) {
+    const double frac = static_cast<double>(t) / d.steps;
+    hs[3 * (t - 1)] = static_cast<float>(d.lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+    hs[3 * (t - 1) + 1] = 1.0f / (1.0f - powf(0.9f, static_cast<float>(t)));
+    hs[3 * (t - 1) + 2] = 1.0f / (1.0f - powf(0.999f, static_cast<float>(t)));
+  }
+  const int one = 1;
+  CUDA_TRY(c, cudaMemcpyAsync(sched, hs.data(), hs.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(step, &one, sizeof one, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(losses, 0, d.steps * sizeof(float), c->stream));
   mcd::MlpBatch b = c->mlp_batch;
-  for (uint32_t step = 1; step <= d.steps; step++) {
-    const double frac = static_cast<double>(step) / d.steps;
-    const float lr = static_cast<float>(d.lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(M_PI * frac))));
-    b.loss = losses + (step - 1);
-    CUDA_TRY(c, mcd::launch_mlp_gather(X, y, n, key, static_cast<int>(step), b, c->stream));
-    CUDA_TRY(c, mcd::mlp_forward_backward(net, b, c->stream));
-    CUDA_TRY(c, mcd::mlp_adam(net, static_cast<int>(step), lr, c->stream));
+  b.loss = losses;
+  const mcd::StepState st{step, sched};
+  auto one_step = [&](cudaStream_t s) -> cudaError_t {
+    cudaError_t e;
+    if ((e = mcd::launch_mlp_gather(X, y, n, key, 0, b, s, step)) != cudaSuccess) return e;
+    if ((e = mcd::mlp_forward_backward(net, b, s, st)) != cudaSuccess) return e;
+    return mcd::mlp_adam(net, st, s);
+  };
+  CUDA_TRY(c, one_step(c->stream));
+  uint32_t done = 1;
+  c->launches += 12;
+  const uint32_t reps = (d.steps - done) / kGraphSteps;
+  if (reps > 0) {
+    // the capture runs on a stream of its own (the context's stream may be
+    // the legacy default stream, which cannot be captured), ordered after
+    // the work queued so far and before what follows by events
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto release = [&]() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+      if (cs) cudaStreamDestroy(cs);
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaError_t ce = cudaSuccess;
+      for (uint32_t k = 0; k < kGraphSteps && ce == cudaSuccess; k++) ce = one_step(cs);
+      e = cudaStreamEndCapture(cs, &graph);
+      if (e == cudaSuccess) e = ce;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev[0], 0);
+    for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) {
+      e = cudaGraphLaunch(exec, cs);
+      done += kGraphSteps;
+      c->launches += 12 * kGraphSteps;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, ev[1], 0);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(cs);
+      release();
+      return fail(c, MC_ERR_DEVICE, std::string("surrogate training graph: ") + cudaGetErrorString(e));
+    }
+    // the stream and graph go once the replays have run
+    CUDA_TRY(c, cudaStreamSynchronize(cs));
+    release();
+  }
+  for (; done < d.steps; done++) {
+    CUDA_TRY(c, one_step(c->stream));
     c->launches += 12;
   }
   std::vector<float> h(d.steps);

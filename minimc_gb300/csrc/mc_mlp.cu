@@ -16,6 +16,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <type_traits>
 
 namespace mcd {
@@ -307,9 +308,19 @@ cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int N, int K, 
   if (!operand_map(&ta, A, lda, M, K, 128) || !operand_map(&tb, B, ldb, N, K, NT)) return cudaErrorInvalidValue;
   auto* kern = &k_gemm<NT, Epi, kF16>;
   const size_t smem = gemm_smem_bytes(NT, k_split);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(gemm_smem_bytes(NT, kGemmMaxK)));
+  // the shared-memory limit is a per-device attribute: set once per device
+  // (so that a captured training step makes no attribute call)
+  static std::atomic<uint32_t> set_on{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  const uint32_t bit = dev < 32 ? 1u << dev : 0u;
+  if (!bit || !(set_on.load() & bit)) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(gemm_smem_bytes(NT, kGemmMaxK)));
+    if (e != cudaSuccess) return e;
+    set_on.fetch_or(bit);
+  }
   kern<<<dim3(M / 128, N / NT, splits), 128, smem, s>>>(ta, tb, GemmArgs{k_split, err}, epi);
   return cudaGetLastError();
 }
@@ -317,8 +328,9 @@ cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int N, int K, 
 // output layer, loss and the first backward step, one sample per thread:
 // out = b4 + w4 . SiLU(Z3); e = out - y; dZ3 = (2e / B) w4 SiLU'(Z3)
 __global__ void __launch_bounds__(128) k_head(const float* Z3, const float* p, const float* y, int B, bf16* dZ3,
-                                              bf16* dZ3t, float* g, float* loss) {
+                                              bf16* dZ3t, float* g, float* loss, const int* step) {
   __shared__ float red[4][kMlpWidth];
+  if (step) loss += *step - 1;
   const int r = blockIdx.x * 128 + threadIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
@@ -362,9 +374,16 @@ __global__ void k_head_forward(const float* Z3, const float* p, int B, float* ou
 }
 
 // Adam (Kingma and Ba), bias-corrected
-__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float c1, float c2) {
+__global__ void k_adam(float* p, const float* g, float* m, float* v, int n, float lr, float c1, float c2,
+                       const float* sched, const int* step) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (step) {
+    const float* row = sched + 3 * (*step - 1);
+    lr = row[0];
+    c1 = row[1];
+    c2 = row[2];
+  }
   const float gi = g[i];
   const float mi = 0.9f * m[i] + 0.1f * gi;
   const float vi = 0.999f * v[i] + 0.001f * gi * gi;
@@ -374,8 +393,10 @@ __global__ void k_adam(float* p, const float* g, float* m, float* v, int n, floa
 }
 
 // FP16 forward weight copies and BF16 transposes from the FP32 master weights
-__global__ void k_refresh(const float* p, f16* W1, f16* W2, f16* W3, bf16* W2t, bf16* W3t) {
+__global__ void k_refresh(const float* p, f16* W1, f16* W2, f16* W3, bf16* W2t, bf16* W3t, int* advance_step) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // the last launch of a step: the next step's counter (nothing here reads it)
+  if (advance_step && i == 0) *advance_step += 1;
   if (i < kMlpWidth * kMlpIn) W1[i] = __float2half_rn(p[kMlpW1 + i]);
   if (i < kMlpWidth * kMlpWidth) {
     const int r = i / kMlpWidth, c = i % kMlpWidth;
@@ -390,8 +411,9 @@ __device__ int g_mlp_err;
 
 }  // namespace
 
-cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s) {
-  k_refresh<<<kMlpWidth * kMlpWidth / 256, 256, 0, s>>>(net.p, net.W1, net.W2, net.W3, net.W2t, net.W3t);
+cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s, int* advance_step) {
+  k_refresh<<<kMlpWidth * kMlpWidth / 256, 256, 0, s>>>(net.p, net.W1, net.W2, net.W3, net.W2t, net.W3t,
+                                                          advance_step);
   return cudaGetLastError();
 }
 
@@ -419,14 +441,14 @@ cudaError_t mlp_forward(const MlpNet& net, const MlpBatch& b, float* out, cudaSt
   return cudaGetLastError();
 }
 
-cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s) {
+cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s, const StepState& st) {
   int* err = mlp_err_ptr();
   const int B = b.B;
   // weight-gradient products split K = B into chunks of 128 samples
   const int splits = B / 128;
   cudaError_t e;
   if ((e = cudaMemsetAsync(net.g, 0, kMlpParams * sizeof(float), s)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(b.loss, 0, sizeof(float), s)) != cudaSuccess) return e;
+  if (!st.step && (e = cudaMemsetAsync(b.loss, 0, sizeof(float), s)) != cudaSuccess) return e;
   if ((e = gemm<64>(b.X, kMlpIn, net.W1, kMlpIn, B, kMlpWidth, kMlpIn, 1, err,
                          EpiForward{net.p + kMlpB1, b.Z1, b.H1, b.H1t, B}, s)) != cudaSuccess)
     return e;
@@ -437,7 +459,7 @@ cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStrea
   if ((e = gemm<64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, B}, s)) != cudaSuccess)
     return e;
-  k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss);
+  k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss, st.step);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // layer 3: dW3 = dZ3^T H2; dH2 = dZ3 W3 -> dZ2
   if ((e = gemm<64>(b.dZ3t, B, b.H2t, B, kMlpWidth, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW3, kMlpWidth}, s)) !=
@@ -460,10 +482,19 @@ cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStrea
 cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s) {
   const float c1 = 1.0f / (1.0f - powf(0.9f, static_cast<float>(step)));
   const float c2 = 1.0f / (1.0f - powf(0.999f, static_cast<float>(step)));
-  k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(net.p, net.g, net.m, net.v, kMlpParams, lr, c1, c2);
+  k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(net.p, net.g, net.m, net.v, kMlpParams, lr, c1, c2, nullptr,
+                                                  nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return mlp_refresh_weights(net, s);
+}
+
+cudaError_t mlp_adam(const MlpNet& net, const StepState& st, cudaStream_t s) {
+  k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(net.p, net.g, net.m, net.v, kMlpParams, 0.0f, 0.0f, 0.0f, st.sched,
+                                                  st.step);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return mlp_refresh_weights(net, s, st.step);
 }
 
 // ---------------------------------------------------------------------------
@@ -632,9 +663,10 @@ __global__ void __launch_bounds__(1024) k_segment_sort(double* v, int K) {
 
 // random batch: row r of the batch is sample philox(key, step, r) mod n
 __global__ void k_gather(const f16* X, const float* y, unsigned long long n, unsigned long long key, int step,
-                         int B, f16* bX, bf16* bXt, float* by) {
+                         const int* step_ptr, int B, f16* bX, bf16* bXt, float* by) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= B) return;
+  if (step_ptr) step = *step_ptr;
   uint32_t c[4] = {static_cast<uint32_t>(r), static_cast<uint32_t>(step), 0x4D4C5000u, 0};
   philox4x32_10(c, static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32));
   const unsigned long long idx = ((static_cast<unsigned long long>(c[0]) << 32) | c[1]) % n;
@@ -723,8 +755,8 @@ cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K,
 }
 
 cudaError_t launch_mlp_gather(const __half* X, const float* y, unsigned long long n, unsigned long long key,
-                              int step, const MlpBatch& b, cudaStream_t s) {
-  k_gather<<<(b.B + 255) / 256, 256, 0, s>>>(X, y, n, key, step, b.B, b.X, b.Xt, b.y);
+                              int step, const MlpBatch& b, cudaStream_t s, const int* step_ptr) {
+  k_gather<<<(b.B + 255) / 256, 256, 0, s>>>(X, y, n, key, step, step_ptr, b.B, b.X, b.Xt, b.y);
   return cudaGetLastError();
 }
 

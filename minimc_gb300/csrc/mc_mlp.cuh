@@ -75,13 +75,25 @@ struct MlpBatch {
   __nv_bfloat16* dZ3t = nullptr; // [128][B]
   __nv_bfloat16* dZ2t = nullptr;
   __nv_bfloat16* dZ1t = nullptr;
-  float* loss = nullptr;         // [1] sum of squared errors
+  float* loss = nullptr;         // [1] sum of squared errors (with a StepState: [steps], one per step)
+};
+
+// A training step whose step-dependent values live on the device, so that
+// one captured CUDA graph replays every step: `step` (1-based) selects the
+// step's batch, its slot of the loss array and its row of `sched`
+// (learning rate and Adam's two bias corrections); the weight refresh at the
+// end of the step advances it.
+struct StepState {
+  int* step = nullptr;
+  const float* sched = nullptr;  // [steps][3]: lr, 1 / (1 - 0.9^t), 1 / (1 - 0.999^t)
 };
 
 // launches (mc_mlp.cu); all stream-ordered
-cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s);
-cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s);
+cudaError_t mlp_refresh_weights(const MlpNet& net, cudaStream_t s, int* advance_step = nullptr);
+// with st.step set, b.loss is the per-step loss array (zeroed by the caller)
+cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStream_t s, const StepState& st = {});
 cudaError_t mlp_adam(const MlpNet& net, int step, float lr, cudaStream_t s);
+cudaError_t mlp_adam(const MlpNet& net, const StepState& st, cudaStream_t s);
 // inference on a batch of inputs (debug/grad-check path): out[B]
 cudaError_t mlp_forward(const MlpNet& net, const MlpBatch& b, float* out, cudaStream_t s);
 
@@ -141,7 +153,7 @@ cudaError_t launch_segment_sort(double* v, unsigned long long n_segments, int K,
 // gathers a random batch (Philox key, step) of B rows of X / y into the
 // batch buffers (and X transposed)
 cudaError_t launch_mlp_gather(const __half* X, const float* y, unsigned long long n, unsigned long long key,
-                              int step, const MlpBatch& b, cudaStream_t s);
+                              int step, const MlpBatch& b, cudaStream_t s, const int* step_ptr = nullptr);
 // sampler-side POD draws used to build the training sets
 cudaError_t launch_tsl_beta_draws(const DevTSL* tsl, const double* E, const double* T, unsigned long long n,
                                   unsigned long long key, double* beta, unsigned long long* failures, cudaStream_t s);
