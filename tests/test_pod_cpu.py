@@ -93,3 +93,23 @@ def test_pipeline_library_loads(tmp_path, built_library):
     xml = synth_tsl.broomstick_xml(tsl, nuc, histories=10, cosine_bins=4, energy_bins=4)
     text = format_output(xml, tmp_path, np.zeros(36), np.zeros(36), 10)
     assert text.startswith("10\n")
+
+
+def test_svd_device_choice(monkeypatch):
+    """Without a GPU the pipeline decomposes with LAPACK; an unknown device
+    name is refused; "cuda" goes to the project's device kernel."""
+    t = table()
+    monkeypatch.setattr(pod, "_gpu_present", lambda: False)
+    U, S, Vh = pod._svd(t.matrix(), None)
+    np.testing.assert_allclose((U * S) @ Vh, t.matrix(), rtol=0, atol=1e-10)
+    with pytest.raises(ValueError, match="unknown SVD device"):
+        pod._svd(t.matrix(), "cpu")
+    called = {}
+
+    def fake(M):
+        called["shape"] = M.shape
+        return np.linalg.svd(M, full_matrices=False)
+
+    monkeypatch.setattr(pod, "_device_svd", fake)
+    pod.truncate(t, 3, "cuda")
+    assert called["shape"] == t.matrix().shape
