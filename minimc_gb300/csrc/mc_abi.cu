@@ -2301,9 +2301,23 @@ int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __half* X, const float* y, uint
   CUDA_TRY(c, cudaMemsetAsync(net.m, 0, mcd::kMlpParams * sizeof(float), c->stream));
   CUDA_TRY(c, cudaMemsetAsync(net.v, 0, mcd::kMlpParams * sizeof(float), c->stream));
   CUDA_TRY(c, mcd::mlp_refresh_weights(net, c->stream));
-  float* losses = mlp_alloc<float>(c, d.steps);
-  float* sched = mlp_alloc<float>(c, 3ull * d.steps);
-  int* step = mlp_alloc<int>(c, 1);
+  // the step state and the per-step losses live for this call only
+  // (cudaFree waits for the device, so an early return frees them safely)
+  struct CallBuffers {
+    std::vector<void*> p;
+    ~CallBuffers() {
+      for (void* q : p) cudaFree(q);
+    }
+    void* get(size_t bytes) {
+      void* q = nullptr;
+      if (cudaMalloc(&q, std::max<size_t>(16, bytes)) != cudaSuccess) return nullptr;
+      p.push_back(q);
+      return q;
+    }
+  } bufs;
+  auto* losses = static_cast<float*>(bufs.get(d.steps * sizeof(float)));
+  auto* sched = static_cast<float*>(bufs.get(3ull * d.steps * sizeof(float)));
+  auto* step = static_cast<int*>(bufs.get(sizeof(int)));
   if (!losses || !sched || !step) return fail(c, MC_ERR_OOM, "surrogate training buffers");
   std::vector<float> hs(3ull * d.steps);
   for (uint32_t t = 1; t <= d.steps; t++) {
