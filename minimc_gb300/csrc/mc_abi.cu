@@ -2361,30 +2361,44 @@ int mlp_train(mc_ctx* c, mcd::MlpNet& net, const __half* X, const float* y, uint
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
+    // a capture that cannot be made (nothing has run yet) leaves the steps
+    // to the eager loop below
+    bool captured = false;
+    if (e == cudaSuccess && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       cudaError_t ce = cudaSuccess;
       for (uint32_t k = 0; k < kGraphSteps && ce == cudaSuccess; k++) ce = one_step(cs);
-      e = cudaStreamEndCapture(cs, &graph);
-      if (e == cudaSuccess) e = ce;
+      const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+      captured = ce == cudaSuccess && ee == cudaSuccess && graph &&
+                 cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+      (void)cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev[0], 0);
-    for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) {
-      e = cudaGraphLaunch(exec, cs);
-      done += kGraphSteps;
-      c->launches += 12 * kGraphSteps;
+    if (e == cudaSuccess && !captured) {
+      release();
+      cs = nullptr;
+      ev[0] = ev[1] = nullptr;
+      graph = nullptr;
+      exec = nullptr;
     }
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], cs);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, ev[1], 0);
+    else if (e == cudaSuccess) {
+      e = cudaEventRecord(ev[0], c->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev[0], 0);
+    }
+    if (exec) {
+      for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) {
+        e = cudaGraphLaunch(exec, cs);
+        done += kGraphSteps;
+        c->launches += 12 * kGraphSteps;
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], cs);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, ev[1], 0);
+    }
     if (e != cudaSuccess) {
-      cudaStreamSynchronize(cs);
+      if (cs) cudaStreamSynchronize(cs);
       release();
       return fail(c, MC_ERR_DEVICE, std::string("surrogate training graph: ") + cudaGetErrorString(e));
     }
     // the stream and graph go once the replays have run
-    CUDA_TRY(c, cudaStreamSynchronize(cs));
+    if (cs) CUDA_TRY(c, cudaStreamSynchronize(cs));
     release();
   }
   for (; done < d.steps; done++) {
