@@ -326,6 +326,53 @@ def test_bank_direct_path_equals_slot_path(fast, built_library):
     assert (guard["key"][half:] == 0xABCDEF).all()
 
 
+@pytest.mark.parametrize("fast", [0, 1])
+def test_bank_direct_path_many_sites_per_cta(fast, built_library):
+    """A high-yield problem (one group, nu = 7.5, fission 70 % of
+    collisions): a CTA's 128 histories yield several hundred sites, so the
+    per-site kernel stages them through many 128-site windows; the direct
+    bank equals the slot path's byte for byte, in device and page-locked
+    memory, and a capacity ending inside a window keeps exactly the first
+    sites."""
+    import ctypes as C
+
+    import torch
+
+    from minimc_gb300 import SITE_DTYPE
+    from minimc_gb300.synth import MGNuclide
+
+    p = synth.one_group_cube(histories=20000, inactive=1, active=1)
+    p.nuclides = [MGNuclide("fuel", capture=np.array([0.1]), scatter=np.array([[0.2]]), fission=np.array([0.7]),
+                            nubar=np.array([7.5]), chi=np.array([[1.0]]))]
+    ctx = gpu_ctx(p.xml())
+    assert ctx.info.max_yield == 8
+    n = 20000
+    sites = _bank_sites(n, 11)
+    cap = n * ctx.info.max_yield
+
+    def pinned(k):
+        return torch.empty(k * SITE_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(SITE_DTYPE)
+
+    opts = dict(rng=RNG_PHILOX, fast_math=fast)
+    ref = np.zeros(cap, SITE_DTYPE)
+    m0 = ctx.transport_bank_into(sites, ref, bank_path=BANK_SLOTS, **opts)
+    assert m0 > 3 * n  # several sites per history: many windows per CTA
+    for out in (np.zeros(cap, SITE_DTYPE), pinned(cap)):
+        m = ctx.transport_bank_into(sites, out, bank_path=BANK_DIRECT, **opts)
+        assert m == m0
+        assert np.array_equal(out[:m].view(np.uint8), ref[:m0].view(np.uint8))
+    part = m0 // 3 + 37  # inside some CTA's window
+    guard = pinned(part + 64)
+    guard[:] = np.zeros(1, SITE_DTYPE)
+    guard["key"][part:] = 0xABCDEF
+    with pytest.raises(MCError):
+        ctx.check(ctx.lib.mc_transport_bank(ctx.h, sites.ctypes.data_as(C.c_void_p), n,
+                                            C.byref(ctx.opts(bank_path=BANK_DIRECT, **opts)),
+                                            guard.ctypes.data_as(C.c_void_p), part, C.byref(C.c_uint64())))
+    assert np.array_equal(guard[:part].view(np.uint8), ref[:part].view(np.uint8))
+    assert (guard["key"][part:] == 0xABCDEF).all()
+
+
 def test_bank_direct_path_keig_cycles(built_library):
     """k-eigenvalue cycles give the same bank sizes (k per cycle) and tallies
     on both bank paths, in both Philox forms."""
