@@ -548,21 +548,22 @@ __global__ void k_scan_blocks(const uint32_t* count, unsigned long long n, unsig
 
 // The direct bank path's prefix sum, from the fission records themselves:
 // history h yields min(n_h, max_yield) sites (sites past max_yield are
-// dropped and counted, as the slot kernel does).  Pass 1 sums each CTA's
-// counts; the one-CTA scan turns the sums into CTA prefixes and the bank
-// size; pass 2 scans each CTA's counts again and writes the counts and the
-// finished offsets.
-__device__ __forceinline__ uint32_t record_sites(const RunParams& rp, unsigned long long i, uint32_t* f_out) {
-  const uint32_t f = i < rp.n ? rp.fis[i].n : 0u;
-  *f_out = f;
-  return f < rp.max_yield ? f : rp.max_yield;
-}
-
+// dropped and counted, as the slot kernel does).  Pass 1 reads each
+// record's n (one field of a 56-byte record, so the pass reads the whole
+// record array), writes the capped counts to the compact count array and
+// sums each CTA's counts; the one-CTA scan turns the sums into CTA
+// prefixes and the bank size; pass 2 scans each CTA's counts again, from
+// the compact array, and writes the finished offsets.
 __global__ void __launch_bounds__(kScanBlock) k_count_block_sums(const RunParams rp, unsigned long long* block_sums) {
   __shared__ unsigned long long warp_sums[32];
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
-  uint32_t f;
-  unsigned long long v = record_sites(rp, i, &f);
+  const uint32_t f = i < rp.n ? rp.fis[i].n : 0u;
+  const uint32_t c = f < rp.max_yield ? f : rp.max_yield;
+  if (i < rp.n) {
+    rp.bank_count[i] = c;
+    if (f > rp.max_yield) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(f - rp.max_yield));
+  }
+  unsigned long long v = c;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = v;
@@ -580,15 +581,10 @@ __global__ void __launch_bounds__(kScanBlock) k_count_offsets(const RunParams rp
                                                               unsigned long long* offsets) {
   __shared__ unsigned long long warp_sums[32];
   const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * kScanBlock + threadIdx.x;
-  uint32_t f;
-  const uint32_t c = record_sites(rp, i, &f);
+  const uint32_t c = i < rp.n ? rp.bank_count[i] : 0u;
   unsigned long long tot;
   const unsigned long long x = cta_scan(c, warp_sums, &tot);
-  if (i < rp.n) {
-    offsets[i] = block_prefix[blockIdx.x] + x - c;
-    rp.bank_count[i] = c;
-    if (f > rp.max_yield) atomicAdd(&rp.ctr->overflow, static_cast<unsigned long long>(f - rp.max_yield));
-  }
+  if (i < rp.n) offsets[i] = block_prefix[blockIdx.x] + x - c;
 }
 
 __global__ void k_scan_sums(unsigned long long* block_sums, unsigned long long nb, unsigned long long* total) {
