@@ -66,7 +66,7 @@ __device__ __forceinline__ void history_mg(const DevWorld& w, const RunParams& r
   float fu = 0, fv = 0, fw = 0;  // the direction in FP32, for the box cells' preselection
   Pending<kPending> pend;
   pend.clear();
-  Scorer sc{&pend, nullptr, rp.n};
+  ScorerT<true> sc{&pend, nullptr, rp.n};
   Site stack[KEIG ? 1 : kStack];
   int sp = 0;
   bool alive = false, done = false;
