@@ -174,13 +174,17 @@ def test_autotuner_candidates(built_library):
     """MC_SCHEDULE_AUTO on a k-eigenvalue run: the tuner times the history
     kernel's five occupancy variants at blocks of 256 and 128 and the event
     schedule with unsorted and sorted collision queues, then keeps the
-    fastest; the run's results do not depend on the choice."""
+    default (variant 1 at 256 threads) unless a candidate beats it by more
+    than 3 %; the run's results do not depend on the choice."""
     p = synth.two_zone_cubes(histories=200000, inactive=3, active=2)
     ctx = gpu_ctx(p.xml())
     r = ctx.run_keigenvalue(rng=RNG_PHILOX, fast_math=1)
     info = ctx.schedule_info()
-    assert len(info["tune_kernel_ms"]) == 12, info
+    t = info["tune_kernel_ms"]
+    assert len(t) == 12, info
     assert info["schedule"] in ("history", "event") and info["block"] in (128, 256)
+    default = info["schedule"] == "history" and info["variant"] == 1 and info["block"] == 256
+    assert default or min(t) < 0.97 * t[1], info
     ref = gpu_ctx(p.xml()).run_keigenvalue(rng=RNG_PHILOX, fast_math=1, schedule=SCHEDULE_HISTORY, variant=1)
     assert np.array_equal(r.bank_size, ref.bank_size)
     np.testing.assert_allclose(r.sum, ref.sum, rtol=FP_RTOL)
