@@ -597,24 +597,52 @@ __global__ void __launch_bounds__(256) k_fission_sites_mg_batch(const DevWorld* 
 // the next run without a memset.
 __global__ void __launch_bounds__(256) k_commit_dense(const RunParams rp) {
   __shared__ double ws[8], wq[8];
+  // per warp, the nonzero scores of one step packed together: the FP64
+  // sums then issue per 32 nonzero scores instead of per 32 histories
+  // (most histories leave a bin at zero, and an FP64 instruction costs the
+  // whole warp however few of its lanes need it)
+  __shared__ double packed[8][128];
   const unsigned b = blockIdx.y;
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double* row = rp.pend + static_cast<size_t>(b) * rp.n;
   double s = 0, q = 0;
   const unsigned long long S = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
   unsigned long long h = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  // four independent loads in flight per thread (the array is read once)
-  for (; h + 3 * S < rp.n; h += 4 * S) {
+  // four independent loads in flight per thread (the array is read once);
+  // the bound is the warp's last lane's, so every lane of a warp takes the
+  // same trips (the shuffles below need the whole warp); what is left goes
+  // to the per-lane loop after it
+  for (unsigned long long hw = h - lane; hw + 31 + 3 * S < rp.n; h += 4 * S, hw += 4 * S) {
     double v[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) v[j] = __ldcs(row + h + j * S);
+    unsigned c = 0;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       if (__double_as_longlong(v[j]) != 0) {
-        s += v[j];
-        q += v[j] * v[j];
+        c++;
         row[h + j * S] = 0;
       }
     }
+    // exclusive prefix of the counts over the warp
+    unsigned x = c;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= static_cast<unsigned>(off)) x += y;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, x, 31);
+    unsigned o = x - c;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (__double_as_longlong(v[j]) != 0) packed[wid][o++] = v[j];
+    __syncwarp();
+    for (unsigned k = lane; k < total; k += 32) {
+      const double t = packed[wid][k];
+      s += t;
+      q += t * t;
+    }
+    __syncwarp();
   }
   for (; h < rp.n; h += S) {
     const double v = row[h];
@@ -628,8 +656,7 @@ __global__ void __launch_bounds__(256) k_commit_dense(const RunParams rp) {
     s += __shfl_down_sync(0xffffffffu, s, off);
     q += __shfl_down_sync(0xffffffffu, q, off);
   }
-  const int wid = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
+  if (lane == 0) {
     ws[wid] = s;
     wq[wid] = q;
   }
