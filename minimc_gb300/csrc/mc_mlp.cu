@@ -327,40 +327,68 @@ cudaError_t gemm(const T* A, int lda, const T* B, int ldb, int M, int N, int K, 
 
 // output layer, loss and the first backward step, one sample per thread:
 // out = b4 + w4 . SiLU(Z3); e = out - y; dZ3 = (2e / B) w4 SiLU'(Z3)
+// One CTA per 32 rows, one thread per column (128): the Z3 rows are read
+// and dZ3's written along the rows (coalesced); a row's output is the sum
+// of its four warps' partial sums; each thread keeps its column's dW4 and
+// db3 sums over the 32 rows in registers (one atomic pair per column per
+// CTA) and writes its column of dZ3^T for the 32 rows as four 16-byte
+// stores.
+constexpr int kHeadRows = 32;
 __global__ void __launch_bounds__(128) k_head(const float* Z3, const float* p, const float* y, int B, bf16* dZ3,
                                               bf16* dZ3t, float* g, float* loss, const int* step) {
-  __shared__ float red[4][kMlpWidth];
+  __shared__ float part[4][kHeadRows];
+  __shared__ float go_s[kHeadRows];
   if (step) loss += *step - 1;
-  const int r = blockIdx.x * 128 + threadIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const float* z = Z3 + static_cast<size_t>(r) * kMlpWidth;
-  float out = p[kMlpB4];
-  for (int j = 0; j < kMlpWidth; j++) out = fmaf(silu_t(z[j]), p[kMlpW4 + j], out);
-  const float e = out - y[r];
-  const float go = 2.0f * e / static_cast<float>(B);
-  const float se = warp_sum(e * e);
-  const float sg = warp_sum(go);
-  if (lane == 0) {
-    atomicAdd(loss, se);
-    atomicAdd(g + kMlpB4, sg);
-  }
-  for (int j = 0; j < kMlpWidth; j++) {
-    const float zj = z[j];
-    const float dz = go * p[kMlpW4 + j] * dsilu(zj);
-    dZ3[static_cast<size_t>(r) * kMlpWidth + j] = __float2bfloat16_rn(dz);
-    dZ3t[static_cast<size_t>(j) * B + r] = __float2bfloat16_rn(dz);
-    const float a = warp_sum(go * silu_t(zj));  // dW4
-    const float b = warp_sum(dz);             // db3
-    if (lane == 0) {
-      red[warp][j] = a;
-    }
-    if (lane == 1) atomicAdd(g + kMlpB3 + j, b);
+  const int c = threadIdx.x;  // column
+  const int row0 = blockIdx.x * kHeadRows;
+  const float w4 = p[kMlpW4 + c];
+  float z[kHeadRows];
+#pragma unroll
+  for (int i = 0; i < kHeadRows; i++) z[i] = Z3[static_cast<size_t>(row0 + i) * kMlpWidth + c];
+#pragma unroll
+  for (int i = 0; i < kHeadRows; i++) {
+    const float s = warp_sum(silu_t(z[i]) * w4);
+    if (lane == 0) part[warp][i] = s;
   }
   __syncthreads();
-  if (threadIdx.x < kMlpWidth) {
-    const int j = threadIdx.x;
-    atomicAdd(g + kMlpW4 + j, red[0][j] + red[1][j] + red[2][j] + red[3][j]);
+  if (warp == 0) {
+    const int i = lane;
+    const float out = p[kMlpB4] + part[0][i] + part[1][i] + part[2][i] + part[3][i];
+    const float e = out - y[row0 + i];
+    const float go = 2.0f * e / static_cast<float>(B);
+    go_s[i] = go;
+    const float se = warp_sum(e * e);
+    const float sg = warp_sum(go);
+    if (lane == 0) {
+      atomicAdd(loss, se);
+      atomicAdd(g + kMlpB4, sg);
+    }
   }
+  __syncthreads();
+  float dw4 = 0.0f, db3 = 0.0f;
+  uint32_t col[kHeadRows / 2];  // this column's dZ for the 32 rows, BF16 pairs
+#pragma unroll
+  for (int i = 0; i < kHeadRows; i += 2) {
+    const float g0 = go_s[i], g1 = go_s[i + 1];
+    const float dz0 = g0 * w4 * dsilu(z[i]);
+    const float dz1 = g1 * w4 * dsilu(z[i + 1]);
+    const bf16 h0 = __float2bfloat16_rn(dz0), h1 = __float2bfloat16_rn(dz1);
+    dZ3[static_cast<size_t>(row0 + i) * kMlpWidth + c] = h0;
+    dZ3[static_cast<size_t>(row0 + i + 1) * kMlpWidth + c] = h1;
+    dw4 += g0 * silu_t(z[i]);
+    dw4 += g1 * silu_t(z[i + 1]);
+    db3 += dz0;
+    db3 += dz1;
+    col[i / 2] = static_cast<uint32_t>(__bfloat16_as_ushort(h0)) | (static_cast<uint32_t>(__bfloat16_as_ushort(h1)) << 16);
+  }
+  // rows row0 .. row0 + 31 of column c: 64 contiguous bytes (B and row0
+  // are multiples of 32, so the address is 64-byte aligned)
+  uint4* dst = reinterpret_cast<uint4*>(dZ3t + static_cast<size_t>(c) * B + row0);
+#pragma unroll
+  for (int k = 0; k < 4; k++) dst[k] = make_uint4(col[4 * k], col[4 * k + 1], col[4 * k + 2], col[4 * k + 3]);
+  atomicAdd(g + kMlpW4 + c, dw4);
+  atomicAdd(g + kMlpB3 + c, db3);
 }
 
 // forward output only
@@ -459,7 +487,7 @@ cudaError_t mlp_forward_backward(const MlpNet& net, const MlpBatch& b, cudaStrea
   if ((e = gemm<64>(b.H2, kMlpWidth, net.W3, kMlpWidth, B, kMlpWidth, kMlpWidth, 1, err,
                          EpiForward{net.p + kMlpB3, b.Z3, nullptr, nullptr, B}, s)) != cudaSuccess)
     return e;
-  k_head<<<B / 128, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss, st.step);
+  k_head<<<B / kHeadRows, 128, 0, s>>>(b.Z3, net.p, b.y, B, b.dZ3, b.dZ3t, net.g, b.loss, st.step);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // layer 3: dW3 = dZ3^T H2; dH2 = dZ3 W3 -> dZ2
   if ((e = gemm<64>(b.dZ3t, B, b.H2t, B, kMlpWidth, kMlpWidth, B, splits, err, EpiAtomic{net.g + kMlpW3, kMlpWidth}, s)) !=
